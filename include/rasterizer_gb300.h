@@ -1,0 +1,156 @@
+/*
+ * rasterizer_gb300 -- C ABI of the GB300 occluder rasteriser.
+ *
+ * Drop-in GPU replacement for the hot path of rawrunprotected/rasterizer
+ * (SoftwareRasterizer/Rasterizer.h:10-61, Occluder.h:7-21): occluder
+ * rasterisation into a hierarchical 16-bit depth buffer and bounding-box
+ * visibility queries against it, bit-exact with the reference's AVX2 path.
+ * Plain C types only; every call returns OCC_OK (0) or a negative status and
+ * occ_last_error() gives a message for the calling thread.
+ *
+ * Execution model: one CUDA stream per context.  Rasterisation is deferred:
+ * occ_raster_rasterize() appends to the rasterizer's command list and the
+ * next query, read-back or flush runs all pending work in one batch of
+ * kernels.  A context and its rasterizers are not thread-safe (nor is the
+ * reference's Rasterizer); several contexts may be used from several threads.
+ */
+#ifndef RASTERIZER_GB300_H
+#define RASTERIZER_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OCC_OK 0
+#define OCC_ERR_INVALID_ARG (-1)
+#define OCC_ERR_OUT_OF_MEMORY (-2)
+#define OCC_ERR_CUDA (-3)
+#define OCC_ERR_CAPACITY (-4)
+#define OCC_ERR_UNSUPPORTED (-5)
+
+typedef struct occ_ctx_s* occ_ctx;
+typedef struct occ_raster_s* occ_raster;
+typedef uint32_t occ_occluder; /* context-scoped occluder id */
+
+/* Per-occluder flags for occ_raster_rasterize_many / batches. */
+#define OCC_NEAR_CLIP 1u /* rasterize<true> (Rasterizer.cpp:713-728, :973-982) */
+#define OCC_GATED 2u     /* decide visibility and near-clip variant on the GPU from the
+                            occluder bounds, as queryVisibility on an empty buffer would
+                            (Rasterizer.cpp:123-281); replaces the caller's query */
+
+const char* occ_last_error(void);
+int occ_version(void);
+
+/* ---- context ---------------------------------------------------------------- */
+int occ_ctx_create(int device, occ_ctx* out);
+int occ_ctx_destroy(occ_ctx ctx);
+int occ_ctx_synchronize(occ_ctx ctx);
+void* occ_ctx_stream(occ_ctx ctx); /* the context's cudaStream_t */
+
+/* ---- occluders (Occluder.h:7-21) --------------------------------------------
+ * Uploads the reference's packed occluder data unchanged: packetCount 32-byte
+ * vectors (Occluder::m_vertexData, m_packetCount; Occluder.cpp:153-156), with
+ * the quantisation box (m_refMin/m_refMax) and bounds (m_boundsMin/m_boundsMax). */
+int occ_occluder_upload(occ_ctx ctx, const uint32_t* packed, uint32_t packetCount, const float refMin[4],
+                        const float refMax[4], const float boundsMin[4], const float boundsMax[4],
+                        occ_occluder* out);
+int occ_occluder_count(occ_ctx ctx, uint32_t* count);
+
+/* ---- rasterizer (Rasterizer.h:13-26) ----------------------------------------- */
+/* Rasterizer::Rasterizer (Rasterizer.cpp:66-74): width, height multiples of 8. */
+int occ_raster_create(occ_ctx ctx, uint32_t width, uint32_t height, occ_raster* out);
+int occ_raster_destroy(occ_raster r);
+/* Rasterizer::setModelViewProjection (Rasterizer.cpp:76-105): row-vector float[16]. */
+int occ_raster_set_mvp(occ_raster r, const float matrix[16]);
+/* Rasterizer::clear (Rasterizer.cpp:107-121): hiZ := 1, depth keeps stale values. */
+int occ_raster_clear(occ_raster r);
+/* Rasterizer::rasterize<possiblyNearClipped> (Rasterizer.cpp:606-1295), deferred. */
+int occ_raster_rasterize(occ_raster r, occ_occluder occ, int possiblyNearClipped);
+/* Many rasterize calls at once; flags[i] = OCC_NEAR_CLIP | OCC_GATED (NULL = all 0). */
+int occ_raster_rasterize_many(occ_raster r, uint32_t n, const occ_occluder* occ, const uint8_t* flags);
+/* Runs pending work; gatedFlags (optional, n of the last OCC_GATED call) receives
+ * per command: bit0 drawn, bit1 near-clipped. */
+int occ_raster_flush(occ_raster r);
+int occ_raster_command_flags(occ_raster r, uint32_t n, uint8_t* out);
+/* Rasterizer::queryVisibility (Rasterizer.cpp:123-281). */
+int occ_raster_query_visibility(occ_raster r, const float boundsMin[4], const float boundsMax[4], int* visible,
+                                int* needsClipping);
+/* Batch of queries from host memory: mins/maxs n float4 each; results one bit per
+ * query in ceil(n/32) words (bit i%32 of word i/32). */
+int occ_raster_query_batch(occ_raster r, uint32_t n, const float* mins, const float* maxs, uint32_t* visibleBits,
+                           uint32_t* needsClippingBits);
+/* Same, all pointers in device memory, asynchronous on the context stream. */
+int occ_raster_query_batch_device(occ_raster r, uint32_t n, const void* dMins, const void* dMaxs,
+                                  void* dVisibleBits, void* dNeedsClippingBits);
+/* Rasterizer::query2D (Rasterizer.cpp:283-349). */
+int occ_raster_query2d(occ_raster r, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ,
+                       int* visible);
+/* Rasterizer::readBackDepth (Rasterizer.cpp:351-399): width*height RGBA8. */
+int occ_raster_read_back_depth(occ_raster r, void* rgba);
+/* Raw buffers in the reference's layout: depth width*height u16 (8x8 blocks,
+ * block-major, 8 rows of 8 pixels), hiZ blocks+8 u16. */
+int occ_raster_read_depth_raw(occ_raster r, uint16_t* out);
+int occ_raster_read_hiz(occ_raster r, uint16_t* out, uint32_t* count);
+int occ_raster_write_depth_raw(occ_raster r, const uint16_t* in);
+int occ_raster_write_hiz(occ_raster r, const uint16_t* in);
+int occ_raster_size(occ_raster r, uint32_t* width, uint32_t* height);
+
+/* ---- batched multi-view ------------------------------------------------------
+ * Sets up, bins, rasterises and queries many views in one batch of kernels. */
+typedef struct {
+  occ_raster raster;
+  const float* mvp;            /* float[16] or NULL (keep the rasterizer's matrix) */
+  int clear;                   /* clear before drawing */
+  uint32_t numOccluders;
+  const occ_occluder* occluders;
+  const uint8_t* flags;        /* per occluder OCC_NEAR_CLIP | OCC_GATED, NULL = all 0 */
+  uint32_t numQueries;
+  const float* queryMins;      /* host, numQueries float4 */
+  const float* queryMaxs;
+  uint32_t* visibleBits;       /* host, ceil(numQueries/32) words, may be NULL */
+  uint32_t* needsClippingBits;
+} occ_view_work;
+int occ_batch_execute(occ_ctx ctx, uint32_t numViews, const occ_view_work* views);
+
+/* Prepared batch: tables and query boxes uploaded once, the per-frame kernel
+ * sequence captured in a CUDA graph.  occ_batch_launch is asynchronous. */
+typedef struct occ_batch_s* occ_batch;
+int occ_batch_prepare(occ_ctx ctx, uint32_t numViews, const occ_view_work* views, occ_batch* out);
+int occ_batch_set_mvp(occ_batch b, uint32_t view, const float matrix[16]);
+int occ_batch_launch(occ_batch b);
+int occ_batch_results(occ_batch b, uint32_t view, uint32_t* visibleBits, uint32_t* needsClippingBits);
+int occ_batch_check(occ_batch b); /* syncs; OCC_ERR_CAPACITY if a launch overflowed */
+/* Runs the frame `iterations` times kernel by kernel with CUDA events between
+ * them on the context stream; msPerKernel[5] receives the mean duration of
+ * setup, scan, fill/row-walk, raster and query. */
+int occ_batch_profile(occ_batch b, uint32_t iterations, float* msPerKernel);
+int occ_batch_destroy(occ_batch b);
+
+/* ---- host-side occluder preparation (QuadDecomposition.h:5-10,
+ *      SurfaceAreaHeuristic.h:5-12, Occluder.h:9) -------------------------------
+ * Byte-identical to the reference's output. */
+/* QuadDecomposition::decompose: indices 3 per triangle -> 4 per quad; out has room
+ * for 4*(nIndices/3) entries; *outCount receives the number written. */
+int occ_quad_decompose(const uint32_t* indices, uint32_t nIndices, const float* vertices, uint32_t nVertices,
+                       uint32_t* out, uint32_t* outCount);
+/* SurfaceAreaHeuristic::generateBatches: aabbs n x (min4, max4); flat receives the
+ * batched quad indices (n entries), offsets numBatches+1 entries (room for n+1). */
+int occ_sah_generate_batches(const float* aabbs, uint32_t n, uint32_t targetSize, uint32_t splitGranularity,
+                             uint32_t* flat, uint32_t* offsets, uint32_t* numBatches);
+/* Occluder::bake: vertices nVertices float4 (multiple of 16, quads of 4);
+ * packedOut nVertices words; returns the packet count (32-byte vectors). */
+int occ_occluder_bake(const float* vertices, uint32_t nVertices, const float refMin[4], const float refMax[4],
+                      uint32_t* packedOut, uint32_t* packetCount, float boundsMin[4], float boundsMax[4],
+                      float center[4]);
+/* The coverage-mask table as the reference builds it on this host
+ * (Rasterizer.cpp:547-604) and the table the GPU uses (generated on x86-64). */
+int occ_build_coverage_table(int64_t* out4096);
+int occ_coverage_table(int64_t* out4096);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RASTERIZER_GB300_H */

@@ -1,0 +1,416 @@
+"""Python mirror of the reference's Rasterizer / Occluder API over the C ABI.
+
+Names and argument meanings follow SoftwareRasterizer/Rasterizer.h:10-61,
+Occluder.h:7-21, QuadDecomposition.h:5-10 and SurfaceAreaHeuristic.h:5-12;
+vectors (__m128 in the reference) are float4 numpy arrays.  The reference's
+asserts become ValueError; GPU or allocation failures raise OccError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._lib import OccError, ViewWork, check, lib
+
+P = C.c_void_p
+
+
+def _f32(a, shape=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if shape is not None and a.shape != shape:
+        a = a.reshape(shape)
+    return a
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(P)
+
+
+def unpack_bits(words: np.ndarray, n: int) -> np.ndarray:
+    """Query result words (bit i%32 of word i/32) -> bool array of n."""
+    b = np.unpackbits(np.ascontiguousarray(words, np.uint32).view(np.uint8), bitorder="little")
+    return b[:n].astype(bool)
+
+
+class Context:
+    """One GPU and one CUDA stream; owns the uploaded occluders."""
+
+    def __init__(self, device: int = 0):
+        h = P()
+        check(lib().occ_ctx_create(device, C.byref(h)), "occ_ctx_create")
+        self.handle = h.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().occ_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def synchronize(self):
+        check(lib().occ_ctx_synchronize(self.handle), "occ_ctx_synchronize")
+
+    @property
+    def stream(self) -> int:
+        return lib().occ_ctx_stream(self.handle) or 0
+
+
+@dataclass
+class Occluder:
+    """A baked occluder (Occluder.h:7-21): packed 11/11/10 vertex words in
+    groups of 8 quads, the quantisation box and the bounds (w = 1)."""
+
+    packed: np.ndarray          # uint32, packetCount * 8 words
+    packetCount: int            # 32-byte vectors (4 per 8 quads)
+    refMin: np.ndarray
+    refMax: np.ndarray
+    boundsMin: np.ndarray
+    boundsMax: np.ndarray
+    center: np.ndarray
+    ids: dict = field(default_factory=dict, repr=False)  # context handle -> occluder id
+
+    @staticmethod
+    def bake(vertices, refMin, refMax) -> "Occluder":
+        """Occluder::bake (Occluder.cpp:7-181): vertices (4 per quad, a multiple of 16)."""
+        v = _f32(vertices).reshape(-1, 4)
+        if len(v) == 0 or len(v) % 16:
+            raise ValueError("vertex count must be a positive multiple of 16 (Occluder.cpp:9)")
+        rmin, rmax = _f32(refMin, (4,)), _f32(refMax, (4,))
+        packed = np.zeros(len(v), np.uint32)
+        pc = C.c_uint32()
+        bmin, bmax, ctr = np.zeros(4, np.float32), np.zeros(4, np.float32), np.zeros(4, np.float32)
+        check(lib().occ_occluder_bake(_ptr(v), len(v), _ptr(rmin), _ptr(rmax), _ptr(packed), C.byref(pc),
+                                      _ptr(bmin), _ptr(bmax), _ptr(ctr)), "occ_occluder_bake")
+        return Occluder(packed, pc.value, rmin, rmax, bmin, bmax, ctr)
+
+    @property
+    def quads(self) -> int:
+        return self.packetCount * 2
+
+    def upload(self, ctx: Context) -> int:
+        """Copies the packed data to the GPU once per context; returns its id."""
+        if ctx.handle in self.ids:
+            return self.ids[ctx.handle]
+        oid = C.c_uint32()
+        check(lib().occ_occluder_upload(ctx.handle, _ptr(self.packed), self.packetCount, _ptr(self.refMin),
+                                        _ptr(self.refMax), _ptr(self.boundsMin), _ptr(self.boundsMax),
+                                        C.byref(oid)), "occ_occluder_upload")
+        self.ids[ctx.handle] = oid.value
+        return oid.value
+
+
+class QuadDecomposition:
+    @staticmethod
+    def decompose(indices, vertices) -> np.ndarray:
+        """QuadDecomposition::decompose (QuadDecomposition.cpp:346-445)."""
+        idx = np.ascontiguousarray(indices, np.uint32)
+        v = _f32(vertices).reshape(-1, 4)
+        out = np.zeros(max(4 * (idx.size // 3), 1), np.uint32)
+        n = C.c_uint32()
+        check(lib().occ_quad_decompose(_ptr(idx), idx.size, _ptr(v), len(v), _ptr(out), C.byref(n)),
+              "occ_quad_decompose")
+        return out[:n.value].copy()
+
+
+class SurfaceAreaHeuristic:
+    @staticmethod
+    def generateBatches(aabbs, targetSize: int, splitGranularity: int) -> list[np.ndarray]:
+        """SurfaceAreaHeuristic::generateBatches (SurfaceAreaHeuristic.cpp:96-104);
+        aabbs: (n, 8) float32 rows of min4, max4."""
+        a = _f32(aabbs).reshape(-1, 8)
+        n = len(a)
+        flat = np.zeros(max(n, 1), np.uint32)
+        offs = np.zeros(n + 2, np.uint32)
+        nb = C.c_uint32()
+        check(lib().occ_sah_generate_batches(_ptr(a), n, targetSize, splitGranularity, _ptr(flat), _ptr(offs),
+                                             C.byref(nb)), "occ_sah_generate_batches")
+        return [flat[offs[i]:offs[i + 1]].copy() for i in range(nb.value)]
+
+
+def bake_scene(vertices, indices, targetSize: int = 512, splitGranularity: int = 8) -> list[Occluder]:
+    """The demo's scene preparation (Main.cpp:86-128): quads, padding to a
+    multiple of 8 quads, per-quad boxes, SAH batches, one occluder per batch
+    quantised in the box of all vertices."""
+    v = _f32(vertices).reshape(-1, 4)
+    q = QuadDecomposition.decompose(indices, v)
+    pad = (-q.size) % 32
+    if pad:
+        q = np.concatenate([q, np.full(pad, q[0], np.uint32)])
+    corners = v[q.reshape(-1, 4)]                     # (nq, 4, 4)
+    aabbs = _quad_boxes(corners)
+    batches = SurfaceAreaHeuristic.generateBatches(aabbs, targetSize, splitGranularity)
+    refMin, refMax = _box_of(v)
+    return [Occluder.bake(corners[b].reshape(-1, 4), refMin, refMax) for b in batches]
+
+
+def _xmin(a, b):  # minps: the second operand unless a < b
+    return np.where(a < b, a, b)
+
+
+def _xmax(a, b):
+    return np.where(a > b, a, b)
+
+
+def _quad_boxes(corners: np.ndarray) -> np.ndarray:
+    lo = np.full((len(corners), 4), np.inf, np.float32)
+    hi = np.full((len(corners), 4), -np.inf, np.float32)
+    for k in range(4):
+        lo = _xmin(lo, corners[:, k])
+        hi = _xmax(hi, corners[:, k])
+    return np.ascontiguousarray(np.concatenate([lo, hi], axis=1), np.float32)
+
+
+def _box_of(v: np.ndarray):
+    """Running minps/maxps over the vertices in order (Main.cpp:109-113)."""
+    if np.isnan(v).any():  # NaN makes the running result order dependent: replay it
+        lo = np.full(4, np.inf, np.float32)
+        hi = np.full(4, -np.inf, np.float32)
+        for p in v:
+            lo = _xmin(lo, p)
+            hi = _xmax(hi, p)
+        return lo.astype(np.float32), hi.astype(np.float32)
+    lo = v.min(axis=0).astype(np.float32)
+    hi = v.max(axis=0).astype(np.float32)
+    # on a tie the running form keeps the later element: only the sign of zero can differ
+    for res in (lo, hi):
+        for a in range(4):
+            if res[a] == 0 and len(v):
+                zeros = np.nonzero(v[:, a] == 0)[0]
+                res[a] = v[zeros[-1], a]
+    return lo, hi
+
+
+class Rasterizer:
+    """Rasterizer (Rasterizer.h:10-61) on the GPU."""
+
+    def __init__(self, ctx: Context, width: int, height: int):
+        if width % 8 or height % 8 or width <= 0 or height <= 0:
+            raise ValueError("width and height must be positive multiples of 8 (Rasterizer.cpp:68)")
+        self.ctx = ctx
+        self.width, self.height = width, height
+        h = P()
+        check(lib().occ_raster_create(ctx.handle, width, height, C.byref(h)), "occ_raster_create")
+        self.handle = h.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().occ_raster_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def blocks(self) -> int:
+        return (self.width // 8) * (self.height // 8)
+
+    def setModelViewProjection(self, matrix) -> None:
+        m = _f32(matrix).reshape(16)
+        check(lib().occ_raster_set_mvp(self.handle, _ptr(m)), "occ_raster_set_mvp")
+
+    def clear(self) -> None:
+        check(lib().occ_raster_clear(self.handle), "occ_raster_clear")
+
+    def rasterize(self, occluder: Occluder, possiblyNearClipped: bool) -> None:
+        oid = occluder.upload(self.ctx)
+        check(lib().occ_raster_rasterize(self.handle, oid, int(bool(possiblyNearClipped))), "occ_raster_rasterize")
+
+    def rasterizeMany(self, occluders, flags=None) -> None:
+        """Many rasterize calls; flags per occluder: 1 = near-clip variant,
+        2 = decide visibility and variant on the GPU from the bounds."""
+        ids = np.array([o.upload(self.ctx) for o in occluders], np.uint32)
+        fl = None if flags is None else np.ascontiguousarray(flags, np.uint8)
+        check(lib().occ_raster_rasterize_many(self.handle, len(ids), _ptr(ids), _ptr(fl)), "occ_raster_rasterize_many")
+
+    def flush(self) -> None:
+        check(lib().occ_raster_flush(self.handle), "occ_raster_flush")
+
+    def commandFlags(self, n: int) -> np.ndarray:
+        out = np.zeros(n, np.uint8)
+        check(lib().occ_raster_command_flags(self.handle, n, _ptr(out)), "occ_raster_command_flags")
+        return out
+
+    def queryVisibility(self, boundsMin, boundsMax):
+        """Rasterizer::queryVisibility -> (visible, needsClipping)."""
+        a, b = _f32(boundsMin, (4,)), _f32(boundsMax, (4,))
+        v, c = C.c_int(), C.c_int()
+        check(lib().occ_raster_query_visibility(self.handle, _ptr(a), _ptr(b), C.byref(v), C.byref(c)),
+              "occ_raster_query_visibility")
+        return bool(v.value), bool(c.value)
+
+    def queryVisibilityBatch(self, mins, maxs):
+        """Many queryVisibility calls -> (visible bool[n], needsClipping bool[n])."""
+        a, b = _f32(mins).reshape(-1, 4), _f32(maxs).reshape(-1, 4)
+        n = len(a)
+        vw = np.zeros((n + 31) // 32, np.uint32)
+        nw = np.zeros((n + 31) // 32, np.uint32)
+        check(lib().occ_raster_query_batch(self.handle, n, _ptr(a), _ptr(b), _ptr(vw), _ptr(nw)),
+              "occ_raster_query_batch")
+        return unpack_bits(vw, n), unpack_bits(nw, n)
+
+    def query2D(self, minX, maxX, minY, maxY, maxZ) -> bool:
+        v = C.c_int()
+        check(lib().occ_raster_query2d(self.handle, minX, maxX, minY, maxY, maxZ, C.byref(v)), "occ_raster_query2d")
+        return bool(v.value)
+
+    def readBackDepth(self) -> np.ndarray:
+        """Rasterizer::readBackDepth -> (height, width, 4) uint8."""
+        out = np.zeros((self.height, self.width, 4), np.uint8)
+        check(lib().occ_raster_read_back_depth(self.handle, _ptr(out)), "occ_raster_read_back_depth")
+        return out
+
+    def readDepthRaw(self) -> np.ndarray:
+        out = np.zeros(self.width * self.height, np.uint16)
+        check(lib().occ_raster_read_depth_raw(self.handle, _ptr(out)), "occ_raster_read_depth_raw")
+        return out
+
+    def readHiZ(self) -> np.ndarray:
+        n = C.c_uint32()
+        check(lib().occ_raster_read_hiz(self.handle, None, C.byref(n)), "occ_raster_read_hiz")
+        out = np.zeros(n.value, np.uint16)
+        check(lib().occ_raster_read_hiz(self.handle, _ptr(out), C.byref(n)), "occ_raster_read_hiz")
+        return out
+
+    def writeDepthRaw(self, depth) -> None:
+        d = np.ascontiguousarray(depth, np.uint16)
+        check(lib().occ_raster_write_depth_raw(self.handle, _ptr(d)), "occ_raster_write_depth_raw")
+
+    def writeHiZ(self, hiz) -> None:
+        h = np.ascontiguousarray(hiz, np.uint16)
+        check(lib().occ_raster_write_hiz(self.handle, _ptr(h)), "occ_raster_write_hiz")
+
+
+class _WorkSet:
+    """Keeps the numpy buffers of an occ_view_work array alive."""
+
+    def __init__(self, ctx: Context, views: list[dict]):
+        self.keep = []
+        self.arr = (ViewWork * len(views))()
+        self.nq = []
+        for i, vw in enumerate(views):
+            r: Rasterizer = vw["raster"]
+            w = self.arr[i]
+            w.raster = r.handle
+            if vw.get("mvp") is not None:
+                m = _f32(vw["mvp"]).reshape(16)
+                self.keep.append(m)
+                w.mvp = _ptr(m)
+            w.clear = int(vw.get("clear", True))
+            occs = vw.get("occluders", [])
+            ids = np.array([o.upload(ctx) for o in occs], np.uint32)
+            self.keep.append(ids)
+            w.numOccluders = len(ids)
+            w.occluders = _ptr(ids)
+            if vw.get("flags") is not None:
+                fl = np.ascontiguousarray(vw["flags"], np.uint8)
+                self.keep.append(fl)
+                w.flags = _ptr(fl)
+            mins = vw.get("mins")
+            n = 0 if mins is None else len(mins)
+            self.nq.append(n)
+            w.numQueries = n
+            if n:
+                a, b = _f32(vw["mins"]).reshape(-1, 4), _f32(vw["maxs"]).reshape(-1, 4)
+                vb = np.zeros((n + 31) // 32, np.uint32)
+                nb = np.zeros((n + 31) // 32, np.uint32)
+                self.keep += [a, b, vb, nb]
+                w.queryMins, w.queryMaxs = _ptr(a), _ptr(b)
+                w.visibleBits, w.needsClippingBits = _ptr(vb), _ptr(nb)
+                vw["_bits"] = (vb, nb)
+        self.views = views
+
+
+def execute_batch(ctx: Context, views: list[dict]):
+    """Rasterise and query many views in one batch of kernels.  Each view is a
+    dict: raster, mvp, clear, occluders, flags, mins, maxs.  Returns per view
+    (visible bool[n], needsClipping bool[n])."""
+    ws = _WorkSet(ctx, views)
+    check(lib().occ_batch_execute(ctx.handle, len(views), ws.arr), "occ_batch_execute")
+    out = []
+    for vw, n in zip(views, ws.nq):
+        if n:
+            vb, nb = vw.pop("_bits")
+            out.append((unpack_bits(vb, n), unpack_bits(nb, n)))
+        else:
+            out.append((np.zeros(0, bool), np.zeros(0, bool)))
+    return out
+
+
+class PreparedBatch:
+    """occ_batch: tables and query boxes resident on the GPU, the frame's
+    kernels captured in a CUDA graph; launch() is asynchronous."""
+
+    def __init__(self, ctx: Context, views: list[dict]):
+        self.ctx = ctx
+        self.ws = _WorkSet(ctx, views)
+        h = P()
+        check(lib().occ_batch_prepare(ctx.handle, len(views), self.ws.arr, C.byref(h)), "occ_batch_prepare")
+        self.handle = h.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().occ_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setModelViewProjection(self, view: int, matrix) -> None:
+        m = _f32(matrix).reshape(16)
+        check(lib().occ_batch_set_mvp(self.handle, view, _ptr(m)), "occ_batch_set_mvp")
+
+    def launch(self) -> None:
+        check(lib().occ_batch_launch(self.handle), "occ_batch_launch")
+
+    def check(self) -> bool:
+        """True if every launch since the last check fitted the scratch; on
+        False the batch has been re-sized and the frames must be re-run."""
+        s = lib().occ_batch_check(self.handle)
+        if s == 0:
+            return True
+        if s == -4:
+            return False
+        check(s, "occ_batch_check")
+        return False
+
+    def profile(self, iterations: int) -> np.ndarray:
+        """Mean ms of (setup, scan, fill/row-walk, raster, query) over `iterations`
+        frames launched kernel by kernel with CUDA events in between."""
+        out = np.zeros(5, np.float32)
+        check(lib().occ_batch_profile(self.handle, iterations, _ptr(out)), "occ_batch_profile")
+        return out
+
+    def results(self, view: int):
+        n = self.ws.nq[view]
+        vb = np.zeros(max((n + 31) // 32, 1), np.uint32)
+        nb = np.zeros(max((n + 31) // 32, 1), np.uint32)
+        check(lib().occ_batch_results(self.handle, view, _ptr(vb), _ptr(nb)), "occ_batch_results")
+        return unpack_bits(vb, n), unpack_bits(nb, n)
+
+
+def coverage_table() -> np.ndarray:
+    t = np.zeros(4096, np.int64)
+    check(lib().occ_coverage_table(_ptr(t)), "occ_coverage_table")
+    return t
+
+
+def build_coverage_table() -> np.ndarray:
+    t = np.zeros(4096, np.int64)
+    check(lib().occ_build_coverage_table(_ptr(t)), "occ_build_coverage_table")
+    return t
+
+
+__all__ = ["Context", "Occluder", "QuadDecomposition", "SurfaceAreaHeuristic", "Rasterizer", "bake_scene",
+           "execute_batch", "PreparedBatch", "OccError", "coverage_table", "build_coverage_table", "unpack_bits"]

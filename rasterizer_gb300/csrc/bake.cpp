@@ -1,0 +1,553 @@
+// Host-side occluder preparation: quad decomposition, SAH batching and the
+// 11/11/10 occluder bake.  The output must be byte-identical to the
+// reference's (the rasteriser is bit-exact only on identical packed input),
+// so each routine follows the steps of its reference counterpart:
+//   decompose        QuadDecomposition.cpp:326-445 (+ Edmonds matching :28-309)
+//   generateBatches  SurfaceAreaHeuristic.cpp:10-104
+//   bake             Occluder.cpp:7-181
+// All float math goes through x86_emu.cuh (separately rounded, x86 NaN rules,
+// RSQRTPS from the measured table), so the result is the same on x86-64 and
+// aarch64 hosts.
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <queue>
+#include <string>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "../../include/rasterizer_gb300.h"
+#include "x86_emu.cuh"
+
+namespace {
+
+using namespace x86;
+
+struct V4 {
+  float v[4];
+};
+
+V4 load4(const float* p)
+{
+  V4 r;
+  std::memcpy(r.v, p, 16);
+  return r;
+}
+
+V4 vsub(const V4& a, const V4& b)
+{
+  V4 r;
+  for (int i = 0; i < 4; ++i) r.v[i] = xsub(a.v[i], b.v[i]);
+  return r;
+}
+
+V4 vadd(const V4& a, const V4& b)
+{
+  V4 r;
+  for (int i = 0; i < 4; ++i) r.v[i] = xadd(a.v[i], b.v[i]);
+  return r;
+}
+
+// cross product of the xyz lanes, w = a.w*b.w - a.w*b.w (VectorMath.h:6-12)
+V4 cross(const V4& a, const V4& b)
+{
+  V4 r;
+  r.v[0] = xsub(xmul(a.v[1], b.v[2]), xmul(a.v[2], b.v[1]));
+  r.v[1] = xsub(xmul(a.v[2], b.v[0]), xmul(a.v[0], b.v[2]));
+  r.v[2] = xsub(xmul(a.v[0], b.v[1]), xmul(a.v[1], b.v[0]));
+  r.v[3] = xsub(xmul(a.v[3], b.v[3]), xmul(a.v[3], b.v[3]));
+  return r;
+}
+
+V4 tri_normal(const V4& a, const V4& b, const V4& c) { return cross(vsub(b, a), vsub(c, a)); }
+
+// v * RSQRTPS(dot3(v, v)) on all four lanes (VectorMath.h:20-23)
+V4 normalize(const V4& v)
+{
+  const float s = rsqrt_host(dp3(v.v, v.v));
+  V4 r;
+  for (int i = 0; i < 4; ++i) r.v[i] = xmul(v.v[i], s);
+  return r;
+}
+
+// COMISS-based predicates: false when unordered
+bool gt_ss(float a, float b) { return a > b; }
+bool ge_ss(float a, float b) { return a >= b; }
+bool lt_ss(float a, float b) { return a < b; }
+
+struct Box {
+  V4 lo, hi;
+  Box()
+  {
+    for (int i = 0; i < 4; ++i) {
+      lo.v[i] = std::numeric_limits<float>::infinity();
+      hi.v[i] = -std::numeric_limits<float>::infinity();
+    }
+  }
+  void grow(const V4& p)
+  {
+    for (int i = 0; i < 4; ++i) {
+      lo.v[i] = xmin(lo.v[i], p.v[i]);
+      hi.v[i] = xmax(hi.v[i], p.v[i]);
+    }
+  }
+  void grow(const Box& b)
+  {
+    for (int i = 0; i < 4; ++i) {
+      lo.v[i] = xmin(lo.v[i], b.lo.v[i]);
+      hi.v[i] = xmax(hi.v[i], b.hi.v[i]);
+    }
+  }
+  float center2(int axis) const { return xadd(lo.v[axis], hi.v[axis]); }
+  // dot(e, e.yzx) over xyz: (ex*ey + ey*ez) + (ez*ex + 0)
+  float area() const
+  {
+    const float e[4] = {xsub(hi.v[0], lo.v[0]), xsub(hi.v[1], lo.v[1]), xsub(hi.v[2], lo.v[2]),
+                        xsub(hi.v[3], lo.v[3])};
+    const float f[4] = {e[1], e[2], e[0], e[3]};
+    return dp3(e, f);
+  }
+};
+
+// ---- maximum matching on the triangle adjacency graph -----------------------------
+// Edmonds' blossom algorithm with the search order of QuadDecomposition.cpp:28-309:
+// a greedy maximal matching in vertex order, then one breadth-first augmenting
+// path search per still-unmatched vertex, blossoms kept in a union-find forest
+// that is invalidated by bumping a per-search stamp.
+class BlossomMatcher {
+ public:
+  explicit BlossomMatcher(const std::vector<std::vector<int>>& adj)
+      : adj_(adj), mate_(adj.size(), -1), bridge_(adj.size()), node_(adj.size())
+  {
+    const int n = (int)adj.size();
+    std::vector<int> open;
+    for (int v = 0; v < n; ++v) {
+      if (mate_[v] != -1) continue;
+      bool paired = false;
+      for (int w : adj_[v])
+        if (mate_[w] == -1) {
+          pair(v, w);
+          paired = true;
+          break;
+        }
+      if (!paired) open.push_back(v);
+    }
+    std::vector<int> path;
+    for (int v : open) {
+      if (mate_[v] != -1) continue;
+      if (search(v, path)) {
+        for (size_t i = 0; i < path.size(); i += 2) pair(path[i], path[i + 1]);
+        path.clear();
+      }
+    }
+  }
+
+  int mate(int v) const { return mate_[v]; }
+
+ private:
+  struct Node {
+    int depth = 0, parent = -1, base = 0, stamp = 0;
+  };
+
+  void pair(int v, int w)
+  {
+    mate_[v] = w;
+    mate_[w] = v;
+  }
+
+  int root_of(int x)
+  {
+    if (node_[x].stamp != stamp_) return x;
+    if (x != node_[x].base) node_[x].base = root_of(node_[x].base);
+    return node_[x].base;
+  }
+
+  void join(int x, int y)
+  {
+    const int rx = root_of(x);
+    node_[rx].base = root_of(y);
+  }
+
+  void make_root(int x)
+  {
+    const int rx = root_of(x);
+    node_[rx].base = x;
+    node_[x].base = x;
+  }
+
+  bool search(int root, std::vector<int>& path)
+  {
+    ++stamp_;
+    node_[root].depth = 0;
+    node_[root].parent = -1;
+    node_[root].stamp = stamp_;
+    node_[root].base = root;
+    frontier_.push(root);
+    while (!frontier_.empty()) {
+      const int v = frontier_.front();
+      frontier_.pop();
+      for (int w : adj_[v]) {
+        if (visit(root, v, w, path)) {
+          while (!frontier_.empty()) frontier_.pop();
+          return true;
+        }
+      }
+    }
+    return false;
+  }
+
+  bool visit(int root, int v, int w, std::vector<int>& path)
+  {
+    const int vb = root_of(v), wb = root_of(w);
+    if (vb == wb) return false;
+    if (node_[wb].stamp != stamp_) {
+      if (mate_[w] == -1) {
+        path.push_back(w);
+        trace(v, root, path);
+        return true;
+      }
+      grow(v, w);
+    } else if (node_[wb].depth % 2 == 0) {
+      contract(v, w);
+    }
+    return false;
+  }
+
+  void grow(int v, int w)
+  {
+    const int u = mate_[w];
+    node_[w].depth = node_[v].depth + 1 + (node_[v].depth & 1);
+    node_[w].parent = v;
+    node_[w].stamp = stamp_;
+    node_[w].base = w;
+    node_[u].depth = node_[w].depth + 1;
+    node_[u].parent = w;
+    node_[u].stamp = stamp_;
+    node_[u].base = u;
+    frontier_.push(u);
+  }
+
+  void contract(int v, int w)
+  {
+    const int b = common_ancestor(v, w);
+    contract_path(b, v, w);
+    contract_path(b, w, v);
+  }
+
+  void contract_path(int b, int v, int w)
+  {
+    int u = root_of(v);
+    while (u != b) {
+      join(b, u);
+      u = mate_[u];
+      join(b, u);
+      make_root(b);
+      frontier_.push(u);
+      bridge_[u] = std::make_pair(v, w);
+      u = root_of(node_[u].parent);
+    }
+  }
+
+  int common_ancestor(int v, int w)
+  {
+    while (w != v) {
+      if (node_[v].depth > node_[w].depth) v = node_[v].parent;
+      else w = node_[w].parent;
+    }
+    return root_of(v);
+  }
+
+  // alternating path from s back to t (appends to path)
+  void trace(int s, int t, std::vector<int>& path)
+  {
+    if (s == t) {
+      path.push_back(s);
+    } else if (node_[s].depth % 2 == 0) {
+      path.push_back(s);
+      path.push_back(mate_[s]);
+      trace(node_[mate_[s]].parent, t, path);
+    } else {
+      const int v = bridge_[s].first, w = bridge_[s].second;
+      path.push_back(s);
+      const size_t from = path.size();
+      trace(v, mate_[s], path);
+      std::reverse(path.begin() + (std::ptrdiff_t)from, path.end());
+      trace(w, t, path);
+    }
+  }
+
+  const std::vector<std::vector<int>>& adj_;
+  std::vector<int> mate_;
+  std::vector<std::pair<int, int>> bridge_;
+  std::vector<Node> node_;
+  std::queue<int> frontier_;
+  int stamp_ = 0;
+};
+
+struct EdgeKeyHash {
+  size_t operator()(const std::pair<uint32_t, uint32_t>& k) const
+  {
+    return std::hash<uint64_t>{}(((uint64_t)k.first << 32) | k.second);
+  }
+};
+
+// Two triangles (v0,v1,v2) and (v2,v3,v0) may form a quad if v1 and v3 lie
+// within 0.5 units of the other triangle's plane (QuadDecomposition.cpp:326-343).
+bool mergeable(const V4& v0, const V4& v1, const V4& v2, const V4& v3)
+{
+  const float maxDepthError = 0.5f;
+  const V4 n0 = normalize(tri_normal(v0, v1, v2));
+  const V4 n2 = normalize(tri_normal(v2, v3, v0));
+  const V4 d = vsub(v1, v3);
+  const float a = fabs_(dp3(n0.v, d.v));
+  const float b = fabs_(dp3(n2.v, d.v));
+  return !(gt_ss(a, maxDepthError) || gt_ss(b, maxDepthError));
+}
+
+std::vector<uint32_t> decompose(const uint32_t* idx, uint32_t nIdx, const float* verts)
+{
+  const uint32_t triCount = nIdx / 3;
+  std::vector<std::vector<int>> adj(triCount);
+  using Key = std::pair<uint32_t, uint32_t>;
+  std::unordered_map<Key, std::vector<std::pair<uint32_t, uint32_t>>, EdgeKeyHash> edges;
+  auto vtx = [&](uint32_t i) { return load4(verts + 4 * (size_t)i); };
+  for (uint32_t t = 0; t < triCount; ++t) {
+    const uint32_t i[3] = {idx[3 * t], idx[3 * t + 1], idx[3 * t + 2]};
+    edges[Key(i[0], i[1])].push_back({t, i[2]});
+    edges[Key(i[1], i[2])].push_back({t, i[0]});
+    edges[Key(i[2], i[0])].push_back({t, i[1]});
+    for (int e = 0; e < 3; ++e) {
+      auto it = edges.find(Key(i[(e + 1) % 3], i[e]));  // the shared edge runs the other way
+      if (it == edges.end()) continue;
+      for (const auto& pr : it->second) {
+        const uint32_t other = pr.first, apex = pr.second;
+        if (mergeable(vtx(i[e]), vtx(apex), vtx(i[(e + 1) % 3]), vtx(i[(e + 2) % 3]))) {
+          adj[t].push_back((int)other);
+          adj[other].push_back((int)t);
+        }
+      }
+    }
+  }
+  BlossomMatcher matching(adj);
+  std::vector<uint32_t> out;
+  out.reserve((size_t)triCount * 4);
+  for (uint32_t t = 0; t < triCount; ++t) {
+    const int m = matching.mate((int)t);
+    const uint32_t i[3] = {idx[3 * t], idx[3 * t + 1], idx[3 * t + 2]};
+    if (m == -1) {
+      out.insert(out.end(), {i[0], i[2], i[1], i[0]});  // lone triangle as a degenerate quad
+      continue;
+    }
+    if (t >= (uint32_t)m) continue;  // emitted with the lower-numbered triangle
+    bool done = false;
+    for (int e = 0; e < 3 && !done; ++e) {
+      auto it = edges.find(Key(i[(e + 1) % 3], i[e]));
+      if (it == edges.end()) continue;
+      for (const auto& pr : it->second)
+        if (pr.first == (uint32_t)m) {
+          out.insert(out.end(), {i[e], i[(e + 2) % 3], i[(e + 1) % 3], pr.second});
+          done = true;
+          break;
+        }
+    }
+  }
+  return out;
+}
+
+// ---- SAH batching -------------------------------------------------------------------
+
+int sah_split(const std::vector<Box>& boxes, uint32_t gran, uint32_t* begin, uint32_t* end)
+{
+  const uint32_t n = (uint32_t)(end - begin);
+  float bestCost = std::numeric_limits<float>::infinity();
+  int bestAxis = -1, bestIndex = -1;
+  std::vector<float> left(n), right(n);
+  for (int axis = 0; axis < 3; ++axis) {
+    std::stable_sort(begin, end, [&](uint32_t a, uint32_t b) {
+      return boxes[a].center2(axis) < boxes[b].center2(axis);
+    });
+    Box acc;
+    for (uint32_t i = 0; i < n; ++i) {
+      acc.grow(boxes[begin[i]]);
+      left[i] = acc.area();
+    }
+    Box acc2;
+    for (int i = (int)n - 1; i >= 0; --i) {
+      acc2.grow(boxes[begin[i]]);
+      right[i] = acc2.area();
+    }
+    for (uint32_t s = gran; s < n - gran; s += gran) {
+      const float cost = xadd(xmul(left[s - 1], i2f((int32_t)s)), xmul(right[s], i2f((int32_t)(n - s))));
+      if (lt_ss(cost, bestCost)) {
+        bestCost = cost;
+        bestAxis = axis;
+        bestIndex = (int)s;
+      }
+    }
+  }
+  if (bestAxis < 0) return -1;
+  std::stable_sort(begin, end, [&](uint32_t a, uint32_t b) {
+    return boxes[a].center2(bestAxis) < boxes[b].center2(bestAxis);
+  });
+  return bestIndex;
+}
+
+void sah_recurse(const std::vector<Box>& boxes, uint32_t target, uint32_t gran, uint32_t* begin, uint32_t* end,
+                 std::vector<std::vector<uint32_t>>& out)
+{
+  // The reference's split search needs more than two split granules (its loop
+  // bound is unsigned), and a split must exist; otherwise keep the range whole.
+  const int split = (size_t)(end - begin) > 2 * (size_t)gran ? sah_split(boxes, gran, begin, end) : -1;
+  if (split < 0) {
+    out.emplace_back(begin, end);
+    return;
+  }
+  uint32_t* range[3] = {begin, begin + split, end};
+  for (int i = 0; i < 2; ++i) {
+    const size_t count = (size_t)(range[i + 1] - range[i]);
+    if (count < target) out.emplace_back(range[i], range[i + 1]);
+    else sah_recurse(boxes, target, gran, range[i], range[i + 1], out);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int occ_quad_decompose(const uint32_t* indices, uint32_t nIndices, const float* vertices, uint32_t nVertices,
+                       uint32_t* out, uint32_t* outCount)
+{
+  if (!indices || !vertices || !out || !outCount || nIndices % 3) return OCC_ERR_INVALID_ARG;
+  for (uint32_t i = 0; i < nIndices; ++i)
+    if (indices[i] >= nVertices) return OCC_ERR_INVALID_ARG;
+  std::vector<uint32_t> q = decompose(indices, nIndices, vertices);
+  std::copy(q.begin(), q.end(), out);
+  *outCount = (uint32_t)q.size();
+  return OCC_OK;
+}
+
+int occ_sah_generate_batches(const float* aabbs, uint32_t n, uint32_t targetSize, uint32_t splitGranularity,
+                             uint32_t* flat, uint32_t* offsets, uint32_t* numBatches)
+{
+  if (!aabbs || !flat || !offsets || !numBatches || !splitGranularity) return OCC_ERR_INVALID_ARG;
+  // The reference's split search needs more than two split granules (its loop
+  // bound n - granularity is unsigned); smaller inputs form a single batch here.
+  if (n <= 2 * splitGranularity) {
+    for (uint32_t i = 0; i < n; ++i) flat[i] = i;
+    offsets[0] = 0;
+    offsets[1] = n;
+    *numBatches = n ? 1 : 0;
+    return OCC_OK;
+  }
+  std::vector<Box> boxes(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    boxes[i].lo = load4(aabbs + 8 * (size_t)i);
+    boxes[i].hi = load4(aabbs + 8 * (size_t)i + 4);
+  }
+  std::vector<uint32_t> order(n);
+  for (uint32_t i = 0; i < n; ++i) order[i] = i;
+  std::vector<std::vector<uint32_t>> batches;
+  sah_recurse(boxes, targetSize, splitGranularity, order.data(), order.data() + n, batches);
+  uint32_t pos = 0;
+  for (size_t b = 0; b < batches.size(); ++b) {
+    offsets[b] = pos;
+    for (uint32_t q : batches[b]) flat[pos++] = q;
+  }
+  offsets[batches.size()] = pos;
+  *numBatches = (uint32_t)batches.size();
+  return OCC_OK;
+}
+
+int occ_occluder_bake(const float* vertices, uint32_t nVertices, const float refMin[4], const float refMax[4],
+                      uint32_t* packedOut, uint32_t* packetCount, float boundsMin[4], float boundsMax[4],
+                      float center[4])
+{
+  if (!vertices || !refMin || !refMax || !packedOut || !packetCount || !boundsMin || !boundsMax || !center)
+    return OCC_ERR_INVALID_ARG;
+  if (nVertices == 0 || nVertices % 16 != 0) return OCC_ERR_INVALID_ARG;  // Occluder.cpp:9 (8 quads per packet)
+  const uint32_t nq = nVertices / 4;
+  auto vtx = [&](uint32_t i) { return load4(vertices + 4 * (size_t)i); };
+
+  // k-means of the quad normals around the six axis directions (Occluder.cpp:11-78)
+  std::vector<V4> normals(nq);
+  for (uint32_t q = 0; q < nq; ++q) {
+    const V4 v0 = vtx(4 * q), v1 = vtx(4 * q + 1), v2 = vtx(4 * q + 2), v3 = vtx(4 * q + 3);
+    normals[q] = normalize(vadd(tri_normal(v0, v1, v2), tri_normal(v0, v2, v3)));
+  }
+  V4 centroid[6] = {{{1, 0, 0, 0}}, {{0, 1, 0, 0}}, {{0, 0, 1, 0}}, {{0, -1, 0, 0}}, {{0, 0, -1, 0}}, {{-1, 0, 0, 0}}};
+  std::vector<uint32_t> cluster(nq, 0);
+  bool changed = true;
+  for (int iter = 0; iter < 10 && changed; ++iter) {
+    changed = false;
+    for (uint32_t q = 0; q < nq; ++q) {
+      float best = -std::numeric_limits<float>::infinity();
+      uint32_t bestK = 0;
+      for (uint32_t k = 0; k < 6; ++k) {
+        const float d = dp3(centroid[k].v, normals[q].v);
+        if (ge_ss(d, best)) {
+          best = d;
+          bestK = k;
+        }
+      }
+      if (cluster[q] != bestK) {
+        cluster[q] = bestK;
+        changed = true;
+      }
+    }
+    for (auto& c : centroid) c = V4{{0, 0, 0, 0}};
+    for (uint32_t q = 0; q < nq; ++q) centroid[cluster[q]] = vadd(centroid[cluster[q]], normals[q]);
+    for (auto& c : centroid) c = normalize(c);
+  }
+  std::vector<uint32_t> order;  // quads grouped by cluster, original order within
+  order.reserve(nq);
+  for (uint32_t k = 0; k < 6; ++k)
+    for (uint32_t q = 0; q < nq; ++q)
+      if (cluster[q] == k) order.push_back(q);
+
+  // 11/11/10 quantisation in the reference box (Occluder.cpp:97-157)
+  const V4 lo = load4(refMin), hi = load4(refMax);
+  V4 inv;
+  for (int i = 0; i < 4; ++i) inv.v[i] = xdiv(1.0f, xsub(hi.v[i], lo.v[i]));
+  uint32_t packets = 0;
+  for (uint32_t g = 0; g < nq; g += 8) {
+    for (uint32_t j = 0; j < 4; ++j) {
+      for (uint32_t l = 0; l < 8; ++l) {
+        const V4 p = vtx(4 * order[g + l] + j);
+        float r[3];
+        for (int a = 0; a < 3; ++a) r[a] = xmul(xsub(p.v[a], lo.v[a]), inv.v[a]);
+        const int32_t X = cvtt(xfmadd(r[0], 2047.0f, 0.5f)) - 1024;
+        const int32_t Y = cvtt(xfmadd(r[1], 2047.0f, 0.5f));
+        const int32_t Z = cvtt(xfmadd(r[2], 1023.0f, 0.5f));
+        packedOut[(size_t)packets * 8 + 8 * j + l] = ((uint32_t)X << 21) | ((uint32_t)Y << 10) | (uint32_t)Z;
+      }
+    }
+    packets += 4;
+  }
+  *packetCount = packets;
+
+  // bounds over the input vertices, w = 1 (Occluder.cpp:162-178)
+  V4 mn, mx;
+  for (int i = 0; i < 4; ++i) {
+    mn.v[i] = std::numeric_limits<float>::infinity();
+    mx.v[i] = -std::numeric_limits<float>::infinity();
+  }
+  for (uint32_t i = 0; i < nVertices; ++i) {
+    const V4 p = vtx(i);
+    for (int a = 0; a < 4; ++a) {
+      mn.v[a] = xmin(p.v[a], mn.v[a]);
+      mx.v[a] = xmax(p.v[a], mx.v[a]);
+    }
+  }
+  mn.v[3] = 1.0f;
+  mx.v[3] = 1.0f;
+  for (int a = 0; a < 4; ++a) {
+    boundsMin[a] = mn.v[a];
+    boundsMax[a] = mx.v[a];
+    center[a] = xmul(xadd(mx.v[a], mn.v[a]), 0.5f);
+  }
+  return OCC_OK;
+}
+
+}  // extern "C"

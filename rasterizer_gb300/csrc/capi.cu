@@ -1,0 +1,1118 @@
+// C ABI of the GB300 occluder rasteriser: contexts, occluder storage,
+// rasterizer targets, deferred command lists, batches and CUDA graphs.
+// Host-side float math here (setModelViewProjection) is compiled with
+// -ffp-contract=off and goes through x86_emu.cuh, like the kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/rasterizer_gb300.h"
+#include "coverage_table.h"
+#include "coverage_table_build.h"
+#include "raster_types.h"
+#include "x86_emu.cuh"
+
+namespace occ {
+cudaError_t launch_flush(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
+                         bool doQuery, cudaStream_t stream);
+cudaError_t launch_read_back(const uint16_t* depth, const uint16_t* hiz, uint32_t width, uint32_t height,
+                             uchar4* out, cudaStream_t stream);
+cudaError_t launch_flush_timed(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
+                               bool doQuery, cudaStream_t stream, cudaEvent_t* ev);
+cudaError_t launch_query2d(const ViewDesc* view, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY,
+                           uint32_t maxZ, uint32_t* out, cudaStream_t stream);
+}  // namespace occ
+
+using namespace occ;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg)
+{
+  g_error = msg;
+  return code;
+}
+
+#define OCC_CUDA(call)                                                                      \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess) return fail(OCC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define OCC_CHECK(call)         \
+  do {                          \
+    int s_ = (call);            \
+    if (s_ != OCC_OK) return s_; \
+  } while (0)
+
+uint32_t div_up(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release()
+  {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  // grows to at least m elements; contents are not kept
+  int reserve(size_t m)
+  {
+    if (m <= n && p) return OCC_OK;
+    release();
+    size_t want = std::max<size_t>(m, 1);
+    cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return fail(OCC_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    n = want;
+    return OCC_OK;
+  }
+};
+
+template <class T>
+struct PinBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  PinBuf() = default;
+  PinBuf(const PinBuf&) = delete;
+  PinBuf& operator=(const PinBuf&) = delete;
+  ~PinBuf()
+  {
+    if (p) cudaFreeHost(p);
+  }
+  int reserve(size_t m)
+  {
+    if (m <= n && p) return OCC_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    size_t want = std::max<size_t>(m, 1);
+    cudaError_t e = cudaMallocHost(&p, want * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return fail(OCC_ERR_OUT_OF_MEMORY, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    }
+    n = want;
+    return OCC_OK;
+  }
+};
+
+struct OccluderRec {
+  uint32_t wordOffset, packetCount;
+  float refMin[4], refMax[4], boundsMin[4], boundsMax[4];
+};
+
+struct PendingCmd {
+  uint32_t occ;
+  uint32_t flags;
+};
+
+// Scratch of one frame batch (grows, never shrinks).
+struct FrameScratch {
+  DevBuf<uint8_t> tables;  // views | cmds | chunks
+  DevBuf<QuadRaster> rec;
+  DevBuf<QuadWalk> walk;
+  DevBuf<Totals> chunkTot, chunkBase, viewTot, viewBase;
+  DevBuf<uint32_t> mat, stStart, stLen, stList, cmdDraw;
+  DevBuf<float> ck;
+  DevBuf<FrameHeader> header;
+  DevBuf<float4> qmin, qmax;
+  DevBuf<uint32_t> visBits, ncBits;
+  uint32_t capCks = 0, capSt = 0;
+};
+
+}  // namespace
+
+struct occ_raster_s;
+
+struct occ_ctx_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DevBuf<uint32_t> pool;  // packed occluder words
+  size_t poolWords = 0;
+  std::vector<OccluderRec> occluders;
+  FrameScratch scratch;
+  PinBuf<uint8_t> stage;  // host staging for tables / queries
+  PinBuf<uint8_t> readback;
+  cudaEvent_t stageFree = nullptr;  // signalled when the last upload from `stage` finished
+  DevBuf<int64_t> table;
+};
+
+struct occ_raster_s {
+  occ_ctx_s* ctx = nullptr;
+  uint32_t width = 0, height = 0, blocksX = 0, blocksY = 0;
+  DevBuf<uint16_t> depth, hiz;
+  float cols[16] = {};
+  float rows[16] = {};
+  bool clearPending = false;
+  std::vector<PendingCmd> pending;
+  std::vector<uint8_t> lastFlags;  // gated results of the last flush, per command
+};
+
+namespace {
+
+// Rasterizer::setModelViewProjection (Rasterizer.cpp:76-105).
+void bake_mvp(const float* m, uint32_t width, uint32_t height, float cols[16], float rows[16])
+{
+  using namespace x86;
+  float row[4][4];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) row[i][j] = m[4 * j + i];
+  std::memcpy(rows, row, sizeof(row));
+  const float sx = (float)width * 0.5f - 4.0f;
+  const float sy = (float)height * 0.5f - 4.0f;
+  const float sz = 0.5f * 2.5237386e-29f;
+  float baked[4][4];
+  for (int j = 0; j < 4; ++j) {
+    baked[0][j] = xmul(xadd(row[0][j], row[3][j]), sx);
+    baked[1][j] = xmul(xadd(row[1][j], row[3][j]), sy);
+    baked[2][j] = xmul(xsub(row[3][j], row[2][j]), sz);
+    baked[3][j] = row[3][j];
+  }
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) cols[4 * j + i] = baked[i][j];
+}
+
+// One view of a batch as the host lays it out.
+struct ViewJob {
+  occ_raster_s* r;
+  const PendingCmd* cmds;
+  uint32_t ncmds;
+  bool clear;
+  uint32_t nq;
+  const float* hmin;  // host query boxes (or null)
+  const float* hmax;
+  const void* dmin;   // device query boxes (single-view zero-copy path)
+  const void* dmax;
+  uint32_t* hvis;     // host outputs
+  uint32_t* hnc;
+  void* dvis;         // device outputs
+  void* dnc;
+};
+
+struct BatchLayout {
+  std::vector<ViewDesc> views;
+  std::vector<Cmd> cmds;
+  std::vector<Chunk> chunks;
+  uint32_t numSt = 0, maxStPerView = 0, numTiles = 0, matSize = 0, querySlots = 0;
+  uint32_t totalQuads = 0;
+};
+
+int build_layout(occ_ctx_s* ctx, const std::vector<ViewJob>& jobs, BatchLayout& L)
+{
+  uint32_t quadBase = 0, chunkBase = 0, tileBase = 0, stBase = 0, matBase = 0, queryBase = 0;
+  for (size_t v = 0; v < jobs.size(); ++v) {
+    const ViewJob& J = jobs[v];
+    occ_raster_s* r = J.r;
+    ViewDesc V{};
+    V.depth = r->depth.p;
+    V.hiz = r->hiz.p;
+    V.width = r->width;
+    V.height = r->height;
+    V.blocksX = r->blocksX;
+    V.blocksY = r->blocksY;
+    std::memcpy(V.cols, r->cols, sizeof(V.cols));
+    std::memcpy(V.rows, r->rows, sizeof(V.rows));
+    V.cmdStart = (uint32_t)L.cmds.size();
+    V.cmdCount = J.ncmds;
+    uint32_t q = quadBase;
+    for (uint32_t i = 0; i < J.ncmds; ++i) {
+      const PendingCmd& pc = J.cmds[i];
+      if (pc.occ >= ctx->occluders.size()) return fail(OCC_ERR_INVALID_ARG, "unknown occluder id");
+      const OccluderRec& o = ctx->occluders[pc.occ];
+      Cmd c{};
+      c.view = (uint32_t)v;
+      c.wordOffset = o.wordOffset;
+      c.quadStart = q;
+      c.quadCount = o.packetCount * 2;
+      c.flags = pc.flags;
+      std::memcpy(c.refMin, o.refMin, 16);
+      std::memcpy(c.refMax, o.refMax, 16);
+      std::memcpy(c.boundsMin, o.boundsMin, 16);
+      std::memcpy(c.boundsMax, o.boundsMax, 16);
+      q += c.quadCount;
+      L.cmds.push_back(c);
+    }
+    const uint32_t nq = q - quadBase;
+    V.chunkStart = chunkBase;
+    V.chunkCount = div_up(nq, kChunk);
+    uint32_t ci = V.cmdStart;  // first command overlapping each chunk
+    for (uint32_t k = 0; k < V.chunkCount; ++k) {
+      Chunk ch{};
+      ch.view = (uint32_t)v;
+      ch.localIndex = k;
+      const uint32_t c0 = quadBase + k * kChunk;
+      const uint32_t c1 = std::min(c0 + kChunk, q);
+      ch.quadCount = c1 - c0;
+      while (ci + 1 < V.cmdStart + V.cmdCount && L.cmds[ci + 1].quadStart <= c0) ++ci;
+      ch.cmdFirst = ci;
+      uint32_t cj = ci;
+      while (cj + 1 < V.cmdStart + V.cmdCount && L.cmds[cj + 1].quadStart < c1) ++cj;
+      ch.cmdCount = cj - ci + 1;
+      if (ch.cmdCount > (uint32_t)kMaxCmdPerChunk) return fail(OCC_ERR_INVALID_ARG, "too many commands per chunk");
+      L.chunks.push_back(ch);
+    }
+    quadBase += V.chunkCount * kChunk;
+    chunkBase += V.chunkCount;
+    V.tilesX = div_up(r->blocksX, kTileW);
+    V.tilesY = div_up(r->blocksY, kTileH);
+    V.tileStart = tileBase;
+    tileBase += V.tilesX * V.tilesY;
+    V.stX = div_up(r->blocksX, kSuperTile);
+    V.stY = div_up(r->blocksY, kSuperTile);
+    V.stBase = stBase;
+    stBase += V.stX * V.stY;
+    L.maxStPerView = std::max(L.maxStPerView, V.stX * V.stY);
+    V.matBase = matBase;
+    matBase += V.stX * V.stY * V.chunkCount;
+    V.queryStart = queryBase;
+    V.queryCount = J.nq;
+    queryBase += div_up(J.nq, 32) * 32;
+    V.flags = J.clear ? kViewClear : 0;
+    L.views.push_back(V);
+  }
+  L.numSt = stBase;
+  L.numTiles = tileBase;
+  L.matSize = matBase;
+  L.querySlots = queryBase;
+  L.totalQuads = quadBase;
+  return OCC_OK;
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Runs one batch: uploads the tables, launches the kernels, reads results.
+// With sync, retries with larger scratch if the first attempt overflowed.
+int run_batch(occ_ctx_s* ctx, FrameScratch& S, std::vector<ViewJob>& jobs, bool sync)
+{
+  BatchLayout L;
+  OCC_CHECK(build_layout(ctx, jobs, L));
+  const uint32_t nv = (uint32_t)L.views.size();
+  const size_t offViews = 0;
+  const size_t offCmds = align_up(offViews + nv * sizeof(ViewDesc), 256);
+  const size_t offChunks = align_up(offCmds + L.cmds.size() * sizeof(Cmd), 256);
+  const size_t tablesBytes = align_up(offChunks + L.chunks.size() * sizeof(Chunk), 256);
+  bool anyHostQuery = false, anyRaster = false;
+  for (auto& J : jobs) {
+    anyHostQuery |= J.nq && J.hmin;
+    anyRaster |= J.ncmds || J.clear;
+  }
+  const size_t offQMin = tablesBytes;
+  const size_t offQMax = offQMin + (anyHostQuery ? (size_t)L.querySlots * 16 : 0);
+  const size_t offHdr = align_up(offQMax + (anyHostQuery ? (size_t)L.querySlots * 16 : 0), 64);
+  const size_t stageBytes = offHdr + 64;
+
+  // host staging (wait until the previous upload from it has finished)
+  OCC_CUDA(cudaEventSynchronize(ctx->stageFree));
+  OCC_CHECK(ctx->stage.reserve(stageBytes));
+  uint8_t* st = ctx->stage.p;
+  std::memcpy(st + offViews, L.views.data(), nv * sizeof(ViewDesc));
+  if (!L.cmds.empty()) std::memcpy(st + offCmds, L.cmds.data(), L.cmds.size() * sizeof(Cmd));
+  if (!L.chunks.empty()) std::memcpy(st + offChunks, L.chunks.data(), L.chunks.size() * sizeof(Chunk));
+  if (anyHostQuery) {
+    std::memset(st + offQMin, 0, (size_t)L.querySlots * 32);
+    for (size_t v = 0; v < jobs.size(); ++v)
+      if (jobs[v].nq && jobs[v].hmin) {
+        std::memcpy(st + offQMin + (size_t)L.views[v].queryStart * 16, jobs[v].hmin, (size_t)jobs[v].nq * 16);
+        std::memcpy(st + offQMax + (size_t)L.views[v].queryStart * 16, jobs[v].hmax, (size_t)jobs[v].nq * 16);
+      }
+  }
+
+  // device scratch
+  OCC_CHECK(S.tables.reserve(tablesBytes));
+  OCC_CHECK(S.rec.reserve(L.totalQuads));
+  OCC_CHECK(S.walk.reserve(L.totalQuads));
+  OCC_CHECK(S.chunkTot.reserve(L.chunks.size()));
+  OCC_CHECK(S.chunkBase.reserve(L.chunks.size()));
+  OCC_CHECK(S.viewTot.reserve(nv));
+  OCC_CHECK(S.viewBase.reserve(nv));
+  OCC_CHECK(S.mat.reserve(L.matSize));
+  OCC_CHECK(S.stStart.reserve(L.numSt));
+  OCC_CHECK(S.stLen.reserve(L.numSt));
+  OCC_CHECK(S.cmdDraw.reserve(L.cmds.size()));
+  if (S.header.n == 0) {
+    OCC_CHECK(S.header.reserve(1));
+    OCC_CUDA(cudaMemsetAsync(S.header.p, 0, sizeof(FrameHeader), ctx->stream));
+    OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  if (S.capSt < L.totalQuads * 2 + 1024) S.capSt = L.totalQuads * 2 + 1024;
+  if (S.capCks < L.totalQuads * 2 + 4096) S.capCks = L.totalQuads * 2 + 4096;
+  uint32_t querySlots = L.querySlots;
+  if (anyHostQuery) {
+    OCC_CHECK(S.qmin.reserve(querySlots));
+    OCC_CHECK(S.qmax.reserve(querySlots));
+  }
+  bool hostBits = false;
+  for (auto& J : jobs) hostBits |= J.nq && (J.hvis || J.hnc);
+  if (hostBits || anyHostQuery) {
+    OCC_CHECK(S.visBits.reserve(querySlots / 32 + 1));
+    OCC_CHECK(S.ncBits.reserve(querySlots / 32 + 1));
+  }
+
+  OCC_CUDA(cudaMemcpyAsync(S.tables.p, st, tablesBytes, cudaMemcpyHostToDevice, ctx->stream));
+  if (anyHostQuery) {
+    OCC_CUDA(cudaMemcpyAsync(S.qmin.p, st + offQMin, (size_t)querySlots * 16, cudaMemcpyHostToDevice, ctx->stream));
+    OCC_CUDA(cudaMemcpyAsync(S.qmax.p, st + offQMax, (size_t)querySlots * 16, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  OCC_CUDA(cudaEventRecord(ctx->stageFree, ctx->stream));
+
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    OCC_CHECK(S.stList.reserve(S.capSt));
+    OCC_CHECK(S.ck.reserve((size_t)S.capCks * kCkFloats));
+    // overflow := 0 and the capacities; totals are recomputed, viewsDone is reset by
+    // the kernels themselves and the sticky overflow bit is kept
+    uint32_t* hs = reinterpret_cast<uint32_t*>(st + offHdr);
+    hs[0] = 0;
+    hs[1] = S.capCks;
+    hs[2] = S.capSt;
+    OCC_CUDA(cudaMemcpyAsync(&S.header.p->overflow, hs, 12, cudaMemcpyHostToDevice, ctx->stream));
+
+    FrameParams P{};
+    P.views = reinterpret_cast<const ViewDesc*>(S.tables.p + offViews);
+    P.numViews = nv;
+    P.cmds = reinterpret_cast<const Cmd*>(S.tables.p + offCmds);
+    P.chunks = reinterpret_cast<const Chunk*>(S.tables.p + offChunks);
+    P.numChunks = (uint32_t)L.chunks.size();
+    P.numTiles = L.numTiles;
+    P.numQuerySlots = querySlots;
+    P.pool = ctx->pool.p;
+    P.rec = S.rec.p;
+    P.walk = S.walk.p;
+    P.chunkTot = S.chunkTot.p;
+    P.chunkBase = S.chunkBase.p;
+    P.mat = S.mat.p;
+    P.stStart = S.stStart.p;
+    P.stLen = S.stLen.p;
+    P.viewTot = S.viewTot.p;
+    P.viewBase = S.viewBase.p;
+    P.stList = S.stList.p;
+    P.ck = S.ck.p;
+    P.header = S.header.p;
+    P.cmdDraw = S.cmdDraw.p;
+    if (anyHostQuery) {
+      P.qmin = S.qmin.p;
+      P.qmax = S.qmax.p;
+    } else if (jobs.size() == 1 && jobs[0].dmin) {
+      P.qmin = static_cast<const float4*>(jobs[0].dmin);
+      P.qmax = static_cast<const float4*>(jobs[0].dmax);
+    }
+    if (jobs.size() == 1 && jobs[0].dvis) {
+      P.visBits = static_cast<uint32_t*>(jobs[0].dvis);
+      P.ncBits = static_cast<uint32_t*>(jobs[0].dnc);
+    } else {
+      P.visBits = S.visBits.p;
+      P.ncBits = S.ncBits.p;
+    }
+    const bool doQuery = querySlots > 0 && P.qmin != nullptr;
+    OCC_CUDA(launch_flush(P, L.numSt, L.maxStPerView, anyRaster, doQuery, ctx->stream));
+    if (!sync) return OCC_OK;
+
+    // read back header, command flags and result bits
+    const size_t nCmd = L.cmds.size();
+    const size_t rbBytes = sizeof(FrameHeader) + nCmd * 4 + (size_t)(querySlots / 32) * 8 + 64;
+    OCC_CHECK(ctx->readback.reserve(rbBytes));
+    uint8_t* rb = ctx->readback.p;
+    OCC_CUDA(cudaMemcpyAsync(rb, S.header.p, sizeof(FrameHeader), cudaMemcpyDeviceToHost, ctx->stream));
+    if (nCmd) OCC_CUDA(cudaMemcpyAsync(rb + sizeof(FrameHeader), S.cmdDraw.p, nCmd * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    uint32_t* bitsOut = reinterpret_cast<uint32_t*>(rb + sizeof(FrameHeader) + nCmd * 4);
+    if (doQuery && P.visBits == S.visBits.p) {
+      OCC_CUDA(cudaMemcpyAsync(bitsOut, S.visBits.p, (size_t)(querySlots / 32) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+      OCC_CUDA(cudaMemcpyAsync(bitsOut + querySlots / 32, S.ncBits.p, (size_t)(querySlots / 32) * 4,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+    FrameHeader Hr;
+    std::memcpy(&Hr, rb, sizeof(Hr));
+    if (anyRaster && Hr.overflow) {
+      S.capCks = std::max(S.capCks, Hr.totalCks + Hr.totalCks / 4 + 1024);
+      S.capSt = std::max(S.capSt, Hr.totalSt + Hr.totalSt / 4 + 1024);
+      continue;
+    }
+    const uint32_t* draw = reinterpret_cast<const uint32_t*>(rb + sizeof(FrameHeader));
+    for (size_t v = 0; v < jobs.size(); ++v) {
+      const ViewDesc& V = L.views[v];
+      jobs[v].r->lastFlags.assign(V.cmdCount, 0);
+      for (uint32_t i = 0; i < V.cmdCount; ++i) jobs[v].r->lastFlags[i] = (uint8_t)draw[V.cmdStart + i];
+      if (doQuery && P.visBits == S.visBits.p && jobs[v].nq) {
+        const uint32_t w0 = V.queryStart / 32, nw = div_up(jobs[v].nq, 32);
+        if (jobs[v].hvis) std::memcpy(jobs[v].hvis, bitsOut + w0, nw * 4);
+        if (jobs[v].hnc) std::memcpy(jobs[v].hnc, bitsOut + querySlots / 32 + w0, nw * 4);
+      }
+    }
+    return OCC_OK;
+  }
+  return fail(OCC_ERR_CAPACITY, "scratch capacity still exceeded after retries");
+}
+
+int flush_raster(occ_raster_s* r, const ViewJob* withQueries)
+{
+  std::vector<ViewJob> jobs(1);
+  ViewJob& J = jobs[0];
+  if (withQueries) J = *withQueries;
+  J.r = r;
+  J.cmds = r->pending.data();
+  J.ncmds = (uint32_t)r->pending.size();
+  J.clear = r->clearPending;
+  if (!J.ncmds && !J.clear && !J.nq) return OCC_OK;
+  const bool sync = !(withQueries && withQueries->dvis);
+  int s = run_batch(r->ctx, r->ctx->scratch, jobs, sync);
+  if (s == OCC_OK) {
+    r->pending.clear();
+    r->clearPending = false;
+  }
+  return s;
+}
+
+}  // namespace
+
+// ==== exported API =======================================================================
+
+extern "C" {
+
+const char* occ_last_error(void) { return g_error.c_str(); }
+int occ_version(void) { return 1; }
+
+int occ_ctx_create(int device, occ_ctx* out)
+{
+  if (!out) return fail(OCC_ERR_INVALID_ARG, "null out");
+  auto ctx = std::make_unique<occ_ctx_s>();
+  ctx->device = device;
+  OCC_CUDA(cudaSetDevice(device));
+  OCC_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  OCC_CUDA(cudaEventCreateWithFlags(&ctx->stageFree, cudaEventDisableTiming));
+  OCC_CUDA(cudaEventRecord(ctx->stageFree, ctx->stream));
+  *out = ctx.release();
+  return OCC_OK;
+}
+
+int occ_ctx_destroy(occ_ctx ctx)
+{
+  if (!ctx) return OCC_OK;
+  cudaStreamSynchronize(ctx->stream);
+  cudaEventDestroy(ctx->stageFree);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return OCC_OK;
+}
+
+int occ_ctx_synchronize(occ_ctx ctx)
+{
+  if (!ctx) return fail(OCC_ERR_INVALID_ARG, "null ctx");
+  OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+  return OCC_OK;
+}
+
+void* occ_ctx_stream(occ_ctx ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int occ_occluder_upload(occ_ctx ctx, const uint32_t* packed, uint32_t packetCount, const float refMin[4],
+                        const float refMax[4], const float boundsMin[4], const float boundsMax[4], occ_occluder* out)
+{
+  if (!ctx || !packed || !refMin || !refMax || !boundsMin || !boundsMax || !out)
+    return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (packetCount == 0 || packetCount % 4 != 0)
+    return fail(OCC_ERR_INVALID_ARG, "packetCount must be a positive multiple of 4 (8 quads per packet group)");
+  const size_t words = (size_t)packetCount * 8;
+  if (ctx->poolWords + words > 0xFFFFFFFFull) return fail(OCC_ERR_CAPACITY, "occluder pool exceeds 2^32 words");
+  if (ctx->poolWords + words > ctx->pool.n) {
+    size_t cap = std::max<size_t>(ctx->pool.n * 2, ctx->poolWords + words);
+    cap = std::max<size_t>(cap, 1 << 16);
+    uint32_t* np = nullptr;
+    cudaError_t e = cudaMalloc(&np, cap * 4);
+    if (e != cudaSuccess) return fail(OCC_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    if (ctx->poolWords) OCC_CUDA(cudaMemcpyAsync(np, ctx->pool.p, ctx->poolWords * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->pool.release();
+    ctx->pool.p = np;
+    ctx->pool.n = cap;
+  }
+  OCC_CUDA(cudaMemcpyAsync(ctx->pool.p + ctx->poolWords, packed, words * 4, cudaMemcpyHostToDevice, ctx->stream));
+  OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+  OccluderRec rec{};
+  rec.wordOffset = (uint32_t)ctx->poolWords;
+  rec.packetCount = packetCount;
+  std::memcpy(rec.refMin, refMin, 16);
+  std::memcpy(rec.refMax, refMax, 16);
+  std::memcpy(rec.boundsMin, boundsMin, 16);
+  std::memcpy(rec.boundsMax, boundsMax, 16);
+  ctx->poolWords += words;
+  ctx->occluders.push_back(rec);
+  *out = (occ_occluder)(ctx->occluders.size() - 1);
+  return OCC_OK;
+}
+
+int occ_occluder_count(occ_ctx ctx, uint32_t* count)
+{
+  if (!ctx || !count) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  *count = (uint32_t)ctx->occluders.size();
+  return OCC_OK;
+}
+
+int occ_raster_create(occ_ctx ctx, uint32_t width, uint32_t height, occ_raster* out)
+{
+  if (!ctx || !out) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (width == 0 || height == 0 || width % 8 || height % 8)
+    return fail(OCC_ERR_INVALID_ARG, "width and height must be positive multiples of 8");
+  if (width > 65528 || height > 65528) return fail(OCC_ERR_INVALID_ARG, "width/height above 65528");
+  auto r = std::make_unique<occ_raster_s>();
+  r->ctx = ctx;
+  r->width = width;
+  r->height = height;
+  r->blocksX = width / 8;
+  r->blocksY = height / 8;
+  const size_t blocks = (size_t)r->blocksX * r->blocksY;
+  OCC_CHECK(r->depth.reserve((size_t)width * height));
+  OCC_CHECK(r->hiz.reserve(blocks + 8));
+  // the reference value-initialises both (Rasterizer.cpp:70-71)
+  OCC_CUDA(cudaMemsetAsync(r->depth.p, 0, (size_t)width * height * 2, ctx->stream));
+  OCC_CUDA(cudaMemsetAsync(r->hiz.p, 0, (blocks + 8) * 2, ctx->stream));
+  OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+  *out = r.release();
+  return OCC_OK;
+}
+
+int occ_raster_destroy(occ_raster r)
+{
+  if (!r) return OCC_OK;
+  cudaStreamSynchronize(r->ctx->stream);
+  delete r;
+  return OCC_OK;
+}
+
+int occ_raster_set_mvp(occ_raster r, const float matrix[16])
+{
+  if (!r || !matrix) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (!r->pending.empty()) OCC_CHECK(flush_raster(r, nullptr));  // pending commands use the old matrix
+  bake_mvp(matrix, r->width, r->height, r->cols, r->rows);
+  return OCC_OK;
+}
+
+int occ_raster_clear(occ_raster r)
+{
+  if (!r) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (!r->pending.empty()) OCC_CHECK(flush_raster(r, nullptr));
+  r->clearPending = true;
+  return OCC_OK;
+}
+
+int occ_raster_rasterize(occ_raster r, occ_occluder occ, int possiblyNearClipped)
+{
+  if (!r) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (occ >= r->ctx->occluders.size()) return fail(OCC_ERR_INVALID_ARG, "unknown occluder id");
+  r->pending.push_back(PendingCmd{occ, possiblyNearClipped ? kCmdNearClip : 0u});
+  return OCC_OK;
+}
+
+int occ_raster_rasterize_many(occ_raster r, uint32_t n, const occ_occluder* occ, const uint8_t* flags)
+{
+  if (!r || (n && !occ)) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  for (uint32_t i = 0; i < n; ++i)
+    if (occ[i] >= r->ctx->occluders.size()) return fail(OCC_ERR_INVALID_ARG, "unknown occluder id");
+  for (uint32_t i = 0; i < n; ++i)
+    r->pending.push_back(PendingCmd{occ[i], flags ? (uint32_t)(flags[i] & (kCmdNearClip | kCmdGated)) : 0u});
+  return OCC_OK;
+}
+
+int occ_raster_flush(occ_raster r)
+{
+  if (!r) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  return flush_raster(r, nullptr);
+}
+
+int occ_raster_command_flags(occ_raster r, uint32_t n, uint8_t* out)
+{
+  if (!r || (n && !out)) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (n > r->lastFlags.size()) return fail(OCC_ERR_INVALID_ARG, "more flags requested than commands flushed");
+  std::memcpy(out, r->lastFlags.data(), n);
+  return OCC_OK;
+}
+
+int occ_raster_query_batch(occ_raster r, uint32_t n, const float* mins, const float* maxs, uint32_t* visibleBits,
+                           uint32_t* needsClippingBits)
+{
+  if (!r || (n && (!mins || !maxs))) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  ViewJob J{};
+  J.nq = n;
+  J.hmin = mins;
+  J.hmax = maxs;
+  J.hvis = visibleBits;
+  J.hnc = needsClippingBits;
+  return flush_raster(r, &J);
+}
+
+int occ_raster_query_visibility(occ_raster r, const float boundsMin[4], const float boundsMax[4], int* visible,
+                                int* needsClipping)
+{
+  if (!visible || !needsClipping) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  uint32_t v = 0, c = 0;
+  OCC_CHECK(occ_raster_query_batch(r, 1, boundsMin, boundsMax, &v, &c));
+  *visible = (int)(v & 1);
+  *needsClipping = (int)(c & 1);
+  return OCC_OK;
+}
+
+int occ_raster_query_batch_device(occ_raster r, uint32_t n, const void* dMins, const void* dMaxs,
+                                  void* dVisibleBits, void* dNeedsClippingBits)
+{
+  if (!r || (n && (!dMins || !dMaxs || !dVisibleBits || !dNeedsClippingBits)))
+    return fail(OCC_ERR_INVALID_ARG, "null argument");
+  ViewJob J{};
+  J.nq = n;
+  J.dmin = dMins;
+  J.dmax = dMaxs;
+  J.dvis = dVisibleBits;
+  J.dnc = dNeedsClippingBits;
+  return flush_raster(r, &J);
+}
+
+int occ_raster_query2d(occ_raster r, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ,
+                       int* visible)
+{
+  if (!r || !visible) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (minX > maxX || minY > maxY || maxX >= r->width || maxY >= r->height)
+    return fail(OCC_ERR_INVALID_ARG, "rectangle outside the buffer");
+  OCC_CHECK(flush_raster(r, nullptr));
+  occ_ctx_s* ctx = r->ctx;
+  ViewDesc V{};
+  V.depth = r->depth.p;
+  V.hiz = r->hiz.p;
+  V.width = r->width;
+  V.height = r->height;
+  V.blocksX = r->blocksX;
+  V.blocksY = r->blocksY;
+  DevBuf<uint8_t> tmp;
+  OCC_CHECK(tmp.reserve(sizeof(ViewDesc) + 16));
+  OCC_CUDA(cudaMemcpyAsync(tmp.p, &V, sizeof(V), cudaMemcpyHostToDevice, ctx->stream));
+  uint32_t* dout = reinterpret_cast<uint32_t*>(tmp.p + sizeof(ViewDesc));
+  OCC_CUDA(launch_query2d(reinterpret_cast<const ViewDesc*>(tmp.p), minX, maxX, minY, maxY, maxZ, dout, ctx->stream));
+  uint32_t hv = 0;
+  OCC_CUDA(cudaMemcpyAsync(&hv, dout, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+  *visible = (int)hv;
+  return OCC_OK;
+}
+
+int occ_raster_read_back_depth(occ_raster r, void* rgba)
+{
+  if (!r || !rgba) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  OCC_CHECK(flush_raster(r, nullptr));
+  occ_ctx_s* ctx = r->ctx;
+  DevBuf<uchar4> out;
+  OCC_CHECK(out.reserve((size_t)r->width * r->height));
+  OCC_CUDA(launch_read_back(r->depth.p, r->hiz.p, r->width, r->height, out.p, ctx->stream));
+  OCC_CUDA(cudaMemcpyAsync(rgba, out.p, (size_t)r->width * r->height * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+  return OCC_OK;
+}
+
+int occ_raster_read_depth_raw(occ_raster r, uint16_t* out)
+{
+  if (!r || !out) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  OCC_CHECK(flush_raster(r, nullptr));
+  OCC_CUDA(cudaMemcpyAsync(out, r->depth.p, (size_t)r->width * r->height * 2, cudaMemcpyDeviceToHost, r->ctx->stream));
+  OCC_CUDA(cudaStreamSynchronize(r->ctx->stream));
+  return OCC_OK;
+}
+
+int occ_raster_read_hiz(occ_raster r, uint16_t* out, uint32_t* count)
+{
+  if (!r) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  const uint32_t n = r->blocksX * r->blocksY + 8;
+  if (count) *count = n;
+  if (!out) return OCC_OK;
+  OCC_CHECK(flush_raster(r, nullptr));
+  OCC_CUDA(cudaMemcpyAsync(out, r->hiz.p, (size_t)n * 2, cudaMemcpyDeviceToHost, r->ctx->stream));
+  OCC_CUDA(cudaStreamSynchronize(r->ctx->stream));
+  return OCC_OK;
+}
+
+int occ_raster_write_depth_raw(occ_raster r, const uint16_t* in)
+{
+  if (!r || !in) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  OCC_CHECK(flush_raster(r, nullptr));
+  OCC_CUDA(cudaMemcpyAsync(r->depth.p, in, (size_t)r->width * r->height * 2, cudaMemcpyHostToDevice, r->ctx->stream));
+  OCC_CUDA(cudaStreamSynchronize(r->ctx->stream));
+  return OCC_OK;
+}
+
+int occ_raster_write_hiz(occ_raster r, const uint16_t* in)
+{
+  if (!r || !in) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  OCC_CHECK(flush_raster(r, nullptr));
+  const uint32_t n = r->blocksX * r->blocksY + 8;
+  OCC_CUDA(cudaMemcpyAsync(r->hiz.p, in, (size_t)n * 2, cudaMemcpyHostToDevice, r->ctx->stream));
+  OCC_CUDA(cudaStreamSynchronize(r->ctx->stream));
+  return OCC_OK;
+}
+
+int occ_raster_size(occ_raster r, uint32_t* width, uint32_t* height)
+{
+  if (!r) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (width) *width = r->width;
+  if (height) *height = r->height;
+  return OCC_OK;
+}
+
+int occ_batch_execute(occ_ctx ctx, uint32_t numViews, const occ_view_work* views)
+{
+  if (!ctx || (numViews && !views)) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  std::vector<std::vector<PendingCmd>> cmds(numViews);
+  std::vector<ViewJob> jobs(numViews);
+  for (uint32_t v = 0; v < numViews; ++v) {
+    const occ_view_work& W = views[v];
+    occ_raster_s* r = W.raster;
+    if (!r || r->ctx != ctx) return fail(OCC_ERR_INVALID_ARG, "view raster missing or from another context");
+    if (W.numQueries && (!W.queryMins || !W.queryMaxs)) return fail(OCC_ERR_INVALID_ARG, "null query boxes");
+    for (uint32_t u = 0; u < v; ++u)
+      if (views[u].raster == r) return fail(OCC_ERR_INVALID_ARG, "a rasterizer appears twice in one batch");
+    if (!r->pending.empty()) OCC_CHECK(flush_raster(r, nullptr));
+    if (W.mvp) bake_mvp(W.mvp, r->width, r->height, r->cols, r->rows);
+    auto& c = cmds[v];
+    c.reserve(W.numOccluders);
+    for (uint32_t i = 0; i < W.numOccluders; ++i) {
+      if (W.occluders[i] >= ctx->occluders.size()) return fail(OCC_ERR_INVALID_ARG, "unknown occluder id");
+      c.push_back(PendingCmd{W.occluders[i], W.flags ? (uint32_t)(W.flags[i] & 3u) : 0u});
+    }
+    ViewJob& J = jobs[v];
+    J.r = r;
+    J.cmds = c.data();
+    J.ncmds = (uint32_t)c.size();
+    J.clear = W.clear != 0 || r->clearPending;
+    J.nq = W.numQueries;
+    J.hmin = W.queryMins;
+    J.hmax = W.queryMaxs;
+    J.hvis = W.visibleBits;
+    J.hnc = W.needsClippingBits;
+  }
+  OCC_CHECK(run_batch(ctx, ctx->scratch, jobs, true));
+  for (uint32_t v = 0; v < numViews; ++v) views[v].raster->clearPending = false;
+  return OCC_OK;
+}
+
+}  // extern "C"
+
+// ==== prepared batches (CUDA graph) ======================================================
+
+namespace {
+constexpr int kRing = 4;
+}
+
+struct occ_batch_s {
+  occ_ctx_s* ctx = nullptr;
+  std::vector<std::vector<PendingCmd>> cmds;
+  std::vector<ViewJob> jobs;
+  BatchLayout L;
+  FrameScratch S;
+  DevBuf<float4> qmin, qmax;
+  DevBuf<uint32_t> vis, nc;
+  PinBuf<uint8_t> ring[kRing];
+  cudaEvent_t ringEv[kRing] = {};
+  int cur = 0;
+  bool dirty = false;
+  size_t offCmds = 0, offChunks = 0, tablesBytes = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t copyNode = nullptr;
+  FrameParams params{};
+  bool anyRaster = false;
+  ~occ_batch_s()
+  {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (auto& e : ringEv)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+namespace {
+
+void write_tables(occ_batch_s* b, uint8_t* dst)
+{
+  std::memcpy(dst, b->L.views.data(), b->L.views.size() * sizeof(ViewDesc));
+  if (!b->L.cmds.empty()) std::memcpy(dst + b->offCmds, b->L.cmds.data(), b->L.cmds.size() * sizeof(Cmd));
+  if (!b->L.chunks.empty()) std::memcpy(dst + b->offChunks, b->L.chunks.data(), b->L.chunks.size() * sizeof(Chunk));
+}
+
+// (Re)captures the per-frame sequence: table upload from the current ring slot,
+// then the five kernels.
+int capture(occ_batch_s* b)
+{
+  occ_ctx_s* ctx = b->ctx;
+  FrameScratch& S = b->S;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  if (b->graph) {
+    cudaGraphDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  OCC_CHECK(S.stList.reserve(S.capSt));
+  OCC_CHECK(S.ck.reserve((size_t)S.capCks * kCkFloats));
+  // capacities into the header (synchronously, outside the graph)
+  uint32_t hs[3] = {0, S.capCks, S.capSt};
+  OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+  OCC_CUDA(cudaMemcpy(&S.header.p->overflow, hs, 12, cudaMemcpyHostToDevice));
+
+  FrameParams P{};
+  P.views = reinterpret_cast<const ViewDesc*>(S.tables.p);
+  P.numViews = (uint32_t)b->L.views.size();
+  P.cmds = reinterpret_cast<const Cmd*>(S.tables.p + b->offCmds);
+  P.chunks = reinterpret_cast<const Chunk*>(S.tables.p + b->offChunks);
+  P.numChunks = (uint32_t)b->L.chunks.size();
+  P.numTiles = b->L.numTiles;
+  P.numQuerySlots = b->L.querySlots;
+  P.pool = ctx->pool.p;
+  P.rec = S.rec.p;
+  P.walk = S.walk.p;
+  P.chunkTot = S.chunkTot.p;
+  P.chunkBase = S.chunkBase.p;
+  P.mat = S.mat.p;
+  P.stStart = S.stStart.p;
+  P.stLen = S.stLen.p;
+  P.viewTot = S.viewTot.p;
+  P.viewBase = S.viewBase.p;
+  P.stList = S.stList.p;
+  P.ck = S.ck.p;
+  P.header = S.header.p;
+  P.cmdDraw = S.cmdDraw.p;
+  P.qmin = b->qmin.p;
+  P.qmax = b->qmax.p;
+  P.visBits = b->vis.p;
+  P.ncBits = b->nc.p;
+  bool anyRaster = false;
+  for (auto& J : b->jobs) anyRaster |= J.ncmds || J.clear;
+  b->params = P;
+  b->anyRaster = anyRaster;
+
+  OCC_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e1 = cudaMemcpyAsync(S.tables.p, b->ring[b->cur].p, b->tablesBytes, cudaMemcpyHostToDevice, ctx->stream);
+  cudaError_t e2 = launch_flush(P, b->L.numSt, b->L.maxStPerView, anyRaster, b->L.querySlots > 0, ctx->stream);
+  cudaGraph_t g = nullptr;
+  cudaError_t e3 = cudaStreamEndCapture(ctx->stream, &g);
+  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(OCC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e1 ? e1 : (e2 ? e2 : e3)));
+  }
+  b->graph = g;
+  size_t n = 0;
+  OCC_CUDA(cudaGraphGetNodes(g, nullptr, &n));
+  std::vector<cudaGraphNode_t> nodes(n);
+  OCC_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
+  b->copyNode = nullptr;
+  for (auto nd : nodes) {
+    cudaGraphNodeType t;
+    OCC_CUDA(cudaGraphNodeGetType(nd, &t));
+    if (t == cudaGraphNodeTypeMemcpy) b->copyNode = nd;
+  }
+  if (!b->copyNode) return fail(OCC_ERR_CUDA, "graph capture lost the table upload");
+  OCC_CUDA(cudaGraphInstantiate(&b->exec, g, 0));
+  return OCC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int occ_batch_prepare(occ_ctx ctx, uint32_t numViews, const occ_view_work* views, occ_batch* out)
+{
+  if (!ctx || !out || !numViews || !views) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  auto b = std::make_unique<occ_batch_s>();
+  b->ctx = ctx;
+  b->cmds.resize(numViews);
+  b->jobs.resize(numViews);
+  for (uint32_t v = 0; v < numViews; ++v) {
+    const occ_view_work& W = views[v];
+    occ_raster_s* r = W.raster;
+    if (!r || r->ctx != ctx) return fail(OCC_ERR_INVALID_ARG, "view raster missing or from another context");
+    if (W.numQueries && (!W.queryMins || !W.queryMaxs)) return fail(OCC_ERR_INVALID_ARG, "null query boxes");
+    for (uint32_t u = 0; u < v; ++u)
+      if (views[u].raster == r) return fail(OCC_ERR_INVALID_ARG, "a rasterizer appears twice in one batch");
+    if (!r->pending.empty()) OCC_CHECK(flush_raster(r, nullptr));
+    if (W.mvp) bake_mvp(W.mvp, r->width, r->height, r->cols, r->rows);
+    for (uint32_t i = 0; i < W.numOccluders; ++i) {
+      if (W.occluders[i] >= ctx->occluders.size()) return fail(OCC_ERR_INVALID_ARG, "unknown occluder id");
+      b->cmds[v].push_back(PendingCmd{W.occluders[i], W.flags ? (uint32_t)(W.flags[i] & 3u) : 0u});
+    }
+    ViewJob& J = b->jobs[v];
+    J.r = r;
+    J.cmds = b->cmds[v].data();
+    J.ncmds = (uint32_t)b->cmds[v].size();
+    J.clear = W.clear != 0;
+    J.nq = W.numQueries;
+    J.hmin = W.queryMins;
+    J.hmax = W.queryMaxs;
+  }
+  // one synchronous run sizes the scratch (and renders one frame)
+  OCC_CHECK(run_batch(ctx, b->S, b->jobs, true));
+  FrameScratch& S = b->S;
+  S.capCks = std::max(S.capCks, 2 * S.capCks + 65536);
+  S.capSt = std::max(S.capSt, 2 * S.capSt + 65536);
+  OCC_CHECK(build_layout(ctx, b->jobs, b->L));
+  const uint32_t nv = (uint32_t)b->L.views.size();
+  b->offCmds = align_up(nv * sizeof(ViewDesc), 256);
+  b->offChunks = align_up(b->offCmds + b->L.cmds.size() * sizeof(Cmd), 256);
+  b->tablesBytes = align_up(b->offChunks + b->L.chunks.size() * sizeof(Chunk), 256);
+  for (int k = 0; k < kRing; ++k) {
+    OCC_CHECK(b->ring[k].reserve(b->tablesBytes));
+    OCC_CUDA(cudaEventCreateWithFlags(&b->ringEv[k], cudaEventDisableTiming));
+    OCC_CUDA(cudaEventRecord(b->ringEv[k], ctx->stream));
+  }
+  write_tables(b.get(), b->ring[0].p);
+  // query boxes, uploaded once
+  const uint32_t slots = b->L.querySlots;
+  if (slots) {
+    OCC_CHECK(b->qmin.reserve(slots));
+    OCC_CHECK(b->qmax.reserve(slots));
+    OCC_CHECK(b->vis.reserve(slots / 32));
+    OCC_CHECK(b->nc.reserve(slots / 32));
+    std::vector<float4> hmin(slots, make_float4(0, 0, 0, 0)), hmax(slots, make_float4(0, 0, 0, 0));
+    for (uint32_t v = 0; v < nv; ++v)
+      if (b->jobs[v].nq) {
+        std::memcpy(&hmin[b->L.views[v].queryStart], b->jobs[v].hmin, (size_t)b->jobs[v].nq * 16);
+        std::memcpy(&hmax[b->L.views[v].queryStart], b->jobs[v].hmax, (size_t)b->jobs[v].nq * 16);
+        b->jobs[v].hmin = b->jobs[v].hmax = nullptr;
+      }
+    OCC_CUDA(cudaMemcpy(b->qmin.p, hmin.data(), (size_t)slots * 16, cudaMemcpyHostToDevice));
+    OCC_CUDA(cudaMemcpy(b->qmax.p, hmax.data(), (size_t)slots * 16, cudaMemcpyHostToDevice));
+  }
+  OCC_CHECK(S.tables.reserve(b->tablesBytes));
+  OCC_CHECK(capture(b.get()));
+  *out = b.release();
+  return OCC_OK;
+}
+
+int occ_batch_set_mvp(occ_batch b, uint32_t view, const float matrix[16])
+{
+  if (!b || !matrix || view >= b->L.views.size()) return fail(OCC_ERR_INVALID_ARG, "bad argument");
+  occ_raster_s* r = b->jobs[view].r;
+  bake_mvp(matrix, r->width, r->height, r->cols, r->rows);
+  std::memcpy(b->L.views[view].cols, r->cols, sizeof(r->cols));
+  std::memcpy(b->L.views[view].rows, r->rows, sizeof(r->rows));
+  b->dirty = true;
+  return OCC_OK;
+}
+
+int occ_batch_launch(occ_batch b)
+{
+  if (!b) return fail(OCC_ERR_INVALID_ARG, "null batch");
+  occ_ctx_s* ctx = b->ctx;
+  if (b->dirty) {
+    const int slot = (b->cur + 1) % kRing;
+    OCC_CUDA(cudaEventSynchronize(b->ringEv[slot]));
+    write_tables(b, b->ring[slot].p);
+    OCC_CUDA(cudaGraphExecMemcpyNodeSetParams1D(b->exec, b->copyNode, b->S.tables.p, b->ring[slot].p,
+                                                b->tablesBytes, cudaMemcpyHostToDevice));
+    b->cur = slot;
+    b->dirty = false;
+  }
+  OCC_CUDA(cudaGraphLaunch(b->exec, ctx->stream));
+  OCC_CUDA(cudaEventRecord(b->ringEv[b->cur], ctx->stream));
+  return OCC_OK;
+}
+
+int occ_batch_results(occ_batch b, uint32_t view, uint32_t* visibleBits, uint32_t* needsClippingBits)
+{
+  if (!b || view >= b->L.views.size()) return fail(OCC_ERR_INVALID_ARG, "bad argument");
+  const ViewDesc& V = b->L.views[view];
+  const size_t nw = div_up(V.queryCount, 32);
+  if (nw) {
+    if (visibleBits)
+      OCC_CUDA(cudaMemcpyAsync(visibleBits, b->vis.p + V.queryStart / 32, nw * 4, cudaMemcpyDeviceToHost, b->ctx->stream));
+    if (needsClippingBits)
+      OCC_CUDA(cudaMemcpyAsync(needsClippingBits, b->nc.p + V.queryStart / 32, nw * 4, cudaMemcpyDeviceToHost,
+                               b->ctx->stream));
+  }
+  OCC_CUDA(cudaStreamSynchronize(b->ctx->stream));
+  return OCC_OK;
+}
+
+int occ_batch_check(occ_batch b)
+{
+  if (!b) return fail(OCC_ERR_INVALID_ARG, "null batch");
+  occ_ctx_s* ctx = b->ctx;
+  OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+  FrameHeader H;
+  OCC_CUDA(cudaMemcpy(&H, b->S.header.p, sizeof(H), cudaMemcpyDeviceToHost));
+  if (!H.sticky) return OCC_OK;
+  // grow to the largest totals seen and capture again; the caller re-runs its frames
+  b->S.capCks = std::max(b->S.capCks, H.maxCks + H.maxCks / 2 + 4096);
+  b->S.capSt = std::max(b->S.capSt, H.maxSt + H.maxSt / 2 + 4096);
+  uint32_t zero[4] = {0, 0, 0, 0};
+  OCC_CUDA(cudaMemcpy(&b->S.header.p->sticky, zero, 12, cudaMemcpyHostToDevice));
+  OCC_CHECK(capture(b));
+  return fail(OCC_ERR_CAPACITY, "a launch exceeded the scratch capacity; grown, re-run the frames");
+}
+
+int occ_batch_profile(occ_batch b, uint32_t iterations, float* msPerKernel)
+{
+  if (!b || !msPerKernel || !iterations) return fail(OCC_ERR_INVALID_ARG, "bad argument");
+  occ_ctx_s* ctx = b->ctx;
+  cudaEvent_t ev[6];
+  for (auto& e : ev) OCC_CUDA(cudaEventCreate(&e));
+  for (int k = 0; k < 5; ++k) msPerKernel[k] = 0.0f;
+  int status = OCC_OK;
+  for (uint32_t it = 0; it < iterations && status == OCC_OK; ++it) {
+    if (b->dirty) {
+      const int slot = (b->cur + 1) % kRing;
+      cudaEventSynchronize(b->ringEv[slot]);
+      write_tables(b, b->ring[slot].p);
+      b->cur = slot;
+      b->dirty = false;
+      OCC_CUDA(cudaGraphExecMemcpyNodeSetParams1D(b->exec, b->copyNode, b->S.tables.p, b->ring[slot].p,
+                                                  b->tablesBytes, cudaMemcpyHostToDevice));
+    }
+    cudaMemcpyAsync(b->S.tables.p, b->ring[b->cur].p, b->tablesBytes, cudaMemcpyHostToDevice, ctx->stream);
+    cudaError_t e = launch_flush_timed(b->params, b->L.numSt, b->L.maxStPerView, b->anyRaster,
+                                       b->L.querySlots > 0, ctx->stream, ev);
+    cudaEventRecord(b->ringEv[b->cur], ctx->stream);
+    if (e != cudaSuccess) status = fail(OCC_ERR_CUDA, std::string("profile launch: ") + cudaGetErrorString(e));
+    if (cudaEventSynchronize(ev[5]) != cudaSuccess) status = fail(OCC_ERR_CUDA, "profile sync");
+    for (int k = 0; k < 5 && status == OCC_OK; ++k) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+      msPerKernel[k] += ms / (float)iterations;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return status;
+}
+
+int occ_batch_destroy(occ_batch b)
+{
+  if (!b) return OCC_OK;
+  cudaStreamSynchronize(b->ctx->stream);
+  delete b;
+  return OCC_OK;
+}
+
+int occ_build_coverage_table(int64_t* out4096)
+{
+  if (!out4096) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  occ_table::build_coverage_table(out4096);
+  return OCC_OK;
+}
+
+int occ_coverage_table(int64_t* out4096)
+{
+  if (!out4096) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  static const unsigned long long t[4096] = {OCC_COVERAGE_TABLE_VALUES};
+  std::memcpy(out4096, t, sizeof(t));
+  return OCC_OK;
+}
+
+}  // extern "C"

@@ -91,11 +91,12 @@ int main(int argc, char** argv)
          " * Intel Xeon (x86-64).  Data, not code: see gen_x86_tables.c for the layout. */\n"
          "#pragma once\n#include <stdint.h>\n\n");
   printf("/* RCPPS(1.m) for m = top 11 mantissa bits; result exponent field is 126 or 127. */\n");
-  printf("static const uint32_t kX86RcpTable[2048] = {\n");
-  for (int i = 0; i < 2048; ++i) printf("0x%08x,%s", rcp_tab[i], (i % 8 == 7) ? "\n" : "");
-  printf("};\n\n/* RSQRTPS: index (E&1)<<11 | top 11 mantissa bits; base exponent 127 (odd) or 128 (even). */\n");
-  printf("static const uint32_t kX86RsqrtTable[4096] = {\n");
-  for (int i = 0; i < 4096; ++i) printf("0x%08x,%s", rsqrt_tab[i], (i % 8 == 7) ? "\n" : "");
-  printf("};\n");
+  printf("#define X86_RCP_TABLE_VALUES \\\n");
+  for (int i = 0; i < 2048; ++i) printf("0x%08x,%s", rcp_tab[i], (i % 8 == 7) ? " \\\n" : "");
+  printf("\n/* RSQRTPS: index (E&1)<<11 | top 11 mantissa bits; base exponent 127 (odd) or 128 (even). */\n");
+  printf("#define X86_RSQRT_TABLE_VALUES \\\n");
+  for (int i = 0; i < 4096; ++i) printf("0x%08x,%s", rsqrt_tab[i], (i % 8 == 7) ? " \\\n" : "");
+  printf("\nstatic const uint32_t kX86RcpTable[2048] = {X86_RCP_TABLE_VALUES};\n");
+  printf("static const uint32_t kX86RsqrtTable[4096] = {X86_RSQRT_TABLE_VALUES};\n");
   return 0;
 }

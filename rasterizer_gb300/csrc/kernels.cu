@@ -1,0 +1,1044 @@
+// GPU occluder rasteriser and visibility queries (sm_103a).
+//
+// One flush runs five kernels over a batch of views (raster_types.h):
+//
+//   k_setup      one CTA per 256-quad chunk: per-occluder prologue and GPU
+//                gating (Rasterizer.cpp:612-655, :123-281), then one thread per
+//                quad does the vertex transform and quad setup
+//                (Rasterizer.cpp:660-1081) and counts the quad's rows, row-walk
+//                checkpoints and 32x32-block super-tiles.
+//   k_scan       order-preserving prefix sums of those counts.
+//   k_fill_walk  one CTA per chunk: writes each super-tile's quad list in
+//                submission order, then walks every (quad, block row) once with
+//                the reference's incremental float adds and stores the edge
+//                offsets and depth lanes every 8 block columns.
+//   k_raster     one warp per 8x4-block warp-tile, one lane per 8x8 block: the
+//                warp reads its super-tile's list 32 entries at a time, ballots
+//                the quads overlapping the tile and applies them in order, each
+//                lane running the reference's per-block body (Rasterizer.cpp:
+//                1098-1292) on its block held in 32 registers.
+//   k_query      one thread per query box (Rasterizer.cpp:123-349), result bits
+//                gathered with ballots.
+//
+// Exactness: every float operation follows the reference's order and
+// rounding (x86_emu.cuh); the block loop sees each quad's primitives in
+// submission order with the hiZ early-out tested against the running hiZ.
+// The only place the rasteriser and the reference differ in control flow is
+// the convex-quad row early exit (Rasterizer.cpp:1161-1165): the blocks it
+// skips fail the same range test it is triggered by, because each edge offset
+// is a monotone sequence along a row (repeated addition of one constant), so
+// the in-range blocks of a row form one interval.  Skipping them or testing
+// them gives the same result.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "coverage_table.h"
+#include "raster_types.h"
+#include "x86_emu.cuh"
+
+namespace occ {
+
+__device__ const unsigned long long kDevCoverage[4096] = {OCC_COVERAGE_TABLE_VALUES};
+
+// Primitive mode for the 8-bit configuration (area signs | W signs << 4),
+// the classification of Rasterizer.cpp:30-64.
+__device__ const uint8_t kDevModeTable[256] = {
+#define CV kModeConvex
+#define T0 kModeTriangle0
+#define T1 kModeTriangle1
+#define CR kModeConcaveRight
+#define CL kModeConcaveLeft
+#define CC kModeConcaveCenter
+#define NO kModeCulled
+  CV, T1, CL, T1, T0, NO, T0, NO,  CR, T1, NO, T1, T0, NO, T0, NO,
+  CV, T1, CL, T1, T0, NO, T0, NO,  NO, T1, CC, T1, T0, NO, T0, NO,
+  CV, NO, CL, T1, T0, NO, T0, NO,  CR, T1, CC, T1, T0, NO, NO, NO,
+  CV, T1, CL, NO, T0, NO, T0, NO,  CR, T1, CC, T1, NO, NO, T0, NO,
+  CV, T1, NO, T1, T0, NO, T0, NO,  CR, T1, CC, T1, T0, NO, T0, NO,
+  NO, T1, CC, T1, T0, NO, T0, NO,  CC, T1, CC, T1, T0, NO, T0, NO,
+  CV, T1, CL, T1, T0, NO, NO, NO,  CR, NO, CC, T1, T0, NO, T0, NO,
+  T1, T1, T1, T1, NO, NO, NO, NO,  T1, T1, T1, NO, NO, NO, NO, NO,
+  CV, T1, CL, T1, NO, NO, T0, NO,  CR, T1, CC, NO, T0, NO, T0, NO,
+  CV, T1, CL, T1, T0, NO, NO, NO,  CR, NO, CC, T1, T0, NO, T0, NO,
+  NO, T1, CL, T1, T0, NO, T0, NO,  CR, T1, CC, T1, T0, NO, T0, NO,
+  CR, T1, NO, T1, T0, NO, T0, NO,  CR, T1, CC, T1, T0, NO, T0, NO,
+  CV, T1, CL, NO, T0, NO, T0, NO,  CR, T1, CC, T1, NO, NO, T0, NO,
+  T0, NO, T0, NO, T0, NO, T0, NO,  T0, NO, T0, NO, T0, NO, NO, NO,
+  CL, T1, CL, T1, T0, NO, T0, NO,  NO, T1, CC, T1, T0, NO, T0, NO,
+  NO, NO, NO, NO, NO, NO, NO, NO,  NO, NO, NO, NO, NO, NO, NO, NO,
+#undef CV
+#undef T0
+#undef T1
+#undef CR
+#undef CL
+#undef CC
+#undef NO
+};
+
+// ---- constants (Rasterizer.cpp:9-17, written as their float values) -----------
+
+__device__ __forceinline__ float kMaxInvW() { return __uint_as_float(0x5F7FFFFFu); }  // sqrtf(FLT_MAX)
+constexpr float kOffsetMul = 70.0f;    // (64 - 1) / (0.45f - -0.45f)
+constexpr float kOffsetAdd = 32.0f;    // 0.5f - -0.45f * 63 / 0.9f
+constexpr float kCkRange = 63.0f;      // OFFSET_QUANTIZATION_FACTOR - 1
+__device__ __forceinline__ float kSlopeMul() { return __uint_as_float(0x3E62BE2Cu); }  // 15.5f / 70.0f
+constexpr float kSlopeAdd = 16.0f;     // (32 - 1) * 0.5f + 0.5f
+__device__ __forceinline__ float kBboxMinAdd() { return __uint_as_float(0x3F1FFF2Eu); }  // 4.9999f / 8.0f
+constexpr float kBboxMaxAdd = 1.375f;  // 11.0f / 8.0f
+
+// ---- small device helpers -----------------------------------------------------------
+
+__device__ __forceinline__ uint32_t vmax_u16x2(uint32_t a, uint32_t b)
+{
+  uint32_t d;
+  asm("max.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+
+__device__ __forceinline__ uint32_t vmin_u16x2(uint32_t a, uint32_t b)
+{
+  uint32_t d;
+  asm("min.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+
+// _mm256_avg_epu16 on two packed pairs: (a + b + 1) >> 1 per 16-bit lane.
+__device__ __forceinline__ uint32_t avg_u16x2(uint32_t a, uint32_t b)
+{
+  return (a | b) - (((a ^ b) >> 1) & 0x7FFF7FFFu);
+}
+
+// packDepthPremultiplied of two lanes: lo -> bits 0..15, hi -> bits 16..31.
+__device__ __forceinline__ uint32_t pack2(float lo, float hi)
+{
+  return x86::pack_depth(lo) | (x86::pack_depth(hi) << 16);
+}
+
+template <int NT>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t& total, uint32_t* sm /* NT/32 */)
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sm[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < NT / 32 ? sm[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < NT / 32) sm[lane] = w;
+  }
+  __syncthreads();
+  uint32_t prefix = warp > 0 ? sm[warp - 1] : 0;
+  total = sm[NT / 32 - 1];
+  __syncthreads();
+  return prefix + x - v;
+}
+
+// ---- queryVisibility front end (Rasterizer.cpp:123-273) ------------------------------
+
+// Returns 0 (not visible), 1 (visible, needs clipping) or 2 (rect + maxZ for query2D).
+__device__ int query_front(const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect, uint32_t* maxZOut)
+{
+  using namespace x86;
+  float ext[4], ctr[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    ext[i] = xsub(bmax[i], bmin[i]);
+    ctr[i] = xadd(bmax[i], bmin[i]);
+  }
+  const float* row3 = V.rows + 12;
+  uint32_t signs = 0;
+#pragma unroll
+  for (int p = 0; p < 6; ++p) {
+    const float* rr = V.rows + 4 * (p >> 1);
+    float plane[4], offs[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      plane[i] = (p & 1) ? xsub(row3[i], rr[i]) : xadd(row3[i], rr[i]);
+      offs[i] = xadd(ctr[i], fxor(ext[i], sign(plane[i])));
+    }
+    signs |= fu(dp4(plane, offs));
+  }
+  if (signs & 0x80000000u) return 0;
+
+  const float* col0 = V.cols;
+  const float* col1 = V.cols + 4;
+  const float* col2 = V.cols + 8;
+  const float* col3 = V.cols + 12;
+  float c[8][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float e0 = xmul(col0[i], ext[0]), e1 = xmul(col1[i], ext[1]), e2 = xmul(col2[i], ext[2]);
+    c[0][i] = xfmadd(col0[i], bmin[0], xfmadd(col1[i], bmin[1], xfmadd(col2[i], bmin[2], col3[i])));
+    c[1][i] = xadd(c[0][i], e0);
+    c[2][i] = xadd(c[0][i], e1);
+    c[4][i] = xadd(c[0][i], e2);
+    c[3][i] = xadd(c[1][i], e1);
+    c[5][i] = xadd(c[4][i], e0);
+    c[6][i] = xadd(c[2][i], e2);
+    c[7][i] = xadd(c[6][i], e0);
+  }
+  float m1[4] = {xmax(ext[0], ext[2]), xmax(ext[1], ext[3]), xmax(ext[2], ext[0]), xmax(ext[3], ext[1])};
+  float me[4] = {xmax(m1[0], m1[1]), xmax(m1[1], m1[0]), xmax(m1[2], m1[3]), xmax(m1[3], m1[2])};
+  bool close = false;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float eps = xmul(me[i], 0.001f);
+    close |= (c[i][3] < eps) || (c[4 + i][3] < eps);
+  }
+  if (close) return 1;
+  float X[8], Y[8], Z[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    float iw = rcp(c[k][3]);
+    X[k] = xmul(c[k][0], iw);
+    Y[k] = xmul(c[k][1], iw);
+    Z[k] = xmul(c[k][2], iw);
+  }
+  float mnX[4], mxX[4], mnY[4], mxY[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    mnX[i] = xmin(X[i], X[4 + i]);
+    mxX[i] = xmax(X[i], X[4 + i]);
+    mnY[i] = xmin(Y[i], Y[4 + i]);
+    mxY[i] = xmax(Y[i], Y[4 + i]);
+  }
+  float mn[4] = {xmin(mnX[0], mnX[2]), xmin(mnY[0], mnY[2]), xmin(mnX[1], mnX[3]), xmin(mnY[1], mnY[3])};
+  float mx[4] = {xmax(mxX[0], mxX[2]), xmax(mxY[0], mxY[2]), xmax(mxX[1], mxX[3]), xmax(mxY[1], mxY[3])};
+  const float limX = i2f((int32_t)(V.width - 1)), limY = i2f((int32_t)(V.height - 1));
+  const float lim[4] = {limX, limY, limX, limY};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    mn[i] = xmax(mn[i], 0.0f);
+    mx[i] = fxor(xmin(mx[i], lim[i]), 0x80000000u);
+  }
+  float bf[4] = {xmin(mn[0], mn[2]), xmin(mx[0], mx[2]), xmin(mn[1], mn[3]), xmin(mx[1], mx[3])};
+  int32_t b[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) b[i] = cvtt(floor_(bf[i]));
+  b[1] = (int32_t)(0u - (uint32_t)b[1]);
+  b[3] = (int32_t)(0u - (uint32_t)b[3]);
+  if (b[0] >= b[1] || b[2] >= b[3]) return 0;
+  uint32_t maxZ = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) maxZ = ::max(maxZ, pack_depth(Z[k]));
+  rect[0] = (uint32_t)b[0];
+  rect[1] = (uint32_t)b[1];
+  rect[2] = (uint32_t)b[2];
+  rect[3] = (uint32_t)b[3];
+  *maxZOut = maxZ;
+  return 2;
+}
+
+// query2D (Rasterizer.cpp:283-349)
+__device__ bool query2d(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ)
+{
+  const uint32_t bx0 = minX >> 3, bx1 = maxX >> 3, by0 = minY >> 3, by1 = maxY >> 3;
+  for (uint32_t by = by0; by <= by1; ++by) {
+    int32_t sy = (int32_t)(minY - 8 * by);
+    sy = sy < 0 ? 0 : sy;
+    int32_t ey = (int32_t)(maxY - 8 * by);
+    ey = ey > 7 ? 7 : ey;
+    const bool interiorLine = sy == 0 && ey == 7;
+    for (uint32_t bx = bx0; bx <= bx1; ++bx) {
+      const uint32_t blk = by * V.blocksX + bx;
+      if (maxZ <= (uint32_t)V.hiz[blk]) continue;
+      int32_t sx = (int32_t)(minX - bx * 8);
+      sx = sx < 0 ? 0 : sx;
+      int32_t ex = (int32_t)(maxX - bx * 8);
+      ex = ex > 7 ? 7 : ex;
+      if (interiorLine && sx == 0 && ex == 7) return true;
+      const uint16_t* d = V.depth + (size_t)blk * 64;
+      for (int32_t y = sy; y <= ey; ++y) {
+        const uint4 row = *reinterpret_cast<const uint4*>(d + 8 * y);
+        const uint32_t w[4] = {row.x, row.y, row.z, row.w};
+#pragma unroll
+        for (int x = 0; x < 8; ++x) {
+          const uint32_t v = (w[x >> 1] >> ((x & 1) * 16)) & 0xFFFFu;
+          if (x >= sx && x <= ex && v < maxZ) return true;
+        }
+      }
+    }
+  }
+  return false;
+}
+
+// ---- per-occluder prologue (Rasterizer.cpp:612-655) ----------------------------------
+
+struct CmdConst {
+  float rows[4][4];  // output i's coefficients for (X word, Y word, Z word, 1)
+  float c0, c1;      // Z = c1 * (1/W) + c0
+  uint32_t draw, nc;
+};
+
+__device__ void cmd_prologue(const ViewDesc& V, const Cmd& cmd, CmdConst& out)
+{
+  using namespace x86;
+  if (cmd.flags & kCmdGated) {
+    // queryVisibility of the bounds against an empty buffer: visible iff in
+    // the frustum and either near the camera plane or covering a nonempty
+    // screen rectangle with a nonzero depth bound.
+    uint32_t rect[4], maxZ = 0;
+    int st = query_front(V, cmd.boundsMin, cmd.boundsMax, rect, &maxZ);
+    out.draw = st == 1 || (st == 2 && maxZ > 0);
+    out.nc = st == 1;
+  } else {
+    out.draw = 1;
+    out.nc = (cmd.flags & kCmdNearClip) ? 1 : 0;
+  }
+  float col[4][4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) col[j][i] = V.cols[4 * j + i];
+  float ext[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) ext[i] = xsub(cmd.refMax[i], cmd.refMin[i]);
+  float c3[4], n0[4], n1[4], n2[4];
+  const float s0 = xmul(ext[0], __uint_as_float(0x2F801002u));  // 1.0f / (2047ull << 21)
+  const float s1 = xmul(ext[1], __uint_as_float(0x35001002u));  // 1.0f / (2047 << 10)
+  const float s2 = xmul(ext[2], __uint_as_float(0x3A802008u));  // 1.0f / 1023
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    c3[i] = xfmadd(col[0][i], cmd.refMin[0], xfmadd(col[1][i], cmd.refMin[1], xfmadd(col[2][i], cmd.refMin[2], col[3][i])));
+    n0[i] = xmul(col[0][i], s0);
+    n1[i] = xmul(col[1][i], s1);
+    n2[i] = xmul(col[2][i], s2);
+    c3[i] = xfmadd(n0[i], 2147483648.0f, c3[i]);  // 1024ull << 21
+    n1[i] = xsub(n1[i], n0[i]);
+    n2[i] = xsub(n2[i], n0[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    out.rows[i][0] = n0[i];
+    out.rows[i][1] = n1[i];
+    out.rows[i][2] = n2[i];
+    out.rows[i][3] = c3[i];
+  }
+  const float w[4] = {2097152.0f, 1024.0f, 1.0f, 1.0f};
+  const float Za = out.rows[2][3], Zb = dp4(out.rows[2], w);
+  const float Wa = out.rows[3][3], Wb = dp4(out.rows[3], w);
+  const float c0 = xdiv(xsub(Za, Zb), xsub(Wa, Wb));
+  out.c0 = c0;
+  out.c1 = xfnmadd(c0, Wa, Za);
+}
+
+// ---- quad setup (one SIMD lane of Rasterizer.cpp:660-1081) ---------------------------
+
+__device__ bool quad_setup(const ViewDesc& V, const uint32_t w4[4], const CmdConst& K, QuadRaster& R, QuadWalk& Wk)
+{
+  using namespace x86;
+  const bool nc = K.nc != 0;
+  float x[4], y[4], z[4], invW[4];
+  uint32_t ws[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float Xf = i2f((int32_t)w4[j]);
+    const float Yf = i2f((int32_t)(w4[j] & (2047u << 10)));
+    const float Zf = i2f((int32_t)(w4[j] & 1023u));
+    const float X = xfmadd(Xf, K.rows[0][0], xfmadd(Yf, K.rows[0][1], xfmadd(Zf, K.rows[0][2], K.rows[0][3])));
+    const float Y = xfmadd(Xf, K.rows[1][0], xfmadd(Yf, K.rows[1][1], xfmadd(Zf, K.rows[1][2], K.rows[1][3])));
+    const float W = xfmadd(Xf, K.rows[3][0], xfmadd(Yf, K.rows[3][1], xfmadd(Zf, K.rows[3][2], K.rows[3][3])));
+    invW[j] = nc ? xmin(kMaxInvW(), xmax(-kMaxInvW(), rcp(W))) : rcp(W);
+    x[j] = xmul(round_even(xmul(X, invW[j])), 0.125f);
+    y[j] = xmul(round_even(xmul(Y, invW[j])), 0.125f);
+    ws[j] = nc ? sign(invW[j]) : 0u;
+  }
+  float eX[5], eY[5];
+  eX[0] = xsub(y[1], y[0]); eX[1] = xsub(y[2], y[1]); eX[2] = xsub(y[3], y[2]); eX[3] = xsub(y[0], y[3]);
+  eY[0] = xsub(x[0], x[1]); eY[1] = xsub(x[1], x[2]); eY[2] = xsub(x[2], x[3]); eY[3] = xsub(x[3], x[0]);
+  const float area0 = xfmsub(eX[0], eY[1], xmul(eX[1], eY[0]));
+  const float area1 = xfmsub(eX[1], eY[2], xmul(eX[2], eY[1]));
+  const float area2 = xfmsub(eX[2], eY[3], xmul(eX[3], eY[2]));
+  const float area3 = xsub(xadd(area0, area2), area1);
+  uint32_t cfg = 0;
+  cfg |= (fxor(area0, ws[0] ^ ws[1] ^ ws[2]) <= 0.0f) ? 1u : 0u;
+  cfg |= (fxor(area1, ws[1] ^ ws[2] ^ ws[3]) <= 0.0f) ? 2u : 0u;
+  cfg |= (fxor(area2, ws[0] ^ ws[2] ^ ws[3]) <= 0.0f) ? 4u : 0u;
+  cfg |= (fxor(area3, ws[1] ^ ws[0] ^ ws[3]) <= 0.0f) ? 8u : 0u;
+  cfg |= (ws[0] >> 27) | (ws[1] >> 26) | (ws[2] >> 25) | (ws[3] >> 24);
+  const int mode = kDevModeTable[cfg];
+  if (mode == kModeCulled) return false;
+
+  float minFx, minFy, maxFx, maxFy;
+  if (nc) {
+    // clipless bounding box (Rasterizer.cpp:820-909)
+    const float infP = 10000.0f, infN = -10000.0f;
+    float mPx[4], mPy[4], MPx[4], MPy[4], mNx[4], mNy[4], MNx[4], MNy[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      mPx[j] = ws[j] ? infP : x[j];
+      mPy[j] = ws[j] ? infP : y[j];
+      MPx[j] = fxor(mPx[j], ws[j]);
+      MPy[j] = fxor(mPy[j], ws[j]);
+      mNx[j] = ws[j] ? x[j] : infP;
+      mNy[j] = ws[j] ? y[j] : infP;
+      MNx[j] = ws[j] ? x[j] : infN;
+      MNy[j] = ws[j] ? y[j] : infN;
+    }
+    const float minPx = xmin(xmin(mPx[0], mPx[1]), xmin(mPx[2], mPx[3]));
+    const float minPy = xmin(xmin(mPy[0], mPy[1]), xmin(mPy[2], mPy[3]));
+    const float maxPx = xmax(xmax(MPx[0], MPx[1]), xmax(MPx[2], MPx[3]));
+    const float maxPy = xmax(xmax(MPy[0], MPy[1]), xmax(MPy[2], MPy[3]));
+    const float minNx = xmin(xmin(mNx[0], mNx[1]), xmin(mNx[2], mNx[3]));
+    const float minNy = xmin(xmin(mNy[0], mNy[1]), xmin(mNy[2], mNy[3]));
+    const float maxNx = xmax(xmax(MNx[0], MNx[1]), xmax(MNx[2], MNx[3]));
+    const float maxNy = xmax(xmax(MNy[0], MNy[1]), xmax(MNy[2], MNy[3]));
+    const float incAx = (maxNx > minPx) ? infN : minPx;
+    const float incAy = (maxNy > minPy) ? infN : minPy;
+    const float incBx = (maxPx > minNx) ? infP : maxPx;
+    const float incBy = (maxPy > minNy) ? infP : maxPy;
+    minFx = xmin(incAx, incBx);
+    minFy = xmin(incAy, incBy);
+    maxFx = xmax(incAx, incBx);
+    maxFy = xmax(incAy, incBy);
+  } else {
+    minFx = xmin(xmin(x[0], x[1]), xmin(x[2], x[3]));
+    minFy = xmin(xmin(y[0], y[1]), xmin(y[2], y[3]));
+    maxFx = xmax(xmax(x[0], x[1]), xmax(x[2], x[3]));
+    maxFy = xmax(xmax(y[0], y[1]), xmax(y[2], y[3]));
+  }
+  int32_t minX = cvtt(xadd(minFx, kBboxMinAdd()));
+  int32_t minY = cvtt(xadd(minFy, kBboxMinAdd()));
+  int32_t maxX = cvtt(xadd(maxFx, kBboxMaxAdd));
+  int32_t maxY = cvtt(xadd(maxFy, kBboxMaxAdd));
+  minX = minX < 0 ? 0 : minX;
+  minY = minY < 0 ? 0 : minY;
+  maxX = maxX > (int32_t)V.blocksX ? (int32_t)V.blocksX : maxX;
+  maxY = maxY > (int32_t)V.blocksY ? (int32_t)V.blocksY : maxY;
+  if (!(maxX > minX && maxY > minY)) return false;
+
+#pragma unroll
+  for (int j = 0; j < 4; ++j) z[j] = xfmadd(invW[j], K.c1, K.c0);
+  float maxZ = xmax(xmax(z[0], z[1]), xmax(z[2], z[3]));
+  if (nc && (ws[0] | ws[1] | ws[2] | ws[3])) maxZ = 1.0f;
+
+  // depth plane of the larger triangle (Rasterizer.cpp:963-999)
+  const bool t0 = mode == kModeTriangle0, t1 = mode == kModeTriangle1;
+  bool greater = fabs_(area0) < fabs_(area2);
+  greater = !t0 && (t1 || greater);
+  const float a = greater ? area2 : area0;
+  const float invArea = nc ? xdiv(1.0f, a) : rcp(a);
+  const float z12 = xsub(z[1], z[2]), z20 = xsub(z[2], z[0]), z30 = xsub(z[3], z[0]);
+  eX[4] = xsub(y[0], y[2]);
+  eY[4] = xsub(x[2], x[0]);
+  const float dx = greater ? xfnmadd(z20, eX[3], xmul(z30, eX[4])) : xfmsub(z20, eX[1], xmul(z12, eX[4]));
+  const float dy = greater ? xfnmadd(z20, eY[3], xmul(z30, eY[4])) : xfmsub(z20, eY[1], xmul(z12, eY[4]));
+  const float plane1 = xmul(invArea, dx);
+  const float plane2 = xmul(invArea, dy);
+  const float x0 = xsub(x[0], i2f(minX));
+  const float y0 = xsub(y[0], i2f(minY));
+  const float plane0 = xfnmadd(x0, plane1, xfnmadd(y0, plane2, z[0]));
+
+  if (t0) { eX[2] = eX[4]; eY[2] = eY[4]; }
+  if (t1) { eX[0] = fxor(eX[4], 0x80000000u); eY[0] = fxor(eY[4], 0x80000000u); }
+  uint32_t flip[4] = {0, 0, 0, 0};
+  if (nc) {
+    flip[0] = ws[0] ^ (t1 ? ws[2] : ws[1]);
+    flip[1] = ws[1] ^ ws[2];
+    flip[2] = ws[2] ^ (t0 ? ws[0] : ws[3]);
+    flip[3] = ws[0] ^ ws[3];
+  }
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {  // normalizeEdge (Rasterizer.cpp:452-468)
+    float invLen = rcp(xadd(fabs_(eX[e]), fabs_(eY[e])));
+    invLen = xmul(nc ? fxor(kOffsetMul, flip[e]) : kOffsetMul, invLen);
+    eX[e] = xmul(eX[e], invLen);
+    eY[e] = xmul(eY[e], invLen);
+  }
+  float off[4];
+  off[0] = xfnmadd(x0, eX[0], xfnmadd(y0, eY[0], kOffsetAdd));
+#pragma unroll
+  for (int e = 1; e < 4; ++e) off[e] = xfnmadd(x[e], eX[e], xfnmadd(y[e], eY[e], kOffsetAdd));
+#pragma unroll
+  for (int e = 1; e < 4; ++e) off[e] = xfmadd(i2f(minX), eX[e], off[e]);
+#pragma unroll
+  for (int e = 1; e < 4; ++e) off[e] = xfmadd(i2f(minY), eY[e], off[e]);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {  // quantizeSlopeLookup (Rasterizer.cpp:482-493)
+    const uint32_t yneg = (eY[e] <= 0.0f) ? 0xFFFFFFFFu : 0u;
+    const uint32_t q = (uint32_t)cvtt(xfmadd(eX[e], kSlopeMul(), kSlopeAdd));
+    R.slope[e] = (uint16_t)(((((q << 1) - yneg) << 6)) & 4095u);
+    R.nx[e] = eX[e];
+    Wk.ny[e] = eY[e];
+    Wk.off[e] = off[e];
+  }
+  R.minX = (uint16_t)minX;
+  R.minY = (uint16_t)minY;
+  R.maxX = (uint16_t)maxX;
+  R.maxY = (uint16_t)maxY;
+  R.maxZ = (uint16_t)pack_depth(maxZ);
+  R.mode = (uint8_t)mode;
+  R.Dx = plane1;
+  R.Dy = plane2;
+  Wk.plane0 = plane0;
+  // Safe when no depth value along the walk can leave the finite range: then
+  // plain IEEE adds give the x86 result bit for bit (no NaN can appear).
+  const float span = i2f((maxX - minX) + (maxY - minY) + 4);
+  const float bound = radd(fabs_(plane0), rmul(span, radd(fabs_(plane1), fabs_(plane2))));
+  const bool safe = bound < 1e37f;  // false for NaN / inf inputs too
+  R.flags = (uint8_t)((nc ? kQuadNearClip : 0) | (safe ? kQuadSafe : 0));
+  return true;
+}
+
+__device__ __forceinline__ uint32_t view_of_chunk(const FrameParams& P, uint32_t c) { return P.chunks[c].view; }
+
+__device__ __forceinline__ uint32_t nck_of(const QuadRaster& R)
+{
+  return (uint32_t)((R.maxX - 1) >> 3) - (uint32_t)(R.minX >> 3) + 1u;
+}
+
+// ---- k_setup -------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
+{
+  extern __shared__ uint32_t s_stCount[];
+  __shared__ CmdConst s_cc[kMaxCmdPerChunk];
+  __shared__ uint32_t s_cmdStart[kMaxCmdPerChunk];
+  __shared__ uint32_t s_scan[kChunk / 32];
+
+  const uint32_t c = blockIdx.x;
+  const Chunk ch = P.chunks[c];
+  const ViewDesc& V = P.views[ch.view];
+  const uint32_t tid = threadIdx.x;
+  const uint32_t nst = V.stX * V.stY;
+  for (uint32_t i = tid; i < nst; i += kChunk) s_stCount[i] = 0;
+  if (tid < ch.cmdCount) {
+    const Cmd cmd = P.cmds[ch.cmdFirst + tid];
+    cmd_prologue(V, cmd, s_cc[tid]);
+    s_cmdStart[tid] = cmd.quadStart;
+    P.cmdDraw[ch.cmdFirst + tid] = s_cc[tid].draw | (s_cc[tid].nc << 1);  // same value from every chunk
+  }
+  __syncthreads();
+
+  const uint32_t q = (c << kChunkShift) + tid;
+  QuadRaster R;
+  QuadWalk Wk;
+  bool valid = false;
+  if (tid < ch.quadCount) {
+    uint32_t k = 0;
+    for (uint32_t i = 1; i < ch.cmdCount; ++i)
+      if (s_cmdStart[i] <= q) k = i;
+    if (s_cc[k].draw) {
+      const Cmd& cmd = P.cmds[ch.cmdFirst + k];
+      const uint32_t local = q - cmd.quadStart;     // quad within the occluder
+      const uint32_t group = local >> 3, lane = local & 7;
+      const uint32_t* base = P.pool + cmd.wordOffset + group * 32;
+      uint32_t w4[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) w4[j] = __ldg(base + 8 * j + lane);
+      valid = quad_setup(V, w4, s_cc[k], R, Wk);
+    }
+  }
+  uint32_t rows = 0, cks = 0;
+  if (valid) {
+    rows = (uint32_t)(R.maxY - R.minY);
+    cks = rows * nck_of(R);
+  } else {
+    R = QuadRaster{};
+    Wk = QuadWalk{};
+  }
+  uint32_t totRows, totCks;
+  const uint32_t rowLocal = block_exclusive_scan<kChunk>(rows, totRows, s_scan);
+  const uint32_t ckLocal = block_exclusive_scan<kChunk>(cks, totCks, s_scan);
+  R.ckLocal = ckLocal;
+  Wk.rowLocal = rowLocal;
+  P.rec[q] = R;
+  P.walk[q] = Wk;
+  if (valid) {
+    const uint32_t sx0 = R.minX / kSuperTile, sx1 = (R.maxX - 1u) / kSuperTile;
+    const uint32_t sy0 = R.minY / kSuperTile, sy1 = (R.maxY - 1u) / kSuperTile;
+    for (uint32_t sy = sy0; sy <= sy1; ++sy)
+      for (uint32_t sx = sx0; sx <= sx1; ++sx) atomicAdd(&s_stCount[sy * V.stX + sx], 1u);
+  }
+  __syncthreads();
+  for (uint32_t s = tid; s < nst; s += kChunk) P.mat[V.matBase + s * V.chunkCount + ch.localIndex] = s_stCount[s];
+  if (tid == 0) P.chunkTot[c] = Totals{totRows, totCks, 0, 0};
+}
+
+// ---- k_scan ----------------------------------------------------------------------------
+// CTAs [0, nst): one super-tile's chunk counts -> exclusive prefix in place, list length.
+// CTAs [nst, nst + views): one view's chunk totals -> chunk bases.  The last CTA
+// to finish lays the super-tile lists and the views' row/checkpoint ranges out
+// back to back and checks the capacities.
+
+__global__ void __launch_bounds__(256) k_scan(FrameParams P, uint32_t numSt)
+{
+  __shared__ uint32_t s_scan[8];
+  __shared__ uint32_t s_last;
+  const uint32_t b = blockIdx.x, tid = threadIdx.x;
+  if (b < numSt) {
+    uint32_t lo = 0, hi = P.numViews - 1;  // view owning super-tile b
+    while (lo < hi) {
+      uint32_t mid = (lo + hi + 1) >> 1;
+      if (P.views[mid].stBase <= b) lo = mid; else hi = mid - 1;
+    }
+    const ViewDesc& V = P.views[lo];
+    uint32_t* m = P.mat + V.matBase + (b - V.stBase) * V.chunkCount;
+    uint32_t carry = 0;
+    for (uint32_t i0 = 0; i0 < V.chunkCount; i0 += 256) {
+      const uint32_t i = i0 + tid;
+      const uint32_t v = i < V.chunkCount ? m[i] : 0;
+      uint32_t tot;
+      const uint32_t ex = block_exclusive_scan<256>(v, tot, s_scan);
+      if (i < V.chunkCount) m[i] = carry + ex;
+      carry += tot;
+    }
+    if (tid == 0) P.stLen[b] = carry;
+  } else {
+    const uint32_t v = b - numSt;
+    const ViewDesc& V = P.views[v];
+    uint32_t carryR = 0, carryC = 0;
+    for (uint32_t i0 = 0; i0 < V.chunkCount; i0 += 256) {
+      const uint32_t i = i0 + tid;
+      Totals t = i < V.chunkCount ? P.chunkTot[V.chunkStart + i] : Totals{0, 0, 0, 0};
+      uint32_t totR, totC;
+      const uint32_t exR = block_exclusive_scan<256>(t.rows, totR, s_scan);
+      const uint32_t exC = block_exclusive_scan<256>(t.cks, totC, s_scan);
+      if (i < V.chunkCount) P.chunkBase[V.chunkStart + i] = Totals{carryR + exR, carryC + exC, 0, 0};
+      carryR += totR;
+      carryC += totC;
+    }
+    if (tid == 0) P.viewTot[v] = Totals{carryR, carryC, 0, 0};
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) s_last = atomicAdd(&P.header->viewsDone, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  uint32_t carry = 0;
+  for (uint32_t i0 = 0; i0 < numSt; i0 += 256) {
+    const uint32_t i = i0 + tid;
+    const uint32_t v = i < numSt ? __ldcg(&P.stLen[i]) : 0;
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan<256>(v, tot, s_scan);
+    if (i < numSt) P.stStart[i] = carry + ex;
+    carry += tot;
+  }
+  uint32_t carryR = 0, carryC = 0;
+  for (uint32_t i0 = 0; i0 < P.numViews; i0 += 256) {
+    const uint32_t i = i0 + tid;
+    Totals t = Totals{0, 0, 0, 0};
+    if (i < P.numViews) {
+      t.rows = __ldcg(&P.viewTot[i].rows);
+      t.cks = __ldcg(&P.viewTot[i].cks);
+    }
+    uint32_t totR, totC;
+    const uint32_t exR = block_exclusive_scan<256>(t.rows, totR, s_scan);
+    const uint32_t exC = block_exclusive_scan<256>(t.cks, totC, s_scan);
+    if (i < P.numViews) P.viewBase[i] = Totals{carryR + exR, carryC + exC, 0, 0};
+    carryR += totR;
+    carryC += totC;
+  }
+  if (tid == 0) {
+    FrameHeader* H = P.header;
+    H->totalRows = carryR;
+    H->totalCks = carryC;
+    H->totalSt = carry;
+    H->overflow = (carryC > H->capCks ? 1u : 0u) | (carry > H->capSt ? 2u : 0u);
+    H->sticky |= H->overflow;
+    H->maxCks = ::max(H->maxCks, carryC);
+    H->maxSt = ::max(H->maxSt, carry);
+    H->viewsDone = 0;
+  }
+}
+
+// ---- k_fill_walk -------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kChunk) k_fill_walk(FrameParams P)
+{
+  __shared__ uint32_t s_scan[kChunk / 32];
+  __shared__ uint32_t s_rowLocal[kChunk];
+  __shared__ int s_rect[4];
+  if (P.header->overflow) return;
+  const uint32_t c = blockIdx.x, tid = threadIdx.x;
+  const Chunk ch = P.chunks[c];
+  const ViewDesc& V = P.views[ch.view];
+  const uint32_t q = (c << kChunkShift) + tid;
+  const QuadRaster R = P.rec[q];
+  const bool valid = tid < ch.quadCount && R.minX < R.maxX;
+  s_rowLocal[tid] = P.walk[q].rowLocal;
+  if (tid == 0) {
+    s_rect[0] = 1 << 30; s_rect[1] = -1; s_rect[2] = 1 << 30; s_rect[3] = -1;
+  }
+  __syncthreads();
+  int sx0 = 0, sx1 = -1, sy0 = 0, sy1 = -1;
+  if (valid) {
+    sx0 = R.minX / kSuperTile; sx1 = (R.maxX - 1) / kSuperTile;
+    sy0 = R.minY / kSuperTile; sy1 = (R.maxY - 1) / kSuperTile;
+    atomicMin(&s_rect[0], sx0); atomicMax(&s_rect[1], sx1);
+    atomicMin(&s_rect[2], sy0); atomicMax(&s_rect[3], sy1);
+  }
+  __syncthreads();
+  const int ux0 = s_rect[0], ux1 = s_rect[1], uy0 = s_rect[2], uy1 = s_rect[3];
+  // super-tile lists, in submission order
+  for (int sy = uy0; sy <= uy1; ++sy)
+    for (int sx = ux0; sx <= ux1; ++sx) {
+      const bool flag = valid && sx >= sx0 && sx <= sx1 && sy >= sy0 && sy <= sy1;
+      uint32_t tot;
+      const uint32_t rank = block_exclusive_scan<kChunk>(flag ? 1u : 0u, tot, s_scan);
+      if (flag) {
+        const uint32_t s = (uint32_t)sy * V.stX + (uint32_t)sx;
+        const uint32_t pos = P.stStart[V.stBase + s] + P.mat[V.matBase + s * V.chunkCount + ch.localIndex] + rank;
+        P.stList[pos] = q;
+      }
+    }
+  // row walk: one thread per (quad, block row) of this chunk
+  const uint32_t rowsTotal = P.chunkTot[c].rows;
+  const uint32_t ckChunk = P.viewBase[ch.view].cks + P.chunkBase[c].cks;
+  const float dsp = -0.4375f;  // -0.5f + 1.0f / 16.0f
+  for (uint32_t r0 = tid; r0 < rowsTotal; r0 += kChunk) {
+    uint32_t lo = 0, hi = ch.quadCount - 1;  // last quad with rowLocal <= r0
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (s_rowLocal[mid] <= r0) lo = mid; else hi = mid - 1;
+    }
+    const uint32_t qq = (c << kChunkShift) + lo;
+    const QuadRaster Q = P.rec[qq];
+    const QuadWalk Wk = P.walk[qq];
+    const uint32_t r = r0 - s_rowLocal[lo];
+    const bool safe = (Q.flags & kQuadSafe) != 0;
+    float depth[8], off[4];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const float lx = dsp + 0.125f * (float)(k & 3);
+      const float ly = dsp + 0.125f * (float)(k >> 2);
+      depth[k] = x86::xfmadd(Q.Dx, lx, x86::xfmadd(Q.Dy, ly, Wk.plane0));
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) off[e] = Wk.off[e];
+    for (uint32_t i = 0; i < r; ++i) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) depth[k] = safe ? x86::radd(depth[k], Q.Dy) : x86::xadd(depth[k], Q.Dy);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) off[e] = x86::radd(off[e], Wk.ny[e]);
+    }
+    const uint32_t nck = nck_of(Q);
+    float4* out = reinterpret_cast<float4*>(P.ck + (size_t)kCkFloats * (ckChunk + Q.ckLocal + r * nck));
+    const uint32_t lastCk = ::max((uint32_t)Q.minX, (uint32_t)(Q.maxX - 1) & ~7u);
+    for (uint32_t bx = Q.minX;; ++bx) {
+      if (bx == Q.minX || (bx & 7u) == 0) {
+        out[0] = make_float4(off[0], off[1], off[2], off[3]);
+        out[1] = make_float4(depth[0], depth[1], depth[2], depth[3]);
+        out[2] = make_float4(depth[4], depth[5], depth[6], depth[7]);
+        out += 3;
+      }
+      if (bx == lastCk) break;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) depth[k] = safe ? x86::radd(Q.Dx, depth[k]) : x86::xadd(Q.Dx, depth[k]);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) off[e] = x86::radd(Q.nx[e], off[e]);
+    }
+  }
+}
+
+// ---- k_raster ------------------------------------------------------------------------
+
+// Applies one quad's fragment to the lane's block (Rasterizer.cpp:1241-1290).
+__device__ __forceinline__ void apply_fragment(uint32_t (&blk)[32], uint32_t& hiz, bool& have,
+                                               const uint16_t* mem, uint64_t mask, const float (&depth)[8],
+                                               float Dx, float Dy, bool safe)
+{
+  float d1[8], d8[8], d9[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    d1[k] = safe ? x86::rfma(Dx, 0.5f, depth[k]) : x86::xfmadd(Dx, 0.5f, depth[k]);
+    d8[k] = safe ? x86::radd(Dy, depth[k]) : x86::xadd(Dy, depth[k]);
+    d9[k] = safe ? x86::radd(Dy, d1[k]) : x86::xadd(Dy, d1[k]);
+  }
+  uint32_t r[10][4];
+  // rows 0/1 from (depth, d1), rows 8/9 from (d8, d9): lanes 0-3 even row, 4-7 odd row
+  r[0][0] = pack2(depth[0], depth[1]); r[0][1] = pack2(depth[2], depth[3]);
+  r[0][2] = pack2(d1[0], d1[1]);       r[0][3] = pack2(d1[2], d1[3]);
+  r[1][0] = pack2(depth[4], depth[5]); r[1][1] = pack2(depth[6], depth[7]);
+  r[1][2] = pack2(d1[4], d1[5]);       r[1][3] = pack2(d1[6], d1[7]);
+  r[8][0] = pack2(d8[0], d8[1]);       r[8][1] = pack2(d8[2], d8[3]);
+  r[8][2] = pack2(d9[0], d9[1]);       r[8][3] = pack2(d9[2], d9[3]);
+  r[9][0] = pack2(d8[4], d8[5]);       r[9][1] = pack2(d8[6], d8[7]);
+  r[9][2] = pack2(d9[4], d9[5]);       r[9][3] = pack2(d9[6], d9[7]);
+#pragma unroll
+  for (int w = 0; w < 4; ++w) {
+    r[4][w] = avg_u16x2(r[0][w], r[8][w]);
+    r[5][w] = avg_u16x2(r[1][w], r[9][w]);
+    r[2][w] = avg_u16x2(r[0][w], r[4][w]);
+    r[3][w] = avg_u16x2(r[1][w], r[5][w]);
+    r[6][w] = avg_u16x2(r[4][w], r[8][w]);
+    r[7][w] = avg_u16x2(r[5][w], r[9][w]);
+  }
+  if (mask != ~0ull) {
+#pragma unroll
+    for (int y = 0; y < 8; ++y) {
+      const int bitpos = (y & 1) ? (y >> 1) : 4 + (y >> 1);
+      const uint64_t bits = (mask >> bitpos) & 0x0101010101010101ull;
+      const uint32_t lo = (uint32_t)bits * 0xFFu, hi = (uint32_t)(bits >> 32) * 0xFFu;
+      r[y][0] &= __byte_perm(lo, 0, 0x1100);
+      r[y][1] &= __byte_perm(lo, 0, 0x3322);
+      r[y][2] &= __byte_perm(hi, 0, 0x1100);
+      r[y][3] &= __byte_perm(hi, 0, 0x3322);
+    }
+  }
+  if (hiz == 1) {
+#pragma unroll
+    for (int y = 0; y < 8; ++y)
+#pragma unroll
+      for (int w = 0; w < 4; ++w) blk[4 * y + w] = r[y][w];
+  } else {
+    if (!have) {
+      const uint4* m = reinterpret_cast<const uint4*>(mem);
+#pragma unroll
+      for (int y = 0; y < 8; ++y) {
+        const uint4 v = m[y];
+        blk[4 * y + 0] = v.x; blk[4 * y + 1] = v.y; blk[4 * y + 2] = v.z; blk[4 * y + 3] = v.w;
+      }
+    }
+#pragma unroll
+    for (int y = 0; y < 8; ++y)
+#pragma unroll
+      for (int w = 0; w < 4; ++w) blk[4 * y + w] = vmax_u16x2(blk[4 * y + w], r[y][w]);
+  }
+  have = true;
+  uint32_t mn = blk[0];
+#pragma unroll
+  for (int i = 1; i < 32; ++i) mn = vmin_u16x2(mn, blk[i]);
+  hiz = ::min(mn & 0xFFFFu, mn >> 16);
+}
+
+__global__ void __launch_bounds__(128) k_raster(FrameParams P)
+{
+  if (P.header->overflow) return;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t wt = blockIdx.x * 4 + warp;
+  if (wt >= P.numTiles) return;
+  uint32_t lo = 0, hi = P.numViews - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (P.views[mid].tileStart <= wt) lo = mid; else hi = mid - 1;
+  }
+  const uint32_t v = lo;
+  const ViewDesc& V = P.views[v];
+  const uint32_t lt = wt - V.tileStart;
+  const uint32_t tx = lt % V.tilesX, ty = lt / V.tilesX;
+  const uint32_t bx = tx * kTileW + (lane & 7), by = ty * kTileH + (lane >> 3);
+  const bool inView = bx < V.blocksX && by < V.blocksY;
+  const uint32_t blk = inView ? by * V.blocksX + bx : 0;
+  const bool clearing = (V.flags & kViewClear) != 0;
+  uint32_t hiz = clearing ? 1u : (inView ? (uint32_t)V.hiz[blk] : 0xFFFFu);
+  bool have = false;
+  uint32_t blkd[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) blkd[i] = 0;
+
+  const uint32_t s = V.stBase + (ty * kTileH / kSuperTile) * V.stX + (tx * kTileW / kSuperTile);
+  const uint32_t listLen = V.cmdCount ? P.stLen[s] : 0;
+  const uint32_t* list = P.stList + (V.cmdCount ? P.stStart[s] : 0);
+  const uint32_t tx0 = tx * kTileW, ty0 = ty * kTileH;
+  const uint32_t ckView = P.viewBase[v].cks;
+  for (uint32_t base = 0; base < listLen; base += 32) {
+    const uint32_t idx = base + lane;
+    uint32_t q = 0;
+    bool ov = false;
+    if (idx < listLen) {
+      q = __ldg(list + idx);
+      const uint2 bb = __ldg(reinterpret_cast<const uint2*>(P.rec + q));
+      const uint32_t qminX = bb.x & 0xFFFFu, qminY = bb.x >> 16, qmaxX = bb.y & 0xFFFFu, qmaxY = bb.y >> 16;
+      ov = qminX < tx0 + kTileW && qmaxX > tx0 && qminY < ty0 + kTileH && qmaxY > ty0;
+    }
+    uint32_t m = __ballot_sync(0xFFFFFFFFu, ov);
+    while (m) {
+      const int j = __ffs(m) - 1;
+      m &= m - 1;
+      const uint32_t qq = __shfl_sync(0xFFFFFFFFu, q, j);
+      const QuadRaster Q = P.rec[qq];
+      const bool inQuad = inView && bx >= Q.minX && bx < Q.maxX && by >= Q.minY && by < Q.maxY;
+      if (!inQuad) continue;
+      if (hiz >= Q.maxZ) continue;
+      // checkpoint for (row by, column xmax(minX, tx0)), then <= 7 column steps
+      const uint32_t cx = ::max((uint32_t)Q.minX, tx0);
+      const uint32_t kk = (cx >> 3) - ((uint32_t)Q.minX >> 3);
+      const uint32_t chunk = qq >> kChunkShift;
+      const uint32_t ckIdx = ckView + P.chunkBase[chunk].cks + Q.ckLocal + (by - Q.minY) * nck_of(Q) + kk;
+      const float4* ck = reinterpret_cast<const float4*>(P.ck + (size_t)kCkFloats * ckIdx);
+      const float4 o = __ldg(ck), d0 = __ldg(ck + 1), d1 = __ldg(ck + 2);
+      float off[4] = {o.x, o.y, o.z, o.w};
+      float depth[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+      const bool safe = (Q.flags & kQuadSafe) != 0;
+      for (uint32_t i = cx; i < bx; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) depth[k] = safe ? x86::radd(Q.Dx, depth[k]) : x86::xadd(Q.Dx, depth[k]);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) off[e] = x86::radd(Q.nx[e], off[e]);
+      }
+      uint64_t mask;
+      if (Q.mode == kModeConvex) {
+        if (off[0] >= kCkRange || off[1] >= kCkRange || off[2] >= kCkRange || off[3] >= kCkRange) continue;
+        mask = ~0ull;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          int32_t oi = x86::cvtt(off[e]);
+          oi = oi < 0 ? 0 : oi;
+          mask &= __ldg(&kDevCoverage[(Q.slope[e] | (uint32_t)oi) & 4095u]);
+        }
+      } else {
+        uint64_t L[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          int32_t oi = x86::cvtt(off[e]);
+          oi = oi < 0 ? 0 : (oi > 63 ? 63 : oi);
+          L[e] = __ldg(&kDevCoverage[(Q.slope[e] | (uint32_t)oi) & 4095u]);
+        }
+        switch (Q.mode) {
+          case kModeTriangle0: mask = L[0] & L[1] & L[2]; break;
+          case kModeTriangle1: mask = L[0] & L[2] & L[3]; break;
+          case kModeConcaveRight: mask = (L[0] | L[3]) & (L[1] & L[2]); break;
+          case kModeConcaveCenter:
+            mask = (Q.flags & kQuadNearClip) ? ((L[0] & L[1]) | (L[2] & L[3])) : ((L[0] & L[3]) & (L[1] | L[2]));
+            break;
+          default: mask = (L[0] & L[3]) & (L[1] | L[2]); break;
+        }
+        if (!mask) continue;
+      }
+      apply_fragment(blkd, hiz, have, V.depth + (size_t)blk * 64, mask, depth, Q.Dx, Q.Dy, safe);
+    }
+  }
+  if (inView) {
+    if (clearing || have) V.hiz[blk] = (uint16_t)hiz;
+    if (have) {
+      uint4* outp = reinterpret_cast<uint4*>(V.depth + (size_t)blk * 64);
+#pragma unroll
+      for (int y = 0; y < 8; ++y)
+        outp[y] = make_uint4(blkd[4 * y], blkd[4 * y + 1], blkd[4 * y + 2], blkd[4 * y + 3]);
+    }
+  }
+  if (clearing && lt == 0 && lane < 8) V.hiz[V.blocksX * V.blocksY + lane] = 1;  // padding entries
+}
+
+// ---- k_query -------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_query(FrameParams P)
+{
+  if (P.header->overflow) return;
+  const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+  bool vis = false, nc = false;
+  if (slot < P.numQuerySlots) {
+    uint32_t lo = 0, hi = P.numViews - 1;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (P.views[mid].queryStart <= slot) lo = mid; else hi = mid - 1;
+    }
+    const ViewDesc& V = P.views[lo];
+    if (slot - V.queryStart < V.queryCount) {
+      const float4 a = P.qmin[slot], b = P.qmax[slot];
+      const float bmin[4] = {a.x, a.y, a.z, a.w}, bmax[4] = {b.x, b.y, b.z, b.w};
+      uint32_t rect[4], maxZ = 0;
+      const int st = query_front(V, bmin, bmax, rect, &maxZ);
+      if (st == 1) {
+        vis = true;
+        nc = true;
+      } else if (st == 2) {
+        vis = query2d(V, rect[0], rect[1], rect[2], rect[3], maxZ);
+      }
+    }
+  }
+  const uint32_t vb = __ballot_sync(0xFFFFFFFFu, vis), nb = __ballot_sync(0xFFFFFFFFu, nc);
+  if ((threadIdx.x & 31) == 0 && slot < P.numQuerySlots) {
+    P.visBits[slot >> 5] = vb;
+    P.ncBits[slot >> 5] = nb;
+  }
+}
+
+__global__ void k_query2d(const ViewDesc* V, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY,
+                          uint32_t maxZ, uint32_t* out)
+{
+  *out = query2d(*V, minX, maxX, minY, maxY, maxZ) ? 1u : 0u;
+}
+
+// ---- readBackDepth (Rasterizer.cpp:351-399) ---------------------------------------------
+
+__global__ void __launch_bounds__(256) k_read_back(const uint16_t* depth, const uint16_t* hiz, uint32_t width,
+                                                   uint32_t height, uint32_t blocksX, uchar4* out)
+{
+  const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t py = blockIdx.y;
+  if (px >= width || py >= height) return;
+  const uint32_t bx = px >> 3, by = py >> 3, blk = by * blocksX + bx;
+  uchar4 res = make_uchar4(0, 0, 0, 0);
+  if (hiz[blk] != 1) {
+    const uint32_t v = depth[(size_t)blk * 64 + 8 * (py & 7) + (px & 7)];
+    const float d = x86::rmul(__uint_as_float(v << 12), 3.9623753e+28f);
+    const float lin = x86::rdiv(0.5f, x86::rsub(1000.25f, x86::rmul(x86::rsub(1.0f, d), 999.75f)));
+    const float s = x86::rmul(25600.0f, lin);
+    // static_cast<uint32_t>(float) on x86-64: 64-bit truncation, low 32 bits
+    const uint32_t di = (s > -9.2233720e18f && s < 9.2233720e18f) ? (uint32_t)(unsigned long long)__float2ll_rz(s) : 0u;
+    res = make_uchar4((unsigned char)(di / 100), (unsigned char)(di % 256), 0, 255);
+  }
+  out[(size_t)py * width + px] = res;
+}
+
+// ---- launchers -------------------------------------------------------------------------
+
+cudaError_t launch_flush(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
+                         bool doQuery, cudaStream_t stream)
+{
+  if (doRaster && P.numChunks) {
+    const size_t smem = (size_t)maxStPerView * sizeof(uint32_t);
+    k_setup<<<P.numChunks, kChunk, smem, stream>>>(P);
+  }
+  if (doRaster) {
+    k_scan<<<numSt + P.numViews, 256, 0, stream>>>(P, numSt);
+    if (P.numChunks) k_fill_walk<<<P.numChunks, kChunk, 0, stream>>>(P);
+    if (P.numTiles) k_raster<<<(P.numTiles + 3) / 4, 128, 0, stream>>>(P);
+  }
+  if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
+  return cudaGetLastError();
+}
+
+// Same sequence with an event recorded before the first and after every kernel
+// (ev[0..5]); kernels that do not run still get their events.
+cudaError_t launch_flush_timed(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
+                               bool doQuery, cudaStream_t stream, cudaEvent_t* ev)
+{
+  cudaEventRecord(ev[0], stream);
+  if (doRaster && P.numChunks)
+    k_setup<<<P.numChunks, kChunk, (size_t)maxStPerView * sizeof(uint32_t), stream>>>(P);
+  cudaEventRecord(ev[1], stream);
+  if (doRaster) k_scan<<<numSt + P.numViews, 256, 0, stream>>>(P, numSt);
+  cudaEventRecord(ev[2], stream);
+  if (doRaster && P.numChunks) k_fill_walk<<<P.numChunks, kChunk, 0, stream>>>(P);
+  cudaEventRecord(ev[3], stream);
+  if (doRaster && P.numTiles) k_raster<<<(P.numTiles + 3) / 4, 128, 0, stream>>>(P);
+  cudaEventRecord(ev[4], stream);
+  if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
+  cudaEventRecord(ev[5], stream);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_read_back(const uint16_t* depth, const uint16_t* hiz, uint32_t width, uint32_t height,
+                             uchar4* out, cudaStream_t stream)
+{
+  dim3 grid((width + 255) / 256, height);
+  k_read_back<<<grid, 256, 0, stream>>>(depth, hiz, width, height, width / 8, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_query2d(const ViewDesc* view, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY,
+                           uint32_t maxZ, uint32_t* out, cudaStream_t stream)
+{
+  k_query2d<<<1, 1, 0, stream>>>(view, minX, maxX, minY, maxY, maxZ, out);
+  return cudaGetLastError();
+}
+
+cudaError_t set_setup_smem_limit(uint32_t bytes)
+{
+  return cudaFuncSetAttribute(k_setup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+}  // namespace occ

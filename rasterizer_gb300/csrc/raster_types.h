@@ -1,0 +1,139 @@
+// Data layout shared by the host launcher (capi.cu) and the kernels (kernels.cu).
+//
+// One flush rasterises the pending commands of one or more views ("rasterizer
+// targets") and then answers their queries.  Everything below is laid out for
+// a batch of views; a single view is a batch of one.
+//
+// Global quad numbering: the commands of a view are concatenated in
+// submission order (each command = one occluder = packets*2 quads); every view
+// starts at a multiple of kChunk so that setup chunk c = quad >> kChunkShift
+// belongs to exactly one view.  Padding quads are invalid.
+#pragma once
+#include <stdint.h>
+
+namespace occ {
+
+constexpr int kChunkShift = 8;
+constexpr int kChunk = 1 << kChunkShift;  // quads per setup CTA
+constexpr int kSuperTile = 32;            // binning super-tile edge, in 8x8 blocks
+constexpr int kTileW = 8;                 // warp-tile: 8 x 4 blocks, one lane per block
+constexpr int kTileH = 4;
+constexpr int kCkSpan = 8;                // row-walk checkpoint every 8 block columns (== kTileW)
+constexpr int kMaxCmdPerChunk = 40;       // commands are >= 8 quads, so <= 33 per chunk
+constexpr int kCkFloats = 12;             // 4 edge offsets + 8 depth lanes
+
+enum : uint32_t {
+  kViewClear = 1u << 0,   // hiZ := 1 before rasterising (Rasterizer::clear)
+};
+
+enum : uint32_t {
+  kCmdNearClip = 1u << 0,  // rasterize<true>
+  kCmdGated = 1u << 1,     // decide draw / near-clip on the GPU from the occluder bounds
+};
+
+enum : uint8_t {
+  kQuadNearClip = 1u << 0,
+  kQuadSafe = 1u << 1,     // depth interpolation cannot overflow: plain IEEE adds are x86-exact
+};
+
+enum : int {
+  kModeCulled = 0, kModeTriangle0, kModeTriangle1, kModeConcaveRight, kModeConcaveLeft,
+  kModeConcaveCenter, kModeConvex
+};
+
+struct ViewDesc {
+  uint16_t* depth;   // width*height u16, 8x8 blocks of 8 rows x 8 pixels, block-major
+  uint16_t* hiz;     // blocks + 8
+  uint32_t width, height, blocksX, blocksY;
+  float cols[16];    // prebaked matrix columns (Rasterizer.cpp:91-104)
+  float rows[16];    // rows of the transposed input matrix (frustum planes)
+  uint32_t cmdStart, cmdCount;
+  uint32_t chunkStart, chunkCount;      // setup chunks of this view (global indices)
+  uint32_t tileStart, tilesX, tilesY;   // warp-tiles of this view (global indices)
+  uint32_t stBase, stX, stY;            // super-tiles (global index base) and grid
+  uint32_t matBase;                     // count matrix base: stX*stY*chunkCount entries
+  uint32_t queryStart, queryCount;      // query slots; queryStart is a multiple of 32
+  uint32_t flags;
+};
+
+struct Cmd {
+  uint32_t view;
+  uint32_t wordOffset;   // first packed word of the occluder in the occluder pool
+  uint32_t quadStart;    // first global quad index
+  uint32_t quadCount;    // 2 * packet vectors
+  uint32_t flags;        // kCmdNearClip / kCmdGated
+  uint32_t pad[3];
+  float refMin[4], refMax[4];
+  float boundsMin[4], boundsMax[4];
+};
+
+struct Chunk {
+  uint32_t view;
+  uint32_t localIndex;   // chunk index within its view
+  uint32_t quadCount;    // real quads in this chunk (the rest is padding)
+  uint32_t cmdFirst;     // first command overlapping the chunk
+  uint32_t cmdCount;     // commands overlapping the chunk
+  uint32_t pad[3];
+};
+
+// Per-quad setup output read by the rasteriser (48 bytes).
+struct QuadRaster {
+  uint16_t minX, minY, maxX, maxY;  // block bbox [min, max); minX == maxX marks an invalid quad
+  uint16_t maxZ;                    // packed 16-bit nearest depth bound
+  uint8_t mode, flags;
+  uint32_t ckLocal;                 // checkpoint offset within the chunk
+  float Dx, Dy;                     // depth plane gradient per block
+  uint16_t slope[4];                // slope part of the table index, per edge
+  float nx[4];                      // normalised edge x coefficients
+};
+
+// Per-quad setup output read by the row walk (48 bytes).
+struct QuadWalk {
+  float plane0;     // depth at the bbox origin
+  float off[4];     // edge offsets at the bbox origin (quantisation units)
+  float ny[4];      // normalised edge y coefficients
+  uint32_t rowLocal; // first row of this quad within the chunk's row numbering
+  uint32_t pad[2];
+};
+
+struct Totals {
+  uint32_t rows, cks, st, pad;
+};
+
+// Device-side frame header: totals, capacities and status.
+struct FrameHeader {
+  uint32_t totalRows, totalCks, totalSt, overflow;
+  uint32_t capCks, capSt, viewsDone, sticky;  // sticky: overflow seen since the last check
+  uint32_t maxCks, maxSt, pad[2];              // largest totals seen since the last check
+};
+
+struct FrameParams {
+  const ViewDesc* views;
+  uint32_t numViews;
+  const Cmd* cmds;
+  const Chunk* chunks;
+  uint32_t numChunks;
+  uint32_t numTiles;     // warp-tiles over all views
+  uint32_t numQuerySlots;
+  const uint32_t* pool;  // packed occluder words
+  QuadRaster* rec;
+  QuadWalk* walk;
+  Totals* chunkTot;      // per chunk totals (rows, cks)
+  Totals* chunkBase;     // per chunk exclusive prefix within the view
+  uint32_t* mat;         // super-tile x chunk counts -> exclusive prefixes (per view, st-major)
+  uint32_t* stStart;     // per global super-tile: list start (global)
+  uint32_t* stLen;
+  Totals* viewTot;
+  Totals* viewBase;
+  uint32_t* viewChunksDone;
+  uint32_t* stList;      // global quad indices, per super-tile, submission order
+  float* ck;             // row-walk checkpoints, kCkFloats floats each
+  FrameHeader* header;
+  const float4* qmin;    // query boxes per slot
+  const float4* qmax;
+  uint32_t* visBits;     // one bit per query slot
+  uint32_t* ncBits;
+  uint32_t* cmdDraw;     // per command: bit0 drawn, bit1 near-clipped (gated result)
+};
+
+}  // namespace occ

@@ -1,0 +1,216 @@
+"""GPU parity: the CUDA rasteriser against the CPU oracle, bit for bit.
+
+Depth (raw, stale blocks included), hiZ, per-occluder gating flags, visibility
+and needs-clipping bits, and readBackDepth must all match exactly.
+"""
+import numpy as np
+import pytest
+
+from rasterizer_gb300 import api, scenes
+from oracle.bindings import Oracle
+
+from helpers import boxes_occluders, city_occluders, gpu_plain_frame, mismatch_report, to_baked
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = api.Context(0)
+    yield c
+    c.close()
+
+
+def _compare(r: api.Rasterizer, orc: Oracle, what=("depth", "hiz", "readback")):
+    errs = []
+    if "depth" in what:
+        errs.append(mismatch_report("depth", r.readDepthRaw(), orc.depth()))
+    if "hiz" in what:
+        errs.append(mismatch_report("hiz", r.readHiZ(), orc.hiz()))
+    if "readback" in what:
+        errs.append(mismatch_report("readback", r.readBackDepth().ravel(), orc.read_back()))
+    errs = [e for e in errs if e]
+    assert not errs, "; ".join(errs)
+
+
+def test_boxes_scene_1080p(ctx):
+    """Plain method, single view, 1920x1080, 64 boxes + ground, 4096 queries."""
+    occ = boxes_occluders()
+    scene = to_baked(occ)
+    mvp = scenes.boxes_camera()
+    mins, maxs = scenes.query_boxes(4096, seed=43)
+    r = api.Rasterizer(ctx, 1920, 1080)
+    flags = gpu_plain_frame(r, occ, mvp)
+    vis, nc = r.queryVisibilityBatch(mins, maxs)
+    orc = Oracle(1920, 1080)
+    oflags = orc.frame_plain(scene, mvp)
+    ovis, onc = orc.query(mins, maxs)
+    assert np.array_equal(flags, oflags)
+    _compare(r, orc)
+    assert not mismatch_report("visible", vis.astype(np.uint8), ovis)
+    assert not mismatch_report("needsClipping", nc.astype(np.uint8), onc)
+    assert vis.sum() > 0 and (~vis).sum() > 0
+
+
+@pytest.mark.parametrize("near_clip", [0, 1])
+def test_explicit_variants(ctx, near_clip):
+    """rasterize<false> and rasterize<true> forced for every occluder."""
+    occ = boxes_occluders()
+    scene = to_baked(occ)
+    mvp = scenes.view_projection((5.0, 3.0, -40.0), (0.1, -0.15, 1.0))
+    r = api.Rasterizer(ctx, 640, 360)
+    orc = Oracle(640, 360)
+    r.clear()
+    orc.clear()
+    r.setModelViewProjection(mvp)
+    orc.set_mvp(mvp)
+    for o, k in zip(occ, range(len(scene))):
+        r.rasterize(o, bool(near_clip))
+        orc.rasterize(scene.packed[k], scene.packets[k], scene.ref[k, :4], scene.ref[k, 4:], bool(near_clip))
+    _compare(r, orc)
+
+
+def test_city_camera_path(ctx):
+    """Dense city, persistent rasterizer across frames of a street-level path
+    (stale depth in cleared blocks is part of the compared state)."""
+    occ = city_occluders()
+    scene = to_baked(occ)
+    mvps, _ = scenes.camera_path(300, seed=7)
+    mins, maxs = scenes.query_boxes(20000, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    r = api.Rasterizer(ctx, 1920, 1080)
+    orc = Oracle(1920, 1080)
+    near_clipped = 0
+    for f in range(0, 300, 20):
+        flags = gpu_plain_frame(r, occ, mvps[f])
+        oflags = orc.frame_plain(scene, mvps[f])
+        assert np.array_equal(flags, oflags), f"frame {f}"
+        near_clipped += int(((flags & 3) == 3).sum())
+        vis, nc = r.queryVisibilityBatch(mins, maxs)
+        ovis, onc = orc.query(mins, maxs)
+        assert not mismatch_report(f"frame {f} visible", vis.astype(np.uint8), ovis)
+        assert not mismatch_report(f"frame {f} needsClipping", nc.astype(np.uint8), onc)
+        _compare(r, orc, ("depth", "hiz"))
+    assert near_clipped > 0
+
+
+@pytest.mark.parametrize("size", [(8, 8), (264, 136), (1032, 520)])
+def test_odd_sizes(ctx, size):
+    """Views whose block grid is not a multiple of the warp-tile or super-tile."""
+    w, h = size
+    occ = boxes_occluders()
+    scene = to_baked(occ)
+    mvp = scenes.view_projection((0.0, 4.0, -30.0), (0.05, -0.1, 1.0), aspect=w / h)
+    r = api.Rasterizer(ctx, w, h)
+    orc = Oracle(w, h)
+    flags = gpu_plain_frame(r, occ, mvp)
+    oflags = orc.frame_plain(scene, mvp)
+    assert np.array_equal(flags, oflags)
+    _compare(r, orc)
+    mins, maxs = scenes.query_boxes(2000, seed=9)
+    vis, nc = r.queryVisibilityBatch(mins, maxs)
+    ovis, onc = orc.query(mins, maxs)
+    assert np.array_equal(vis.astype(np.uint8), ovis) and np.array_equal(nc.astype(np.uint8), onc)
+
+
+def test_stale_state_without_clear(ctx):
+    """Seeded depth and hiZ (values 0..65535, including the cleared marker 1)
+    and no clear: merging against memory and the hiZ == 1 overwrite rule."""
+    rng = np.random.default_rng(5)
+    w, h = 320, 200
+    occ = boxes_occluders()
+    scene = to_baked(occ)
+    depth = rng.integers(0, 65536, w * h, dtype=np.uint16)
+    hiz = rng.choice(np.array([0, 1, 2, 500, 30000, 65535], np.uint16), (w // 8) * (h // 8) + 8)
+    r = api.Rasterizer(ctx, w, h)
+    orc = Oracle(w, h)
+    r.writeDepthRaw(depth)
+    r.writeHiZ(hiz)
+    orc.write_depth(depth)
+    orc.write_hiz(hiz)
+    mvp = scenes.view_projection((0.0, 2.0, -25.0), (0.0, 0.0, 1.0), aspect=w / h)
+    r.setModelViewProjection(mvp)
+    orc.set_mvp(mvp)
+    for k, o in enumerate(occ):
+        r.rasterize(o, False)
+        orc.rasterize(scene.packed[k], scene.packets[k], scene.ref[k, :4], scene.ref[k, 4:], False)
+    _compare(r, orc)
+    mins, maxs = scenes.query_boxes(3000, seed=10)
+    vis, nc = r.queryVisibilityBatch(mins, maxs)
+    ovis, onc = orc.query(mins, maxs)
+    assert np.array_equal(vis.astype(np.uint8), ovis) and np.array_equal(nc.astype(np.uint8), onc)
+
+
+def test_query_only_and_query2d(ctx):
+    occ = boxes_occluders()
+    scene = to_baked(occ)
+    r = api.Rasterizer(ctx, 640, 480)
+    orc = Oracle(640, 480)
+    mvp = scenes.view_projection((0.0, 1.7, -60.0), (0.0, 0.0, 1.0), aspect=640 / 480)
+    gpu_plain_frame(r, occ, mvp)
+    orc.frame_plain(scene, mvp)
+    rng = np.random.default_rng(3)
+    for _ in range(40):
+        x0, x1 = sorted(rng.integers(0, 640, 2))
+        y0, y1 = sorted(rng.integers(0, 480, 2))
+        z = int(rng.integers(0, 65536))
+        assert r.query2D(x0, x1, y0, y1, z) == bool(orc.lib.orc_query2d(orc.h, x0, x1, y0, y1, z))
+
+
+def test_4k_view_full_block_index(ctx):
+    """3840x2160 (129,600 blocks): the GPU uses the full 32-bit block index;
+    the oracle is run with the same correction of Rasterizer.cpp:1054."""
+    occ = boxes_occluders()
+    scene = to_baked(occ)
+    mvp = scenes.boxes_camera(3840, 2160)
+    r = api.Rasterizer(ctx, 3840, 2160)
+    orc = Oracle(3840, 2160)
+    orc.set_block_index_wrap(False)
+    gpu_plain_frame(r, occ, mvp)
+    orc.frame_plain(scene, mvp)
+    _compare(r, orc, ("depth", "hiz"))
+
+
+def test_batched_views_match_single_views(ctx):
+    """Several views of uneven size in one batch == each view on the oracle."""
+    occ = boxes_occluders()
+    scene = to_baked(occ)
+    sizes = [(1024, 1024), (512, 512), (256, 128), (1920, 1080), (640, 360)]
+    views, oracles = [], []
+    for i, (w, h) in enumerate(sizes):
+        ang = 0.4 * i
+        mvp = scenes.view_projection((40 * np.sin(ang), 2.0 + i, -40 * np.cos(ang)),
+                                     (-np.sin(ang), -0.05, np.cos(ang)), aspect=w / h)
+        mins, maxs = scenes.query_boxes(1000 + 300 * i, seed=100 + i)
+        r = api.Rasterizer(ctx, w, h)
+        views.append(dict(raster=r, mvp=mvp, clear=True, occluders=occ, flags=np.full(len(occ), 2, np.uint8),
+                          mins=mins, maxs=maxs))
+        orc = Oracle(w, h)
+        orc.frame_plain(scene, mvp)
+        oracles.append((orc, orc.query(mins, maxs)))
+    res = api.execute_batch(ctx, views)
+    for v, (orc, (ovis, onc)) in zip(views, oracles):
+        _compare(v["raster"], orc, ("depth", "hiz"))
+    for (vis, nc), (orc, (ovis, onc)) in zip(res, oracles):
+        assert np.array_equal(vis.astype(np.uint8), ovis) and np.array_equal(nc.astype(np.uint8), onc)
+
+
+def test_prepared_batch_graph(ctx):
+    """CUDA-graph launches with a changing matrix reproduce the oracle."""
+    occ = boxes_occluders()
+    scene = to_baked(occ)
+    mins, maxs = scenes.query_boxes(4096, seed=43)
+    r = api.Rasterizer(ctx, 1920, 1080)
+    mvps = [scenes.view_projection((x, 1.7, -60.0), (0.0, 0.0, 1.0)) for x in (0.0, 10.0, -20.0)]
+    b = api.PreparedBatch(ctx, [dict(raster=r, mvp=mvps[0], clear=True, occluders=occ,
+                                     flags=np.full(len(occ), 2, np.uint8), mins=mins, maxs=maxs)])
+    orc = Oracle(1920, 1080)
+    for m in mvps:
+        b.setModelViewProjection(0, m)
+        b.launch()
+        assert b.check()
+        vis, nc = b.results(0)
+        orc.frame_plain(scene, m)
+        ovis, onc = orc.query(mins, maxs)
+        assert np.array_equal(vis.astype(np.uint8), ovis) and np.array_equal(nc.astype(np.uint8), onc)
+        _compare(r, orc, ("depth", "hiz"))
+    b.close()
