@@ -1,0 +1,396 @@
+"""Benchmark: views/s of the plain all-occluder path on one GB300.
+
+Workload (the dense-city configuration): a seeded 64x64 grid of extruded
+buildings, 259,534 triangles baked by the library into 386 occluders (129,768
+quads), rendered at 1920x1080 along a seeded 300-frame street-level camera
+path; every frame clears, gates all occluders on the GPU from their bounds
+(queryVisibility on an empty buffer, as the plain loop does), rasterises the
+visible ones and answers 100,000 query boxes (lognormal extents).  One step =
+one frame = one view.  The rasterizer persists across frames (stale depth in
+cleared blocks, as in the reference).
+
+  value    device time of the frame's kernels (CUDA events on the library's
+           stream, inputs resident in HBM, L2 flushed between steps);
+  e2e      the same frames through the reference-facing API with host
+           buffers: clear / setModelViewProjection / rasterize (gated) /
+           queryVisibility batch, host->device and device->host copies inside;
+  cpu_baseline  the CPU oracle (portable restatement of the reference) on one
+           host core, on a bounded sample of the same frames.
+
+--impl reference times the reference's CPU algorithm (the oracle port: the
+reference's AVX2 build cannot run on the Arm host) with all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "views/sec @1080p: plain vs batched+learned on 1 GB300; culls kept vs full, 0 false"
+W, H = 1920, 1080
+NQ = 100_000
+FRAMES = 300
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload():
+    from rasterizer_gb300 import scenes
+    mesh = scenes.city_scene()
+    mvps, eyes = scenes.camera_path(FRAMES, seed=7)
+    mins, maxs = scenes.query_boxes(NQ, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    return mesh, mvps, mins, maxs
+
+
+def workload_desc(mesh, occ):
+    quads = sum(o.quads for o in occ)
+    return (f"dense city 64x64 buildings ({mesh.triangles} tris -> {quads} quads in {len(occ)} occluders), "
+            f"{W}x{H}, {FRAMES}-frame seeded street-level camera path, {NQ} lognormal query boxes per frame, "
+            f"plain all-occluder loop gated on the GPU")
+
+
+# ---- clocks -------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.tmp = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                       "-lms", "100"], stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.tmp.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.tmp.read().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9 or f[0] != str(self.device):
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.tmp.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---- CPU legs -------------------------------------------------------------------------
+
+_CPU_STATE = None
+
+
+def _cpu_state():
+    """Per-process CPU oracle state: the baked city, the path, the queries and
+    one persistent Oracle rasterizer (built once per process)."""
+    global _CPU_STATE
+    if _CPU_STATE is None:
+        sys.path.insert(0, ROOT)
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from oracle.bindings import Oracle
+        from helpers import city_occluders, to_baked
+        from rasterizer_gb300 import scenes
+        scene = to_baked(city_occluders())
+        mvps, _ = scenes.camera_path(FRAMES, seed=7)
+        mins, maxs = scenes.query_boxes(NQ, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+        _CPU_STATE = (scene, mvps, mins, maxs, Oracle(W, H))
+    return _CPU_STATE
+
+
+def _cpu_frame(f: int) -> int:
+    """One frame (plain loop + all queries) on the CPU oracle."""
+    scene, mvps, mins, maxs, orc = _cpu_state()
+    orc.frame_plain(scene, mvps[f % FRAMES])
+    orc.query(mins, maxs)
+    return 1
+
+
+def cpu_baseline(budget_s: float = 12.0, max_frames: int = 60):
+    _cpu_state()
+    _cpu_frame(0)  # warm-up
+    done, t0 = 0, time.perf_counter()
+    while done < max_frames and time.perf_counter() - t0 < budget_s:
+        _cpu_frame(done)
+        done += 1
+    secs = time.perf_counter() - t0
+    return {"value": done / secs, "unit": "views/s", "cores": 1, "kind": "port",
+            "sample": f"{done} frames of the same workload (frames 0..{done - 1} of the path, with all "
+                      f"{NQ} queries each), 1 host thread, CPU oracle (portable restatement; the "
+                      f"reference's AVX2 build does not run on the Arm host)"}
+
+
+def _warm(_):
+    _cpu_frame(0)
+    return 0
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm on all host cores (oracle port),
+    one frame per step, steps spread over one process per core."""
+    import multiprocessing as mp
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import bindings
+    bindings.build_oracle()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_warm, range(cores), chunksize=1)
+        pool.map(_cpu_frame, range(args.warmup * cores), chunksize=1)
+        t0 = time.perf_counter()
+        total = sum(pool.map(_cpu_frame, range(args.steps), chunksize=1))
+        dt = time.perf_counter() - t0
+    value = total / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "views/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/u16",
+            "data": "synthetic",
+            "config": {"workload": "dense city 64x64 buildings (259,534 tris), 1920x1080, 300-frame street path, "
+                                   "100k lognormal query boxes per frame, plain all-occluder loop"},
+            "cpu_baseline": {"value": value, "unit": "views/s", "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} frames (one per step, {cores} worker processes, each with "
+                                       f"its own persistent rasterizer); CPU oracle, because the reference's "
+                                       f"AVX2 build cannot run on aarch64"},
+            "e2e": {"value": value, "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---- GPU leg --------------------------------------------------------------------------
+
+def algorithmic_bytes(q_setup: int, nq: int):
+    """Per-launch algorithmic bytes: packed quads read (16 B/quad), depth
+    written once (2 B/pixel), hiZ cleared and written (2+2 B/block), query
+    boxes read (32 B) and two result bits written per query."""
+    blocks = (W // 8) * (H // 8)
+    return {
+        "k_setup": 16 * q_setup,
+        "k_raster": 2 * W * H + 4 * blocks,
+        "k_query": 32 * nq + nq // 4,
+        "frame": 16 * q_setup + 2 * W * H + 4 * blocks + 32 * nq + nq // 4,
+    }
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    # CPU baseline first (rank 0, N=1 only), before any GPU work
+    cpu = cpu_baseline() if (rank == 0 and world == 1 and not args.no_cpu) else None
+
+    from rasterizer_gb300 import api
+    mesh, mvps, mins, maxs = workload()
+    occ = api.bake_scene(mesh.vertices, mesh.indices)
+    ctx = api.Context(local)
+    r = api.Rasterizer(ctx, W, H)
+    flags = np.full(len(occ), 2, np.uint8)  # OCC_GATED
+    batch = api.PreparedBatch(ctx, [dict(raster=r, mvp=mvps[0], clear=True, occluders=occ, flags=flags,
+                                         mins=mins, maxs=maxs)])
+    # size the scratch for every frame of the path
+    for attempt in range(3):
+        for f in range(FRAMES):
+            batch.setModelViewProjection(0, mvps[f])
+            batch.launch()
+        if batch.check():
+            break
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+
+    def flush_l2(i):
+        with torch.cuda.stream(stream):
+            flush.fill_(i)
+
+    for i in range(args.warmup):
+        batch.setModelViewProjection(0, mvps[i % FRAMES])
+        batch.launch()
+        flush_l2(i)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local) if rank == 0 else None
+    time.sleep(0.3 if sampler else 0)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        batch.setModelViewProjection(0, mvps[i % FRAMES])
+        starts[i].record(stream)
+        batch.launch()
+        ends[i].record(stream)
+        flush_l2(i)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if world > 1:
+        dist.barrier()
+    clocks = sampler.stop() if sampler else None
+    ok = batch.check()
+    dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    t_max = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+    dev_ms = float(t_max.item())
+
+    # per-kernel device times (kernel by kernel, events in between, same stream)
+    prof = batch.profile(min(args.steps, 300))
+    names = ["k_setup", "k_scan", "k_fill_walk", "k_raster", "k_query"]
+    kern = {n: float(v) for n, v in zip(names, prof)}
+    top = max(kern, key=kern.get)
+    q_setup = sum(o.quads for o in occ)
+    alg = algorithmic_bytes(q_setup, NQ)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_note = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peak, peak_note = float(json.load(f)["hbm_gbs"]), "measured"
+    traffic = load_traffic()
+    roof_kernel = top if top in alg else "k_query"
+    achieved = alg[roof_kernel] / (kern[roof_kernel] * 1e-3) / 1e9
+    frame_ms = sum(kern.values())
+
+    # end to end through the reference-facing API with host buffers
+    e2e_steps = max(10, min(args.steps // 10, 100))
+    for i in range(3):
+        r.clear()
+        r.setModelViewProjection(mvps[i])
+        r.rasterizeMany(occ, flags)
+        r.queryVisibilityBatch(mins, maxs)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for i in range(e2e_steps):
+        r.clear()
+        r.setModelViewProjection(mvps[i % FRAMES])
+        r.rasterizeMany(occ, flags)
+        r.queryVisibilityBatch(mins, maxs)
+    e2e_s = time.perf_counter() - t1
+    n_chunks = sum((o.quads + 255) // 256 for o in occ)  # upper bound of the chunk table
+    h2d = NQ * 32 + 216 + 96 * len(occ) + 32 * ((q_setup + 255) // 256) + 12
+    d2h = 2 * 4 * ((NQ + 31) // 32) + 4 * len(occ) + 48
+    del n_chunks
+
+    value = world * args.steps / (dev_ms * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "views/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32/u16", "data": "synthetic",
+        "config": {"workload": workload_desc(mesh, occ), "resolution": f"{W}x{H}", "queries_per_view": NQ,
+                   "occluders": len(occ), "quads": q_setup, "l2": "flushed between steps (256 MB write, outside "
+                   "the timed events)", "timing": "CUDA events on the library stream around each frame's graph "
+                   "launch; max over ranks", "parallelism": f"replicas x{world}"},
+        "queries_per_s": value * NQ,
+        "wall_views_per_s": world * args.steps / wall,
+        "kernels_ms": kern,
+        "roofline": {"bound": "hbm", "kernel": roof_kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_note,
+                     "traffic": traffic.get(roof_kernel), "algorithmic_bytes": alg[roof_kernel],
+                     "frame_achieved": alg["frame"] / (frame_ms * 1e-3) / 1e9},
+        "e2e": {"value": world * e2e_steps / e2e_s, "unit": "views/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "path": "Rasterizer.clear/setModelViewProjection/rasterizeMany(gated)/queryVisibilityBatch "
+                        "(Python mirror -> C ABI), host numpy buffers, wall clock"},
+        "gpu_launches": 5 * args.steps,
+        "clocks": clocks,
+        "capacity_ok": bool(ok),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    batch.close()
+    r.close()
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_profile_frames(frames: int, start: int = 0):
+    """A short GPU-only run for profilers: prepare the batch, then `frames`
+    graph launches along the camera path (no CPU leg, no timing)."""
+    from rasterizer_gb300 import api
+    mesh, mvps, mins, maxs = workload()
+    occ = api.bake_scene(mesh.vertices, mesh.indices)
+    ctx = api.Context(0)
+    r = api.Rasterizer(ctx, W, H)
+    flags = np.full(len(occ), 2, np.uint8)
+    batch = api.PreparedBatch(ctx, [dict(raster=r, mvp=mvps[start], clear=True, occluders=occ, flags=flags,
+                                         mins=mins, maxs=maxs)])
+    for f in range(frames):
+        batch.setModelViewProjection(0, mvps[(start + f) % FRAMES])
+        batch.launch()
+    ok = batch.check()
+    vis, _ = batch.results(0)
+    print(json.dumps({"frames": frames, "capacity_ok": ok, "visible_last": int(vis.sum())}), flush=True)
+    batch.close()
+    r.close()
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--profile-run", type=int, default=0, metavar="FRAMES",
+                    help="only launch FRAMES frames (for ncu); prints a status line")
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=30)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.profile_run:
+        run_profile_frames(args.profile_run)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()
