@@ -71,6 +71,8 @@ def oracle_lib():
         lib.orc_write_hiz.argtypes = [P, P]
         lib.orc_read_counters.argtypes = [P, P]
         lib.orc_frame_plain.argtypes = [P, U32, P, P, P, P, P, P]
+        lib.orc_setup_dump.restype = U32
+        lib.orc_setup_dump.argtypes = [P, P, U32, P, P, C.c_int, P]
         _oracle_lib = lib
     return _oracle_lib
 
@@ -218,6 +220,14 @@ class Oracle:
         c = np.zeros(5, np.uint64)
         self.lib.orc_read_counters(self.h, _ptr(c))
         return c
+
+    def setup_dump(self, packed, packets, ref_min, ref_max, near_clip: bool) -> np.ndarray:
+        """(n, 6) int32: minX, minY, maxX, maxY, maxZ, mode of each valid quad."""
+        out = np.zeros((int(packets) * 2, 6), np.int32)
+        n = self.lib.orc_setup_dump(self.h, _ptr(packed), int(packets),
+                                    _ptr(np.ascontiguousarray(ref_min, np.float32)),
+                                    _ptr(np.ascontiguousarray(ref_max, np.float32)), int(near_clip), _ptr(out))
+        return out[:n]
 
     def frame_plain(self, scene: BakedScene, mvp, order=None):
         idx = np.arange(len(scene)) if order is None else np.asarray(order)

@@ -581,6 +581,28 @@ static void quad_raster(orc_raster* r, const QuadSetup* s, int nc)
   }
 }
 
+/* Setup of every quad of one occluder without rasterising (statistics for the
+ * tests and benchmarks): per valid quad minX, minY, maxX, maxY (blocks,
+ * [min, max)), maxZ, mode.  Returns the number of valid quads written. */
+uint32_t orc_setup_dump(orc_raster* r, const uint32_t* packed, uint32_t packetCount, const float* refMin,
+                        const float* refMax, int nearClip, int32_t* out6)
+{
+  float rows[4][4], c0, c1;
+  occluder_prologue(r, refMin, refMax, rows, &c0, &c1);
+  uint32_t n = 0;
+  for (uint32_t p = 0; p + 4 <= packetCount; p += 4) {
+    const uint32_t* base = packed + (size_t)p * 8;
+    for (int q = 0; q < 8; ++q) {
+      uint32_t w4[4] = {base[q], base[8 + q], base[16 + q], base[24 + q]};
+      QuadSetup s;
+      if (!quad_setup(r, w4, rows, c0, c1, nearClip, &s)) continue;
+      int32_t* o = out6 + 6 * n++;
+      o[0] = s.minX; o[1] = s.minY; o[2] = s.minX + s.rangeX; o[3] = s.minY + s.rangeY; o[4] = s.maxZ; o[5] = s.mode;
+    }
+  }
+  return n;
+}
+
 void orc_rasterize(orc_raster* r, const uint32_t* packed, uint32_t packetCount, const float* refMin,
                    const float* refMax, int nearClip)
 {

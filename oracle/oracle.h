@@ -40,6 +40,9 @@ void orc_clear(orc_raster* r);                              /* Rasterizer.cpp:10
 void orc_rasterize(orc_raster* r, const uint32_t* packed, uint32_t packetCount,
                    const float* refMin, const float* refMax, int nearClip);
 
+uint32_t orc_setup_dump(orc_raster* r, const uint32_t* packed, uint32_t packetCount, const float* refMin,
+                        const float* refMax, int nearClip, int32_t* out6);
+
 int orc_query(orc_raster* r, const float* bmin, const float* bmax, int* needsClipping); /* :123-281 */
 int orc_query2d(const orc_raster* r, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY,
                 uint32_t maxZ);                                                         /* :283-349 */

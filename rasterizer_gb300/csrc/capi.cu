@@ -24,6 +24,9 @@ cudaError_t launch_read_back(const uint16_t* depth, const uint16_t* hiz, uint32_
                              uchar4* out, cudaStream_t stream);
 cudaError_t launch_flush_timed(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
                                bool doQuery, cudaStream_t stream, cudaEvent_t* ev);
+cudaError_t set_kernel_attributes();
+cudaError_t launch_tile_hiz(const uint16_t* hiz, uint16_t* tileHiz, uint32_t blocksX, uint32_t blocksY,
+                            cudaStream_t stream);
 cudaError_t launch_query2d(const ViewDesc* view, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY,
                            uint32_t maxZ, uint32_t* out, cudaStream_t stream);
 }  // namespace occ
@@ -128,7 +131,8 @@ struct FrameScratch {
   DevBuf<QuadRaster> rec;
   DevBuf<QuadWalk> walk;
   DevBuf<Totals> chunkTot, chunkBase, viewTot, viewBase;
-  DevBuf<uint32_t> mat, stStart, stLen, stList, cmdDraw;
+  DevBuf<uint32_t> mat, stStart, stLen, cmdDraw, ckBase;
+  DevBuf<uint4> stList;
   DevBuf<float> ck;
   DevBuf<FrameHeader> header;
   DevBuf<float4> qmin, qmax;
@@ -156,7 +160,7 @@ struct occ_ctx_s {
 struct occ_raster_s {
   occ_ctx_s* ctx = nullptr;
   uint32_t width = 0, height = 0, blocksX = 0, blocksY = 0;
-  DevBuf<uint16_t> depth, hiz;
+  DevBuf<uint16_t> depth, hiz, tileHiz;
   float cols[16] = {};
   float rows[16] = {};
   bool clearPending = false;
@@ -222,6 +226,7 @@ int build_layout(occ_ctx_s* ctx, const std::vector<ViewJob>& jobs, BatchLayout& 
     ViewDesc V{};
     V.depth = r->depth.p;
     V.hiz = r->hiz.p;
+    V.tileHiz = r->tileHiz.p;
     V.width = r->width;
     V.height = r->height;
     V.blocksX = r->blocksX;
@@ -337,6 +342,7 @@ int run_batch(occ_ctx_s* ctx, FrameScratch& S, std::vector<ViewJob>& jobs, bool 
   OCC_CHECK(S.tables.reserve(tablesBytes));
   OCC_CHECK(S.rec.reserve(L.totalQuads));
   OCC_CHECK(S.walk.reserve(L.totalQuads));
+  OCC_CHECK(S.ckBase.reserve(L.totalQuads));
   OCC_CHECK(S.chunkTot.reserve(L.chunks.size()));
   OCC_CHECK(S.chunkBase.reserve(L.chunks.size()));
   OCC_CHECK(S.viewTot.reserve(nv));
@@ -393,6 +399,7 @@ int run_batch(occ_ctx_s* ctx, FrameScratch& S, std::vector<ViewJob>& jobs, bool 
     P.pool = ctx->pool.p;
     P.rec = S.rec.p;
     P.walk = S.walk.p;
+    P.ckBase = S.ckBase.p;
     P.chunkTot = S.chunkTot.p;
     P.chunkBase = S.chunkBase.p;
     P.mat = S.mat.p;
@@ -493,6 +500,7 @@ int occ_ctx_create(int device, occ_ctx* out)
   auto ctx = std::make_unique<occ_ctx_s>();
   ctx->device = device;
   OCC_CUDA(cudaSetDevice(device));
+  OCC_CUDA(set_kernel_attributes());
   OCC_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   OCC_CUDA(cudaEventCreateWithFlags(&ctx->stageFree, cudaEventDisableTiming));
   OCC_CUDA(cudaEventRecord(ctx->stageFree, ctx->stream));
@@ -568,6 +576,8 @@ int occ_raster_create(occ_ctx ctx, uint32_t width, uint32_t height, occ_raster* 
   if (width == 0 || height == 0 || width % 8 || height % 8)
     return fail(OCC_ERR_INVALID_ARG, "width and height must be positive multiples of 8");
   if (width > 65528 || height > 65528) return fail(OCC_ERR_INVALID_ARG, "width/height above 65528");
+  if ((size_t)div_up(width / 8, kSuperTile) * div_up(height / 8, kSuperTile) > (size_t)kMaxStPerView)
+    return fail(OCC_ERR_UNSUPPORTED, "view too large: more than 3072 binning super-tiles (128x128 pixels each)");
   auto r = std::make_unique<occ_raster_s>();
   r->ctx = ctx;
   r->width = width;
@@ -577,9 +587,12 @@ int occ_raster_create(occ_ctx ctx, uint32_t width, uint32_t height, occ_raster* 
   const size_t blocks = (size_t)r->blocksX * r->blocksY;
   OCC_CHECK(r->depth.reserve((size_t)width * height));
   OCC_CHECK(r->hiz.reserve(blocks + 8));
+  const size_t tiles = (size_t)div_up(r->blocksX, kTileW) * div_up(r->blocksY, kTileH);
+  OCC_CHECK(r->tileHiz.reserve(tiles));
   // the reference value-initialises both (Rasterizer.cpp:70-71)
   OCC_CUDA(cudaMemsetAsync(r->depth.p, 0, (size_t)width * height * 2, ctx->stream));
   OCC_CUDA(cudaMemsetAsync(r->hiz.p, 0, (blocks + 8) * 2, ctx->stream));
+  OCC_CUDA(cudaMemsetAsync(r->tileHiz.p, 0, tiles * 2, ctx->stream));
   OCC_CUDA(cudaStreamSynchronize(ctx->stream));
   *out = r.release();
   return OCC_OK;
@@ -690,6 +703,7 @@ int occ_raster_query2d(occ_raster r, uint32_t minX, uint32_t maxX, uint32_t minY
   ViewDesc V{};
   V.depth = r->depth.p;
   V.hiz = r->hiz.p;
+  V.tileHiz = r->tileHiz.p;
   V.width = r->width;
   V.height = r->height;
   V.blocksX = r->blocksX;
@@ -755,6 +769,7 @@ int occ_raster_write_hiz(occ_raster r, const uint16_t* in)
   OCC_CHECK(flush_raster(r, nullptr));
   const uint32_t n = r->blocksX * r->blocksY + 8;
   OCC_CUDA(cudaMemcpyAsync(r->hiz.p, in, (size_t)n * 2, cudaMemcpyHostToDevice, r->ctx->stream));
+  OCC_CUDA(launch_tile_hiz(r->hiz.p, r->tileHiz.p, r->blocksX, r->blocksY, r->ctx->stream));
   OCC_CUDA(cudaStreamSynchronize(r->ctx->stream));
   return OCC_OK;
 }
@@ -879,6 +894,7 @@ int capture(occ_batch_s* b)
   P.pool = ctx->pool.p;
   P.rec = S.rec.p;
   P.walk = S.walk.p;
+  P.ckBase = S.ckBase.p;
   P.chunkTot = S.chunkTot.p;
   P.chunkBase = S.chunkBase.p;
   P.mat = S.mat.p;

@@ -238,17 +238,25 @@ __device__ int query_front(const ViewDesc& V, const float* bmin, const float* bm
   return 2;
 }
 
-// query2D (Rasterizer.cpp:283-349)
-__device__ bool query2d(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ)
+// query2D (Rasterizer.cpp:283-349), split by warp-tile.  The reference skips
+// every block whose hiZ >= maxZ; a warp-tile whose minimum hiZ is >= maxZ is
+// skipped as a whole, which skips exactly the same blocks.  The result is the
+// OR over blocks, so tiles and blocks may be visited in any order.
+
+// Blocks of tile (tx, ty) inside the block rectangle [bx0,bx1]x[by0,by1].
+__device__ bool query2d_tile(const ViewDesc& V, uint32_t tx, uint32_t ty, uint32_t minX, uint32_t maxX,
+                             uint32_t minY, uint32_t maxY, uint32_t maxZ)
 {
   const uint32_t bx0 = minX >> 3, bx1 = maxX >> 3, by0 = minY >> 3, by1 = maxY >> 3;
-  for (uint32_t by = by0; by <= by1; ++by) {
+  const uint32_t ya = ::max(by0, ty * kTileH), yb = ::min(by1, ty * kTileH + kTileH - 1);
+  const uint32_t xa = ::max(bx0, tx * kTileW), xb = ::min(bx1, tx * kTileW + kTileW - 1);
+  for (uint32_t by = ya; by <= yb; ++by) {
     int32_t sy = (int32_t)(minY - 8 * by);
     sy = sy < 0 ? 0 : sy;
     int32_t ey = (int32_t)(maxY - 8 * by);
     ey = ey > 7 ? 7 : ey;
     const bool interiorLine = sy == 0 && ey == 7;
-    for (uint32_t bx = bx0; bx <= bx1; ++bx) {
+    for (uint32_t bx = xa; bx <= xb; ++bx) {
       const uint32_t blk = by * V.blocksX + bx;
       if (maxZ <= (uint32_t)V.hiz[blk]) continue;
       int32_t sx = (int32_t)(minX - bx * 8);
@@ -268,6 +276,19 @@ __device__ bool query2d(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_
       }
     }
   }
+  return false;
+}
+
+__device__ bool query2d(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ)
+{
+  const uint32_t tilesX = (V.blocksX + kTileW - 1) / kTileW;
+  const uint32_t tx0 = (minX >> 3) / kTileW, tx1 = (maxX >> 3) / kTileW;
+  const uint32_t ty0 = (minY >> 3) / kTileH, ty1 = (maxY >> 3) / kTileH;
+  for (uint32_t ty = ty0; ty <= ty1; ++ty)
+    for (uint32_t tx = tx0; tx <= tx1; ++tx) {
+      if (maxZ <= (uint32_t)V.tileHiz[ty * tilesX + tx]) continue;
+      if (query2d_tile(V, tx, ty, minX, maxX, minY, maxY, maxZ)) return true;
+    }
   return false;
 }
 
@@ -656,16 +677,18 @@ __global__ void __launch_bounds__(256) k_scan(FrameParams P, uint32_t numSt)
 
 __global__ void __launch_bounds__(kChunk) k_fill_walk(FrameParams P)
 {
-  __shared__ uint32_t s_scan[kChunk / 32];
+  extern __shared__ uint32_t s_dyn[];  // per union super-tile: 8 warp ballots + 8 warp prefixes
   __shared__ uint32_t s_rowLocal[kChunk];
   __shared__ int s_rect[4];
   if (P.header->overflow) return;
-  const uint32_t c = blockIdx.x, tid = threadIdx.x;
+  const uint32_t c = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const Chunk ch = P.chunks[c];
   const ViewDesc& V = P.views[ch.view];
   const uint32_t q = (c << kChunkShift) + tid;
   const QuadRaster R = P.rec[q];
   const bool valid = tid < ch.quadCount && R.minX < R.maxX;
+  const uint32_t ckChunk = P.viewBase[ch.view].cks + P.chunkBase[c].cks;
+  if (valid) P.ckBase[q] = ckChunk + R.ckLocal;
   s_rowLocal[tid] = P.walk[q].rowLocal;
   if (tid == 0) {
     s_rect[0] = 1 << 30; s_rect[1] = -1; s_rect[2] = 1 << 30; s_rect[3] = -1;
@@ -679,22 +702,43 @@ __global__ void __launch_bounds__(kChunk) k_fill_walk(FrameParams P)
     atomicMin(&s_rect[2], sy0); atomicMax(&s_rect[3], sy1);
   }
   __syncthreads();
+  // super-tile lists in submission order: per super-tile of the chunk's union
+  // rectangle, one ballot per warp, then a prefix over the 8 warps
   const int ux0 = s_rect[0], ux1 = s_rect[1], uy0 = s_rect[2], uy1 = s_rect[3];
-  // super-tile lists, in submission order
-  for (int sy = uy0; sy <= uy1; ++sy)
-    for (int sx = ux0; sx <= ux1; ++sx) {
-      const bool flag = valid && sx >= sx0 && sx <= sx1 && sy >= sy0 && sy <= sy1;
-      uint32_t tot;
-      const uint32_t rank = block_exclusive_scan<kChunk>(flag ? 1u : 0u, tot, s_scan);
-      if (flag) {
-        const uint32_t s = (uint32_t)sy * V.stX + (uint32_t)sx;
-        const uint32_t pos = P.stStart[V.stBase + s] + P.mat[V.matBase + s * V.chunkCount + ch.localIndex] + rank;
-        P.stList[pos] = q;
-      }
+  const int uw = ux1 - ux0 + 1;
+  const int nu = ux1 >= ux0 ? uw * (uy1 - uy0 + 1) : 0;
+  uint32_t* s_bal = s_dyn;                    // [nu][8]
+  uint32_t* s_pre = s_dyn + (size_t)nu * 8;   // [nu][8]
+  for (int u = 0; u < nu; ++u) {
+    const int sx = ux0 + u % uw, sy = uy0 + u / uw;
+    const bool flag = valid && sx >= sx0 && sx <= sx1 && sy >= sy0 && sy <= sy1;
+    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, flag);
+    if (lane == 0) s_bal[u * 8 + warp] = bal;
+  }
+  __syncthreads();
+  for (int u = tid; u < nu; u += kChunk) {
+    uint32_t acc = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+      s_pre[u * 8 + w] = acc;
+      acc += __popc(s_bal[u * 8 + w]);
     }
+  }
+  __syncthreads();
+  if (valid) {
+    const uint32_t lt = (1u << lane) - 1u;
+    const uint4 entry = make_uint4(q, (uint32_t)R.minX | ((uint32_t)R.minY << 16),
+                                   (uint32_t)R.maxX | ((uint32_t)R.maxY << 16), (uint32_t)R.maxZ);
+    for (int sy = sy0; sy <= sy1; ++sy)
+      for (int sx = sx0; sx <= sx1; ++sx) {
+        const int u = (sy - uy0) * uw + (sx - ux0);
+        const uint32_t rank = s_pre[u * 8 + warp] + __popc(s_bal[u * 8 + warp] & lt);
+        const uint32_t s = (uint32_t)sy * V.stX + (uint32_t)sx;
+        P.stList[P.stStart[V.stBase + s] + P.mat[V.matBase + s * V.chunkCount + ch.localIndex] + rank] = entry;
+      }
+  }
   // row walk: one thread per (quad, block row) of this chunk
   const uint32_t rowsTotal = P.chunkTot[c].rows;
-  const uint32_t ckChunk = P.viewBase[ch.view].cks + P.chunkBase[c].cks;
   const float dsp = -0.4375f;  // -0.5f + 1.0f / 16.0f
   for (uint32_t r0 = tid; r0 < rowsTotal; r0 += kChunk) {
     uint32_t lo = 0, hi = ch.quadCount - 1;  // last quad with rowLocal <= r0
@@ -742,25 +786,97 @@ __global__ void __launch_bounds__(kChunk) k_fill_walk(FrameParams P)
 }
 
 // ---- k_raster ------------------------------------------------------------------------
+//
+// One CTA of 128 threads per 8x4-block tile.  Thread t owns pixel rows
+// 2*(t%4), 2*(t%4)+1 of block t/4 (8 packed words in registers); the four
+// threads of a block keep its hiZ in step.  The CTA walks its super-tile's
+// quad list in order, keeps the quads that overlap the tile and are not
+// already hidden in an ordered local list, and turns them into (quad, block)
+// fragments, 128 at a time: every thread computes one fragment (coverage mask,
+// packed depth rows), then each block's four threads merge the fragments aimed
+// at it in list order with the reference's hiZ test, fast-clear overwrite and
+// max-merge (Rasterizer.cpp:1148-1290).
 
-// Applies one quad's fragment to the lane's block (Rasterizer.cpp:1241-1290).
-__device__ __forceinline__ void apply_fragment(uint32_t (&blk)[32], uint32_t& hiz, bool& have,
-                                               const uint16_t* mem, uint64_t mask, const float (&depth)[8],
-                                               float Dx, float Dy, bool safe)
+constexpr int kRasterThreads = 128;
+constexpr int kLocalCap = 512;   // overlapping quads buffered per tile
+constexpr int kFragStride = 33;  // words per fragment slot (padding: conflict-free banks)
+constexpr int kScanPerRound = 256;
+
+struct RasterSmem {
+  uint32_t lq[kLocalCap];        // quad index
+  uint32_t lrect[kLocalCap];     // quad rect within the tile: x0 | y0 << 3 | w << 5 | h << 9
+  uint32_t loff[kLocalCap];      // first fragment of each local quad
+  uint32_t frag[kRasterThreads * kFragStride];
+  uint32_t meta[kRasterThreads]; // per fragment slot: maxZ << 16 | valid << 5 | target block
+  uint32_t bmask[32][4];         // per block: fragment slots aimed at it
+  uint32_t hiz[32];              // per block: current hiZ
+  uint32_t scan[kRasterThreads / 32];
+  uint32_t n;
+};
+
+// Fragment of quad Q at block (bx, by): packed depth rows with the coverage
+// mask applied.  Returns false if the reference would skip the block (convex
+// quad outside the offset range, or an empty mask).
+__device__ __forceinline__ bool make_fragment(const FrameParams& P, const QuadRaster& Q, uint32_t ckq,
+                                              uint32_t bx, uint32_t by, uint32_t tx0, uint32_t (&r)[10][4])
 {
-  float d1[8], d8[8], d9[8];
+  const uint32_t cx = ::max((uint32_t)Q.minX, tx0);
+  const uint32_t kk = (cx >> 3) - ((uint32_t)Q.minX >> 3);
+  const uint32_t ckIdx = ckq + (by - Q.minY) * nck_of(Q) + kk;
+  const float4* ck = reinterpret_cast<const float4*>(P.ck + (size_t)kCkFloats * ckIdx);
+  const float4 o = __ldg(ck), d0 = __ldg(ck + 1), d1 = __ldg(ck + 2);
+  float off[4] = {o.x, o.y, o.z, o.w};
+  float depth[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+  const bool safe = (Q.flags & kQuadSafe) != 0;
+  for (uint32_t i = cx; i < bx; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) depth[k] = safe ? x86::radd(Q.Dx, depth[k]) : x86::xadd(Q.Dx, depth[k]);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) off[e] = x86::radd(Q.nx[e], off[e]);
+  }
+  uint64_t mask;
+  if (Q.mode == kModeConvex) {
+    if (off[0] >= kCkRange || off[1] >= kCkRange || off[2] >= kCkRange || off[3] >= kCkRange) return false;
+    mask = ~0ull;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      int32_t oi = x86::cvtt(off[e]);
+      oi = oi < 0 ? 0 : oi;
+      mask &= __ldg(&kDevCoverage[(Q.slope[e] | (uint32_t)oi) & 4095u]);
+    }
+  } else {
+    uint64_t L[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      int32_t oi = x86::cvtt(off[e]);
+      oi = oi < 0 ? 0 : (oi > 63 ? 63 : oi);
+      L[e] = __ldg(&kDevCoverage[(Q.slope[e] | (uint32_t)oi) & 4095u]);
+    }
+    switch (Q.mode) {
+      case kModeTriangle0: mask = L[0] & L[1] & L[2]; break;
+      case kModeTriangle1: mask = L[0] & L[2] & L[3]; break;
+      case kModeConcaveRight: mask = (L[0] | L[3]) & (L[1] & L[2]); break;
+      case kModeConcaveCenter:
+        mask = (Q.flags & kQuadNearClip) ? ((L[0] & L[1]) | (L[2] & L[3])) : ((L[0] & L[3]) & (L[1] | L[2]));
+        break;
+      default: mask = (L[0] & L[3]) & (L[1] | L[2]); break;
+    }
+    if (!mask) return false;
+  }
+  // depth rows (Rasterizer.cpp:1241-1268): rows 0/1 from (depth, d1), rows 8/9
+  // from (d8, d9), rows 2-7 by rounding averages of packed values
+  const float Dx = Q.Dx, Dy = Q.Dy;
+  float d1v[8], d8[8], d9[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    d1[k] = safe ? x86::rfma(Dx, 0.5f, depth[k]) : x86::xfmadd(Dx, 0.5f, depth[k]);
+    d1v[k] = safe ? x86::rfma(Dx, 0.5f, depth[k]) : x86::xfmadd(Dx, 0.5f, depth[k]);
     d8[k] = safe ? x86::radd(Dy, depth[k]) : x86::xadd(Dy, depth[k]);
-    d9[k] = safe ? x86::radd(Dy, d1[k]) : x86::xadd(Dy, d1[k]);
+    d9[k] = safe ? x86::radd(Dy, d1v[k]) : x86::xadd(Dy, d1v[k]);
   }
-  uint32_t r[10][4];
-  // rows 0/1 from (depth, d1), rows 8/9 from (d8, d9): lanes 0-3 even row, 4-7 odd row
   r[0][0] = pack2(depth[0], depth[1]); r[0][1] = pack2(depth[2], depth[3]);
-  r[0][2] = pack2(d1[0], d1[1]);       r[0][3] = pack2(d1[2], d1[3]);
+  r[0][2] = pack2(d1v[0], d1v[1]);     r[0][3] = pack2(d1v[2], d1v[3]);
   r[1][0] = pack2(depth[4], depth[5]); r[1][1] = pack2(depth[6], depth[7]);
-  r[1][2] = pack2(d1[4], d1[5]);       r[1][3] = pack2(d1[6], d1[7]);
+  r[1][2] = pack2(d1v[4], d1v[5]);     r[1][3] = pack2(d1v[6], d1v[7]);
   r[8][0] = pack2(d8[0], d8[1]);       r[8][1] = pack2(d8[2], d8[3]);
   r[8][2] = pack2(d9[0], d9[1]);       r[8][3] = pack2(d9[2], d9[3]);
   r[9][0] = pack2(d8[4], d8[5]);       r[9][1] = pack2(d8[6], d8[7]);
@@ -786,37 +902,123 @@ __device__ __forceinline__ void apply_fragment(uint32_t (&blk)[32], uint32_t& hi
       r[y][3] &= __byte_perm(hi, 0, 0x3322);
     }
   }
-  if (hiz == 1) {
-#pragma unroll
-    for (int y = 0; y < 8; ++y)
-#pragma unroll
-      for (int w = 0; w < 4; ++w) blk[4 * y + w] = r[y][w];
-  } else {
-    if (!have) {
-      const uint4* m = reinterpret_cast<const uint4*>(mem);
-#pragma unroll
-      for (int y = 0; y < 8; ++y) {
-        const uint4 v = m[y];
-        blk[4 * y + 0] = v.x; blk[4 * y + 1] = v.y; blk[4 * y + 2] = v.z; blk[4 * y + 3] = v.w;
-      }
-    }
-#pragma unroll
-    for (int y = 0; y < 8; ++y)
-#pragma unroll
-      for (int w = 0; w < 4; ++w) blk[4 * y + w] = vmax_u16x2(blk[4 * y + w], r[y][w]);
-  }
-  have = true;
-  uint32_t mn = blk[0];
-#pragma unroll
-  for (int i = 1; i < 32; ++i) mn = vmin_u16x2(mn, blk[i]);
-  hiz = ::min(mn & 0xFFFFu, mn >> 16);
+  return true;
 }
 
-__global__ void __launch_bounds__(128) k_raster(FrameParams P)
+// Runs the buffered local list: fragments in order, 128 at a time.
+__device__ __forceinline__ void raster_local_list(const FrameParams& P, const ViewDesc& V, RasterSmem& S, uint32_t n,
+                                                  uint32_t tx0, uint32_t ty0, uint32_t tid, uint32_t blk, bool inView,
+                                                  uint32_t (&rows)[8], uint32_t& hiz, bool& have)
 {
+  const uint32_t lane = tid & 31;
+  const uint32_t rp = tid & 3;  // row pair owned by this thread
+  const uint32_t myBlock = tid >> 2;
+  const uint32_t groupMask = 0xFu << (lane & ~3u);
+  // exclusive prefix of fragment counts over the local list
+  uint32_t carry = 0;
+  for (uint32_t i0 = 0; i0 < n; i0 += kRasterThreads) {
+    const uint32_t i = i0 + tid;
+    uint32_t c = 0;
+    if (i < n) {
+      const uint32_t rc = S.lrect[i];
+      c = ((rc >> 5) & 15u) * ((rc >> 9) & 7u);
+    }
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan<kRasterThreads>(c, tot, S.scan);
+    if (i < n) S.loff[i] = carry + ex;
+    carry += tot;
+  }
+  const uint32_t F = carry;
+  __syncthreads();
+  for (uint32_t f0 = 0; f0 < F; f0 += kRasterThreads) {
+    if (tid < 32 * 4) (&S.bmask[0][0])[tid] = 0;
+    const uint32_t f = f0 + tid;
+    uint32_t target = 0, q = 0, bx = 0, by = 0;
+    const bool haveF = f < F;
+    if (haveF) {
+      uint32_t lo = 0, hi = n - 1;  // last local quad whose first fragment is <= f
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (S.loff[mid] <= f) lo = mid; else hi = mid - 1;
+      }
+      const uint32_t k = f - S.loff[lo];
+      const uint32_t rc = S.lrect[lo];
+      const uint32_t rw = (rc >> 5) & 15u;
+      const uint32_t rr = k / rw, cc = k - rr * rw;
+      const uint32_t lx = (rc & 7u) + cc, ly = ((rc >> 3) & 3u) + rr;
+      target = ly * kTileW + lx;
+      bx = tx0 + lx;
+      by = ty0 + ly;
+      q = S.lq[lo];
+    }
+    __syncthreads();  // bmask cleared
+    uint32_t meta = 0;
+    if (haveF) {
+      const QuadRaster Q = P.rec[q];
+      const uint32_t ckq = __ldg(P.ckBase + q);
+      const uint32_t ownerHiz = S.hiz[target];
+      // Early skip: hiZ only falls through the fast-clear overwrite (1 -> 0),
+      // so a block with hiZ >= maxZ now still has it when this fragment's
+      // turn comes, unless hiZ == 1 and maxZ == 1.
+      const bool skip = ownerHiz >= Q.maxZ && !(ownerHiz == 1 && Q.maxZ == 1);
+      uint32_t r[10][4];
+      if (!skip && make_fragment(P, Q, ckq, bx, by, tx0, r)) {
+        uint32_t* dst = S.frag + tid * kFragStride;
+#pragma unroll
+        for (int y = 0; y < 8; ++y)
+#pragma unroll
+          for (int w = 0; w < 4; ++w) dst[4 * y + w] = r[y][w];
+        meta = ((uint32_t)Q.maxZ << 16) | 32u | target;
+        atomicOr(&S.bmask[target][tid >> 5], 1u << lane);
+      }
+    }
+    S.meta[tid] = meta;
+    __syncthreads();
+    // merge, in slot order, the fragments aimed at this thread's block
+    if (inView) {
+#pragma unroll 1
+      for (int wd = 0; wd < 4; ++wd) {
+        uint32_t mine = S.bmask[myBlock][wd];
+        while (mine) {
+          const uint32_t slot = 32u * wd + __ffs(mine) - 1;
+          mine &= mine - 1;
+          const uint32_t mz = S.meta[slot] >> 16;
+          if (hiz >= mz) continue;  // the reference's hiZ test (Rasterizer.cpp:1148-1152)
+          const uint32_t* src = S.frag + slot * kFragStride + 8 * rp;
+          if (hiz == 1) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) rows[i] = src[i];
+          } else {
+            if (!have) {
+              const uint4* m = reinterpret_cast<const uint4*>(V.depth + (size_t)blk * 64 + 16 * rp);
+              const uint4 a = m[0], b = m[1];
+              rows[0] = a.x; rows[1] = a.y; rows[2] = a.z; rows[3] = a.w;
+              rows[4] = b.x; rows[5] = b.y; rows[6] = b.z; rows[7] = b.w;
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) rows[i] = vmax_u16x2(rows[i], src[i]);
+          }
+          have = true;
+          uint32_t mn = rows[0];
+#pragma unroll
+          for (int i = 1; i < 8; ++i) mn = vmin_u16x2(mn, rows[i]);
+          mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 1));
+          mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 2));
+          hiz = ::min(mn & 0xFFFFu, mn >> 16);
+        }
+      }
+      if (rp == 0) S.hiz[myBlock] = hiz;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kRasterThreads, 4) k_raster(FrameParams P)
+{
+  __shared__ RasterSmem S;
   if (P.header->overflow) return;
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t wt = blockIdx.x * 4 + warp;
+  const uint32_t tid = threadIdx.x, lane = tid & 31;
+  const uint32_t wt = blockIdx.x;
   if (wt >= P.numTiles) return;
   uint32_t lo = 0, hi = P.numViews - 1;
   while (lo < hi) {
@@ -827,98 +1029,106 @@ __global__ void __launch_bounds__(128) k_raster(FrameParams P)
   const ViewDesc& V = P.views[v];
   const uint32_t lt = wt - V.tileStart;
   const uint32_t tx = lt % V.tilesX, ty = lt / V.tilesX;
-  const uint32_t bx = tx * kTileW + (lane & 7), by = ty * kTileH + (lane >> 3);
+  const uint32_t tx0 = tx * kTileW, ty0 = ty * kTileH;
+  const uint32_t myBlock = tid >> 2, rp = tid & 3;
+  const uint32_t bx = tx0 + (myBlock & 7), by = ty0 + (myBlock >> 3);
   const bool inView = bx < V.blocksX && by < V.blocksY;
   const uint32_t blk = inView ? by * V.blocksX + bx : 0;
   const bool clearing = (V.flags & kViewClear) != 0;
   uint32_t hiz = clearing ? 1u : (inView ? (uint32_t)V.hiz[blk] : 0xFFFFu);
   bool have = false;
-  uint32_t blkd[32];
+  uint32_t rows[8];
 #pragma unroll
-  for (int i = 0; i < 32; ++i) blkd[i] = 0;
+  for (int i = 0; i < 8; ++i) rows[i] = 0;
+  if (rp == 0) S.hiz[myBlock] = hiz;
+  __syncthreads();
 
-  const uint32_t s = V.stBase + (ty * kTileH / kSuperTile) * V.stX + (tx * kTileW / kSuperTile);
+  const uint32_t s = V.stBase + (ty0 / kSuperTile) * V.stX + (tx0 / kSuperTile);
   const uint32_t listLen = V.cmdCount ? P.stLen[s] : 0;
-  const uint32_t* list = P.stList + (V.cmdCount ? P.stStart[s] : 0);
-  const uint32_t tx0 = tx * kTileW, ty0 = ty * kTileH;
-  const uint32_t ckView = P.viewBase[v].cks;
-  for (uint32_t base = 0; base < listLen; base += 32) {
-    const uint32_t idx = base + lane;
-    uint32_t q = 0;
-    bool ov = false;
-    if (idx < listLen) {
-      q = __ldg(list + idx);
-      const uint2 bb = __ldg(reinterpret_cast<const uint2*>(P.rec + q));
-      const uint32_t qminX = bb.x & 0xFFFFu, qminY = bb.x >> 16, qmaxX = bb.y & 0xFFFFu, qmaxY = bb.y >> 16;
-      ov = qminX < tx0 + kTileW && qmaxX > tx0 && qminY < ty0 + kTileH && qmaxY > ty0;
+  const uint4* list = P.stList + (V.cmdCount ? P.stStart[s] : 0);
+  uint32_t n = 0;
+  // kScanPerRound list entries per round (two per thread), appended to the
+  // local list in list order unless already hidden in every block they touch
+  for (uint32_t base = 0; base < listLen; base += kScanPerRound) {
+    uint4 e[2];
+    bool ov[2];
+    uint32_t rect[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const uint32_t idx = base + kRasterThreads * k + tid;
+      e[k] = idx < listLen ? __ldg(list + idx) : make_uint4(0, 0, 0, 0);
     }
-    uint32_t m = __ballot_sync(0xFFFFFFFFu, ov);
-    while (m) {
-      const int j = __ffs(m) - 1;
-      m &= m - 1;
-      const uint32_t qq = __shfl_sync(0xFFFFFFFFu, q, j);
-      const QuadRaster Q = P.rec[qq];
-      const bool inQuad = inView && bx >= Q.minX && bx < Q.maxX && by >= Q.minY && by < Q.maxY;
-      if (!inQuad) continue;
-      if (hiz >= Q.maxZ) continue;
-      // checkpoint for (row by, column xmax(minX, tx0)), then <= 7 column steps
-      const uint32_t cx = ::max((uint32_t)Q.minX, tx0);
-      const uint32_t kk = (cx >> 3) - ((uint32_t)Q.minX >> 3);
-      const uint32_t chunk = qq >> kChunkShift;
-      const uint32_t ckIdx = ckView + P.chunkBase[chunk].cks + Q.ckLocal + (by - Q.minY) * nck_of(Q) + kk;
-      const float4* ck = reinterpret_cast<const float4*>(P.ck + (size_t)kCkFloats * ckIdx);
-      const float4 o = __ldg(ck), d0 = __ldg(ck + 1), d1 = __ldg(ck + 2);
-      float off[4] = {o.x, o.y, o.z, o.w};
-      float depth[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
-      const bool safe = (Q.flags & kQuadSafe) != 0;
-      for (uint32_t i = cx; i < bx; ++i) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) depth[k] = safe ? x86::radd(Q.Dx, depth[k]) : x86::xadd(Q.Dx, depth[k]);
-#pragma unroll
-        for (int e = 0; e < 4; ++e) off[e] = x86::radd(Q.nx[e], off[e]);
+    for (int k = 0; k < 2; ++k) {
+      const uint32_t qx0 = e[k].y & 0xFFFFu, qy0 = e[k].y >> 16, qx1 = e[k].z & 0xFFFFu, qy1 = e[k].z >> 16;
+      const uint32_t x0 = ::max(qx0, tx0), x1 = ::min(qx1, tx0 + kTileW);
+      const uint32_t y0 = ::max(qy0, ty0), y1 = ::min(qy1, ty0 + kTileH);
+      bool o = x0 < x1 && y0 < y1;  // padding entries have an empty box
+      if (o) {
+        // hidden if every block it touches here already has hiZ >= its maxZ
+        // (exact for the rest of the list: see raster_local_list)
+        const uint32_t mz = e[k].w;
+        bool hidden = true;
+        for (uint32_t yy = y0 - ty0; yy < y1 - ty0 && hidden; ++yy)
+          for (uint32_t xx = x0 - tx0; xx < x1 - tx0; ++xx) {
+            const uint32_t h = S.hiz[yy * kTileW + xx];
+            if (!(h >= mz && !(h == 1 && mz == 1))) {
+              hidden = false;
+              break;
+            }
+          }
+        o = !hidden;
       }
-      uint64_t mask;
-      if (Q.mode == kModeConvex) {
-        if (off[0] >= kCkRange || off[1] >= kCkRange || off[2] >= kCkRange || off[3] >= kCkRange) continue;
-        mask = ~0ull;
+      ov[k] = o;
+      rect[k] = (x0 - tx0) | ((y0 - ty0) << 3) | ((x1 - x0) << 5) | ((y1 - y0) << 9);
+    }
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          int32_t oi = x86::cvtt(off[e]);
-          oi = oi < 0 ? 0 : oi;
-          mask &= __ldg(&kDevCoverage[(Q.slope[e] | (uint32_t)oi) & 4095u]);
-        }
-      } else {
-        uint64_t L[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          int32_t oi = x86::cvtt(off[e]);
-          oi = oi < 0 ? 0 : (oi > 63 ? 63 : oi);
-          L[e] = __ldg(&kDevCoverage[(Q.slope[e] | (uint32_t)oi) & 4095u]);
-        }
-        switch (Q.mode) {
-          case kModeTriangle0: mask = L[0] & L[1] & L[2]; break;
-          case kModeTriangle1: mask = L[0] & L[2] & L[3]; break;
-          case kModeConcaveRight: mask = (L[0] | L[3]) & (L[1] & L[2]); break;
-          case kModeConcaveCenter:
-            mask = (Q.flags & kQuadNearClip) ? ((L[0] & L[1]) | (L[2] & L[3])) : ((L[0] & L[3]) & (L[1] | L[2]));
-            break;
-          default: mask = (L[0] & L[3]) & (L[1] | L[2]); break;
-        }
-        if (!mask) continue;
+    for (int k = 0; k < 2; ++k) {
+      uint32_t tot;
+      const uint32_t pos = n + block_exclusive_scan<kRasterThreads>(ov[k] ? 1u : 0u, tot, S.scan);
+      if (ov[k]) {
+        S.lq[pos] = e[k].x;
+        S.lrect[pos] = rect[k];
       }
-      apply_fragment(blkd, hiz, have, V.depth + (size_t)blk * 64, mask, depth, Q.Dx, Q.Dy, safe);
+      n += tot;
+    }
+    __syncthreads();
+    if (n > (uint32_t)(kLocalCap - kScanPerRound) || (base + kScanPerRound >= listLen && n > 0)) {
+      raster_local_list(P, V, S, n, tx0, ty0, tid, blk, inView, rows, hiz, have);
+      n = 0;
     }
   }
   if (inView) {
-    if (clearing || have) V.hiz[blk] = (uint16_t)hiz;
+    if ((clearing || have) && rp == 0) V.hiz[blk] = (uint16_t)hiz;
     if (have) {
-      uint4* outp = reinterpret_cast<uint4*>(V.depth + (size_t)blk * 64);
-#pragma unroll
-      for (int y = 0; y < 8; ++y)
-        outp[y] = make_uint4(blkd[4 * y], blkd[4 * y + 1], blkd[4 * y + 2], blkd[4 * y + 3]);
+      uint4* outp = reinterpret_cast<uint4*>(V.depth + (size_t)blk * 64 + 16 * rp);
+      outp[0] = make_uint4(rows[0], rows[1], rows[2], rows[3]);
+      outp[1] = make_uint4(rows[4], rows[5], rows[6], rows[7]);
     }
   }
-  if (clearing && lt == 0 && lane < 8) V.hiz[V.blocksX * V.blocksY + lane] = 1;  // padding entries
+  if (clearing && lt == 0 && tid < 8) V.hiz[V.blocksX * V.blocksY + tid] = 1;  // padding entries
+  // per-tile minimum hiZ for the queries
+  uint32_t tmin = (inView && rp == 0) ? hiz : 0xFFFFu;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) tmin = ::min(tmin, __shfl_xor_sync(0xFFFFFFFFu, tmin, o));
+  if (lane == 0) S.scan[tid >> 5] = tmin;
+  __syncthreads();
+  if (tid == 0) V.tileHiz[lt] = (uint16_t)::min(::min(S.scan[0], S.scan[1]), ::min(S.scan[2], S.scan[3]));
+}
+
+// Recomputes the per-warp-tile hiZ minimum of one view (after hiZ was written
+// from the host).  One warp per tile.
+__global__ void __launch_bounds__(128) k_tile_hiz(const uint16_t* hiz, uint16_t* tileHiz, uint32_t blocksX,
+                                                  uint32_t blocksY, uint32_t tilesX, uint32_t tiles)
+{
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t t = blockIdx.x * 4 + (threadIdx.x >> 5);
+  if (t >= tiles) return;
+  const uint32_t bx = (t % tilesX) * kTileW + (lane & 7), by = (t / tilesX) * kTileH + (lane >> 3);
+  uint32_t m = (bx < blocksX && by < blocksY) ? hiz[by * blocksX + bx] : 0xFFFFu;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = ::min(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+  if (lane == 0) tileHiz[t] = (uint16_t)m;
 }
 
 // ---- k_query -------------------------------------------------------------------------
@@ -927,29 +1137,60 @@ __global__ void __launch_bounds__(256) k_query(FrameParams P)
 {
   if (P.header->overflow) return;
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-  bool vis = false, nc = false;
+  const uint32_t lane = threadIdx.x & 31;
+  bool vis = false, nc = false, big = false;
+  uint32_t rect[4] = {0, 0, 0, 0}, maxZ = 0, view = 0;
   if (slot < P.numQuerySlots) {
     uint32_t lo = 0, hi = P.numViews - 1;
     while (lo < hi) {
       const uint32_t mid = (lo + hi + 1) >> 1;
       if (P.views[mid].queryStart <= slot) lo = mid; else hi = mid - 1;
     }
+    view = lo;
     const ViewDesc& V = P.views[lo];
     if (slot - V.queryStart < V.queryCount) {
       const float4 a = P.qmin[slot], b = P.qmax[slot];
       const float bmin[4] = {a.x, a.y, a.z, a.w}, bmax[4] = {b.x, b.y, b.z, b.w};
-      uint32_t rect[4], maxZ = 0;
       const int st = query_front(V, bmin, bmax, rect, &maxZ);
       if (st == 1) {
         vis = true;
         nc = true;
       } else if (st == 2) {
-        vis = query2d(V, rect[0], rect[1], rect[2], rect[3], maxZ);
+        const uint32_t ntx = (rect[1] >> 3) / kTileW - (rect[0] >> 3) / kTileW + 1;
+        const uint32_t nty = (rect[3] >> 3) / kTileH - (rect[2] >> 3) / kTileH + 1;
+        big = ntx * nty > 2;
+        if (!big) vis = query2d(V, rect[0], rect[1], rect[2], rect[3], maxZ);
       }
     }
   }
+  // boxes spanning more than two warp-tiles: the whole warp tests one box at a
+  // time, one tile per lane
+  uint32_t bigMask = __ballot_sync(0xFFFFFFFFu, big);
+  while (bigMask) {
+    const int j = __ffs(bigMask) - 1;
+    bigMask &= bigMask - 1;
+    const uint32_t minX = __shfl_sync(0xFFFFFFFFu, rect[0], j), maxX = __shfl_sync(0xFFFFFFFFu, rect[1], j);
+    const uint32_t minY = __shfl_sync(0xFFFFFFFFu, rect[2], j), maxY = __shfl_sync(0xFFFFFFFFu, rect[3], j);
+    const uint32_t mz = __shfl_sync(0xFFFFFFFFu, maxZ, j), vj = __shfl_sync(0xFFFFFFFFu, view, j);
+    const ViewDesc& V = P.views[vj];
+    const uint32_t tilesX = (V.blocksX + kTileW - 1) / kTileW;
+    const uint32_t tx0 = (minX >> 3) / kTileW, tx1 = (maxX >> 3) / kTileW;
+    const uint32_t ty0 = (minY >> 3) / kTileH, ty1 = (maxY >> 3) / kTileH;
+    const uint32_t ntx = tx1 - tx0 + 1, nt = ntx * (ty1 - ty0 + 1);
+    bool found = false;
+    for (uint32_t t0 = 0; t0 < nt && !found; t0 += 32) {
+      const uint32_t t = t0 + lane;
+      bool hit = false;
+      if (t < nt) {
+        const uint32_t tx = tx0 + t % ntx, ty = ty0 + t / ntx;
+        if (mz > (uint32_t)V.tileHiz[ty * tilesX + tx]) hit = query2d_tile(V, tx, ty, minX, maxX, minY, maxY, mz);
+      }
+      found = __ballot_sync(0xFFFFFFFFu, hit) != 0;
+    }
+    if ((int)lane == j) vis = found;
+  }
   const uint32_t vb = __ballot_sync(0xFFFFFFFFu, vis), nb = __ballot_sync(0xFFFFFFFFu, nc);
-  if ((threadIdx.x & 31) == 0 && slot < P.numQuerySlots) {
+  if (lane == 0 && slot < P.numQuerySlots) {
     P.visBits[slot >> 5] = vb;
     P.ncBits[slot >> 5] = nb;
   }
@@ -994,8 +1235,8 @@ cudaError_t launch_flush(const FrameParams& P, uint32_t numSt, uint32_t maxStPer
   }
   if (doRaster) {
     k_scan<<<numSt + P.numViews, 256, 0, stream>>>(P, numSt);
-    if (P.numChunks) k_fill_walk<<<P.numChunks, kChunk, 0, stream>>>(P);
-    if (P.numTiles) k_raster<<<(P.numTiles + 3) / 4, 128, 0, stream>>>(P);
+    if (P.numChunks) k_fill_walk<<<P.numChunks, kChunk, (size_t)maxStPerView * 64, stream>>>(P);
+    if (P.numTiles) k_raster<<<P.numTiles, kRasterThreads, 0, stream>>>(P);
   }
   if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
   return cudaGetLastError();
@@ -1012,9 +1253,9 @@ cudaError_t launch_flush_timed(const FrameParams& P, uint32_t numSt, uint32_t ma
   cudaEventRecord(ev[1], stream);
   if (doRaster) k_scan<<<numSt + P.numViews, 256, 0, stream>>>(P, numSt);
   cudaEventRecord(ev[2], stream);
-  if (doRaster && P.numChunks) k_fill_walk<<<P.numChunks, kChunk, 0, stream>>>(P);
+  if (doRaster && P.numChunks) k_fill_walk<<<P.numChunks, kChunk, (size_t)maxStPerView * 64, stream>>>(P);
   cudaEventRecord(ev[3], stream);
-  if (doRaster && P.numTiles) k_raster<<<(P.numTiles + 3) / 4, 128, 0, stream>>>(P);
+  if (doRaster && P.numTiles) k_raster<<<P.numTiles, kRasterThreads, 0, stream>>>(P);
   cudaEventRecord(ev[4], stream);
   if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
   cudaEventRecord(ev[5], stream);
@@ -1036,9 +1277,22 @@ cudaError_t launch_query2d(const ViewDesc* view, uint32_t minX, uint32_t maxX, u
   return cudaGetLastError();
 }
 
-cudaError_t set_setup_smem_limit(uint32_t bytes)
+cudaError_t launch_tile_hiz(const uint16_t* hiz, uint16_t* tileHiz, uint32_t blocksX, uint32_t blocksY,
+                            cudaStream_t stream)
 {
-  return cudaFuncSetAttribute(k_setup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  const uint32_t tilesX = (blocksX + kTileW - 1) / kTileW, tilesY = (blocksY + kTileH - 1) / kTileH;
+  const uint32_t tiles = tilesX * tilesY;
+  k_tile_hiz<<<(tiles + 3) / 4, 128, 0, stream>>>(hiz, tileHiz, blocksX, blocksY, tilesX, tiles);
+  return cudaGetLastError();
+}
+
+// Dynamic shared memory of k_setup (4 B per super-tile of the largest view)
+// and k_fill_walk (64 B per super-tile) may exceed the 48 KB default.
+cudaError_t set_kernel_attributes()
+{
+  cudaError_t e = cudaFuncSetAttribute(k_setup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 4));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_fill_walk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 64));
 }
 
 }  // namespace occ

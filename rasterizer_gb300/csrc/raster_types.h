@@ -15,12 +15,13 @@ namespace occ {
 
 constexpr int kChunkShift = 8;
 constexpr int kChunk = 1 << kChunkShift;  // quads per setup CTA
-constexpr int kSuperTile = 32;            // binning super-tile edge, in 8x8 blocks
+constexpr int kSuperTile = 16;            // binning super-tile edge, in 8x8 blocks (multiple of kTileW, kTileH)
 constexpr int kTileW = 8;                 // warp-tile: 8 x 4 blocks, one lane per block
 constexpr int kTileH = 4;
 constexpr int kCkSpan = 8;                // row-walk checkpoint every 8 block columns (== kTileW)
 constexpr int kMaxCmdPerChunk = 40;       // commands are >= 8 quads, so <= 33 per chunk
 constexpr int kCkFloats = 12;             // 4 edge offsets + 8 depth lanes
+constexpr int kMaxStPerView = 3072;       // super-tiles per view (e.g. 12288 x 6144 pixels)
 
 enum : uint32_t {
   kViewClear = 1u << 0,   // hiZ := 1 before rasterising (Rasterizer::clear)
@@ -44,6 +45,7 @@ enum : int {
 struct ViewDesc {
   uint16_t* depth;   // width*height u16, 8x8 blocks of 8 rows x 8 pixels, block-major
   uint16_t* hiz;     // blocks + 8
+  uint16_t* tileHiz; // per warp-tile (8x4 blocks, row-major): min of the tile's hiZ values
   uint32_t width, height, blocksX, blocksY;
   float cols[16];    // prebaked matrix columns (Rasterizer.cpp:91-104)
   float rows[16];    // rows of the transposed input matrix (frustum planes)
@@ -126,7 +128,8 @@ struct FrameParams {
   Totals* viewTot;
   Totals* viewBase;
   uint32_t* viewChunksDone;
-  uint32_t* stList;      // global quad indices, per super-tile, submission order
+  uint4* stList;         // per super-tile, submission order: {quad, minX | minY << 16, maxX | maxY << 16, maxZ}
+  uint32_t* ckBase;      // per quad: global index of its first row-walk checkpoint
   float* ck;             // row-walk checkpoints, kCkFloats floats each
   FrameHeader* header;
   const float4* qmin;    // query boxes per slot
