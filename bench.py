@@ -199,6 +199,22 @@ def algorithmic_bytes(q_setup: int, nq: int):
     }
 
 
+def max_over_ranks(ms: float, world: int, device) -> float:
+    """Device time of a replica; with several ranks, the maximum over ranks."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def views_per_s(steps: int, world: int, device_ms: float) -> float:
+    """Whole-job throughput: every rank renders `steps` views in the slowest rank's time."""
+    return world * steps / (device_ms * 1e-3)
+
+
 def load_traffic():
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
@@ -272,15 +288,11 @@ def run_gpu(args):
         dist.barrier()
     clocks = sampler.stop() if sampler else None
     ok = batch.check()
-    dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    t_max = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    dev_ms = float(t_max.item())
+    dev_ms = max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(starts, ends)), world, dev)
 
     # per-kernel device times (kernel by kernel, events in between, same stream)
     prof = batch.profile(min(args.steps, 300))
-    names = ["k_setup", "k_scan", "k_fill_walk", "k_raster", "k_query"]
+    names = ["k_setup", "k_scan", "k_fill", "k_walk", "k_raster", "k_query"]
     kern = {n: float(v) for n, v in zip(names, prof)}
     top = max(kern, key=kern.get)
     q_setup = sum(o.quads for o in occ)
@@ -315,7 +327,7 @@ def run_gpu(args):
     d2h = 2 * 4 * ((NQ + 31) // 32) + 4 * len(occ) + 48
     del n_chunks
 
-    value = world * args.steps / (dev_ms * 1e-3)
+    value = views_per_s(args.steps, world, dev_ms)
     line = {
         "metric": METRIC, "value": value, "unit": "views/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
@@ -335,7 +347,7 @@ def run_gpu(args):
                 "d2h_bytes_per_step": d2h,
                 "path": "Rasterizer.clear/setModelViewProjection/rasterizeMany(gated)/queryVisibilityBatch "
                         "(Python mirror -> C ABI), host numpy buffers, wall clock"},
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": 6 * args.steps,
         "clocks": clocks,
         "capacity_ok": bool(ok),
     }

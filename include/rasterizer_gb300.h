@@ -123,8 +123,8 @@ int occ_batch_launch(occ_batch b);
 int occ_batch_results(occ_batch b, uint32_t view, uint32_t* visibleBits, uint32_t* needsClippingBits);
 int occ_batch_check(occ_batch b); /* syncs; OCC_ERR_CAPACITY if a launch overflowed */
 /* Runs the frame `iterations` times kernel by kernel with CUDA events between
- * them on the context stream; msPerKernel[5] receives the mean duration of
- * setup, scan, fill/row-walk, raster and query. */
+ * them on the context stream; msPerKernel[6] receives the mean duration of
+ * setup, scan, list fill, row walk, raster and query. */
 int occ_batch_profile(occ_batch b, uint32_t iterations, float* msPerKernel);
 int occ_batch_destroy(occ_batch b);
 

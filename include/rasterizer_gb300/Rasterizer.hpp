@@ -1,0 +1,197 @@
+// C++ facade with the reference's class names and signatures
+// (SoftwareRasterizer/Rasterizer.h:10-61, Occluder.h:7-21,
+// QuadDecomposition.h:5-10, SurfaceAreaHeuristic.h:5-12) over the C ABI of
+// librasterizer_gb300.  Header only; link with -lrasterizer_gb300.
+//
+// Differences a caller of the reference sees:
+//  * a Context (one GPU, one CUDA stream) is passed to the Rasterizer and to
+//    Occluder::upload;
+//  * vectors are Vec4 (four floats) instead of __m128; with SSE available the
+//    __m128 overloads are provided too;
+//  * rasterize() is deferred: the next query, read-back or flush runs the
+//    pending work on the GPU in one batch (results are those of immediate
+//    execution);
+//  * errors throw gb300::Error instead of asserting.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../rasterizer_gb300.h"
+
+#if defined(__SSE__) || defined(_M_X64)
+#include <xmmintrin.h>
+#define GB300_HAVE_M128 1
+#endif
+
+namespace gb300 {
+
+struct Error : std::runtime_error {
+  int status;
+  Error(int s, const std::string& where) : std::runtime_error(where + ": " + occ_last_error()), status(s) {}
+};
+
+inline void check(int s, const char* where)
+{
+  if (s != OCC_OK) throw Error(s, where);
+}
+
+struct Vec4 {
+  float v[4];
+};
+
+class Context {
+ public:
+  explicit Context(int device = 0) { check(occ_ctx_create(device, &h_), "occ_ctx_create"); }
+  ~Context() { occ_ctx_destroy(h_); }
+  Context(const Context&) = delete;
+  Context& operator=(const Context&) = delete;
+  occ_ctx handle() const { return h_; }
+  void synchronize() { check(occ_ctx_synchronize(h_), "occ_ctx_synchronize"); }
+
+ private:
+  occ_ctx h_ = nullptr;
+};
+
+// Occluder::bake output (Occluder.h:7-21): packed 11/11/10 words, 8 quads per
+// 4 vectors, quantisation box, bounds with w = 1.
+struct Occluder {
+  static std::unique_ptr<Occluder> bake(const std::vector<Vec4>& vertices, Vec4 refMin, Vec4 refMax)
+  {
+    auto o = std::make_unique<Occluder>();
+    o->m_vertexData.resize(vertices.size());
+    check(occ_occluder_bake(&vertices[0].v[0], (uint32_t)vertices.size(), refMin.v, refMax.v, o->m_vertexData.data(),
+                            &o->m_packetCount, o->m_boundsMin.v, o->m_boundsMax.v, o->m_center.v),
+          "occ_occluder_bake");
+    o->m_vertexData.resize((size_t)o->m_packetCount * 8);
+    o->m_refMin = refMin;
+    o->m_refMax = refMax;
+    return o;
+  }
+
+  // Copies the packed data to the GPU once per context.
+  occ_occluder upload(Context& ctx) const
+  {
+    if (m_uploadedTo != ctx.handle()) {
+      check(occ_occluder_upload(ctx.handle(), m_vertexData.data(), m_packetCount, m_refMin.v, m_refMax.v,
+                                m_boundsMin.v, m_boundsMax.v, &m_id),
+            "occ_occluder_upload");
+      m_uploadedTo = ctx.handle();
+    }
+    return m_id;
+  }
+
+  Vec4 m_center{}, m_refMin{}, m_refMax{}, m_boundsMin{}, m_boundsMax{};
+  std::vector<uint32_t> m_vertexData;
+  uint32_t m_packetCount = 0;
+
+ private:
+  mutable occ_ctx m_uploadedTo = nullptr;
+  mutable occ_occluder m_id = 0;
+};
+
+class Rasterizer {
+ public:
+  Rasterizer(Context& ctx, uint32_t width, uint32_t height) : ctx_(ctx), w_(width), h_(height)
+  {
+    check(occ_raster_create(ctx.handle(), width, height, &r_), "occ_raster_create");
+  }
+  ~Rasterizer() { occ_raster_destroy(r_); }
+  Rasterizer(const Rasterizer&) = delete;
+  Rasterizer& operator=(const Rasterizer&) = delete;
+
+  void setModelViewProjection(const float* matrix) { check(occ_raster_set_mvp(r_, matrix), "occ_raster_set_mvp"); }
+  void clear() { check(occ_raster_clear(r_), "occ_raster_clear"); }
+
+  template <bool possiblyNearClipped>
+  void rasterize(const Occluder& occluder)
+  {
+    check(occ_raster_rasterize(r_, occluder.upload(ctx_), possiblyNearClipped ? 1 : 0), "occ_raster_rasterize");
+  }
+
+  bool queryVisibility(Vec4 boundsMin, Vec4 boundsMax, bool& needsClipping)
+  {
+    int v = 0, c = 0;
+    check(occ_raster_query_visibility(r_, boundsMin.v, boundsMax.v, &v, &c), "occ_raster_query_visibility");
+    needsClipping = c != 0;
+    return v != 0;
+  }
+
+#ifdef GB300_HAVE_M128
+  bool queryVisibility(__m128 boundsMin, __m128 boundsMax, bool& needsClipping)
+  {
+    Vec4 a, b;
+    _mm_storeu_ps(a.v, boundsMin);
+    _mm_storeu_ps(b.v, boundsMax);
+    return queryVisibility(a, b, needsClipping);
+  }
+#endif
+
+  bool query2D(uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ) const
+  {
+    int v = 0;
+    check(occ_raster_query2d(r_, minX, maxX, minY, maxY, maxZ, &v), "occ_raster_query2d");
+    return v != 0;
+  }
+
+  void readBackDepth(void* target) const { check(occ_raster_read_back_depth(r_, target), "occ_raster_read_back_depth"); }
+
+  // Batch form of queryVisibility: one bit per box (bit i%32 of word i/32).
+  void queryVisibilityBatch(uint32_t n, const Vec4* mins, const Vec4* maxs, uint32_t* visibleBits,
+                            uint32_t* needsClippingBits)
+  {
+    check(occ_raster_query_batch(r_, n, &mins[0].v[0], &maxs[0].v[0], visibleBits, needsClippingBits),
+          "occ_raster_query_batch");
+  }
+
+  void flush() { check(occ_raster_flush(r_), "occ_raster_flush"); }
+  occ_raster handle() const { return r_; }
+
+ private:
+  Context& ctx_;
+  occ_raster r_ = nullptr;
+  uint32_t w_, h_;
+};
+
+struct QuadDecomposition {
+  static std::vector<uint32_t> decompose(const std::vector<uint32_t>& indices, const std::vector<Vec4>& vertices)
+  {
+    std::vector<uint32_t> out(4 * (indices.size() / 3) + 4);
+    uint32_t n = 0;
+    check(occ_quad_decompose(indices.data(), (uint32_t)indices.size(), &vertices[0].v[0], (uint32_t)vertices.size(),
+                             out.data(), &n),
+          "occ_quad_decompose");
+    out.resize(n);
+    return out;
+  }
+};
+
+struct Aabb {
+  Vec4 m_min{}, m_max{};
+};
+
+struct SurfaceAreaHeuristic {
+  static std::vector<std::vector<uint32_t>> generateBatches(const std::vector<Aabb>& aabbs, uint32_t targetSize,
+                                                            uint32_t splitGranularity)
+  {
+    const uint32_t n = (uint32_t)aabbs.size();
+    std::vector<float> flatBoxes((size_t)n * 8);
+    for (uint32_t i = 0; i < n; ++i) {
+      std::memcpy(&flatBoxes[8 * (size_t)i], aabbs[i].m_min.v, 16);
+      std::memcpy(&flatBoxes[8 * (size_t)i + 4], aabbs[i].m_max.v, 16);
+    }
+    std::vector<uint32_t> flat(n + 1), offsets(n + 2);
+    uint32_t nb = 0;
+    check(occ_sah_generate_batches(flatBoxes.data(), n, targetSize, splitGranularity, flat.data(), offsets.data(), &nb),
+          "occ_sah_generate_batches");
+    std::vector<std::vector<uint32_t>> out(nb);
+    for (uint32_t b = 0; b < nb; ++b) out[b].assign(flat.begin() + offsets[b], flat.begin() + offsets[b + 1]);
+    return out;
+  }
+};
+
+}  // namespace gb300

@@ -386,9 +386,9 @@ class PreparedBatch:
         return False
 
     def profile(self, iterations: int) -> np.ndarray:
-        """Mean ms of (setup, scan, fill/row-walk, raster, query) over `iterations`
-        frames launched kernel by kernel with CUDA events in between."""
-        out = np.zeros(5, np.float32)
+        """Mean ms of (setup, scan, list fill, row walk, raster, query) over
+        `iterations` frames launched kernel by kernel with CUDA events in between."""
+        out = np.zeros(6, np.float32)
         check(lib().occ_batch_profile(self.handle, iterations, _ptr(out)), "occ_batch_profile")
         return out
 

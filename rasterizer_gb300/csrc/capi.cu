@@ -134,6 +134,7 @@ struct FrameScratch {
   DevBuf<uint32_t> mat, stStart, stLen, cmdDraw, ckBase;
   DevBuf<uint4> stList;
   DevBuf<float> ck;
+  DevBuf<uint2> rowOwner;  // sized like the checkpoints (a row has at least one)
   DevBuf<FrameHeader> header;
   DevBuf<float4> qmin, qmax;
   DevBuf<uint32_t> visBits, ncBits;
@@ -380,6 +381,7 @@ int run_batch(occ_ctx_s* ctx, FrameScratch& S, std::vector<ViewJob>& jobs, bool 
   for (int attempt = 0; attempt < 4; ++attempt) {
     OCC_CHECK(S.stList.reserve(S.capSt));
     OCC_CHECK(S.ck.reserve((size_t)S.capCks * kCkFloats));
+    OCC_CHECK(S.rowOwner.reserve(S.capCks));
     // overflow := 0 and the capacities; totals are recomputed, viewsDone is reset by
     // the kernels themselves and the sticky overflow bit is kept
     uint32_t* hs = reinterpret_cast<uint32_t*>(st + offHdr);
@@ -409,6 +411,7 @@ int run_batch(occ_ctx_s* ctx, FrameScratch& S, std::vector<ViewJob>& jobs, bool 
     P.viewBase = S.viewBase.p;
     P.stList = S.stList.p;
     P.ck = S.ck.p;
+    P.rowOwner = S.rowOwner.p;
     P.header = S.header.p;
     P.cmdDraw = S.cmdDraw.p;
     if (anyHostQuery) {
@@ -878,6 +881,7 @@ int capture(occ_batch_s* b)
   }
   OCC_CHECK(S.stList.reserve(S.capSt));
   OCC_CHECK(S.ck.reserve((size_t)S.capCks * kCkFloats));
+  OCC_CHECK(S.rowOwner.reserve(S.capCks));
   // capacities into the header (synchronously, outside the graph)
   uint32_t hs[3] = {0, S.capCks, S.capSt};
   OCC_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -904,6 +908,7 @@ int capture(occ_batch_s* b)
   P.viewBase = S.viewBase.p;
   P.stList = S.stList.p;
   P.ck = S.ck.p;
+  P.rowOwner = S.rowOwner.p;
   P.header = S.header.p;
   P.cmdDraw = S.cmdDraw.p;
   P.qmin = b->qmin.p;
@@ -1078,9 +1083,9 @@ int occ_batch_profile(occ_batch b, uint32_t iterations, float* msPerKernel)
 {
   if (!b || !msPerKernel || !iterations) return fail(OCC_ERR_INVALID_ARG, "bad argument");
   occ_ctx_s* ctx = b->ctx;
-  cudaEvent_t ev[6];
+  cudaEvent_t ev[7];
   for (auto& e : ev) OCC_CUDA(cudaEventCreate(&e));
-  for (int k = 0; k < 5; ++k) msPerKernel[k] = 0.0f;
+  for (int k = 0; k < 6; ++k) msPerKernel[k] = 0.0f;
   int status = OCC_OK;
   for (uint32_t it = 0; it < iterations && status == OCC_OK; ++it) {
     if (b->dirty) {
@@ -1097,8 +1102,8 @@ int occ_batch_profile(occ_batch b, uint32_t iterations, float* msPerKernel)
                                        b->L.querySlots > 0, ctx->stream, ev);
     cudaEventRecord(b->ringEv[b->cur], ctx->stream);
     if (e != cudaSuccess) status = fail(OCC_ERR_CUDA, std::string("profile launch: ") + cudaGetErrorString(e));
-    if (cudaEventSynchronize(ev[5]) != cudaSuccess) status = fail(OCC_ERR_CUDA, "profile sync");
-    for (int k = 0; k < 5 && status == OCC_OK; ++k) {
+    if (cudaEventSynchronize(ev[6]) != cudaSuccess) status = fail(OCC_ERR_CUDA, "profile sync");
+    for (int k = 0; k < 6 && status == OCC_OK; ++k) {
       float ms = 0;
       cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
       msPerKernel[k] += ms / (float)iterations;

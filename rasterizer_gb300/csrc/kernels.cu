@@ -1,24 +1,25 @@
 // GPU occluder rasteriser and visibility queries (sm_103a).
 //
-// One flush runs five kernels over a batch of views (raster_types.h):
+// One flush runs six kernels over a batch of views (raster_types.h):
 //
-//   k_setup      one CTA per 256-quad chunk: per-occluder prologue and GPU
-//                gating (Rasterizer.cpp:612-655, :123-281), then one thread per
-//                quad does the vertex transform and quad setup
-//                (Rasterizer.cpp:660-1081) and counts the quad's rows, row-walk
-//                checkpoints and 32x32-block super-tiles.
-//   k_scan       order-preserving prefix sums of those counts.
-//   k_fill_walk  one CTA per chunk: writes each super-tile's quad list in
-//                submission order, then walks every (quad, block row) once with
-//                the reference's incremental float adds and stores the edge
-//                offsets and depth lanes every 8 block columns.
-//   k_raster     one warp per 8x4-block warp-tile, one lane per 8x8 block: the
-//                warp reads its super-tile's list 32 entries at a time, ballots
-//                the quads overlapping the tile and applies them in order, each
-//                lane running the reference's per-block body (Rasterizer.cpp:
-//                1098-1292) on its block held in 32 registers.
-//   k_query      one thread per query box (Rasterizer.cpp:123-349), result bits
-//                gathered with ballots.
+//   k_setup     one CTA per 256-quad chunk: per-occluder prologue and GPU
+//               gating (Rasterizer.cpp:612-655, :123-281), then one thread per
+//               quad does the vertex transform and quad setup
+//               (Rasterizer.cpp:660-1081) and counts the quad's rows, row-walk
+//               checkpoints and 16x16-block super-tiles.
+//   k_scan      order-preserving prefix sums of those counts.
+//   k_fill      one CTA per chunk: writes each super-tile's quad list in
+//               submission order and the (quad, row) list of the row walk.
+//   k_walk      one thread per (quad, block row): the reference's incremental
+//               float adds along the row, storing the edge offsets and depth
+//               lanes every 8 block columns.
+//   k_raster    one CTA per 8x4-block tile, four threads per 8x8 block: the CTA
+//               filters its super-tile's list into the quads overlapping the
+//               tile, computes (quad, block) fragments 128 at a time and merges
+//               them per block in list order (Rasterizer.cpp:1098-1292).
+//   k_query     one thread per query box (Rasterizer.cpp:123-349); boxes over
+//               more than two tiles are tested by the whole warp; result bits
+//               gathered with ballots.
 //
 // Exactness: every float operation follows the reference's order and
 // rounding (x86_emu.cuh); the block loop sees each quad's primitives in
@@ -39,6 +40,9 @@
 namespace occ {
 
 __device__ const unsigned long long kDevCoverage[4096] = {OCC_COVERAGE_TABLE_VALUES};
+
+// Row-walk grid: a few CTAs per SM, grid-striding over the batch's rows.
+static uint32_t g_walkBlocks = 152 * 8;
 
 // Primitive mode for the 8-bit configuration (area signs | W signs << 4),
 // the classification of Rasterizer.cpp:30-64.
@@ -142,17 +146,63 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t& t
   return prefix + x - v;
 }
 
+// ---- arithmetic policies -------------------------------------------------------------
+// ExactOps applies the x86 NaN rules to every result.  FastOps uses plain IEEE
+// operations and only records whether any result was NaN: without a NaN the
+// two are bit-identical, so callers run FastOps and fall back to ExactOps for
+// the rare inputs that produce one.
+
+struct ExactOps {
+  __device__ __forceinline__ float add(float a, float b) { return x86::xadd(a, b); }
+  __device__ __forceinline__ float sub(float a, float b) { return x86::xsub(a, b); }
+  __device__ __forceinline__ float mul(float a, float b) { return x86::xmul(a, b); }
+  __device__ __forceinline__ float div(float a, float b) { return x86::xdiv(a, b); }
+  __device__ __forceinline__ float fmadd(float a, float b, float c) { return x86::xfmadd(a, b, c); }
+  __device__ __forceinline__ float fmsub(float a, float b, float c) { return x86::xfmsub(a, b, c); }
+  __device__ __forceinline__ float fnmadd(float a, float b, float c) { return x86::xfnmadd(a, b, c); }
+  __device__ __forceinline__ float round(float a) { return x86::round_even(a); }
+  __device__ __forceinline__ float floor(float a) { return x86::floor_(a); }
+  __device__ __forceinline__ float dp4(const float* a, const float* b)
+  {
+    return add(add(mul(a[0], b[0]), mul(a[1], b[1])), add(mul(a[2], b[2]), mul(a[3], b[3])));
+  }
+};
+
+struct FastOps {
+  bool nan = false;
+  __device__ __forceinline__ float chk(float r)
+  {
+    nan |= r != r;
+    return r;
+  }
+  __device__ __forceinline__ float add(float a, float b) { return chk(x86::radd(a, b)); }
+  __device__ __forceinline__ float sub(float a, float b) { return chk(x86::rsub(a, b)); }
+  __device__ __forceinline__ float mul(float a, float b) { return chk(x86::rmul(a, b)); }
+  __device__ __forceinline__ float div(float a, float b) { return chk(x86::rdiv(a, b)); }
+  __device__ __forceinline__ float fmadd(float a, float b, float c) { return chk(x86::rfma(a, b, c)); }
+  __device__ __forceinline__ float fmsub(float a, float b, float c) { return chk(x86::rfma(a, b, -c)); }
+  __device__ __forceinline__ float fnmadd(float a, float b, float c) { return chk(x86::rfma(-a, b, c)); }
+  __device__ __forceinline__ float round(float a) { return chk(rintf(a)); }
+  __device__ __forceinline__ float floor(float a) { return chk(floorf(a)); }
+  __device__ __forceinline__ float dp4(const float* a, const float* b)
+  {
+    return add(add(mul(a[0], b[0]), mul(a[1], b[1])), add(mul(a[2], b[2]), mul(a[3], b[3])));
+  }
+};
+
 // ---- queryVisibility front end (Rasterizer.cpp:123-273) ------------------------------
 
 // Returns 0 (not visible), 1 (visible, needs clipping) or 2 (rect + maxZ for query2D).
-__device__ int query_front(const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect, uint32_t* maxZOut)
+template <class Ops>
+__device__ __forceinline__ int query_front_t(Ops& o, const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect, uint32_t* maxZOut)
 {
-  using namespace x86;
+  using x86::xmin; using x86::xmax; using x86::fxor; using x86::fabs_; using x86::sign; using x86::fu;
+  using x86::cvtt; using x86::i2f; using x86::rcp; using x86::pack_depth; using x86::radd; using x86::rmul;
   float ext[4], ctr[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    ext[i] = xsub(bmax[i], bmin[i]);
-    ctr[i] = xadd(bmax[i], bmin[i]);
+    ext[i] = o.sub(bmax[i], bmin[i]);
+    ctr[i] = o.add(bmax[i], bmin[i]);
   }
   const float* row3 = V.rows + 12;
   uint32_t signs = 0;
@@ -162,10 +212,10 @@ __device__ int query_front(const ViewDesc& V, const float* bmin, const float* bm
     float plane[4], offs[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      plane[i] = (p & 1) ? xsub(row3[i], rr[i]) : xadd(row3[i], rr[i]);
-      offs[i] = xadd(ctr[i], fxor(ext[i], sign(plane[i])));
+      plane[i] = (p & 1) ? o.sub(row3[i], rr[i]) : o.add(row3[i], rr[i]);
+      offs[i] = o.add(ctr[i], fxor(ext[i], sign(plane[i])));
     }
-    signs |= fu(dp4(plane, offs));
+    signs |= fu(o.dp4(plane, offs));
   }
   if (signs & 0x80000000u) return 0;
 
@@ -176,22 +226,22 @@ __device__ int query_front(const ViewDesc& V, const float* bmin, const float* bm
   float c[8][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    float e0 = xmul(col0[i], ext[0]), e1 = xmul(col1[i], ext[1]), e2 = xmul(col2[i], ext[2]);
-    c[0][i] = xfmadd(col0[i], bmin[0], xfmadd(col1[i], bmin[1], xfmadd(col2[i], bmin[2], col3[i])));
-    c[1][i] = xadd(c[0][i], e0);
-    c[2][i] = xadd(c[0][i], e1);
-    c[4][i] = xadd(c[0][i], e2);
-    c[3][i] = xadd(c[1][i], e1);
-    c[5][i] = xadd(c[4][i], e0);
-    c[6][i] = xadd(c[2][i], e2);
-    c[7][i] = xadd(c[6][i], e0);
+    float e0 = o.mul(col0[i], ext[0]), e1 = o.mul(col1[i], ext[1]), e2 = o.mul(col2[i], ext[2]);
+    c[0][i] = o.fmadd(col0[i], bmin[0], o.fmadd(col1[i], bmin[1], o.fmadd(col2[i], bmin[2], col3[i])));
+    c[1][i] = o.add(c[0][i], e0);
+    c[2][i] = o.add(c[0][i], e1);
+    c[4][i] = o.add(c[0][i], e2);
+    c[3][i] = o.add(c[1][i], e1);
+    c[5][i] = o.add(c[4][i], e0);
+    c[6][i] = o.add(c[2][i], e2);
+    c[7][i] = o.add(c[6][i], e0);
   }
   float m1[4] = {xmax(ext[0], ext[2]), xmax(ext[1], ext[3]), xmax(ext[2], ext[0]), xmax(ext[3], ext[1])};
   float me[4] = {xmax(m1[0], m1[1]), xmax(m1[1], m1[0]), xmax(m1[2], m1[3]), xmax(m1[3], m1[2])};
   bool close = false;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    float eps = xmul(me[i], 0.001f);
+    float eps = o.mul(me[i], 0.001f);
     close |= (c[i][3] < eps) || (c[4 + i][3] < eps);
   }
   if (close) return 1;
@@ -199,9 +249,9 @@ __device__ int query_front(const ViewDesc& V, const float* bmin, const float* bm
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     float iw = rcp(c[k][3]);
-    X[k] = xmul(c[k][0], iw);
-    Y[k] = xmul(c[k][1], iw);
-    Z[k] = xmul(c[k][2], iw);
+    X[k] = o.mul(c[k][0], iw);
+    Y[k] = o.mul(c[k][1], iw);
+    Z[k] = o.mul(c[k][2], iw);
   }
   float mnX[4], mxX[4], mnY[4], mxY[4];
 #pragma unroll
@@ -223,7 +273,7 @@ __device__ int query_front(const ViewDesc& V, const float* bmin, const float* bm
   float bf[4] = {xmin(mn[0], mn[2]), xmin(mx[0], mx[2]), xmin(mn[1], mn[3]), xmin(mx[1], mx[3])};
   int32_t b[4];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) b[i] = cvtt(floor_(bf[i]));
+  for (int i = 0; i < 4; ++i) b[i] = cvtt(o.floor(bf[i]));
   b[1] = (int32_t)(0u - (uint32_t)b[1]);
   b[3] = (int32_t)(0u - (uint32_t)b[3]);
   if (b[0] >= b[1] || b[2] >= b[3]) return 0;
@@ -236,6 +286,23 @@ __device__ int query_front(const ViewDesc& V, const float* bmin, const float* bm
   rect[3] = (uint32_t)b[3];
   *maxZOut = maxZ;
   return 2;
+}
+
+__device__ __noinline__ int query_front_exact(const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect,
+                                              uint32_t* maxZOut)
+{
+  ExactOps o;
+  return query_front_t(o, V, bmin, bmax, rect, maxZOut);
+}
+
+// Returns 0 (not visible), 1 (visible, needs clipping) or 2 (rect + maxZ for query2D).
+__device__ __forceinline__ int query_front(const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect,
+                                           uint32_t* maxZOut)
+{
+  FastOps f;
+  const int st = query_front_t(f, V, bmin, bmax, rect, maxZOut);
+  if (!f.nan) return st;
+  return query_front_exact(V, bmin, bmax, rect, maxZOut);
 }
 
 // query2D (Rasterizer.cpp:283-349), split by warp-tile.  The reference skips
@@ -300,9 +367,11 @@ struct CmdConst {
   uint32_t draw, nc;
 };
 
-__device__ void cmd_prologue(const ViewDesc& V, const Cmd& cmd, CmdConst& out)
+template <class Ops>
+__device__ __forceinline__ void cmd_prologue_t(Ops& o, const ViewDesc& V, const Cmd& cmd, CmdConst& out)
 {
-  using namespace x86;
+  using x86::xmin; using x86::xmax; using x86::fxor; using x86::fabs_; using x86::sign; using x86::fu;
+  using x86::cvtt; using x86::i2f; using x86::rcp; using x86::pack_depth; using x86::radd; using x86::rmul;
   if (cmd.flags & kCmdGated) {
     // queryVisibility of the bounds against an empty buffer: visible iff in
     // the frustum and either near the camera plane or covering a nonempty
@@ -322,20 +391,20 @@ __device__ void cmd_prologue(const ViewDesc& V, const Cmd& cmd, CmdConst& out)
     for (int i = 0; i < 4; ++i) col[j][i] = V.cols[4 * j + i];
   float ext[3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) ext[i] = xsub(cmd.refMax[i], cmd.refMin[i]);
+  for (int i = 0; i < 3; ++i) ext[i] = o.sub(cmd.refMax[i], cmd.refMin[i]);
   float c3[4], n0[4], n1[4], n2[4];
-  const float s0 = xmul(ext[0], __uint_as_float(0x2F801002u));  // 1.0f / (2047ull << 21)
-  const float s1 = xmul(ext[1], __uint_as_float(0x35001002u));  // 1.0f / (2047 << 10)
-  const float s2 = xmul(ext[2], __uint_as_float(0x3A802008u));  // 1.0f / 1023
+  const float s0 = o.mul(ext[0], __uint_as_float(0x2F801002u));  // 1.0f / (2047ull << 21)
+  const float s1 = o.mul(ext[1], __uint_as_float(0x35001002u));  // 1.0f / (2047 << 10)
+  const float s2 = o.mul(ext[2], __uint_as_float(0x3A802008u));  // 1.0f / 1023
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    c3[i] = xfmadd(col[0][i], cmd.refMin[0], xfmadd(col[1][i], cmd.refMin[1], xfmadd(col[2][i], cmd.refMin[2], col[3][i])));
-    n0[i] = xmul(col[0][i], s0);
-    n1[i] = xmul(col[1][i], s1);
-    n2[i] = xmul(col[2][i], s2);
-    c3[i] = xfmadd(n0[i], 2147483648.0f, c3[i]);  // 1024ull << 21
-    n1[i] = xsub(n1[i], n0[i]);
-    n2[i] = xsub(n2[i], n0[i]);
+    c3[i] = o.fmadd(col[0][i], cmd.refMin[0], o.fmadd(col[1][i], cmd.refMin[1], o.fmadd(col[2][i], cmd.refMin[2], col[3][i])));
+    n0[i] = o.mul(col[0][i], s0);
+    n1[i] = o.mul(col[1][i], s1);
+    n2[i] = o.mul(col[2][i], s2);
+    c3[i] = o.fmadd(n0[i], 2147483648.0f, c3[i]);  // 1024ull << 21
+    n1[i] = o.sub(n1[i], n0[i]);
+    n2[i] = o.sub(n2[i], n0[i]);
   }
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
@@ -345,18 +414,34 @@ __device__ void cmd_prologue(const ViewDesc& V, const Cmd& cmd, CmdConst& out)
     out.rows[i][3] = c3[i];
   }
   const float w[4] = {2097152.0f, 1024.0f, 1.0f, 1.0f};
-  const float Za = out.rows[2][3], Zb = dp4(out.rows[2], w);
-  const float Wa = out.rows[3][3], Wb = dp4(out.rows[3], w);
-  const float c0 = xdiv(xsub(Za, Zb), xsub(Wa, Wb));
+  const float Za = out.rows[2][3], Zb = o.dp4(out.rows[2], w);
+  const float Wa = out.rows[3][3], Wb = o.dp4(out.rows[3], w);
+  const float c0 = o.div(o.sub(Za, Zb), o.sub(Wa, Wb));
   out.c0 = c0;
-  out.c1 = xfnmadd(c0, Wa, Za);
+  out.c1 = o.fnmadd(c0, Wa, Za);
+}
+
+__device__ __noinline__ void cmd_prologue_exact(const ViewDesc& V, const Cmd& cmd, CmdConst& out)
+{
+  ExactOps o;
+  cmd_prologue_t(o, V, cmd, out);
+}
+
+__device__ __forceinline__ void cmd_prologue(const ViewDesc& V, const Cmd& cmd, CmdConst& out)
+{
+  FastOps f;
+  cmd_prologue_t(f, V, cmd, out);
+  if (f.nan) cmd_prologue_exact(V, cmd, out);
 }
 
 // ---- quad setup (one SIMD lane of Rasterizer.cpp:660-1081) ---------------------------
 
-__device__ bool quad_setup(const ViewDesc& V, const uint32_t w4[4], const CmdConst& K, QuadRaster& R, QuadWalk& Wk)
+template <class Ops>
+__device__ __forceinline__ bool quad_setup_t(Ops& o, const ViewDesc& V, const uint32_t w4[4], const CmdConst& K,
+                                             QuadRaster& R, QuadWalk& Wk)
 {
-  using namespace x86;
+  using x86::xmin; using x86::xmax; using x86::fxor; using x86::fabs_; using x86::sign; using x86::fu;
+  using x86::cvtt; using x86::i2f; using x86::rcp; using x86::pack_depth; using x86::radd; using x86::rmul;
   const bool nc = K.nc != 0;
   float x[4], y[4], z[4], invW[4];
   uint32_t ws[4];
@@ -365,21 +450,21 @@ __device__ bool quad_setup(const ViewDesc& V, const uint32_t w4[4], const CmdCon
     const float Xf = i2f((int32_t)w4[j]);
     const float Yf = i2f((int32_t)(w4[j] & (2047u << 10)));
     const float Zf = i2f((int32_t)(w4[j] & 1023u));
-    const float X = xfmadd(Xf, K.rows[0][0], xfmadd(Yf, K.rows[0][1], xfmadd(Zf, K.rows[0][2], K.rows[0][3])));
-    const float Y = xfmadd(Xf, K.rows[1][0], xfmadd(Yf, K.rows[1][1], xfmadd(Zf, K.rows[1][2], K.rows[1][3])));
-    const float W = xfmadd(Xf, K.rows[3][0], xfmadd(Yf, K.rows[3][1], xfmadd(Zf, K.rows[3][2], K.rows[3][3])));
+    const float X = o.fmadd(Xf, K.rows[0][0], o.fmadd(Yf, K.rows[0][1], o.fmadd(Zf, K.rows[0][2], K.rows[0][3])));
+    const float Y = o.fmadd(Xf, K.rows[1][0], o.fmadd(Yf, K.rows[1][1], o.fmadd(Zf, K.rows[1][2], K.rows[1][3])));
+    const float W = o.fmadd(Xf, K.rows[3][0], o.fmadd(Yf, K.rows[3][1], o.fmadd(Zf, K.rows[3][2], K.rows[3][3])));
     invW[j] = nc ? xmin(kMaxInvW(), xmax(-kMaxInvW(), rcp(W))) : rcp(W);
-    x[j] = xmul(round_even(xmul(X, invW[j])), 0.125f);
-    y[j] = xmul(round_even(xmul(Y, invW[j])), 0.125f);
+    x[j] = o.mul(o.round(o.mul(X, invW[j])), 0.125f);
+    y[j] = o.mul(o.round(o.mul(Y, invW[j])), 0.125f);
     ws[j] = nc ? sign(invW[j]) : 0u;
   }
   float eX[5], eY[5];
-  eX[0] = xsub(y[1], y[0]); eX[1] = xsub(y[2], y[1]); eX[2] = xsub(y[3], y[2]); eX[3] = xsub(y[0], y[3]);
-  eY[0] = xsub(x[0], x[1]); eY[1] = xsub(x[1], x[2]); eY[2] = xsub(x[2], x[3]); eY[3] = xsub(x[3], x[0]);
-  const float area0 = xfmsub(eX[0], eY[1], xmul(eX[1], eY[0]));
-  const float area1 = xfmsub(eX[1], eY[2], xmul(eX[2], eY[1]));
-  const float area2 = xfmsub(eX[2], eY[3], xmul(eX[3], eY[2]));
-  const float area3 = xsub(xadd(area0, area2), area1);
+  eX[0] = o.sub(y[1], y[0]); eX[1] = o.sub(y[2], y[1]); eX[2] = o.sub(y[3], y[2]); eX[3] = o.sub(y[0], y[3]);
+  eY[0] = o.sub(x[0], x[1]); eY[1] = o.sub(x[1], x[2]); eY[2] = o.sub(x[2], x[3]); eY[3] = o.sub(x[3], x[0]);
+  const float area0 = o.fmsub(eX[0], eY[1], o.mul(eX[1], eY[0]));
+  const float area1 = o.fmsub(eX[1], eY[2], o.mul(eX[2], eY[1]));
+  const float area2 = o.fmsub(eX[2], eY[3], o.mul(eX[3], eY[2]));
+  const float area3 = o.sub(o.add(area0, area2), area1);
   uint32_t cfg = 0;
   cfg |= (fxor(area0, ws[0] ^ ws[1] ^ ws[2]) <= 0.0f) ? 1u : 0u;
   cfg |= (fxor(area1, ws[1] ^ ws[2] ^ ws[3]) <= 0.0f) ? 2u : 0u;
@@ -427,10 +512,10 @@ __device__ bool quad_setup(const ViewDesc& V, const uint32_t w4[4], const CmdCon
     maxFx = xmax(xmax(x[0], x[1]), xmax(x[2], x[3]));
     maxFy = xmax(xmax(y[0], y[1]), xmax(y[2], y[3]));
   }
-  int32_t minX = cvtt(xadd(minFx, kBboxMinAdd()));
-  int32_t minY = cvtt(xadd(minFy, kBboxMinAdd()));
-  int32_t maxX = cvtt(xadd(maxFx, kBboxMaxAdd));
-  int32_t maxY = cvtt(xadd(maxFy, kBboxMaxAdd));
+  int32_t minX = cvtt(o.add(minFx, kBboxMinAdd()));
+  int32_t minY = cvtt(o.add(minFy, kBboxMinAdd()));
+  int32_t maxX = cvtt(o.add(maxFx, kBboxMaxAdd));
+  int32_t maxY = cvtt(o.add(maxFy, kBboxMaxAdd));
   minX = minX < 0 ? 0 : minX;
   minY = minY < 0 ? 0 : minY;
   maxX = maxX > (int32_t)V.blocksX ? (int32_t)V.blocksX : maxX;
@@ -438,7 +523,7 @@ __device__ bool quad_setup(const ViewDesc& V, const uint32_t w4[4], const CmdCon
   if (!(maxX > minX && maxY > minY)) return false;
 
 #pragma unroll
-  for (int j = 0; j < 4; ++j) z[j] = xfmadd(invW[j], K.c1, K.c0);
+  for (int j = 0; j < 4; ++j) z[j] = o.fmadd(invW[j], K.c1, K.c0);
   float maxZ = xmax(xmax(z[0], z[1]), xmax(z[2], z[3]));
   if (nc && (ws[0] | ws[1] | ws[2] | ws[3])) maxZ = 1.0f;
 
@@ -447,17 +532,17 @@ __device__ bool quad_setup(const ViewDesc& V, const uint32_t w4[4], const CmdCon
   bool greater = fabs_(area0) < fabs_(area2);
   greater = !t0 && (t1 || greater);
   const float a = greater ? area2 : area0;
-  const float invArea = nc ? xdiv(1.0f, a) : rcp(a);
-  const float z12 = xsub(z[1], z[2]), z20 = xsub(z[2], z[0]), z30 = xsub(z[3], z[0]);
-  eX[4] = xsub(y[0], y[2]);
-  eY[4] = xsub(x[2], x[0]);
-  const float dx = greater ? xfnmadd(z20, eX[3], xmul(z30, eX[4])) : xfmsub(z20, eX[1], xmul(z12, eX[4]));
-  const float dy = greater ? xfnmadd(z20, eY[3], xmul(z30, eY[4])) : xfmsub(z20, eY[1], xmul(z12, eY[4]));
-  const float plane1 = xmul(invArea, dx);
-  const float plane2 = xmul(invArea, dy);
-  const float x0 = xsub(x[0], i2f(minX));
-  const float y0 = xsub(y[0], i2f(minY));
-  const float plane0 = xfnmadd(x0, plane1, xfnmadd(y0, plane2, z[0]));
+  const float invArea = nc ? o.div(1.0f, a) : rcp(a);
+  const float z12 = o.sub(z[1], z[2]), z20 = o.sub(z[2], z[0]), z30 = o.sub(z[3], z[0]);
+  eX[4] = o.sub(y[0], y[2]);
+  eY[4] = o.sub(x[2], x[0]);
+  const float dx = greater ? o.fnmadd(z20, eX[3], o.mul(z30, eX[4])) : o.fmsub(z20, eX[1], o.mul(z12, eX[4]));
+  const float dy = greater ? o.fnmadd(z20, eY[3], o.mul(z30, eY[4])) : o.fmsub(z20, eY[1], o.mul(z12, eY[4]));
+  const float plane1 = o.mul(invArea, dx);
+  const float plane2 = o.mul(invArea, dy);
+  const float x0 = o.sub(x[0], i2f(minX));
+  const float y0 = o.sub(y[0], i2f(minY));
+  const float plane0 = o.fnmadd(x0, plane1, o.fnmadd(y0, plane2, z[0]));
 
   if (t0) { eX[2] = eX[4]; eY[2] = eY[4]; }
   if (t1) { eX[0] = fxor(eX[4], 0x80000000u); eY[0] = fxor(eY[4], 0x80000000u); }
@@ -470,23 +555,23 @@ __device__ bool quad_setup(const ViewDesc& V, const uint32_t w4[4], const CmdCon
   }
 #pragma unroll
   for (int e = 0; e < 4; ++e) {  // normalizeEdge (Rasterizer.cpp:452-468)
-    float invLen = rcp(xadd(fabs_(eX[e]), fabs_(eY[e])));
-    invLen = xmul(nc ? fxor(kOffsetMul, flip[e]) : kOffsetMul, invLen);
-    eX[e] = xmul(eX[e], invLen);
-    eY[e] = xmul(eY[e], invLen);
+    float invLen = rcp(o.add(fabs_(eX[e]), fabs_(eY[e])));
+    invLen = o.mul(nc ? fxor(kOffsetMul, flip[e]) : kOffsetMul, invLen);
+    eX[e] = o.mul(eX[e], invLen);
+    eY[e] = o.mul(eY[e], invLen);
   }
   float off[4];
-  off[0] = xfnmadd(x0, eX[0], xfnmadd(y0, eY[0], kOffsetAdd));
+  off[0] = o.fnmadd(x0, eX[0], o.fnmadd(y0, eY[0], kOffsetAdd));
 #pragma unroll
-  for (int e = 1; e < 4; ++e) off[e] = xfnmadd(x[e], eX[e], xfnmadd(y[e], eY[e], kOffsetAdd));
+  for (int e = 1; e < 4; ++e) off[e] = o.fnmadd(x[e], eX[e], o.fnmadd(y[e], eY[e], kOffsetAdd));
 #pragma unroll
-  for (int e = 1; e < 4; ++e) off[e] = xfmadd(i2f(minX), eX[e], off[e]);
+  for (int e = 1; e < 4; ++e) off[e] = o.fmadd(i2f(minX), eX[e], off[e]);
 #pragma unroll
-  for (int e = 1; e < 4; ++e) off[e] = xfmadd(i2f(minY), eY[e], off[e]);
+  for (int e = 1; e < 4; ++e) off[e] = o.fmadd(i2f(minY), eY[e], off[e]);
 #pragma unroll
   for (int e = 0; e < 4; ++e) {  // quantizeSlopeLookup (Rasterizer.cpp:482-493)
     const uint32_t yneg = (eY[e] <= 0.0f) ? 0xFFFFFFFFu : 0u;
-    const uint32_t q = (uint32_t)cvtt(xfmadd(eX[e], kSlopeMul(), kSlopeAdd));
+    const uint32_t q = (uint32_t)cvtt(o.fmadd(eX[e], kSlopeMul(), kSlopeAdd));
     R.slope[e] = (uint16_t)(((((q << 1) - yneg) << 6)) & 4095u);
     R.nx[e] = eX[e];
     Wk.ny[e] = eY[e];
@@ -508,6 +593,22 @@ __device__ bool quad_setup(const ViewDesc& V, const uint32_t w4[4], const CmdCon
   const bool safe = bound < 1e37f;  // false for NaN / inf inputs too
   R.flags = (uint8_t)((nc ? kQuadNearClip : 0) | (safe ? kQuadSafe : 0));
   return true;
+}
+
+__device__ __noinline__ bool quad_setup_exact(const ViewDesc& V, const uint32_t w4[4], const CmdConst& K,
+                                              QuadRaster& R, QuadWalk& Wk)
+{
+  ExactOps o;
+  return quad_setup_t(o, V, w4, K, R, Wk);
+}
+
+__device__ __forceinline__ bool quad_setup(const ViewDesc& V, const uint32_t w4[4], const CmdConst& K, QuadRaster& R,
+                                           QuadWalk& Wk)
+{
+  FastOps f;
+  const bool ok = quad_setup_t(f, V, w4, K, R, Wk);
+  if (!f.nan) return ok;
+  return quad_setup_exact(V, w4, K, R, Wk);
 }
 
 __device__ __forceinline__ uint32_t view_of_chunk(const FrameParams& P, uint32_t c) { return P.chunks[c].view; }
@@ -673,9 +774,9 @@ __global__ void __launch_bounds__(256) k_scan(FrameParams P, uint32_t numSt)
   }
 }
 
-// ---- k_fill_walk -------------------------------------------------------------------------
+// ---- k_fill -------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kChunk) k_fill_walk(FrameParams P)
+__global__ void __launch_bounds__(kChunk) k_fill(FrameParams P)
 {
   extern __shared__ uint32_t s_dyn[];  // per union super-tile: 8 warp ballots + 8 warp prefixes
   __shared__ uint32_t s_rowLocal[kChunk];
@@ -689,7 +790,7 @@ __global__ void __launch_bounds__(kChunk) k_fill_walk(FrameParams P)
   const bool valid = tid < ch.quadCount && R.minX < R.maxX;
   const uint32_t ckChunk = P.viewBase[ch.view].cks + P.chunkBase[c].cks;
   if (valid) P.ckBase[q] = ckChunk + R.ckLocal;
-  s_rowLocal[tid] = P.walk[q].rowLocal;
+  s_rowLocal[tid] = P.walk[q].rowLocal;  // this thread's quad only
   if (tid == 0) {
     s_rect[0] = 1 << 30; s_rect[1] = -1; s_rect[2] = 1 << 30; s_rect[3] = -1;
   }
@@ -737,19 +838,29 @@ __global__ void __launch_bounds__(kChunk) k_fill_walk(FrameParams P)
         P.stList[P.stStart[V.stBase + s] + P.mat[V.matBase + s * V.chunkCount + ch.localIndex] + rank] = entry;
       }
   }
-  // row walk: one thread per (quad, block row) of this chunk
-  const uint32_t rowsTotal = P.chunkTot[c].rows;
+  // rows of this chunk's quads -> (quad, row) entries for the row walk
+  if (valid) {
+    const uint32_t rowG = P.viewBase[ch.view].rows + P.chunkBase[c].rows + s_rowLocal[tid];
+    const uint32_t rows = (uint32_t)(R.maxY - R.minY);
+    for (uint32_t i = 0; i < rows; ++i) P.rowOwner[rowG + i] = make_uint2(q, i);
+  }
+}
+
+// ---- k_walk ---------------------------------------------------------------------------
+// One thread per (quad, block row) of the whole batch: the reference's
+// incremental adds along the row (Rasterizer.cpp:1125-1146), storing the edge
+// offsets and depth lanes at the quad's first column and every 8 block columns.
+
+__global__ void __launch_bounds__(256) k_walk(FrameParams P)
+{
+  if (P.header->overflow) return;
+  const uint32_t total = P.header->totalRows;
   const float dsp = -0.4375f;  // -0.5f + 1.0f / 16.0f
-  for (uint32_t r0 = tid; r0 < rowsTotal; r0 += kChunk) {
-    uint32_t lo = 0, hi = ch.quadCount - 1;  // last quad with rowLocal <= r0
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi + 1) >> 1;
-      if (s_rowLocal[mid] <= r0) lo = mid; else hi = mid - 1;
-    }
-    const uint32_t qq = (c << kChunkShift) + lo;
+  for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < total; row += gridDim.x * blockDim.x) {
+    const uint2 own = P.rowOwner[row];
+    const uint32_t qq = own.x, r = own.y;
     const QuadRaster Q = P.rec[qq];
     const QuadWalk Wk = P.walk[qq];
-    const uint32_t r = r0 - s_rowLocal[lo];
     const bool safe = (Q.flags & kQuadSafe) != 0;
     float depth[8], off[4];
 #pragma unroll
@@ -767,7 +878,7 @@ __global__ void __launch_bounds__(kChunk) k_fill_walk(FrameParams P)
       for (int e = 0; e < 4; ++e) off[e] = x86::radd(off[e], Wk.ny[e]);
     }
     const uint32_t nck = nck_of(Q);
-    float4* out = reinterpret_cast<float4*>(P.ck + (size_t)kCkFloats * (ckChunk + Q.ckLocal + r * nck));
+    float4* out = reinterpret_cast<float4*>(P.ck + (size_t)kCkFloats * (P.ckBase[qq] + r * nck));
     const uint32_t lastCk = ::max((uint32_t)Q.minX, (uint32_t)(Q.maxX - 1) & ~7u);
     for (uint32_t bx = Q.minX;; ++bx) {
       if (bx == Q.minX || (bx & 7u) == 0) {
@@ -787,20 +898,20 @@ __global__ void __launch_bounds__(kChunk) k_fill_walk(FrameParams P)
 
 // ---- k_raster ------------------------------------------------------------------------
 //
-// One CTA of 128 threads per 8x4-block tile.  Thread t owns pixel rows
-// 2*(t%4), 2*(t%4)+1 of block t/4 (8 packed words in registers); the four
-// threads of a block keep its hiZ in step.  The CTA walks its super-tile's
+// One CTA of 256 threads per 8x4-block tile.  Thread t owns pixel row t%8 of
+// block t/8 (4 packed words in registers); the eight threads of a block keep
+// its hiZ in step.  The CTA walks its super-tile's
 // quad list in order, keeps the quads that overlap the tile and are not
 // already hidden in an ordered local list, and turns them into (quad, block)
-// fragments, 128 at a time: every thread computes one fragment (coverage mask,
-// packed depth rows), then each block's four threads merge the fragments aimed
+// fragments, 256 at a time: every thread computes one fragment (coverage mask,
+// packed depth rows), then each block's eight threads merge the fragments aimed
 // at it in list order with the reference's hiZ test, fast-clear overwrite and
 // max-merge (Rasterizer.cpp:1148-1290).
 
-constexpr int kRasterThreads = 128;
-constexpr int kLocalCap = 512;   // overlapping quads buffered per tile
+constexpr int kRasterThreads = 256;
+constexpr int kLocalCap = 768;   // overlapping quads buffered per tile
 constexpr int kFragStride = 33;  // words per fragment slot (padding: conflict-free banks)
-constexpr int kScanPerRound = 256;
+constexpr int kScanPerRound = 512;
 
 struct RasterSmem {
   uint32_t lq[kLocalCap];        // quad index
@@ -808,7 +919,7 @@ struct RasterSmem {
   uint32_t loff[kLocalCap];      // first fragment of each local quad
   uint32_t frag[kRasterThreads * kFragStride];
   uint32_t meta[kRasterThreads]; // per fragment slot: maxZ << 16 | valid << 5 | target block
-  uint32_t bmask[32][4];         // per block: fragment slots aimed at it
+  uint32_t bmask[32][kRasterThreads / 32];  // per block: fragment slots aimed at it
   uint32_t hiz[32];              // per block: current hiZ
   uint32_t scan[kRasterThreads / 32];
   uint32_t n;
@@ -905,15 +1016,15 @@ __device__ __forceinline__ bool make_fragment(const FrameParams& P, const QuadRa
   return true;
 }
 
-// Runs the buffered local list: fragments in order, 128 at a time.
+// Runs the buffered local list: fragments in order, kRasterThreads at a time.
 __device__ __forceinline__ void raster_local_list(const FrameParams& P, const ViewDesc& V, RasterSmem& S, uint32_t n,
                                                   uint32_t tx0, uint32_t ty0, uint32_t tid, uint32_t blk, bool inView,
-                                                  uint32_t (&rows)[8], uint32_t& hiz, bool& have)
+                                                  uint32_t (&row)[4], uint32_t& hiz, bool& have)
 {
   const uint32_t lane = tid & 31;
-  const uint32_t rp = tid & 3;  // row pair owned by this thread
-  const uint32_t myBlock = tid >> 2;
-  const uint32_t groupMask = 0xFu << (lane & ~3u);
+  const uint32_t py = tid & 7;  // pixel row owned by this thread
+  const uint32_t myBlock = tid >> 3;
+  const uint32_t groupMask = 0xFFu << (lane & ~7u);
   // exclusive prefix of fragment counts over the local list
   uint32_t carry = 0;
   for (uint32_t i0 = 0; i0 < n; i0 += kRasterThreads) {
@@ -931,7 +1042,7 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
   const uint32_t F = carry;
   __syncthreads();
   for (uint32_t f0 = 0; f0 < F; f0 += kRasterThreads) {
-    if (tid < 32 * 4) (&S.bmask[0][0])[tid] = 0;
+    (&S.bmask[0][0])[tid] = 0;  // 32 blocks x (kRasterThreads / 32) words == kRasterThreads
     const uint32_t f = f0 + tid;
     uint32_t target = 0, q = 0, bx = 0, by = 0;
     const bool haveF = f < F;
@@ -977,43 +1088,40 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
     // merge, in slot order, the fragments aimed at this thread's block
     if (inView) {
 #pragma unroll 1
-      for (int wd = 0; wd < 4; ++wd) {
+      for (int wd = 0; wd < kRasterThreads / 32; ++wd) {
         uint32_t mine = S.bmask[myBlock][wd];
         while (mine) {
           const uint32_t slot = 32u * wd + __ffs(mine) - 1;
           mine &= mine - 1;
           const uint32_t mz = S.meta[slot] >> 16;
           if (hiz >= mz) continue;  // the reference's hiZ test (Rasterizer.cpp:1148-1152)
-          const uint32_t* src = S.frag + slot * kFragStride + 8 * rp;
+          const uint32_t* src = S.frag + slot * kFragStride + 4 * py;
           if (hiz == 1) {
 #pragma unroll
-            for (int i = 0; i < 8; ++i) rows[i] = src[i];
+            for (int i = 0; i < 4; ++i) row[i] = src[i];
           } else {
             if (!have) {
-              const uint4* m = reinterpret_cast<const uint4*>(V.depth + (size_t)blk * 64 + 16 * rp);
-              const uint4 a = m[0], b = m[1];
-              rows[0] = a.x; rows[1] = a.y; rows[2] = a.z; rows[3] = a.w;
-              rows[4] = b.x; rows[5] = b.y; rows[6] = b.z; rows[7] = b.w;
+              const uint4 a = *reinterpret_cast<const uint4*>(V.depth + (size_t)blk * 64 + 8 * py);
+              row[0] = a.x; row[1] = a.y; row[2] = a.z; row[3] = a.w;
             }
 #pragma unroll
-            for (int i = 0; i < 8; ++i) rows[i] = vmax_u16x2(rows[i], src[i]);
+            for (int i = 0; i < 4; ++i) row[i] = vmax_u16x2(row[i], src[i]);
           }
           have = true;
-          uint32_t mn = rows[0];
-#pragma unroll
-          for (int i = 1; i < 8; ++i) mn = vmin_u16x2(mn, rows[i]);
+          uint32_t mn = vmin_u16x2(vmin_u16x2(row[0], row[1]), vmin_u16x2(row[2], row[3]));
           mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 1));
           mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 2));
+          mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 4));
           hiz = ::min(mn & 0xFFFFu, mn >> 16);
         }
       }
-      if (rp == 0) S.hiz[myBlock] = hiz;
+      if (py == 0) S.hiz[myBlock] = hiz;
     }
     __syncthreads();
   }
 }
 
-__global__ void __launch_bounds__(kRasterThreads, 4) k_raster(FrameParams P)
+__global__ void __launch_bounds__(kRasterThreads, 2) k_raster(FrameParams P)
 {
   __shared__ RasterSmem S;
   if (P.header->overflow) return;
@@ -1030,17 +1138,15 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(FrameParams P)
   const uint32_t lt = wt - V.tileStart;
   const uint32_t tx = lt % V.tilesX, ty = lt / V.tilesX;
   const uint32_t tx0 = tx * kTileW, ty0 = ty * kTileH;
-  const uint32_t myBlock = tid >> 2, rp = tid & 3;
+  const uint32_t myBlock = tid >> 3, py = tid & 7;
   const uint32_t bx = tx0 + (myBlock & 7), by = ty0 + (myBlock >> 3);
   const bool inView = bx < V.blocksX && by < V.blocksY;
   const uint32_t blk = inView ? by * V.blocksX + bx : 0;
   const bool clearing = (V.flags & kViewClear) != 0;
   uint32_t hiz = clearing ? 1u : (inView ? (uint32_t)V.hiz[blk] : 0xFFFFu);
   bool have = false;
-  uint32_t rows[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) rows[i] = 0;
-  if (rp == 0) S.hiz[myBlock] = hiz;
+  uint32_t row[4] = {0, 0, 0, 0};
+  if (py == 0) S.hiz[myBlock] = hiz;
   __syncthreads();
 
   const uint32_t s = V.stBase + (ty0 / kSuperTile) * V.stX + (tx0 / kSuperTile);
@@ -1094,26 +1200,27 @@ __global__ void __launch_bounds__(kRasterThreads, 4) k_raster(FrameParams P)
     }
     __syncthreads();
     if (n > (uint32_t)(kLocalCap - kScanPerRound) || (base + kScanPerRound >= listLen && n > 0)) {
-      raster_local_list(P, V, S, n, tx0, ty0, tid, blk, inView, rows, hiz, have);
+      raster_local_list(P, V, S, n, tx0, ty0, tid, blk, inView, row, hiz, have);
       n = 0;
     }
   }
   if (inView) {
-    if ((clearing || have) && rp == 0) V.hiz[blk] = (uint16_t)hiz;
-    if (have) {
-      uint4* outp = reinterpret_cast<uint4*>(V.depth + (size_t)blk * 64 + 16 * rp);
-      outp[0] = make_uint4(rows[0], rows[1], rows[2], rows[3]);
-      outp[1] = make_uint4(rows[4], rows[5], rows[6], rows[7]);
-    }
+    if ((clearing || have) && py == 0) V.hiz[blk] = (uint16_t)hiz;
+    if (have) *reinterpret_cast<uint4*>(V.depth + (size_t)blk * 64 + 8 * py) = make_uint4(row[0], row[1], row[2], row[3]);
   }
   if (clearing && lt == 0 && tid < 8) V.hiz[V.blocksX * V.blocksY + tid] = 1;  // padding entries
   // per-tile minimum hiZ for the queries
-  uint32_t tmin = (inView && rp == 0) ? hiz : 0xFFFFu;
+  uint32_t tmin = (inView && py == 0) ? hiz : 0xFFFFu;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) tmin = ::min(tmin, __shfl_xor_sync(0xFFFFFFFFu, tmin, o));
   if (lane == 0) S.scan[tid >> 5] = tmin;
   __syncthreads();
-  if (tid == 0) V.tileHiz[lt] = (uint16_t)::min(::min(S.scan[0], S.scan[1]), ::min(S.scan[2], S.scan[3]));
+  if (tid == 0) {
+    uint32_t m = S.scan[0];
+#pragma unroll
+    for (int w = 1; w < kRasterThreads / 32; ++w) m = ::min(m, S.scan[w]);
+    V.tileHiz[lt] = (uint16_t)m;
+  }
 }
 
 // Recomputes the per-warp-tile hiZ minimum of one view (after hiZ was written
@@ -1235,7 +1342,10 @@ cudaError_t launch_flush(const FrameParams& P, uint32_t numSt, uint32_t maxStPer
   }
   if (doRaster) {
     k_scan<<<numSt + P.numViews, 256, 0, stream>>>(P, numSt);
-    if (P.numChunks) k_fill_walk<<<P.numChunks, kChunk, (size_t)maxStPerView * 64, stream>>>(P);
+    if (P.numChunks) {
+      k_fill<<<P.numChunks, kChunk, (size_t)maxStPerView * 64, stream>>>(P);
+      k_walk<<<g_walkBlocks, 256, 0, stream>>>(P);
+    }
     if (P.numTiles) k_raster<<<P.numTiles, kRasterThreads, 0, stream>>>(P);
   }
   if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
@@ -1244,6 +1354,8 @@ cudaError_t launch_flush(const FrameParams& P, uint32_t numSt, uint32_t maxStPer
 
 // Same sequence with an event recorded before the first and after every kernel
 // (ev[0..5]); kernels that do not run still get their events.
+// Same sequence with an event recorded before the first and after every kernel
+// (ev[0..6]); kernels that do not run still get their events.
 cudaError_t launch_flush_timed(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
                                bool doQuery, cudaStream_t stream, cudaEvent_t* ev)
 {
@@ -1253,12 +1365,14 @@ cudaError_t launch_flush_timed(const FrameParams& P, uint32_t numSt, uint32_t ma
   cudaEventRecord(ev[1], stream);
   if (doRaster) k_scan<<<numSt + P.numViews, 256, 0, stream>>>(P, numSt);
   cudaEventRecord(ev[2], stream);
-  if (doRaster && P.numChunks) k_fill_walk<<<P.numChunks, kChunk, (size_t)maxStPerView * 64, stream>>>(P);
+  if (doRaster && P.numChunks) k_fill<<<P.numChunks, kChunk, (size_t)maxStPerView * 64, stream>>>(P);
   cudaEventRecord(ev[3], stream);
-  if (doRaster && P.numTiles) k_raster<<<P.numTiles, kRasterThreads, 0, stream>>>(P);
+  if (doRaster && P.numChunks) k_walk<<<g_walkBlocks, 256, 0, stream>>>(P);
   cudaEventRecord(ev[4], stream);
-  if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
+  if (doRaster && P.numTiles) k_raster<<<P.numTiles, kRasterThreads, 0, stream>>>(P);
   cudaEventRecord(ev[5], stream);
+  if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
+  cudaEventRecord(ev[6], stream);
   return cudaGetLastError();
 }
 
@@ -1287,12 +1401,16 @@ cudaError_t launch_tile_hiz(const uint16_t* hiz, uint16_t* tileHiz, uint32_t blo
 }
 
 // Dynamic shared memory of k_setup (4 B per super-tile of the largest view)
-// and k_fill_walk (64 B per super-tile) may exceed the 48 KB default.
+// and k_fill (64 B per super-tile) may exceed the 48 KB default.
 cudaError_t set_kernel_attributes()
 {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
+    g_walkBlocks = (uint32_t)sms * 8;
   cudaError_t e = cudaFuncSetAttribute(k_setup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 4));
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_fill_walk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 64));
+  return cudaFuncSetAttribute(k_fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 64));
 }
 
 }  // namespace occ

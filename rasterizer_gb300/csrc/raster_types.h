@@ -130,6 +130,7 @@ struct FrameParams {
   uint32_t* viewChunksDone;
   uint4* stList;         // per super-tile, submission order: {quad, minX | minY << 16, maxX | maxY << 16, maxZ}
   uint32_t* ckBase;      // per quad: global index of its first row-walk checkpoint
+  uint2* rowOwner;       // per block row of the batch: {quad, row within the quad}
   float* ck;             // row-walk checkpoints, kCkFloats floats each
   FrameHeader* header;
   const float4* qmin;    // query boxes per slot

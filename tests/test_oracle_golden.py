@@ -1,0 +1,86 @@
+"""The CPU oracle and the library's host bake against fixtures produced by the
+reference itself (tests/golden/make_golden.py).  Runs on any host; on the
+aarch64 GPU host this is what pins the portable oracle to the x86 reference."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.bindings import Oracle
+from rasterizer_gb300 import api, scenes
+
+from helpers import boxes_occluders, city_occluders, to_baked
+from golden.make_golden import CITY_FRAMES, digest, scene_digest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = json.load(open(os.path.join(HERE, "golden", "golden.json")))
+SMALL = np.load(os.path.join(HERE, "golden", "golden_small.npz"))
+
+
+def test_coverage_tables():
+    """The oracle's table (built on this host as Rasterizer.cpp:547-604 does)
+    and the library's embedded table both equal the reference's."""
+    assert digest(Oracle(8, 8).table()) == GOLDEN["coverage_table"]
+    assert digest(api.coverage_table()) == GOLDEN["coverage_table"]
+    assert np.array_equal(api.coverage_table(), SMALL["table"])
+
+
+def test_scene_generators_are_stable():
+    assert scenes.boxes_scene().digest() == GOLDEN["boxes"]["mesh"]
+    assert scenes.city_scene().digest() == GOLDEN["city"]["mesh"]
+
+
+def test_bake_matches_reference_bake():
+    """QuadDecomposition + SAH + Occluder::bake of the library, byte-identical."""
+    occ = boxes_occluders()
+    assert len(occ) == GOLDEN["boxes"]["occluders"]
+    assert scene_digest(to_baked(occ)) == GOLDEN["boxes"]["bake"]
+    occ = city_occluders()
+    assert len(occ) == GOLDEN["city"]["occluders"]
+    assert sum(o.quads for o in occ) == GOLDEN["city"]["quads"]
+    assert scene_digest(to_baked(occ)) == GOLDEN["city"]["bake"]
+
+
+def test_small_frame_raw():
+    sc = to_baked(boxes_occluders())
+    orc = Oracle(320, 200)
+    flags = orc.frame_plain(sc, SMALL["mvp"])
+    qm, qM = scenes.query_boxes(1024, seed=45)
+    vis, nc = orc.query(qm, qM)
+    assert np.array_equal(flags, SMALL["flags"])
+    assert np.array_equal(orc.depth(), SMALL["depth"])
+    assert np.array_equal(orc.hiz(), SMALL["hiz"])
+    assert np.array_equal(vis, SMALL["visible"]) and np.array_equal(nc, SMALL["needsClipping"])
+    assert np.array_equal(orc.read_back(), SMALL["readback"])
+
+
+def _check_frame(orc, flags, vis, nc, g):
+    got = {"flags": digest(flags), "depth": digest(orc.depth()), "hiz": digest(orc.hiz()),
+           "visible": digest(vis), "needsClipping": digest(nc), "readback": digest(orc.read_back())}
+    bad = [k for k in got if got[k] != g[k]]
+    assert not bad, f"oracle differs from the reference in {bad}"
+
+
+def test_boxes_frame_1080p():
+    sc = to_baked(boxes_occluders())
+    orc = Oracle(1920, 1080)
+    flags = orc.frame_plain(sc, scenes.boxes_camera())
+    mins, maxs = scenes.query_boxes(4096, seed=43)
+    vis, nc = orc.query(mins, maxs)
+    _check_frame(orc, flags, vis, nc, GOLDEN["boxes"]["frames"][0])
+
+
+def test_city_frames():
+    """Six frames of the street-level path on one persistent rasterizer
+    (near-clipped occluders and stale depth included)."""
+    sc = to_baked(city_occluders())
+    mvps, _ = scenes.camera_path(300, seed=7)
+    mins, maxs = scenes.query_boxes(20000, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    orc = Oracle(1920, 1080)
+    assert tuple(GOLDEN["city"]["frame_indices"]) == CITY_FRAMES
+    for f, g in zip(CITY_FRAMES, GOLDEN["city"]["frames"]):
+        flags = orc.frame_plain(sc, mvps[f])
+        vis, nc = orc.query(mins, maxs)
+        _check_frame(orc, flags, vis, nc, g)
+        assert g["near_clipped"] == int(((flags & 3) == 3).sum())
