@@ -84,6 +84,22 @@ int occ_raster_query_batch(occ_raster r, uint32_t n, const float* mins, const fl
 /* Same, all pointers in device memory, asynchronous on the context stream. */
 int occ_raster_query_batch_device(occ_raster r, uint32_t n, const void* dMins, const void* dMaxs,
                                   void* dVisibleBits, void* dNeedsClippingBits);
+/* No counterpart in the reference (its queries never allocate).  The same
+ * queries as occ_raster_query_batch for callers that must not allocate device
+ * memory: code in a cudaLaunchHostFunc callback, where CUDA calls may not
+ * synchronise; frame loops with a fixed memory budget reserved at start-up;
+ * engines that forbid cudaMalloc/cudaFree on their hot thread because both can
+ * stall the whole device.  Boxes and result bits are staged in one fixed
+ * device array of OCC_NOALLOC_MAX_QUERIES boxes (about 2 MiB, held on every
+ * GPU that loads the library until exit); larger n is rejected.  The first
+ * call on a device looks up the array's device address, so make that first
+ * call before any stream capture.  All calls on a device share the array:
+ * calls whose work overlaps on the GPU race and must be serialised.  Pending
+ * rasterisation is not run here (running it may allocate): flush first.
+ * Synchronous: returns when the bits are in the host buffers. */
+#define OCC_NOALLOC_MAX_QUERIES 65536u
+int occ_raster_query_batch_noalloc(occ_raster r, uint32_t n, const float* mins, const float* maxs,
+                                   uint32_t* visibleBits, uint32_t* needsClippingBits);
 /* Rasterizer::query2D (Rasterizer.cpp:283-349). */
 int occ_raster_query2d(occ_raster r, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ,
                        int* visible);

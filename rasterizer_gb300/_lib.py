@@ -45,6 +45,7 @@ SIGNATURES = {
     "occ_raster_query_visibility": (I32, [P, P, P, C.POINTER(I32), C.POINTER(I32)]),
     "occ_raster_query_batch": (I32, [P, U32, P, P, P, P]),
     "occ_raster_query_batch_device": (I32, [P, U32, P, P, P, P]),
+    "occ_raster_query_batch_noalloc": (I32, [P, U32, P, P, P, P]),
     "occ_raster_query2d": (I32, [P, U32, U32, U32, U32, U32, C.POINTER(I32)]),
     "occ_raster_read_back_depth": (I32, [P, P]),
     "occ_raster_read_depth_raw": (I32, [P, P]),

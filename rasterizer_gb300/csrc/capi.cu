@@ -25,6 +25,8 @@ cudaError_t launch_read_back(const uint16_t* depth, const uint16_t* hiz, uint32_
 cudaError_t launch_flush_timed(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
                                bool doQuery, cudaStream_t stream, cudaEvent_t* ev);
 cudaError_t set_kernel_attributes();
+cudaError_t query_noalloc(int device, const ViewDesc& view, uint32_t n, const float* mins, const float* maxs,
+                          uint32_t* visibleBits, uint32_t* needsClippingBits, cudaStream_t stream);
 cudaError_t launch_tile_hiz(const uint16_t* hiz, uint16_t* tileHiz, uint32_t blocksX, uint32_t blocksY,
                             cudaStream_t stream);
 cudaError_t launch_query2d(const ViewDesc* view, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY,
@@ -693,6 +695,34 @@ int occ_raster_query_batch_device(occ_raster r, uint32_t n, const void* dMins, c
   J.dvis = dVisibleBits;
   J.dnc = dNeedsClippingBits;
   return flush_raster(r, &J);
+}
+
+int occ_raster_query_batch_noalloc(occ_raster r, uint32_t n, const float* mins, const float* maxs,
+                                   uint32_t* visibleBits, uint32_t* needsClippingBits)
+{
+  if (!r || (n && (!mins || !maxs))) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (n > kNoAllocMaxQueries)
+    return fail(OCC_ERR_INVALID_ARG, "occ_raster_query_batch_noalloc takes at most 65536 boxes per call");
+  if (!r->pending.empty() || r->clearPending)
+    return fail(OCC_ERR_INVALID_ARG, "rasterisation is pending: call occ_raster_flush first (it may allocate)");
+  ViewDesc V{};
+  V.depth = r->depth.p;
+  V.hiz = r->hiz.p;
+  V.tileHiz = r->tileHiz.p;
+  V.width = r->width;
+  V.height = r->height;
+  V.blocksX = r->blocksX;
+  V.blocksY = r->blocksY;
+  std::memcpy(V.cols, r->cols, sizeof(V.cols));
+  std::memcpy(V.rows, r->rows, sizeof(V.rows));
+  V.queryCount = n;
+  int prev = 0;
+  OCC_CUDA(cudaGetDevice(&prev));
+  if (prev != r->ctx->device) OCC_CUDA(cudaSetDevice(r->ctx->device));
+  const cudaError_t e = query_noalloc(r->ctx->device, V, n, mins, maxs, visibleBits, needsClippingBits, r->ctx->stream);
+  if (prev != r->ctx->device) cudaSetDevice(prev);
+  if (e != cudaSuccess) return fail(OCC_ERR_CUDA, std::string("occ_raster_query_batch_noalloc: ") + cudaGetErrorString(e));
+  return OCC_OK;
 }
 
 int occ_raster_query2d(occ_raster r, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ,

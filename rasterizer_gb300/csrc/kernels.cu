@@ -33,6 +33,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "coverage_table.h"
 #include "raster_types.h"
 #include "x86_emu.cuh"
@@ -1411,6 +1413,104 @@ cudaError_t set_kernel_attributes()
   cudaError_t e = cudaFuncSetAttribute(k_setup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 4));
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 64));
+}
+
+// ---- queries without device allocation -------------------------------------------------
+//
+// Callers that must not allocate device memory -- code running in a
+// cudaLaunchHostFunc callback (where CUDA API calls are not allowed to
+// synchronise), frame loops with a fixed memory budget that reserve
+// everything at start-up, or engines that forbid cudaMalloc/cudaFree on their
+// hot thread because both can stall the whole device -- still need to test
+// boxes against a rasterizer.  For them occ_raster_query_batch_noalloc stages
+// the boxes and the result bits in the fixed array below instead of in
+// per-context buffers that grow on demand.
+//
+// The array holds at most kNoAllocMaxQueries boxes (about 2 MiB in all) and
+// lives on every GPU that loads this library until the process exits.  All
+// calls on a device share it and it keeps the last call's contents; nothing in
+// it needs clearing, because each call writes every word it later reads.
+// Calls whose work overlaps on the GPU (several host threads, several streams)
+// race on the array and must be serialised by the caller.
+
+struct NoAllocScratch {
+  ViewDesc view;
+  float4 qmin[kNoAllocMaxQueries];
+  float4 qmax[kNoAllocMaxQueries];
+  uint32_t vis[kNoAllocMaxQueries / 32];
+  uint32_t nc[kNoAllocMaxQueries / 32];
+};
+
+static __device__ __align__(256) unsigned char g_queryScratch[sizeof(NoAllocScratch)];
+
+// Same queries as k_query for one view, staged in the fixed array.
+__global__ void __launch_bounds__(256) k_query_noalloc(NoAllocScratch* S, uint32_t n)
+{
+  const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31;
+  const ViewDesc& V = S->view;
+  bool vis = false, nc = false;
+  if (slot < n) {
+    const float4 a = S->qmin[slot], b = S->qmax[slot];
+    const float bmin[4] = {a.x, a.y, a.z, a.w}, bmax[4] = {b.x, b.y, b.z, b.w};
+    uint32_t rect[4], maxZ = 0;
+    const int st = query_front(V, bmin, bmax, rect, &maxZ);
+    if (st == 1) {
+      vis = true;
+      nc = true;
+    } else if (st == 2) {
+      vis = query2d(V, rect[0], rect[1], rect[2], rect[3], maxZ);
+    }
+  }
+  const uint32_t vb = __ballot_sync(0xFFFFFFFFu, vis), nb = __ballot_sync(0xFFFFFFFFu, nc);
+  if (lane == 0 && slot < ((n + 31) & ~31u)) {
+    S->vis[slot >> 5] = vb;
+    S->nc[slot >> 5] = nb;
+  }
+}
+
+// Device address of the fixed array, looked up once per device with that
+// device current (a host-side reference to g_queryScratch is only a stand-in
+// for the symbol, not a device address).
+static void* g_queryScratchAddr[64];
+static std::mutex g_queryScratchLock;
+
+static cudaError_t query_scratch_address(int device, NoAllocScratch** out)
+{
+  if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> guard(g_queryScratchLock);
+  if (!g_queryScratchAddr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_queryScratch);
+    if (e != cudaSuccess) return e;
+    g_queryScratchAddr[device] = p;
+  }
+  *out = static_cast<NoAllocScratch*>(g_queryScratchAddr[device]);
+  return cudaSuccess;
+}
+
+// Stages boxes and bits in the fixed array; no device memory is allocated.
+// The caller has made `device` current and checked n <= kNoAllocMaxQueries.
+cudaError_t query_noalloc(int device, const ViewDesc& view, uint32_t n, const float* mins, const float* maxs,
+                          uint32_t* visibleBits, uint32_t* needsClippingBits, cudaStream_t stream)
+{
+  NoAllocScratch* S = nullptr;
+  cudaError_t e = query_scratch_address(device, &S);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(&S->view, &view, sizeof(ViewDesc), cudaMemcpyHostToDevice, stream)) != cudaSuccess) return e;
+  if (n) {
+    if ((e = cudaMemcpyAsync(S->qmin, mins, (size_t)n * 16, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(S->qmax, maxs, (size_t)n * 16, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return e;
+    k_query_noalloc<<<(n + 255) / 256, 256, 0, stream>>>(S, n);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const size_t words = (n + 31) / 32;
+    if (visibleBits && (e = cudaMemcpyAsync(visibleBits, S->vis, words * 4, cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
+      return e;
+    if (needsClippingBits &&
+        (e = cudaMemcpyAsync(needsClippingBits, S->nc, words * 4, cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
+      return e;
+  }
+  return cudaStreamSynchronize(stream);
 }
 
 }  // namespace occ

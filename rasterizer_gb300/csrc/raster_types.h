@@ -22,6 +22,7 @@ constexpr int kCkSpan = 8;                // row-walk checkpoint every 8 block c
 constexpr int kMaxCmdPerChunk = 40;       // commands are >= 8 quads, so <= 33 per chunk
 constexpr int kCkFloats = 12;             // 4 edge offsets + 8 depth lanes
 constexpr int kMaxStPerView = 3072;       // super-tiles per view (e.g. 12288 x 6144 pixels)
+constexpr uint32_t kNoAllocMaxQueries = 65536;  // boxes per occ_raster_query_batch_noalloc call
 
 enum : uint32_t {
   kViewClear = 1u << 0,   // hiZ := 1 before rasterising (Rasterizer::clear)
