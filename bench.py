@@ -223,6 +223,65 @@ def load_traffic():
     return {}
 
 
+def run_batched(ctx_dev: int, occ, steps: int):
+    """The 256-view workload: every view's occluder subset gated on the GPU and
+    its queries answered, all views in one prepared batch (one CUDA graph
+    launch) versus the same views one single-view launch at a time.  Returns
+    a dict for the bench line."""
+    import torch
+    from rasterizer_gb300 import api, scenes
+    centers = np.stack([o.center for o in occ])
+    quads = np.array([o.quads for o in occ])
+    pmin, pmax = scenes.query_boxes(NQ, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    specs = scenes.multiview_workload(centers, quads, NQ)
+    ctx = api.Context(ctx_dev)
+    views = []
+    for s in specs:
+        sel = [occ[i] for i in s.occluders]
+        views.append(dict(raster=api.Rasterizer(ctx, s.width, s.height), mvp=s.mvp, clear=True, occluders=sel,
+                          flags=np.full(len(sel), 2, np.uint8), mins=pmin[s.query_start:s.query_start + s.query_count],
+                          maxs=pmax[s.query_start:s.query_start + s.query_count]))
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", ctx_dev))
+
+    def timed(launch, reps):
+        for _ in range(2):
+            launch()
+        ctx.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            launch()
+        b.record(stream)
+        ctx.synchronize()
+        return a.elapsed_time(b) / reps
+
+    batch = api.PreparedBatch(ctx, views)
+    ok = batch.check()
+    ms_batched = timed(batch.launch, steps)
+    ok = batch.check() and ok
+    batch.close()
+    singles = [api.PreparedBatch(ctx, [v]) for v in views]
+
+    def all_single():
+        for b in singles:
+            b.launch()
+
+    ms_single = timed(all_single, max(1, steps // 2))
+    ok = all(b.check() for b in singles) and ok
+    for b in singles:
+        b.close()
+    n = len(views)
+    return {"views": n, "pixels": int(sum(s.width * s.height for s in specs)),
+            "quads_set_up": int(sum(int(quads[s.occluders].sum()) for s in specs)),
+            "queries": int(sum(s.query_count for s in specs)),
+            "batched_views_per_s": n / (ms_batched * 1e-3), "batched_ms_per_launch": ms_batched,
+            "single_view_views_per_s": n / (ms_single * 1e-3), "single_view_ms_per_round": ms_single,
+            "speedup": ms_single / ms_batched, "capacity_ok": bool(ok),
+            "note": "64x1024^2 cascades + 96x512^2 cube faces + 96 probe views 256x128..1920x1080, "
+                    "per-view occluder subsets 1k-200k tris, 10k-100k queries per view; all occluders gated on the "
+                    "GPU (no learned selection yet)"}
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -328,6 +387,8 @@ def run_gpu(args):
     del n_chunks
 
     value = views_per_s(args.steps, world, dev_ms)
+    batched = run_batched(local, occ, steps=5) if not args.no_batched else None
+
     line = {
         "metric": METRIC, "value": value, "unit": "views/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
@@ -351,6 +412,8 @@ def run_gpu(args):
         "clocks": clocks,
         "capacity_ok": bool(ok),
     }
+    if batched is not None:
+        line["batched"] = batched
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if rank == 0:
@@ -393,6 +456,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=30)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 256-view batched leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

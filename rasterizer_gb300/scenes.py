@@ -255,3 +255,81 @@ def camera_path(frames: int, seed: int, grid: int = 64, cell: float = 16.0, ctrl
         out[f] = view_projection(eye, direction, aspect=aspect)
         eyes[f, :3] = eye
     return out, eyes
+
+
+# ---- many views of one scene ----------------------------------------------------------
+
+@dataclass
+class ViewSpec:
+    kind: str            # "cascade", "cube", "probe"
+    width: int
+    height: int
+    mvp: np.ndarray      # float[16]
+    eye: np.ndarray      # (3,)
+    occluders: np.ndarray  # indices into the scene's occluder list, nearest first
+    query_start: int
+    query_count: int
+
+
+def _pick_occluders(centers: np.ndarray, tris: np.ndarray, eye, budget: int) -> np.ndarray:
+    """Occluders nearest to the eye until their triangles reach `budget` (>= 1)."""
+    d = ((centers[:, :3] - np.asarray(eye)[None, :]) ** 2).sum(axis=1)
+    order = np.argsort(d, kind="stable")
+    total = np.cumsum(tris[order])
+    n = int(np.searchsorted(total, budget) + 1)
+    return order[:max(1, min(n, len(order)))].astype(np.uint32)
+
+
+def multiview_workload(centers: np.ndarray, quads: np.ndarray, n_query_pool: int, seed: int = 3,
+                       grid: int = 64, cell: float = 16.0, counts=(64, 96, 96)):
+    """256 views of the city by default: `counts[0]` 1024x1024 shadow-cascade
+    views (perspective spot views from above along one light direction),
+    `counts[1]` 512x512 cube-map faces (groups of six around street-level
+    probes), `counts[2]` probe views of random size (multiples of 8 between
+    256x128 and 1920x1080).  Each view draws the occluders nearest to its eye
+    up to a budget of 1k-200k triangles (a quad counts as two), and queries a
+    contiguous range of 10k-100k boxes of the query pool."""
+    rng = np.random.default_rng(seed)
+    tris = 2 * np.asarray(quads, np.int64)
+    half = grid * cell / 2
+    streets = city_streets(grid, cell)
+    views: list[ViewSpec] = []
+
+    def queries():
+        n = int(rng.integers(10_000, min(100_000, n_query_pool) + 1))
+        start = int(rng.integers(0, n_query_pool - n + 1))
+        return start, n
+
+    light = np.array([0.35, -1.0, 0.25])
+    light /= np.linalg.norm(light)
+    for k in range(counts[0]):
+        target = np.array([rng.uniform(-half * 0.6, half * 0.6), 0.0, rng.uniform(-half * 0.6, half * 0.6)])
+        eye = target - light * 400.0
+        mvp = view_projection(eye, light, up=(0.0, 0.0, 1.0), fov_y=math.radians(25.0), aspect=1.0,
+                              near=1.0, far=5000.0)
+        budget = int(rng.integers(1_000, 200_001))
+        s, n = queries()
+        views.append(ViewSpec("cascade", 1024, 1024, mvp, eye, _pick_occluders(centers, tris, eye, budget), s, n))
+    faces = [((1, 0, 0), (0, 1, 0)), ((-1, 0, 0), (0, 1, 0)), ((0, 1, 0), (0, 0, -1)),
+             ((0, -1, 0), (0, 0, 1)), ((0, 0, 1), (0, 1, 0)), ((0, 0, -1), (0, 1, 0))]
+    for p in range((counts[1] + 5) // 6):
+        eye = np.array([rng.choice(streets), 1.7 + rng.uniform(0, 6), rng.choice(streets)])
+        budget = int(rng.integers(1_000, 200_001))
+        occ = _pick_occluders(centers, tris, eye, budget)
+        for d, up in faces:
+            if len(views) >= counts[0] + counts[1]:
+                break
+            mvp = view_projection(eye, d, up=up, fov_y=math.radians(90.0), aspect=1.0, near=0.5)
+            s, n = queries()
+            views.append(ViewSpec("cube", 512, 512, mvp, eye, occ, s, n))
+    for k in range(counts[2]):
+        w = int(rng.integers(32, 241)) * 8
+        h = int(rng.integers(16, 136)) * 8
+        eye = np.array([rng.choice(streets) + rng.uniform(-3, 3), 1.7, rng.choice(streets) + rng.uniform(-3, 3)])
+        yaw = rng.uniform(0, 2 * math.pi)
+        d = (math.cos(yaw), -0.05, math.sin(yaw))
+        mvp = view_projection(eye, d, fov_y=math.radians(60.0), aspect=w / h)
+        budget = int(rng.integers(1_000, 200_001))
+        s, n = queries()
+        views.append(ViewSpec("probe", w, h, mvp, eye, _pick_occluders(centers, tris, eye, budget), s, n))
+    return views

@@ -214,3 +214,32 @@ def test_prepared_batch_graph(ctx):
         assert np.array_equal(vis.astype(np.uint8), ovis) and np.array_equal(nc.astype(np.uint8), onc)
         _compare(r, orc, ("depth", "hiz"))
     b.close()
+
+
+def test_multiview_workload_subset(ctx):
+    """Views of the 256-view workload (cascades, cube faces, probe views with
+    their own occluder subsets and query ranges) in one batch == the oracle,
+    view by view."""
+    occ = city_occluders()
+    scene = to_baked(occ)
+    centers = np.stack([o.center for o in occ])
+    quads = np.array([o.quads for o in occ])
+    pool_min, pool_max = scenes.query_boxes(100_000, seed=44, footprint=300.0, lognormal=(0.0, 1.0),
+                                            y_range=(0.0, 20.0))
+    specs = scenes.multiview_workload(centers, quads, len(pool_min))
+    pick = specs[:2] + specs[64:70] + specs[160:163]
+    views = []
+    for s in pick:
+        r = api.Rasterizer(ctx, s.width, s.height)
+        sel = [occ[i] for i in s.occluders]
+        views.append(dict(raster=r, mvp=s.mvp, clear=True, occluders=sel, flags=np.full(len(sel), 2, np.uint8),
+                          mins=pool_min[s.query_start:s.query_start + s.query_count],
+                          maxs=pool_max[s.query_start:s.query_start + s.query_count]))
+    res = api.execute_batch(ctx, views)
+    for s, v, (vis, nc) in zip(pick, views, res):
+        orc = Oracle(s.width, s.height)
+        orc.frame_plain(scene, s.mvp, order=s.occluders)
+        ovis, onc = orc.query(v["mins"], v["maxs"])
+        _compare(v["raster"], orc, ("depth", "hiz"))
+        assert np.array_equal(vis.astype(np.uint8), ovis), s.kind
+        assert np.array_equal(nc.astype(np.uint8), onc), s.kind
