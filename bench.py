@@ -282,6 +282,119 @@ def run_batched(ctx_dev: int, occ, steps: int):
                     "GPU (no learned selection yet)"}
 
 
+def _time_launches(ctx, stream, launch, reps, before=None):
+    """Mean device ms per launch: CUDA events on the library's stream around
+    each launch (`before(i)` runs outside the events)."""
+    import torch
+    for i in range(3):
+        if before:
+            before(i)
+        launch()
+    ctx.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for i, (a, b) in enumerate(evs):
+        if before:
+            before(i)
+        a.record(stream)
+        launch()
+        b.record(stream)
+    ctx.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs) / reps
+
+
+def run_learned(ctx_dev: int, occ, steps: int):
+    """Learned occluder selection.  Trains the selector on the GPU (labels from
+    the rasteriser over seeded poses), picks per workload the smallest
+    candidate fraction K that keeps >= 99% of the occlusion culls on held-out
+    validation views, then reports on held-out test views: culls kept vs the
+    full frames, false culls, the nearest-first ranking at the same K, and
+    views/s of the batched + learned launch against the plain paths."""
+    import torch
+    from rasterizer_gb300 import api, learned as L, scenes
+    pmin, pmax = scenes.query_boxes(NQ, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    centers = np.stack([o.center for o in occ])
+    quads = np.array([o.quads for o in occ])
+    ctx = api.Context(ctx_dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", ctx_dev))
+    t = L.Timer()
+    net, report = L.train_selector(ctx, occ, NQ, log=None)
+    out = {"training": dict(report, seconds=t.lap())}
+    fracs = (0.05, 0.1, 0.2, 0.35, 0.5)
+
+    def pick(tracks_val):
+        full = L.run_full(ctx, occ, tracks_val, pmin, pmax)
+        for f in fracs:
+            if L.evaluate_learned(ctx, occ, tracks_val, pmin, pmax, net, f, full).retained >= 0.99:
+                return f
+        return 1.0
+
+    # street level, 1920x1080 (the dense-city configuration with learned selection)
+    k_st = pick(L.street_tracks(6, 30, seed0=6000, n_occluders=len(occ), queries=NQ))
+    test = L.street_tracks(8, 30, seed0=5000, n_occluders=len(occ), queries=NQ)
+    full = L.run_full(ctx, occ, test, pmin, pmax)
+    sweep = {}
+    for f in fracs:
+        a = L.evaluate_learned(ctx, occ, test, pmin, pmax, net, f, full)
+        b = L.evaluate_heuristic(ctx, occ, test, pmin, pmax, "nearest", f, full)
+        sweep[str(f)] = {"learned": a.as_dict(), "nearest_first": b.as_dict()}
+    # throughput: 64 street views at 1080p per launch, moving along their paths
+    paths = L.street_tracks(64, 64, seed0=7000, n_occluders=len(occ), queries=NQ)
+    views = L._views(ctx, occ, paths, pmin, pmax)
+
+    def mover(b, tracks=paths, frames=64):
+        def before(i):
+            for v, tr in enumerate(tracks):
+                b.setModelViewProjection(v, tr.mvps[i % frames])
+        return before
+
+    plain = api.PreparedBatch(ctx, views)
+    ms_plain = _time_launches(ctx, stream, plain.launch, steps, mover(plain))
+    ok = plain.check()
+    plain.close()
+    sel = api.PreparedBatch(ctx, views)
+    sel.setSelection(net, k_st, trackWins=True)
+    ms_sel = _time_launches(ctx, stream, sel.launch, steps, mover(sel))
+    ok = sel.check() and ok
+    prof = sel.profile(10)
+    sel.close()
+    for v in views:
+        v["raster"].close()
+    out["street_1080p"] = {
+        "k_fraction": k_st, "test_views": f"{len(test)} held-out paths x 30 frames", "sweep": sweep,
+        "at_k": sweep.get(str(k_st)),
+        "batched_plain_views_per_s": 64 / (ms_plain * 1e-3),
+        "batched_learned_views_per_s": 64 / (ms_sel * 1e-3),
+        "learned_kernels_ms_per_launch": dict(zip(["k_setup", "k_scan", "k_fill", "k_walk", "k_raster", "k_query",
+                                                    "selection"], [float(x) for x in prof])),
+        "views_per_launch": 64, "capacity_ok": bool(ok)}
+    # the 256-view workload (mixed resolutions)
+    k_mv = pick(L.multiview_tracks(centers, quads, NQ, frames=4, seed=9))
+    test = L.multiview_tracks(centers, quads, NQ, frames=4, seed=3)
+    full = L.run_full(ctx, occ, test, pmin, pmax)
+    a = L.evaluate_learned(ctx, occ, test, pmin, pmax, net, k_mv, full)
+    b = L.evaluate_heuristic(ctx, occ, test, pmin, pmax, "nearest", k_mv, full)
+    views = L._views(ctx, occ, test, pmin, pmax)
+    plain = api.PreparedBatch(ctx, views)
+    ms_plain = _time_launches(ctx, stream, plain.launch, steps, mover(plain, test, 4))
+    ok = plain.check()
+    plain.close()
+    sel = api.PreparedBatch(ctx, views)
+    sel.setSelection(net, k_mv, trackWins=True)
+    ms_sel = _time_launches(ctx, stream, sel.launch, steps, mover(sel, test, 4))
+    ok = sel.check() and ok
+    sel.close()
+    for v in views:
+        v["raster"].close()
+    out["multiview_256"] = {"k_fraction": k_mv, "learned": a.as_dict(), "nearest_first": b.as_dict(),
+                            "batched_plain_views_per_s": len(test) / (ms_plain * 1e-3),
+                            "batched_learned_views_per_s": len(test) / (ms_sel * 1e-3),
+                            "batched_learned_ms_per_launch": ms_sel, "capacity_ok": bool(ok)}
+    out["seconds"] = t.lap() + out["training"]["seconds"]
+    net.close()
+    ctx.close()
+    return out
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -388,6 +501,7 @@ def run_gpu(args):
 
     value = views_per_s(args.steps, world, dev_ms)
     batched = run_batched(local, occ, steps=5) if not args.no_batched else None
+    learned = run_learned(local, occ, steps=20) if not args.no_learned else None
 
     line = {
         "metric": METRIC, "value": value, "unit": "views/s", "n_gpus": world, "steps": args.steps,
@@ -414,6 +528,11 @@ def run_gpu(args):
     }
     if batched is not None:
         line["batched"] = batched
+    if learned is not None:
+        line["learned"] = learned
+        if batched is not None:
+            line["learned"]["multiview_256"]["speedup_vs_single_view_plain"] = (
+                learned["multiview_256"]["batched_learned_views_per_s"] / batched["single_view_views_per_s"])
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if rank == 0:
@@ -457,6 +576,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-view batched leg")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-selection leg (training included)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

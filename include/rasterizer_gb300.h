@@ -139,10 +139,50 @@ int occ_batch_launch(occ_batch b);
 int occ_batch_results(occ_batch b, uint32_t view, uint32_t* visibleBits, uint32_t* needsClippingBits);
 int occ_batch_check(occ_batch b); /* syncs; OCC_ERR_CAPACITY if a launch overflowed */
 /* Runs the frame `iterations` times kernel by kernel with CUDA events between
- * them on the context stream; msPerKernel[6] receives the mean duration of
- * setup, scan, list fill, row walk, raster and query. */
+ * them on the context stream; msPerKernel[7] receives the mean duration of
+ * setup, scan, list fill, row walk, raster, query and (when selection is on,
+ * see occ_batch_set_selection) the selection kernels before them. */
 int occ_batch_profile(occ_batch b, uint32_t iterations, float* msPerKernel);
 int occ_batch_destroy(occ_batch b);
+
+/* ---- learned occluder selection (replaces Main.cpp:184-206's distance-sorted
+ *      loop) ------------------------------------------------------------------
+ * An MLP 16 -> 64 -> 64 -> 1 (bf16 tensor-core inference, fp32 master weights)
+ * scores each occluder of a view from features of its bounds (screen rect,
+ * depth bounds, distance, size, quads) and the pixels it won in the previous
+ * launch; only the top fraction of each view's candidates is rasterised. */
+typedef struct occ_mlp_s* occ_mlp;
+#define OCC_MLP_FEATURES 16
+int occ_mlp_param_count(void); /* 5313 floats: W1t[64][16] b1[64] W2t[64][64] b2[64] w3[64] b3 */
+int occ_mlp_create(occ_ctx ctx, uint32_t seed, occ_mlp* out);
+int occ_mlp_destroy(occ_mlp m);
+int occ_mlp_get_params(occ_mlp m, float* out);
+int occ_mlp_set_params(occ_mlp m, const float* in);
+/* host arrays: features n x 16, scores n */
+int occ_mlp_forward(occ_mlp m, uint32_t n, const float* features, float* scores);
+/* mean-squared-error loss and its gradient (param_count floats) without an update */
+int occ_mlp_gradients(occ_mlp m, uint32_t n, const float* features, const float* targets, float* loss, float* grads);
+/* Training state for checkpoints: fp32 weights, Adam moments (param_count
+ * floats each; any pointer may be NULL on get) and the Adam step count. */
+int occ_mlp_get_state(occ_mlp m, float* params, float* adamM, float* adamV, uint32_t* step);
+int occ_mlp_set_state(occ_mlp m, const float* params, const float* adamM, const float* adamV, uint32_t step);
+/* one Adam step (beta 0.9 / 0.999) on one batch */
+int occ_mlp_train_step(occ_mlp m, uint32_t n, const float* features, const float* targets, float lr, float* loss);
+/* On a prepared batch: mlp != NULL keeps ceil(fraction * candidates) occluders
+ * per view (top scores); trackWins counts per occluder the pixels whose final
+ * depth it produced (labels, and the next launch's previous-frame feature). */
+int occ_batch_set_selection(occ_batch b, occ_mlp mlp, float fraction, int trackWins);
+/* With enable != 0, each launch first zeroes the depth of every view it
+ * clears.  The reference's clear only marks blocks (hiZ := 1) and its
+ * queryVisibility still reads the old depth of a cleared block that a query
+ * box covers partially (Rasterizer.cpp:305-344), so a frame's results depend
+ * on the frames before it; zeroed depth makes each frame stand alone (used to
+ * compare a selected subset against the full frame).  No reference counterpart. */
+int occ_batch_set_zero_depth(occ_batch b, int enable);
+/* Per occluder of the view, after the last launch: its features, pixel wins,
+ * candidate flag (passes the visibility test), selected flag and score. */
+int occ_batch_read_selection(occ_batch b, uint32_t view, float* features, uint32_t* wins, uint8_t* candidate,
+                             uint8_t* selected, float* scores);
 
 /* ---- host-side occluder preparation (QuadDecomposition.h:5-10,
  *      SurfaceAreaHeuristic.h:5-12, Occluder.h:9) -------------------------------

@@ -61,6 +61,19 @@ SIGNATURES = {
     "occ_batch_check": (I32, [P]),
     "occ_batch_profile": (I32, [P, U32, P]),
     "occ_batch_destroy": (I32, [P]),
+    "occ_batch_set_selection": (I32, [P, P, C.c_float, I32]),
+    "occ_batch_read_selection": (I32, [P, U32, P, P, P, P, P]),
+    "occ_batch_set_zero_depth": (I32, [P, I32]),
+    "occ_mlp_param_count": (I32, []),
+    "occ_mlp_create": (I32, [P, U32, C.POINTER(P)]),
+    "occ_mlp_destroy": (I32, [P]),
+    "occ_mlp_get_params": (I32, [P, P]),
+    "occ_mlp_get_state": (I32, [P, P, P, P, C.POINTER(U32)]),
+    "occ_mlp_set_state": (I32, [P, P, P, P, U32]),
+    "occ_mlp_set_params": (I32, [P, P]),
+    "occ_mlp_forward": (I32, [P, U32, P, P]),
+    "occ_mlp_gradients": (I32, [P, U32, P, P, C.POINTER(C.c_float), P]),
+    "occ_mlp_train_step": (I32, [P, U32, P, P, C.c_float, C.POINTER(C.c_float)]),
     "occ_quad_decompose": (I32, [P, U32, P, U32, P, C.POINTER(U32)]),
     "occ_sah_generate_batches": (I32, [P, U32, U32, U32, P, P, C.POINTER(U32)]),
     "occ_occluder_bake": (I32, [P, U32, P, P, P, C.POINTER(U32), P, P, P]),

@@ -8,6 +8,8 @@ asserts become ValueError; GPU or allocation failures raise OccError.
 from __future__ import annotations
 
 import ctypes as C
+import itertools
+import weakref
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -34,16 +36,27 @@ def unpack_bits(words: np.ndarray, n: int) -> np.ndarray:
     return b[:n].astype(bool)
 
 
+_context_serial = itertools.count(1)
+
+
 class Context:
-    """One GPU and one CUDA stream; owns the uploaded occluders."""
+    """One GPU and one CUDA stream; owns the uploaded occluders.  Closing it
+    first closes the rasterizers, batches and selectors made on it."""
 
     def __init__(self, device: int = 0):
         h = P()
         check(lib().occ_ctx_create(device, C.byref(h)), "occ_ctx_create")
         self.handle = h.value
+        self.serial = next(_context_serial)  # never reused, unlike the handle's address
+        self._children = weakref.WeakSet()
+
+    def _adopt(self, child) -> None:
+        self._children.add(child)
 
     def close(self):
         if getattr(self, "handle", None):
+            for c in list(getattr(self, "_children", ())):
+                c.close()
             lib().occ_ctx_destroy(self.handle)
             self.handle = None
 
@@ -73,7 +86,7 @@ class Occluder:
     boundsMin: np.ndarray
     boundsMax: np.ndarray
     center: np.ndarray
-    ids: dict = field(default_factory=dict, repr=False)  # context handle -> occluder id
+    ids: dict = field(default_factory=dict, repr=False)  # context serial -> occluder id
 
     @staticmethod
     def bake(vertices, refMin, refMax) -> "Occluder":
@@ -95,13 +108,13 @@ class Occluder:
 
     def upload(self, ctx: Context) -> int:
         """Copies the packed data to the GPU once per context; returns its id."""
-        if ctx.handle in self.ids:
-            return self.ids[ctx.handle]
+        if ctx.serial in self.ids:
+            return self.ids[ctx.serial]
         oid = C.c_uint32()
         check(lib().occ_occluder_upload(ctx.handle, _ptr(self.packed), self.packetCount, _ptr(self.refMin),
                                         _ptr(self.refMax), _ptr(self.boundsMin), _ptr(self.boundsMax),
                                         C.byref(oid)), "occ_occluder_upload")
-        self.ids[ctx.handle] = oid.value
+        self.ids[ctx.serial] = oid.value
         return oid.value
 
 
@@ -197,6 +210,7 @@ class Rasterizer:
         h = P()
         check(lib().occ_raster_create(ctx.handle, width, height, C.byref(h)), "occ_raster_create")
         self.handle = h.value
+        ctx._adopt(self)
 
     def close(self):
         if getattr(self, "handle", None):
@@ -296,6 +310,7 @@ class _WorkSet:
         self.keep = []
         self.arr = (ViewWork * len(views))()
         self.nq = []
+        self.ncmd = []
         for i, vw in enumerate(views):
             r: Rasterizer = vw["raster"]
             w = self.arr[i]
@@ -310,6 +325,7 @@ class _WorkSet:
             self.keep.append(ids)
             w.numOccluders = len(ids)
             w.occluders = _ptr(ids)
+            self.ncmd.append(len(ids))
             if vw.get("flags") is not None:
                 fl = np.ascontiguousarray(vw["flags"], np.uint8)
                 self.keep.append(fl)
@@ -355,6 +371,7 @@ class PreparedBatch:
         h = P()
         check(lib().occ_batch_prepare(ctx.handle, len(views), self.ws.arr, C.byref(h)), "occ_batch_prepare")
         self.handle = h.value
+        ctx._adopt(self)
 
     def close(self):
         if getattr(self, "handle", None):
@@ -386,10 +403,40 @@ class PreparedBatch:
         return False
 
     def profile(self, iterations: int) -> np.ndarray:
-        """Mean ms of (setup, scan, list fill, row walk, raster, query) over
-        `iterations` frames launched kernel by kernel with CUDA events in between."""
-        out = np.zeros(6, np.float32)
+        """Mean ms of (setup, scan, list fill, row walk, raster, query, selection)
+        over `iterations` frames launched kernel by kernel with CUDA events in
+        between (selection is 0 unless setSelection enabled it)."""
+        out = np.zeros(7, np.float32)
         check(lib().occ_batch_profile(self.handle, iterations, _ptr(out)), "occ_batch_profile")
+        return out
+
+    def setSelection(self, mlp: "OccluderSelector | None", fraction: float = 1.0, trackWins: bool = False) -> None:
+        """With `mlp`, each launch rasterises only the top ceil(fraction x
+        candidates) occluders of every view by the network's score; with
+        `trackWins`, each launch counts per occluder the pixels whose final
+        depth it produced (read with selection())."""
+        check(lib().occ_batch_set_selection(self.handle, mlp.handle if mlp is not None else None, float(fraction),
+                                            int(bool(trackWins))), "occ_batch_set_selection")
+        self._selector = mlp  # the captured launch reads the network's weights
+
+    def setZeroDepth(self, enable: bool) -> None:
+        """Zero each cleared view's depth at the start of every launch, so a
+        frame's queries do not see depth left by earlier frames in cleared
+        blocks (which the reference's queryVisibility reads)."""
+        check(lib().occ_batch_set_zero_depth(self.handle, int(bool(enable))), "occ_batch_set_zero_depth")
+
+    def selection(self, view: int) -> dict:
+        """Per occluder of `view` after the last launch: features (n x 16, the
+        previous-launch wins among them), wins, candidate, selected, score."""
+        n = self.ws.ncmd[view]
+        out = dict(features=np.zeros((n, 16), np.float32), wins=np.zeros(n, np.uint32),
+                   candidate=np.zeros(n, np.uint8), selected=np.zeros(n, np.uint8), score=np.zeros(n, np.float32))
+        if n:
+            check(lib().occ_batch_read_selection(self.handle, view, _ptr(out["features"]), _ptr(out["wins"]),
+                                                 _ptr(out["candidate"]), _ptr(out["selected"]), _ptr(out["score"])),
+                  "occ_batch_read_selection")
+        out["candidate"] = out["candidate"].astype(bool)
+        out["selected"] = out["selected"].astype(bool)
         return out
 
     def results(self, view: int):
@@ -398,6 +445,90 @@ class PreparedBatch:
         nb = np.zeros(max((n + 31) // 32, 1), np.uint32)
         check(lib().occ_batch_results(self.handle, view, _ptr(vb), _ptr(nb)), "occ_batch_results")
         return unpack_bits(vb, n), unpack_bits(nb, n)
+
+
+class OccluderSelector:
+    """The learned occluder selector: an MLP 16 -> 64 -> 64 -> 1 with ReLU
+    (bf16 tensor-core inference, fp32 master weights, Adam), trained on the
+    device.  Parameters are a flat float32 vector: W1 (64 x 16, row n holds the
+    weights into hidden unit n), b1 (64), W2 (64 x 64, same), b2 (64), w3 (64), b3."""
+
+    FEATURES = 16
+    HIDDEN = 64
+
+    def __init__(self, ctx: Context, seed: int = 0):
+        self.ctx = ctx
+        h = P()
+        check(lib().occ_mlp_create(ctx.handle, seed, C.byref(h)), "occ_mlp_create")
+        self.handle = h.value
+        ctx._adopt(self)
+        self.nparams = lib().occ_mlp_param_count()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().occ_mlp_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.nparams, np.float32)
+        check(lib().occ_mlp_get_params(self.handle, _ptr(out)), "occ_mlp_get_params")
+        return out
+
+    def setParams(self, p) -> None:
+        p = _f32(p).reshape(self.nparams)
+        check(lib().occ_mlp_set_params(self.handle, _ptr(p)), "occ_mlp_set_params")
+
+    CHECKPOINT_VERSION = 1
+
+    def save(self, path) -> None:
+        """Weights and Adam state with a format header (resume with load)."""
+        p = np.zeros(self.nparams, np.float32)
+        m = np.zeros_like(p)
+        v = np.zeros_like(p)
+        step = C.c_uint32()
+        check(lib().occ_mlp_get_state(self.handle, _ptr(p), _ptr(m), _ptr(v), C.byref(step)), "occ_mlp_get_state")
+        header = np.array([self.CHECKPOINT_VERSION, self.FEATURES, self.HIDDEN, self.nparams, step.value], np.int64)
+        with open(path, "wb") as f:
+            np.savez(f, magic=np.frombuffer(b"OCCMLP", np.uint8), header=header, params=p, adam_m=m, adam_v=v)
+
+    def load(self, path) -> None:
+        with np.load(path) as z:
+            if bytes(z["magic"]) != b"OCCMLP":
+                raise ValueError(f"{path}: not an occluder-selector checkpoint")
+            ver, feats, hidden, n, step = (int(x) for x in z["header"])
+            if ver != self.CHECKPOINT_VERSION or feats != self.FEATURES or hidden != self.HIDDEN or n != self.nparams:
+                raise ValueError(f"{path}: checkpoint version {ver} ({feats}-{hidden}, {n} params) does not match")
+            p, m, v = (np.ascontiguousarray(z[k], np.float32) for k in ("params", "adam_m", "adam_v"))
+        check(lib().occ_mlp_set_state(self.handle, _ptr(p), _ptr(m), _ptr(v), step), "occ_mlp_set_state")
+
+    def forward(self, features) -> np.ndarray:
+        x = _f32(features).reshape(-1, self.FEATURES)
+        out = np.zeros(len(x), np.float32)
+        check(lib().occ_mlp_forward(self.handle, len(x), _ptr(x), _ptr(out)), "occ_mlp_forward")
+        return out
+
+    def gradients(self, features, targets):
+        x = _f32(features).reshape(-1, self.FEATURES)
+        t = _f32(targets).reshape(len(x))
+        g = np.zeros(self.nparams, np.float32)
+        loss = C.c_float()
+        check(lib().occ_mlp_gradients(self.handle, len(x), _ptr(x), _ptr(t), C.byref(loss), _ptr(g)),
+              "occ_mlp_gradients")
+        return float(loss.value), g
+
+    def trainStep(self, features, targets, lr: float = 1e-3) -> float:
+        x = _f32(features).reshape(-1, self.FEATURES)
+        t = _f32(targets).reshape(len(x))
+        loss = C.c_float()
+        check(lib().occ_mlp_train_step(self.handle, len(x), _ptr(x), _ptr(t), float(lr), C.byref(loss)),
+              "occ_mlp_train_step")
+        return float(loss.value)
 
 
 def coverage_table() -> np.ndarray:
@@ -413,4 +544,4 @@ def build_coverage_table() -> np.ndarray:
 
 
 __all__ = ["Context", "Occluder", "QuadDecomposition", "SurfaceAreaHeuristic", "Rasterizer", "bake_scene",
-           "execute_batch", "PreparedBatch", "OccError", "coverage_table", "build_coverage_table", "unpack_bits"]
+           "execute_batch", "PreparedBatch", "OccluderSelector", "OccError", "coverage_table", "build_coverage_table", "unpack_bits"]

@@ -25,6 +25,16 @@ cudaError_t launch_read_back(const uint16_t* depth, const uint16_t* hiz, uint32_
 cudaError_t launch_flush_timed(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
                                bool doQuery, cudaStream_t stream, cudaEvent_t* ev);
 cudaError_t set_kernel_attributes();
+cudaError_t launch_selection(const FrameParams& P, uint32_t numCmds, bool useMlp, cudaStream_t stream);
+cudaError_t launch_mlp_forward(const float* feat, uint32_t M, const MlpDevice* mlp, float* score, float* h1, float* h2,
+                               float* xb, cudaStream_t stream);
+cudaError_t launch_mlp_backward(const float* score, const float* target, uint32_t B, const MlpDevice* mlp,
+                                const float* xb, const float* h1, const float* h2, float* ds, float* dh1, float* dh2,
+                                float* err2, float* grad, cudaStream_t stream);
+cudaError_t launch_mlp_publish(const float* params, MlpDevice* mlp, cudaStream_t stream);
+cudaError_t launch_adam(float* params, const float* grad, float* m, float* v, float lr, uint32_t step,
+                        cudaStream_t stream);
+int mlp_param_count();
 cudaError_t query_noalloc(int device, const ViewDesc& view, uint32_t n, const float* mins, const float* maxs,
                           uint32_t* visibleBits, uint32_t* needsClippingBits, cudaStream_t stream);
 cudaError_t launch_tile_hiz(const uint16_t* hiz, uint16_t* tileHiz, uint32_t blocksX, uint32_t blocksY,
@@ -859,6 +869,16 @@ namespace {
 constexpr int kRing = 4;
 }
 
+struct occ_mlp_s {
+  occ_ctx_s* ctx = nullptr;
+  DevBuf<float> params, m, v, grad;  // fp32 master weights, Adam moments, gradient (+ loss)
+  DevBuf<MlpDevice> dev;             // the kernels' copy (bf16 matrices)
+  DevBuf<float> feat, target, score, xb, h1, h2, ds, dh1, dh2, err2;  // training batch
+  uint32_t step = 0;
+};
+
+static const MlpDevice* mlp_device(const occ_mlp_s* m) { return m->dev.p; }
+
 struct occ_batch_s {
   occ_ctx_s* ctx = nullptr;
   std::vector<std::vector<PendingCmd>> cmds;
@@ -877,6 +897,14 @@ struct occ_batch_s {
   cudaGraphNode_t copyNode = nullptr;
   FrameParams params{};
   bool anyRaster = false;
+  // learned selection / win counts
+  const struct occ_mlp_s* mlp = nullptr;
+  float selectFrac = 1.0f;
+  bool trackWins = false, features = false;
+  bool zeroDepth = false;  // zero every view's depth at the start of each launch
+  DevBuf<float> feat, score;
+  DevBuf<uint8_t> cand, select;
+  DevBuf<uint32_t> wins;
   ~occ_batch_s()
   {
     if (exec) cudaGraphExecDestroy(exec);
@@ -947,12 +975,29 @@ int capture(occ_batch_s* b)
   P.ncBits = b->nc.p;
   bool anyRaster = false;
   for (auto& J : b->jobs) anyRaster |= J.ncmds || J.clear;
+  const uint32_t numCmds = (uint32_t)b->L.cmds.size();
+  if (b->features) {
+    P.feat = b->feat.p;
+    P.cand = b->cand.p;
+    P.wins = b->trackWins ? b->wins.p : nullptr;
+    if (b->mlp) {
+      P.score = b->score.p;
+      P.select = b->select.p;
+      P.mlp = mlp_device(b->mlp);
+      P.selectFrac = b->selectFrac;
+    }
+  }
   b->params = P;
   b->anyRaster = anyRaster;
 
   OCC_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t e1 = cudaMemcpyAsync(S.tables.p, b->ring[b->cur].p, b->tablesBytes, cudaMemcpyHostToDevice, ctx->stream);
-  cudaError_t e2 = launch_flush(P, b->L.numSt, b->L.maxStPerView, anyRaster, b->L.querySlots > 0, ctx->stream);
+  if (b->zeroDepth)
+    for (auto& J : b->jobs)
+      if (e1 == cudaSuccess && J.clear)
+        e1 = cudaMemsetAsync(J.r->depth.p, 0, (size_t)J.r->width * J.r->height * sizeof(uint16_t), ctx->stream);
+  cudaError_t e2 = b->features ? launch_selection(P, numCmds, b->mlp != nullptr, ctx->stream) : cudaSuccess;
+  if (e2 == cudaSuccess) e2 = launch_flush(P, b->L.numSt, b->L.maxStPerView, anyRaster, b->L.querySlots > 0, ctx->stream);
   cudaGraph_t g = nullptr;
   cudaError_t e3 = cudaStreamEndCapture(ctx->stream, &g);
   if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
@@ -1113,9 +1158,9 @@ int occ_batch_profile(occ_batch b, uint32_t iterations, float* msPerKernel)
 {
   if (!b || !msPerKernel || !iterations) return fail(OCC_ERR_INVALID_ARG, "bad argument");
   occ_ctx_s* ctx = b->ctx;
-  cudaEvent_t ev[7];
+  cudaEvent_t ev[8];
   for (auto& e : ev) OCC_CUDA(cudaEventCreate(&e));
-  for (int k = 0; k < 6; ++k) msPerKernel[k] = 0.0f;
+  for (int k = 0; k < 7; ++k) msPerKernel[k] = 0.0f;
   int status = OCC_OK;
   for (uint32_t it = 0; it < iterations && status == OCC_OK; ++it) {
     if (b->dirty) {
@@ -1128,7 +1173,10 @@ int occ_batch_profile(occ_batch b, uint32_t iterations, float* msPerKernel)
                                                   b->tablesBytes, cudaMemcpyHostToDevice));
     }
     cudaMemcpyAsync(b->S.tables.p, b->ring[b->cur].p, b->tablesBytes, cudaMemcpyHostToDevice, ctx->stream);
-    cudaError_t e = launch_flush_timed(b->params, b->L.numSt, b->L.maxStPerView, b->anyRaster,
+    cudaEventRecord(ev[7], ctx->stream);
+    cudaError_t e = b->features ? launch_selection(b->params, (uint32_t)b->L.cmds.size(), b->mlp != nullptr, ctx->stream)
+                                : cudaSuccess;
+    if (e == cudaSuccess) e = launch_flush_timed(b->params, b->L.numSt, b->L.maxStPerView, b->anyRaster,
                                        b->L.querySlots > 0, ctx->stream, ev);
     cudaEventRecord(b->ringEv[b->cur], ctx->stream);
     if (e != cudaSuccess) status = fail(OCC_ERR_CUDA, std::string("profile launch: ") + cudaGetErrorString(e));
@@ -1138,9 +1186,67 @@ int occ_batch_profile(occ_batch b, uint32_t iterations, float* msPerKernel)
       cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
       msPerKernel[k] += ms / (float)iterations;
     }
+    if (status == OCC_OK) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[7], ev[0]);
+      msPerKernel[6] += ms / (float)iterations;
+    }
   }
   for (auto& e : ev) cudaEventDestroy(e);
   return status;
+}
+
+int occ_batch_set_selection(occ_batch b, occ_mlp mlp, float fraction, int trackWins)
+{
+  if (!b) return fail(OCC_ERR_INVALID_ARG, "null batch");
+  if (mlp && !(fraction > 0.0f && fraction <= 1.0f)) return fail(OCC_ERR_INVALID_ARG, "fraction must be in (0, 1]");
+  if (mlp && mlp->ctx != b->ctx) return fail(OCC_ERR_INVALID_ARG, "network from another context");
+  const size_t n = std::max<size_t>(b->L.cmds.size(), 1);
+  b->features = mlp != nullptr || trackWins != 0;
+  b->mlp = mlp;
+  b->selectFrac = fraction;
+  b->trackWins = trackWins != 0;
+  if (b->features) {
+    OCC_CHECK(b->feat.reserve(n * kFeatures));
+    OCC_CHECK(b->score.reserve(n));
+    OCC_CHECK(b->cand.reserve(n));
+    OCC_CHECK(b->select.reserve(n));
+    OCC_CHECK(b->wins.reserve(n));
+    OCC_CUDA(cudaMemsetAsync(b->wins.p, 0, n * 4, b->ctx->stream));
+    OCC_CUDA(cudaMemsetAsync(b->score.p, 0, n * 4, b->ctx->stream));
+    if (!b->L.cmds.empty())  // no launch before: nothing drawn
+      OCC_CUDA(cudaMemsetAsync(b->S.cmdDraw.p, 0, b->L.cmds.size() * 4, b->ctx->stream));
+  }
+  return capture(b);
+}
+
+int occ_batch_set_zero_depth(occ_batch b, int enable)
+{
+  if (!b) return fail(OCC_ERR_INVALID_ARG, "null batch");
+  b->zeroDepth = enable != 0;
+  return capture(b);
+}
+
+int occ_batch_read_selection(occ_batch b, uint32_t view, float* features, uint32_t* wins, uint8_t* candidate,
+                             uint8_t* selected, float* scores)
+{
+  if (!b || view >= b->L.views.size()) return fail(OCC_ERR_INVALID_ARG, "bad argument");
+  if (!b->features) return fail(OCC_ERR_INVALID_ARG, "selection / win counting is not enabled on this batch");
+  const ViewDesc& V = b->L.views[view];
+  cudaStream_t st = b->ctx->stream;
+  const size_t c0 = V.cmdStart, n = V.cmdCount;
+  if (n) {
+    if (features) OCC_CUDA(cudaMemcpyAsync(features, b->feat.p + c0 * kFeatures, n * kFeatures * 4, cudaMemcpyDeviceToHost, st));
+    if (wins) OCC_CUDA(cudaMemcpyAsync(wins, b->wins.p + c0, n * 4, cudaMemcpyDeviceToHost, st));
+    if (candidate) OCC_CUDA(cudaMemcpyAsync(candidate, b->cand.p + c0, n, cudaMemcpyDeviceToHost, st));
+    if (selected) {
+      if (b->mlp) OCC_CUDA(cudaMemcpyAsync(selected, b->select.p + c0, n, cudaMemcpyDeviceToHost, st));
+      else OCC_CUDA(cudaMemcpyAsync(selected, b->cand.p + c0, n, cudaMemcpyDeviceToHost, st));
+    }
+    if (scores) OCC_CUDA(cudaMemcpyAsync(scores, b->score.p + c0, n * 4, cudaMemcpyDeviceToHost, st));
+  }
+  OCC_CUDA(cudaStreamSynchronize(st));
+  return OCC_OK;
 }
 
 int occ_batch_destroy(occ_batch b)
@@ -1163,6 +1269,158 @@ int occ_coverage_table(int64_t* out4096)
   if (!out4096) return fail(OCC_ERR_INVALID_ARG, "null argument");
   static const unsigned long long t[4096] = {OCC_COVERAGE_TABLE_VALUES};
   std::memcpy(out4096, t, sizeof(t));
+  return OCC_OK;
+}
+
+
+int occ_mlp_param_count(void) { return mlp_param_count(); }
+
+int occ_mlp_create(occ_ctx ctx, uint32_t seed, occ_mlp* out)
+{
+  if (!ctx || !out) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  auto m = std::make_unique<occ_mlp_s>();
+  m->ctx = ctx;
+  const int np = mlp_param_count();
+  OCC_CHECK(m->params.reserve(np));
+  OCC_CHECK(m->m.reserve(np));
+  OCC_CHECK(m->v.reserve(np));
+  OCC_CHECK(m->grad.reserve(np + 1));
+  OCC_CHECK(m->dev.reserve(1));
+  // He-normal initialisation (fixed seed, host RNG), zero biases
+  std::vector<float> p(np, 0.0f);
+  uint64_t st = 0x9E3779B97F4A7C15ull ^ seed;
+  auto next = [&]() {
+    st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+    return (double)(st >> 11) * (1.0 / 9007199254740992.0);
+  };
+  auto normal = [&]() {
+    double u1 = next(), u2 = next();
+    if (u1 < 1e-300) u1 = 1e-300;
+    return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+  };
+  const int nW1 = kHidden * kFeatures, nW2 = kHidden * kHidden;
+  for (int i = 0; i < nW1; ++i) p[i] = (float)(normal() * std::sqrt(2.0 / kFeatures));
+  for (int i = 0; i < nW2; ++i) p[nW1 + kHidden + i] = (float)(normal() * std::sqrt(2.0 / kHidden));
+  for (int i = 0; i < kHidden; ++i) p[nW1 + kHidden + nW2 + kHidden + i] = (float)(normal() * std::sqrt(1.0 / kHidden));
+  OCC_CUDA(cudaMemcpyAsync(m->params.p, p.data(), (size_t)np * 4, cudaMemcpyHostToDevice, ctx->stream));
+  OCC_CUDA(cudaMemsetAsync(m->m.p, 0, (size_t)np * 4, ctx->stream));
+  OCC_CUDA(cudaMemsetAsync(m->v.p, 0, (size_t)np * 4, ctx->stream));
+  OCC_CUDA(cudaMemsetAsync(m->dev.p, 0, sizeof(MlpDevice), ctx->stream));
+  OCC_CUDA(launch_mlp_publish(m->params.p, m->dev.p, ctx->stream));
+  OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+  *out = m.release();
+  return OCC_OK;
+}
+
+int occ_mlp_destroy(occ_mlp m)
+{
+  if (!m) return OCC_OK;
+  cudaStreamSynchronize(m->ctx->stream);
+  delete m;
+  return OCC_OK;
+}
+
+int occ_mlp_get_params(occ_mlp m, float* out)
+{
+  if (!m || !out) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  OCC_CUDA(cudaMemcpyAsync(out, m->params.p, (size_t)mlp_param_count() * 4, cudaMemcpyDeviceToHost, m->ctx->stream));
+  OCC_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  return OCC_OK;
+}
+
+int occ_mlp_set_params(occ_mlp m, const float* in)
+{
+  if (!m || !in) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  OCC_CUDA(cudaMemcpyAsync(m->params.p, in, (size_t)mlp_param_count() * 4, cudaMemcpyHostToDevice, m->ctx->stream));
+  OCC_CUDA(launch_mlp_publish(m->params.p, m->dev.p, m->ctx->stream));
+  OCC_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  return OCC_OK;
+}
+
+int occ_mlp_get_state(occ_mlp m, float* params, float* adamM, float* adamV, uint32_t* step)
+{
+  if (!m) return fail(OCC_ERR_INVALID_ARG, "null network");
+  const size_t bytes = (size_t)mlp_param_count() * 4;
+  cudaStream_t st = m->ctx->stream;
+  if (params) OCC_CUDA(cudaMemcpyAsync(params, m->params.p, bytes, cudaMemcpyDeviceToHost, st));
+  if (adamM) OCC_CUDA(cudaMemcpyAsync(adamM, m->m.p, bytes, cudaMemcpyDeviceToHost, st));
+  if (adamV) OCC_CUDA(cudaMemcpyAsync(adamV, m->v.p, bytes, cudaMemcpyDeviceToHost, st));
+  if (step) *step = m->step;
+  OCC_CUDA(cudaStreamSynchronize(st));
+  return OCC_OK;
+}
+
+int occ_mlp_set_state(occ_mlp m, const float* params, const float* adamM, const float* adamV, uint32_t step)
+{
+  if (!m || !params || !adamM || !adamV) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  const size_t bytes = (size_t)mlp_param_count() * 4;
+  cudaStream_t st = m->ctx->stream;
+  OCC_CUDA(cudaMemcpyAsync(m->params.p, params, bytes, cudaMemcpyHostToDevice, st));
+  OCC_CUDA(cudaMemcpyAsync(m->m.p, adamM, bytes, cudaMemcpyHostToDevice, st));
+  OCC_CUDA(cudaMemcpyAsync(m->v.p, adamV, bytes, cudaMemcpyHostToDevice, st));
+  OCC_CUDA(launch_mlp_publish(m->params.p, m->dev.p, st));
+  OCC_CUDA(cudaStreamSynchronize(st));
+  m->step = step;
+  return OCC_OK;
+}
+
+static int mlp_batch(occ_mlp m, uint32_t n, const float* features, const float* targets)
+{
+  OCC_CHECK(m->feat.reserve((size_t)n * kFeatures));
+  OCC_CHECK(m->score.reserve(n));
+  OCC_CHECK(m->target.reserve(n));
+  OCC_CHECK(m->xb.reserve((size_t)n * kFeatures));
+  OCC_CHECK(m->h1.reserve((size_t)n * kHidden));
+  OCC_CHECK(m->h2.reserve((size_t)n * kHidden));
+  OCC_CHECK(m->ds.reserve(n));
+  OCC_CHECK(m->dh1.reserve((size_t)n * kHidden));
+  OCC_CHECK(m->dh2.reserve((size_t)n * kHidden));
+  OCC_CHECK(m->err2.reserve(n));
+  cudaStream_t st = m->ctx->stream;
+  OCC_CUDA(cudaMemcpyAsync(m->feat.p, features, (size_t)n * kFeatures * 4, cudaMemcpyHostToDevice, st));
+  if (targets) OCC_CUDA(cudaMemcpyAsync(m->target.p, targets, (size_t)n * 4, cudaMemcpyHostToDevice, st));
+  return OCC_OK;
+}
+
+int occ_mlp_forward(occ_mlp m, uint32_t n, const float* features, float* scores)
+{
+  if (!m || (n && (!features || !scores))) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (!n) return OCC_OK;
+  OCC_CHECK(mlp_batch(m, n, features, nullptr));
+  cudaStream_t st = m->ctx->stream;
+  OCC_CUDA(launch_mlp_forward(m->feat.p, n, m->dev.p, m->score.p, nullptr, nullptr, nullptr, st));
+  OCC_CUDA(cudaMemcpyAsync(scores, m->score.p, (size_t)n * 4, cudaMemcpyDeviceToHost, st));
+  OCC_CUDA(cudaStreamSynchronize(st));
+  return OCC_OK;
+}
+
+int occ_mlp_gradients(occ_mlp m, uint32_t n, const float* features, const float* targets, float* loss, float* grads)
+{
+  if (!m || !n || !features || !targets) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  OCC_CHECK(mlp_batch(m, n, features, targets));
+  cudaStream_t st = m->ctx->stream;
+  OCC_CUDA(launch_mlp_forward(m->feat.p, n, m->dev.p, m->score.p, m->h1.p, m->h2.p, m->xb.p, st));
+  OCC_CUDA(launch_mlp_backward(m->score.p, m->target.p, n, m->dev.p, m->xb.p, m->h1.p, m->h2.p, m->ds.p, m->dh1.p,
+                               m->dh2.p, m->err2.p, m->grad.p, st));
+  const int np = mlp_param_count();
+  if (grads) OCC_CUDA(cudaMemcpyAsync(grads, m->grad.p, (size_t)np * 4, cudaMemcpyDeviceToHost, st));
+  if (loss) OCC_CUDA(cudaMemcpyAsync(loss, m->grad.p + np, 4, cudaMemcpyDeviceToHost, st));
+  OCC_CUDA(cudaStreamSynchronize(st));
+  return OCC_OK;
+}
+
+int occ_mlp_train_step(occ_mlp m, uint32_t n, const float* features, const float* targets, float lr, float* loss)
+{
+  if (!m || !n || !features || !targets) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  OCC_CHECK(mlp_batch(m, n, features, targets));
+  cudaStream_t st = m->ctx->stream;
+  OCC_CUDA(launch_mlp_forward(m->feat.p, n, m->dev.p, m->score.p, m->h1.p, m->h2.p, m->xb.p, st));
+  OCC_CUDA(launch_mlp_backward(m->score.p, m->target.p, n, m->dev.p, m->xb.p, m->h1.p, m->h2.p, m->ds.p, m->dh1.p,
+                               m->dh2.p, m->err2.p, m->grad.p, st));
+  OCC_CUDA(launch_adam(m->params.p, m->grad.p, m->m.p, m->v.p, lr, ++m->step, st));
+  OCC_CUDA(launch_mlp_publish(m->params.p, m->dev.p, st));
+  if (loss) OCC_CUDA(cudaMemcpyAsync(loss, m->grad.p + mlp_param_count(), 4, cudaMemcpyDeviceToHost, st));
+  OCC_CUDA(cudaStreamSynchronize(st));
   return OCC_OK;
 }
 

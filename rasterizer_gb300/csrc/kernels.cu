@@ -36,6 +36,7 @@
 #include <mutex>
 
 #include "coverage_table.h"
+#include "query_front.cuh"
 #include "raster_types.h"
 #include "x86_emu.cuh"
 
@@ -146,165 +147,6 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t& t
   total = sm[NT / 32 - 1];
   __syncthreads();
   return prefix + x - v;
-}
-
-// ---- arithmetic policies -------------------------------------------------------------
-// ExactOps applies the x86 NaN rules to every result.  FastOps uses plain IEEE
-// operations and only records whether any result was NaN: without a NaN the
-// two are bit-identical, so callers run FastOps and fall back to ExactOps for
-// the rare inputs that produce one.
-
-struct ExactOps {
-  __device__ __forceinline__ float add(float a, float b) { return x86::xadd(a, b); }
-  __device__ __forceinline__ float sub(float a, float b) { return x86::xsub(a, b); }
-  __device__ __forceinline__ float mul(float a, float b) { return x86::xmul(a, b); }
-  __device__ __forceinline__ float div(float a, float b) { return x86::xdiv(a, b); }
-  __device__ __forceinline__ float fmadd(float a, float b, float c) { return x86::xfmadd(a, b, c); }
-  __device__ __forceinline__ float fmsub(float a, float b, float c) { return x86::xfmsub(a, b, c); }
-  __device__ __forceinline__ float fnmadd(float a, float b, float c) { return x86::xfnmadd(a, b, c); }
-  __device__ __forceinline__ float round(float a) { return x86::round_even(a); }
-  __device__ __forceinline__ float floor(float a) { return x86::floor_(a); }
-  __device__ __forceinline__ float dp4(const float* a, const float* b)
-  {
-    return add(add(mul(a[0], b[0]), mul(a[1], b[1])), add(mul(a[2], b[2]), mul(a[3], b[3])));
-  }
-};
-
-struct FastOps {
-  bool nan = false;
-  __device__ __forceinline__ float chk(float r)
-  {
-    nan |= r != r;
-    return r;
-  }
-  __device__ __forceinline__ float add(float a, float b) { return chk(x86::radd(a, b)); }
-  __device__ __forceinline__ float sub(float a, float b) { return chk(x86::rsub(a, b)); }
-  __device__ __forceinline__ float mul(float a, float b) { return chk(x86::rmul(a, b)); }
-  __device__ __forceinline__ float div(float a, float b) { return chk(x86::rdiv(a, b)); }
-  __device__ __forceinline__ float fmadd(float a, float b, float c) { return chk(x86::rfma(a, b, c)); }
-  __device__ __forceinline__ float fmsub(float a, float b, float c) { return chk(x86::rfma(a, b, -c)); }
-  __device__ __forceinline__ float fnmadd(float a, float b, float c) { return chk(x86::rfma(-a, b, c)); }
-  __device__ __forceinline__ float round(float a) { return chk(rintf(a)); }
-  __device__ __forceinline__ float floor(float a) { return chk(floorf(a)); }
-  __device__ __forceinline__ float dp4(const float* a, const float* b)
-  {
-    return add(add(mul(a[0], b[0]), mul(a[1], b[1])), add(mul(a[2], b[2]), mul(a[3], b[3])));
-  }
-};
-
-// ---- queryVisibility front end (Rasterizer.cpp:123-273) ------------------------------
-
-// Returns 0 (not visible), 1 (visible, needs clipping) or 2 (rect + maxZ for query2D).
-template <class Ops>
-__device__ __forceinline__ int query_front_t(Ops& o, const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect, uint32_t* maxZOut)
-{
-  using x86::xmin; using x86::xmax; using x86::fxor; using x86::fabs_; using x86::sign; using x86::fu;
-  using x86::cvtt; using x86::i2f; using x86::rcp; using x86::pack_depth; using x86::radd; using x86::rmul;
-  float ext[4], ctr[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    ext[i] = o.sub(bmax[i], bmin[i]);
-    ctr[i] = o.add(bmax[i], bmin[i]);
-  }
-  const float* row3 = V.rows + 12;
-  uint32_t signs = 0;
-#pragma unroll
-  for (int p = 0; p < 6; ++p) {
-    const float* rr = V.rows + 4 * (p >> 1);
-    float plane[4], offs[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      plane[i] = (p & 1) ? o.sub(row3[i], rr[i]) : o.add(row3[i], rr[i]);
-      offs[i] = o.add(ctr[i], fxor(ext[i], sign(plane[i])));
-    }
-    signs |= fu(o.dp4(plane, offs));
-  }
-  if (signs & 0x80000000u) return 0;
-
-  const float* col0 = V.cols;
-  const float* col1 = V.cols + 4;
-  const float* col2 = V.cols + 8;
-  const float* col3 = V.cols + 12;
-  float c[8][4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    float e0 = o.mul(col0[i], ext[0]), e1 = o.mul(col1[i], ext[1]), e2 = o.mul(col2[i], ext[2]);
-    c[0][i] = o.fmadd(col0[i], bmin[0], o.fmadd(col1[i], bmin[1], o.fmadd(col2[i], bmin[2], col3[i])));
-    c[1][i] = o.add(c[0][i], e0);
-    c[2][i] = o.add(c[0][i], e1);
-    c[4][i] = o.add(c[0][i], e2);
-    c[3][i] = o.add(c[1][i], e1);
-    c[5][i] = o.add(c[4][i], e0);
-    c[6][i] = o.add(c[2][i], e2);
-    c[7][i] = o.add(c[6][i], e0);
-  }
-  float m1[4] = {xmax(ext[0], ext[2]), xmax(ext[1], ext[3]), xmax(ext[2], ext[0]), xmax(ext[3], ext[1])};
-  float me[4] = {xmax(m1[0], m1[1]), xmax(m1[1], m1[0]), xmax(m1[2], m1[3]), xmax(m1[3], m1[2])};
-  bool close = false;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    float eps = o.mul(me[i], 0.001f);
-    close |= (c[i][3] < eps) || (c[4 + i][3] < eps);
-  }
-  if (close) return 1;
-  float X[8], Y[8], Z[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    float iw = rcp(c[k][3]);
-    X[k] = o.mul(c[k][0], iw);
-    Y[k] = o.mul(c[k][1], iw);
-    Z[k] = o.mul(c[k][2], iw);
-  }
-  float mnX[4], mxX[4], mnY[4], mxY[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    mnX[i] = xmin(X[i], X[4 + i]);
-    mxX[i] = xmax(X[i], X[4 + i]);
-    mnY[i] = xmin(Y[i], Y[4 + i]);
-    mxY[i] = xmax(Y[i], Y[4 + i]);
-  }
-  float mn[4] = {xmin(mnX[0], mnX[2]), xmin(mnY[0], mnY[2]), xmin(mnX[1], mnX[3]), xmin(mnY[1], mnY[3])};
-  float mx[4] = {xmax(mxX[0], mxX[2]), xmax(mxY[0], mxY[2]), xmax(mxX[1], mxX[3]), xmax(mxY[1], mxY[3])};
-  const float limX = i2f((int32_t)(V.width - 1)), limY = i2f((int32_t)(V.height - 1));
-  const float lim[4] = {limX, limY, limX, limY};
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    mn[i] = xmax(mn[i], 0.0f);
-    mx[i] = fxor(xmin(mx[i], lim[i]), 0x80000000u);
-  }
-  float bf[4] = {xmin(mn[0], mn[2]), xmin(mx[0], mx[2]), xmin(mn[1], mn[3]), xmin(mx[1], mx[3])};
-  int32_t b[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) b[i] = cvtt(o.floor(bf[i]));
-  b[1] = (int32_t)(0u - (uint32_t)b[1]);
-  b[3] = (int32_t)(0u - (uint32_t)b[3]);
-  if (b[0] >= b[1] || b[2] >= b[3]) return 0;
-  uint32_t maxZ = 0;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) maxZ = ::max(maxZ, pack_depth(Z[k]));
-  rect[0] = (uint32_t)b[0];
-  rect[1] = (uint32_t)b[1];
-  rect[2] = (uint32_t)b[2];
-  rect[3] = (uint32_t)b[3];
-  *maxZOut = maxZ;
-  return 2;
-}
-
-__device__ __noinline__ int query_front_exact(const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect,
-                                              uint32_t* maxZOut)
-{
-  ExactOps o;
-  return query_front_t(o, V, bmin, bmax, rect, maxZOut);
-}
-
-// Returns 0 (not visible), 1 (visible, needs clipping) or 2 (rect + maxZ for query2D).
-__device__ __forceinline__ int query_front(const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect,
-                                           uint32_t* maxZOut)
-{
-  FastOps f;
-  const int st = query_front_t(f, V, bmin, bmax, rect, maxZOut);
-  if (!f.nan) return st;
-  return query_front_exact(V, bmin, bmax, rect, maxZOut);
 }
 
 // query2D (Rasterizer.cpp:283-349), split by warp-tile.  The reference skips
@@ -638,6 +480,7 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
   if (tid < ch.cmdCount) {
     const Cmd cmd = P.cmds[ch.cmdFirst + tid];
     cmd_prologue(V, cmd, s_cc[tid]);
+    if (P.select && !P.select[ch.cmdFirst + tid]) s_cc[tid].draw = 0;  // not among the view's top-K
     s_cmdStart[tid] = cmd.quadStart;
     P.cmdDraw[ch.cmdFirst + tid] = s_cc[tid].draw | (s_cc[tid].nc << 1);  // same value from every chunk
   }
@@ -660,6 +503,7 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
 #pragma unroll
       for (int j = 0; j < 4; ++j) w4[j] = __ldg(base + 8 * j + lane);
       valid = quad_setup(V, w4, s_cc[k], R, Wk);
+      Wk.pad[0] = ch.cmdFirst + k;  // command of this quad (win counts)
     }
   }
   uint32_t rows = 0, cks = 0;
@@ -921,6 +765,7 @@ struct RasterSmem {
   uint32_t loff[kLocalCap];      // first fragment of each local quad
   uint32_t frag[kRasterThreads * kFragStride];
   uint32_t meta[kRasterThreads]; // per fragment slot: maxZ << 16 | valid << 5 | target block
+  uint32_t fcmd[kRasterThreads]; // per fragment slot: command (win counting only)
   uint32_t bmask[32][kRasterThreads / 32];  // per block: fragment slots aimed at it
   uint32_t hiz[32];              // per block: current hiZ
   uint32_t scan[kRasterThreads / 32];
@@ -1019,9 +864,11 @@ __device__ __forceinline__ bool make_fragment(const FrameParams& P, const QuadRa
 }
 
 // Runs the buffered local list: fragments in order, kRasterThreads at a time.
+// With kWins, own[x] tracks the command (+1) that produced pixel x's value.
+template <bool kWins>
 __device__ __forceinline__ void raster_local_list(const FrameParams& P, const ViewDesc& V, RasterSmem& S, uint32_t n,
                                                   uint32_t tx0, uint32_t ty0, uint32_t tid, uint32_t blk, bool inView,
-                                                  uint32_t (&row)[4], uint32_t& hiz, bool& have)
+                                                  uint32_t (&row)[4], uint32_t& hiz, bool& have, uint32_t (&own)[8])
 {
   const uint32_t lane = tid & 31;
   const uint32_t py = tid & 7;  // pixel row owned by this thread
@@ -1082,6 +929,7 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
 #pragma unroll
           for (int w = 0; w < 4; ++w) dst[4 * y + w] = r[y][w];
         meta = ((uint32_t)Q.maxZ << 16) | 32u | target;
+        if (kWins) S.fcmd[tid] = P.walk[q].pad[0];
         atomicOr(&S.bmask[target][tid >> 5], 1u << lane);
       }
     }
@@ -1100,14 +948,28 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
           const uint32_t* src = S.frag + slot * kFragStride + 4 * py;
           if (hiz == 1) {
 #pragma unroll
-            for (int i = 0; i < 4; ++i) row[i] = src[i];
+            for (int i = 0; i < 4; ++i) {
+              if (kWins) {
+                const uint32_t c1 = S.fcmd[slot] + 1;
+                own[2 * i] = (src[i] & 0xFFFFu) ? c1 : 0u;
+                own[2 * i + 1] = (src[i] >> 16) ? c1 : 0u;
+              }
+              row[i] = src[i];
+            }
           } else {
             if (!have) {
               const uint4 a = *reinterpret_cast<const uint4*>(V.depth + (size_t)blk * 64 + 8 * py);
               row[0] = a.x; row[1] = a.y; row[2] = a.z; row[3] = a.w;
             }
 #pragma unroll
-            for (int i = 0; i < 4; ++i) row[i] = vmax_u16x2(row[i], src[i]);
+            for (int i = 0; i < 4; ++i) {
+              if (kWins) {
+                const uint32_t c1 = S.fcmd[slot] + 1;
+                if ((src[i] & 0xFFFFu) > (row[i] & 0xFFFFu)) own[2 * i] = c1;
+                if ((src[i] >> 16) > (row[i] >> 16)) own[2 * i + 1] = c1;
+              }
+              row[i] = vmax_u16x2(row[i], src[i]);
+            }
           }
           have = true;
           uint32_t mn = vmin_u16x2(vmin_u16x2(row[0], row[1]), vmin_u16x2(row[2], row[3]));
@@ -1123,6 +985,7 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
   }
 }
 
+template <bool kWins>
 __global__ void __launch_bounds__(kRasterThreads, 2) k_raster(FrameParams P)
 {
   __shared__ RasterSmem S;
@@ -1148,6 +1011,7 @@ __global__ void __launch_bounds__(kRasterThreads, 2) k_raster(FrameParams P)
   uint32_t hiz = clearing ? 1u : (inView ? (uint32_t)V.hiz[blk] : 0xFFFFu);
   bool have = false;
   uint32_t row[4] = {0, 0, 0, 0};
+  uint32_t own[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (py == 0) S.hiz[myBlock] = hiz;
   __syncthreads();
 
@@ -1202,7 +1066,7 @@ __global__ void __launch_bounds__(kRasterThreads, 2) k_raster(FrameParams P)
     }
     __syncthreads();
     if (n > (uint32_t)(kLocalCap - kScanPerRound) || (base + kScanPerRound >= listLen && n > 0)) {
-      raster_local_list(P, V, S, n, tx0, ty0, tid, blk, inView, row, hiz, have);
+      raster_local_list<kWins>(P, V, S, n, tx0, ty0, tid, blk, inView, row, hiz, have, own);
       n = 0;
     }
   }
@@ -1211,6 +1075,17 @@ __global__ void __launch_bounds__(kRasterThreads, 2) k_raster(FrameParams P)
     if (have) *reinterpret_cast<uint4*>(V.depth + (size_t)blk * 64 + 8 * py) = make_uint4(row[0], row[1], row[2], row[3]);
   }
   if (clearing && lt == 0 && tid < 8) V.hiz[V.blocksX * V.blocksY + tid] = 1;  // padding entries
+  if (kWins) {
+    // a pixel is won by the command whose fragment set its final value (the
+    // fast-clear overwrite or a strictly larger max-merge); one atomic per
+    // distinct command per warp and pixel column
+#pragma unroll
+    for (int x = 0; x < 8; ++x) {
+      const uint32_t key = inView ? own[x] : 0u;
+      const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+      if (key && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&P.wins[key - 1], (uint32_t)__popc(peers));
+    }
+  }
   // per-tile minimum hiZ for the queries
   uint32_t tmin = (inView && py == 0) ? hiz : 0xFFFFu;
 #pragma unroll
@@ -1348,7 +1223,10 @@ cudaError_t launch_flush(const FrameParams& P, uint32_t numSt, uint32_t maxStPer
       k_fill<<<P.numChunks, kChunk, (size_t)maxStPerView * 64, stream>>>(P);
       k_walk<<<g_walkBlocks, 256, 0, stream>>>(P);
     }
-    if (P.numTiles) k_raster<<<P.numTiles, kRasterThreads, 0, stream>>>(P);
+    if (P.numTiles) {
+      if (P.wins) k_raster<true><<<P.numTiles, kRasterThreads, 0, stream>>>(P);
+      else k_raster<false><<<P.numTiles, kRasterThreads, 0, stream>>>(P);
+    }
   }
   if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
   return cudaGetLastError();
@@ -1371,7 +1249,10 @@ cudaError_t launch_flush_timed(const FrameParams& P, uint32_t numSt, uint32_t ma
   cudaEventRecord(ev[3], stream);
   if (doRaster && P.numChunks) k_walk<<<g_walkBlocks, 256, 0, stream>>>(P);
   cudaEventRecord(ev[4], stream);
-  if (doRaster && P.numTiles) k_raster<<<P.numTiles, kRasterThreads, 0, stream>>>(P);
+  if (doRaster && P.numTiles) {
+    if (P.wins) k_raster<true><<<P.numTiles, kRasterThreads, 0, stream>>>(P);
+    else k_raster<false><<<P.numTiles, kRasterThreads, 0, stream>>>(P);
+  }
   cudaEventRecord(ev[5], stream);
   if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
   cudaEventRecord(ev[6], stream);

@@ -99,6 +99,21 @@ struct QuadWalk {
   uint32_t pad[2];
 };
 
+constexpr int kFeatures = 16;  // per-occluder features of the learned selector
+constexpr int kHidden = 64;    // MLP 16 -> 64 -> 64 -> 1
+
+// MLP weights as the kernels read them: bf16 matrices stored output-major
+// (w1t[n][k], w2t[n][k]), fp32 biases and output layer.
+struct MlpDevice {
+  uint16_t w1t[kHidden * kFeatures];
+  uint16_t w2t[kHidden * kHidden];
+  float b1[kHidden];
+  float b2[kHidden];
+  float w3[kHidden];
+  float b3;
+  float pad[3];
+};
+
 struct Totals {
   uint32_t rows, cks, st, pad;
 };
@@ -139,6 +154,15 @@ struct FrameParams {
   uint32_t* visBits;     // one bit per query slot
   uint32_t* ncBits;
   uint32_t* cmdDraw;     // per command: bit0 drawn, bit1 near-clipped (gated result)
+  // learned occluder selection and win counts (all optional)
+  float* feat;           // per command: kFeatures features
+  float* score;          // per command: MLP score
+  uint8_t* cand;         // per command: passes the gating test (selection candidate)
+  uint8_t* select;       // per command: 1 = rasterise; null = every command
+  uint32_t* wins;        // per command: pixels whose final depth it produced (read as the
+                         // previous frame's wins by the feature kernel, then reset)
+  const MlpDevice* mlp;
+  float selectFrac;      // fraction of each view's candidates kept
 };
 
 }  // namespace occ

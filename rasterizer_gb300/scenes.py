@@ -269,6 +269,22 @@ class ViewSpec:
     occluders: np.ndarray  # indices into the scene's occluder list, nearest first
     query_start: int
     query_count: int
+    camera: dict = None  # view_projection arguments (eye, direction, up, fov_y, aspect, near)
+
+    def moved(self, offset) -> np.ndarray:
+        """The view's matrix with the eye displaced by `offset` (3,)."""
+        cam = dict(self.camera)
+        cam["eye"] = np.asarray(cam["eye"], np.float64) + np.asarray(offset, np.float64)
+        return view_projection(**cam)
+
+
+def view_track(spec: ViewSpec, frames: int, seed: int, speed: float = 0.6) -> np.ndarray:
+    """(frames, 16) matrices of `spec` with its eye drifting horizontally
+    `speed` units per frame along a seeded direction (frame 0 = spec.mvp)."""
+    rng = np.random.default_rng(seed)
+    a = rng.uniform(0, 2 * math.pi)
+    step = speed * np.array([math.cos(a), 0.0, math.sin(a)])
+    return np.stack([spec.mvp if f == 0 else spec.moved(step * f) for f in range(frames)]).astype(np.float32)
 
 
 def _pick_occluders(centers: np.ndarray, tris: np.ndarray, eye, budget: int) -> np.ndarray:
@@ -305,11 +321,12 @@ def multiview_workload(centers: np.ndarray, quads: np.ndarray, n_query_pool: int
     for k in range(counts[0]):
         target = np.array([rng.uniform(-half * 0.6, half * 0.6), 0.0, rng.uniform(-half * 0.6, half * 0.6)])
         eye = target - light * 400.0
-        mvp = view_projection(eye, light, up=(0.0, 0.0, 1.0), fov_y=math.radians(25.0), aspect=1.0,
-                              near=1.0, far=5000.0)
+        cam = dict(eye=eye, direction=light, up=(0.0, 0.0, 1.0), fov_y=math.radians(25.0), aspect=1.0, near=1.0)
+        mvp = view_projection(**cam)
         budget = int(rng.integers(1_000, 200_001))
         s, n = queries()
-        views.append(ViewSpec("cascade", 1024, 1024, mvp, eye, _pick_occluders(centers, tris, eye, budget), s, n))
+        views.append(ViewSpec("cascade", 1024, 1024, mvp, eye, _pick_occluders(centers, tris, eye, budget), s, n,
+                              cam))
     faces = [((1, 0, 0), (0, 1, 0)), ((-1, 0, 0), (0, 1, 0)), ((0, 1, 0), (0, 0, -1)),
              ((0, -1, 0), (0, 0, 1)), ((0, 0, 1), (0, 1, 0)), ((0, 0, -1), (0, 1, 0))]
     for p in range((counts[1] + 5) // 6):
@@ -319,17 +336,19 @@ def multiview_workload(centers: np.ndarray, quads: np.ndarray, n_query_pool: int
         for d, up in faces:
             if len(views) >= counts[0] + counts[1]:
                 break
-            mvp = view_projection(eye, d, up=up, fov_y=math.radians(90.0), aspect=1.0, near=0.5)
+            cam = dict(eye=eye, direction=d, up=up, fov_y=math.radians(90.0), aspect=1.0, near=0.5)
+            mvp = view_projection(**cam)
             s, n = queries()
-            views.append(ViewSpec("cube", 512, 512, mvp, eye, occ, s, n))
+            views.append(ViewSpec("cube", 512, 512, mvp, eye, occ, s, n, cam))
     for k in range(counts[2]):
         w = int(rng.integers(32, 241)) * 8
         h = int(rng.integers(16, 136)) * 8
         eye = np.array([rng.choice(streets) + rng.uniform(-3, 3), 1.7, rng.choice(streets) + rng.uniform(-3, 3)])
         yaw = rng.uniform(0, 2 * math.pi)
         d = (math.cos(yaw), -0.05, math.sin(yaw))
-        mvp = view_projection(eye, d, fov_y=math.radians(60.0), aspect=w / h)
+        cam = dict(eye=eye, direction=d, fov_y=math.radians(60.0), aspect=w / h)
+        mvp = view_projection(**cam)
         budget = int(rng.integers(1_000, 200_001))
         s, n = queries()
-        views.append(ViewSpec("probe", w, h, mvp, eye, _pick_occluders(centers, tris, eye, budget), s, n))
+        views.append(ViewSpec("probe", w, h, mvp, eye, _pick_occluders(centers, tris, eye, budget), s, n, cam))
     return views

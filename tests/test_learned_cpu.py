@@ -1,0 +1,58 @@
+"""CPU tests of the learned-selection host logic: training targets, the eye
+recovered from a view matrix, and the cull accounting."""
+import numpy as np
+
+from rasterizer_gb300 import learned as L
+from rasterizer_gb300 import scenes
+from oracle import mlp as ref
+
+
+def test_targets():
+    lab = dict(wins=np.array([0, 5, 10, 0, 3, 3, 100]), wh=np.full(7, 100), group=np.array([0, 0, 0, 1, 1, 1, 1]))
+    t = L.targets(lab, "log_view")
+    assert np.allclose(t, np.log2(1 + lab["wins"]) / np.log2(101))
+    r = L.targets(lab, "rank")
+    assert r[2] == 1.0 and r[6] == 1.0 and r[0] == 0 and r[3] == 0
+    assert 0 < r[1] < 1
+    m = L.targets(lab, "log_max")
+    assert np.all(m <= 1) and m[0] == 0
+
+
+def test_eye_of_view_matrix():
+    mvps, eyes = scenes.camera_path(20, seed=3)
+    for m, e in zip(mvps, eyes):
+        got = L._eye_of(np.asarray(m, np.float64).reshape(4, 4))
+        assert np.allclose(got, e[:3], atol=2e-3 * max(1.0, np.abs(e[:3]).max()))
+
+
+def test_cull_stats():
+    st = L.CullStats()
+    full = dict(culled=np.array([1, 1, 1, 0, 0], bool), visible_empty=np.array([1, 1, 0, 1, 1], bool),
+                candidate=np.array([1, 1, 0], bool))
+    st.add(np.array([1, 0, 1, 0, 0], bool), full, np.array([1, 0, 0], bool), np.array([10, 20, 30]))
+    assert (st.full, st.kept, st.false, st.full_all, st.kept_all) == (2, 1, 0, 3, 2)
+    assert (st.candidates, st.drawn, st.quads_candidates, st.quads_drawn) == (2, 1, 30, 10)
+    assert st.retained == 0.5
+
+
+def test_reference_gradient_matches_finite_differences():
+    """The CPU reference's gradient (bf16 roundings as identity) against
+    central differences of its own forward with the roundings removed."""
+    rng = np.random.default_rng(0)
+    p = rng.normal(0, 0.3, ref.PARAMS).astype(np.float32)
+    x = rng.uniform(0, 1, (40, 16)).astype(np.float32)
+    t = rng.uniform(0, 1, 40).astype(np.float32)
+    saved = ref.bf16
+    ref.bf16 = lambda a: np.asarray(a, np.float32)
+    try:
+        _, g = ref.gradients(p, x, t)
+        for i in rng.choice(ref.PARAMS, 25, replace=False):
+            h = 1e-3
+            pp, pm = p.astype(np.float64).copy(), p.astype(np.float64).copy()
+            pp[i] += h
+            pm[i] -= h
+            fp = np.mean((ref.forward(pp.astype(np.float32), x) - t) ** 2)
+            fm = np.mean((ref.forward(pm.astype(np.float32), x) - t) ** 2)
+            assert abs((fp - fm) / (2 * h) - g[i]) < 2e-3 * max(1.0, abs(g[i])), i
+    finally:
+        ref.bf16 = saved
