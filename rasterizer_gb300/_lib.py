@@ -64,6 +64,7 @@ SIGNATURES = {
     "occ_batch_set_selection": (I32, [P, P, C.c_float, I32]),
     "occ_batch_read_selection": (I32, [P, U32, P, P, P, P, P]),
     "occ_batch_set_zero_depth": (I32, [P, I32]),
+    "occ_batch_stats": (I32, [P, P]),
     "occ_mlp_param_count": (I32, []),
     "occ_mlp_create": (I32, [P, U32, C.POINTER(P)]),
     "occ_mlp_destroy": (I32, [P]),

@@ -419,6 +419,13 @@ class PreparedBatch:
                                             int(bool(trackWins))), "occ_batch_set_selection")
         self._selector = mlp  # the captured launch reads the network's weights
 
+    def stats(self) -> dict:
+        """Work counts of the last launch."""
+        out = np.zeros(6, np.uint32)
+        check(lib().occ_batch_stats(self.handle, _ptr(out)), "occ_batch_stats")
+        keys = ("rows", "checkpoints", "list_entries", "active_chunks", "active_tiles", "chunks")
+        return {k: int(v) for k, v in zip(keys, out)}
+
     def setZeroDepth(self, enable: bool) -> None:
         """Zero each cleared view's depth at the start of every launch, so a
         frame's queries do not see depth left by earlier frames in cleared

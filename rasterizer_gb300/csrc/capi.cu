@@ -143,7 +143,8 @@ struct FrameScratch {
   DevBuf<QuadRaster> rec;
   DevBuf<QuadWalk> walk;
   DevBuf<Totals> chunkTot, chunkBase, viewTot, viewBase;
-  DevBuf<uint32_t> mat, stStart, stLen, cmdDraw, ckBase;
+  DevBuf<uint32_t> mat, stStart, stLen, cmdDraw, ckBase, activeChunks;
+  DevBuf<uint2> activeTiles;
   DevBuf<uint4> stList;
   DevBuf<float> ck;
   DevBuf<uint2> rowOwner;  // sized like the checkpoints (a row has at least one)
@@ -364,6 +365,8 @@ int run_batch(occ_ctx_s* ctx, FrameScratch& S, std::vector<ViewJob>& jobs, bool 
   OCC_CHECK(S.stStart.reserve(L.numSt));
   OCC_CHECK(S.stLen.reserve(L.numSt));
   OCC_CHECK(S.cmdDraw.reserve(L.cmds.size()));
+  OCC_CHECK(S.activeChunks.reserve(L.chunks.size()));
+  OCC_CHECK(S.activeTiles.reserve(L.numTiles));
   if (S.header.n == 0) {
     OCC_CHECK(S.header.reserve(1));
     OCC_CUDA(cudaMemsetAsync(S.header.p, 0, sizeof(FrameHeader), ctx->stream));
@@ -405,6 +408,10 @@ int run_batch(occ_ctx_s* ctx, FrameScratch& S, std::vector<ViewJob>& jobs, bool 
     FrameParams P{};
     P.views = reinterpret_cast<const ViewDesc*>(S.tables.p + offViews);
     P.numViews = nv;
+    P.numCmds = (uint32_t)L.cmds.size();
+    P.matSize = L.matSize;
+    P.activeChunkList = S.activeChunks.p;
+    P.activeTileList = S.activeTiles.p;
     P.cmds = reinterpret_cast<const Cmd*>(S.tables.p + offCmds);
     P.chunks = reinterpret_cast<const Chunk*>(S.tables.p + offChunks);
     P.numChunks = (uint32_t)L.chunks.size();
@@ -948,6 +955,10 @@ int capture(occ_batch_s* b)
   FrameParams P{};
   P.views = reinterpret_cast<const ViewDesc*>(S.tables.p);
   P.numViews = (uint32_t)b->L.views.size();
+  P.numCmds = (uint32_t)b->L.cmds.size();
+  P.matSize = b->L.matSize;
+  P.activeChunkList = S.activeChunks.p;
+  P.activeTileList = S.activeTiles.p;
   P.cmds = reinterpret_cast<const Cmd*>(S.tables.p + b->offCmds);
   P.chunks = reinterpret_cast<const Chunk*>(S.tables.p + b->offChunks);
   P.numChunks = (uint32_t)b->L.chunks.size();
@@ -1218,6 +1229,21 @@ int occ_batch_set_selection(occ_batch b, occ_mlp mlp, float fraction, int trackW
       OCC_CUDA(cudaMemsetAsync(b->S.cmdDraw.p, 0, b->L.cmds.size() * 4, b->ctx->stream));
   }
   return capture(b);
+}
+
+int occ_batch_stats(occ_batch b, uint32_t out[6])
+{
+  if (!b || !out) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  FrameHeader H;
+  OCC_CUDA(cudaStreamSynchronize(b->ctx->stream));
+  OCC_CUDA(cudaMemcpy(&H, b->S.header.p, sizeof(H), cudaMemcpyDeviceToHost));
+  out[0] = H.totalRows;
+  out[1] = H.totalCks;
+  out[2] = H.totalSt;
+  out[3] = H.activeChunks;
+  out[4] = H.activeTiles;
+  out[5] = (uint32_t)b->L.chunks.size();
+  return OCC_OK;
 }
 
 int occ_batch_set_zero_depth(occ_batch b, int enable)

@@ -46,6 +46,11 @@ __device__ const unsigned long long kDevCoverage[4096] = {OCC_COVERAGE_TABLE_VAL
 
 // Row-walk grid: a few CTAs per SM, grid-striding over the batch's rows.
 static uint32_t g_walkBlocks = 152 * 8;
+// Persistent grids of the setup / list-fill / raster kernels (resident CTAs x SMs),
+// looping over the launch's active chunks and tiles.
+static uint32_t g_setupBlocks = 152 * 4;
+static uint32_t g_fillBlocks = 152 * 4;
+static uint32_t g_rasterBlocks = 152 * 2;
 
 // Primitive mode for the 8-bit configuration (area signs | W signs << 4),
 // the classification of Rasterizer.cpp:30-64.
@@ -216,18 +221,6 @@ __device__ __forceinline__ void cmd_prologue_t(Ops& o, const ViewDesc& V, const 
 {
   using x86::xmin; using x86::xmax; using x86::fxor; using x86::fabs_; using x86::sign; using x86::fu;
   using x86::cvtt; using x86::i2f; using x86::rcp; using x86::pack_depth; using x86::radd; using x86::rmul;
-  if (cmd.flags & kCmdGated) {
-    // queryVisibility of the bounds against an empty buffer: visible iff in
-    // the frustum and either near the camera plane or covering a nonempty
-    // screen rectangle with a nonzero depth bound.
-    uint32_t rect[4], maxZ = 0;
-    int st = query_front(V, cmd.boundsMin, cmd.boundsMax, rect, &maxZ);
-    out.draw = st == 1 || (st == 2 && maxZ > 0);
-    out.nc = st == 1;
-  } else {
-    out.draw = 1;
-    out.nc = (cmd.flags & kCmdNearClip) ? 1 : 0;
-  }
   float col[4][4];
 #pragma unroll
   for (int j = 0; j < 4; ++j)
@@ -462,6 +455,56 @@ __device__ __forceinline__ uint32_t nck_of(const QuadRaster& R)
   return (uint32_t)((R.maxX - 1) >> 3) - (uint32_t)(R.minX >> 3) + 1u;
 }
 
+// ---- k_gate / k_chunk_gate ------------------------------------------------------------
+// One thread per command: whether it is drawn and with which variant.  A gated
+// command runs queryVisibility of its bounds against an empty buffer: drawn
+// iff in the frustum and either near the camera plane or covering a nonempty
+// screen rectangle with a nonzero depth bound; needs clipping iff near the
+// camera plane.  With a selection, commands outside the view's top-K are not
+// drawn.
+
+__global__ void __launch_bounds__(256) k_gate(FrameParams P)
+{
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= P.numCmds) return;
+  const Cmd& cmd = P.cmds[c];
+  uint32_t draw = 1, nc = (cmd.flags & kCmdNearClip) ? 1u : 0u;
+  if (cmd.flags & kCmdGated) {
+    uint32_t rect[4], maxZ = 0;
+    const int st = query_front(P.views[cmd.view], cmd.boundsMin, cmd.boundsMax, rect, &maxZ);
+    draw = (st == 1 || (st == 2 && maxZ > 0)) ? 1u : 0u;
+    nc = st == 1 ? 1u : 0u;
+  }
+  if (P.select && !P.select[c]) draw = 0;  // not among the view's top-K
+  P.cmdDraw[c] = draw | (nc << 1);
+}
+
+// One thread per chunk: chunks with a drawn command go to the active list (in
+// any order: a chunk's outputs do not depend on where it is processed); the
+// others contribute no rows, checkpoints or list entries.
+__global__ void __launch_bounds__(256) k_chunk_gate(FrameParams P)
+{
+  __shared__ uint32_t s_n, s_base;
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  bool active = false;
+  if (c < P.numChunks) {
+    const Chunk ch = P.chunks[c];
+    for (uint32_t k = 0; k < ch.cmdCount && !active; ++k) active = (P.cmdDraw[ch.cmdFirst + k] & 1u) != 0;
+    if (!active) P.chunkTot[c] = Totals{0, 0, 0, 0};
+  }
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t bal = __ballot_sync(0xFFFFFFFFu, active);
+  uint32_t wbase = 0;
+  if (lane == 0 && bal) wbase = atomicAdd(&s_n, (uint32_t)__popc(bal));
+  __syncthreads();
+  if (threadIdx.x == 0 && s_n) s_base = atomicAdd(&P.header->activeChunks, s_n);
+  __syncthreads();
+  wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
+  if (active) P.activeChunkList[s_base + wbase + __popc(bal & ((1u << lane) - 1u))] = c;
+}
+
 // ---- k_setup -------------------------------------------------------------------------
 
 __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
@@ -471,65 +514,70 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
   __shared__ uint32_t s_cmdStart[kMaxCmdPerChunk];
   __shared__ uint32_t s_scan[kChunk / 32];
 
-  const uint32_t c = blockIdx.x;
-  const Chunk ch = P.chunks[c];
-  const ViewDesc& V = P.views[ch.view];
   const uint32_t tid = threadIdx.x;
-  const uint32_t nst = V.stX * V.stY;
-  for (uint32_t i = tid; i < nst; i += kChunk) s_stCount[i] = 0;
-  if (tid < ch.cmdCount) {
-    const Cmd cmd = P.cmds[ch.cmdFirst + tid];
-    cmd_prologue(V, cmd, s_cc[tid]);
-    if (P.select && !P.select[ch.cmdFirst + tid]) s_cc[tid].draw = 0;  // not among the view's top-K
-    s_cmdStart[tid] = cmd.quadStart;
-    P.cmdDraw[ch.cmdFirst + tid] = s_cc[tid].draw | (s_cc[tid].nc << 1);  // same value from every chunk
-  }
-  __syncthreads();
-
-  const uint32_t q = (c << kChunkShift) + tid;
-  QuadRaster R;
-  QuadWalk Wk;
-  bool valid = false;
-  if (tid < ch.quadCount) {
-    uint32_t k = 0;
-    for (uint32_t i = 1; i < ch.cmdCount; ++i)
-      if (s_cmdStart[i] <= q) k = i;
-    if (s_cc[k].draw) {
-      const Cmd& cmd = P.cmds[ch.cmdFirst + k];
-      const uint32_t local = q - cmd.quadStart;     // quad within the occluder
-      const uint32_t group = local >> 3, lane = local & 7;
-      const uint32_t* base = P.pool + cmd.wordOffset + group * 32;
-      uint32_t w4[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) w4[j] = __ldg(base + 8 * j + lane);
-      valid = quad_setup(V, w4, s_cc[k], R, Wk);
-      Wk.pad[0] = ch.cmdFirst + k;  // command of this quad (win counts)
+  const uint32_t nActive = P.header->activeChunks;
+  for (uint32_t ai = blockIdx.x; ai < nActive; ai += gridDim.x) {
+    const uint32_t c = P.activeChunkList[ai];
+    const Chunk ch = P.chunks[c];
+    const ViewDesc& V = P.views[ch.view];
+    const uint32_t nst = V.stX * V.stY;
+    for (uint32_t i = tid; i < nst; i += kChunk) s_stCount[i] = 0;
+    if (tid < ch.cmdCount) {
+      const Cmd cmd = P.cmds[ch.cmdFirst + tid];
+      const uint32_t dn = P.cmdDraw[ch.cmdFirst + tid];  // k_gate
+      if (dn & 1u) cmd_prologue(V, cmd, s_cc[tid]);
+      s_cc[tid].draw = dn & 1u;
+      s_cc[tid].nc = dn >> 1;
+      s_cmdStart[tid] = cmd.quadStart;
     }
+    __syncthreads();
+
+    const uint32_t q = (c << kChunkShift) + tid;
+    QuadRaster R;
+    QuadWalk Wk;
+    bool valid = false;
+    if (tid < ch.quadCount) {
+      uint32_t k = 0;
+      for (uint32_t i = 1; i < ch.cmdCount; ++i)
+        if (s_cmdStart[i] <= q) k = i;
+      if (s_cc[k].draw) {
+        const Cmd& cmd = P.cmds[ch.cmdFirst + k];
+        const uint32_t local = q - cmd.quadStart;     // quad within the occluder
+        const uint32_t group = local >> 3, lane = local & 7;
+        const uint32_t* base = P.pool + cmd.wordOffset + group * 32;
+        uint32_t w4[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) w4[j] = __ldg(base + 8 * j + lane);
+        valid = quad_setup(V, w4, s_cc[k], R, Wk);
+        Wk.pad[0] = ch.cmdFirst + k;  // command of this quad (win counts)
+      }
+    }
+    uint32_t rows = 0, cks = 0;
+    if (valid) {
+      rows = (uint32_t)(R.maxY - R.minY);
+      cks = rows * nck_of(R);
+    } else {
+      R = QuadRaster{};
+      Wk = QuadWalk{};
+    }
+    uint32_t totRows, totCks;
+    const uint32_t rowLocal = block_exclusive_scan<kChunk>(rows, totRows, s_scan);
+    const uint32_t ckLocal = block_exclusive_scan<kChunk>(cks, totCks, s_scan);
+    R.ckLocal = ckLocal;
+    Wk.rowLocal = rowLocal;
+    P.rec[q] = R;
+    P.walk[q] = Wk;
+    if (valid) {
+      const uint32_t sx0 = R.minX / kSuperTile, sx1 = (R.maxX - 1u) / kSuperTile;
+      const uint32_t sy0 = R.minY / kSuperTile, sy1 = (R.maxY - 1u) / kSuperTile;
+      for (uint32_t sy = sy0; sy <= sy1; ++sy)
+        for (uint32_t sx = sx0; sx <= sx1; ++sx) atomicAdd(&s_stCount[sy * V.stX + sx], 1u);
+    }
+    __syncthreads();
+    for (uint32_t st = tid; st < nst; st += kChunk) P.mat[V.matBase + st * V.chunkCount + ch.localIndex] = s_stCount[st];
+    if (tid == 0) P.chunkTot[c] = Totals{totRows, totCks, 0, 0};
+    __syncthreads();  // shared arrays are reused by the next chunk
   }
-  uint32_t rows = 0, cks = 0;
-  if (valid) {
-    rows = (uint32_t)(R.maxY - R.minY);
-    cks = rows * nck_of(R);
-  } else {
-    R = QuadRaster{};
-    Wk = QuadWalk{};
-  }
-  uint32_t totRows, totCks;
-  const uint32_t rowLocal = block_exclusive_scan<kChunk>(rows, totRows, s_scan);
-  const uint32_t ckLocal = block_exclusive_scan<kChunk>(cks, totCks, s_scan);
-  R.ckLocal = ckLocal;
-  Wk.rowLocal = rowLocal;
-  P.rec[q] = R;
-  P.walk[q] = Wk;
-  if (valid) {
-    const uint32_t sx0 = R.minX / kSuperTile, sx1 = (R.maxX - 1u) / kSuperTile;
-    const uint32_t sy0 = R.minY / kSuperTile, sy1 = (R.maxY - 1u) / kSuperTile;
-    for (uint32_t sy = sy0; sy <= sy1; ++sy)
-      for (uint32_t sx = sx0; sx <= sx1; ++sx) atomicAdd(&s_stCount[sy * V.stX + sx], 1u);
-  }
-  __syncthreads();
-  for (uint32_t s = tid; s < nst; s += kChunk) P.mat[V.matBase + s * V.chunkCount + ch.localIndex] = s_stCount[s];
-  if (tid == 0) P.chunkTot[c] = Totals{totRows, totCks, 0, 0};
 }
 
 // ---- k_scan ----------------------------------------------------------------------------
@@ -628,67 +676,72 @@ __global__ void __launch_bounds__(kChunk) k_fill(FrameParams P)
   __shared__ uint32_t s_rowLocal[kChunk];
   __shared__ int s_rect[4];
   if (P.header->overflow) return;
-  const uint32_t c = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const Chunk ch = P.chunks[c];
-  const ViewDesc& V = P.views[ch.view];
-  const uint32_t q = (c << kChunkShift) + tid;
-  const QuadRaster R = P.rec[q];
-  const bool valid = tid < ch.quadCount && R.minX < R.maxX;
-  const uint32_t ckChunk = P.viewBase[ch.view].cks + P.chunkBase[c].cks;
-  if (valid) P.ckBase[q] = ckChunk + R.ckLocal;
-  s_rowLocal[tid] = P.walk[q].rowLocal;  // this thread's quad only
-  if (tid == 0) {
-    s_rect[0] = 1 << 30; s_rect[1] = -1; s_rect[2] = 1 << 30; s_rect[3] = -1;
-  }
-  __syncthreads();
-  int sx0 = 0, sx1 = -1, sy0 = 0, sy1 = -1;
-  if (valid) {
-    sx0 = R.minX / kSuperTile; sx1 = (R.maxX - 1) / kSuperTile;
-    sy0 = R.minY / kSuperTile; sy1 = (R.maxY - 1) / kSuperTile;
-    atomicMin(&s_rect[0], sx0); atomicMax(&s_rect[1], sx1);
-    atomicMin(&s_rect[2], sy0); atomicMax(&s_rect[3], sy1);
-  }
-  __syncthreads();
-  // super-tile lists in submission order: per super-tile of the chunk's union
-  // rectangle, one ballot per warp, then a prefix over the 8 warps
-  const int ux0 = s_rect[0], ux1 = s_rect[1], uy0 = s_rect[2], uy1 = s_rect[3];
-  const int uw = ux1 - ux0 + 1;
-  const int nu = ux1 >= ux0 ? uw * (uy1 - uy0 + 1) : 0;
-  uint32_t* s_bal = s_dyn;                    // [nu][8]
-  uint32_t* s_pre = s_dyn + (size_t)nu * 8;   // [nu][8]
-  for (int u = 0; u < nu; ++u) {
-    const int sx = ux0 + u % uw, sy = uy0 + u / uw;
-    const bool flag = valid && sx >= sx0 && sx <= sx1 && sy >= sy0 && sy <= sy1;
-    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, flag);
-    if (lane == 0) s_bal[u * 8 + warp] = bal;
-  }
-  __syncthreads();
-  for (int u = tid; u < nu; u += kChunk) {
-    uint32_t acc = 0;
-#pragma unroll
-    for (int w = 0; w < 8; ++w) {
-      s_pre[u * 8 + w] = acc;
-      acc += __popc(s_bal[u * 8 + w]);
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t nActive = P.header->activeChunks;
+  for (uint32_t ai = blockIdx.x; ai < nActive; ai += gridDim.x) {
+    const uint32_t c = P.activeChunkList[ai];
+    const Chunk ch = P.chunks[c];
+    const ViewDesc& V = P.views[ch.view];
+    const uint32_t q = (c << kChunkShift) + tid;
+    const QuadRaster R = P.rec[q];
+    const bool valid = tid < ch.quadCount && R.minX < R.maxX;
+    const uint32_t ckChunk = P.viewBase[ch.view].cks + P.chunkBase[c].cks;
+    if (valid) P.ckBase[q] = ckChunk + R.ckLocal;
+    s_rowLocal[tid] = P.walk[q].rowLocal;  // this thread's quad only
+    if (tid == 0) {
+      s_rect[0] = 1 << 30; s_rect[1] = -1; s_rect[2] = 1 << 30; s_rect[3] = -1;
     }
-  }
-  __syncthreads();
-  if (valid) {
-    const uint32_t lt = (1u << lane) - 1u;
-    const uint4 entry = make_uint4(q, (uint32_t)R.minX | ((uint32_t)R.minY << 16),
-                                   (uint32_t)R.maxX | ((uint32_t)R.maxY << 16), (uint32_t)R.maxZ);
-    for (int sy = sy0; sy <= sy1; ++sy)
-      for (int sx = sx0; sx <= sx1; ++sx) {
-        const int u = (sy - uy0) * uw + (sx - ux0);
-        const uint32_t rank = s_pre[u * 8 + warp] + __popc(s_bal[u * 8 + warp] & lt);
-        const uint32_t s = (uint32_t)sy * V.stX + (uint32_t)sx;
-        P.stList[P.stStart[V.stBase + s] + P.mat[V.matBase + s * V.chunkCount + ch.localIndex] + rank] = entry;
+    __syncthreads();
+    int sx0 = 0, sx1 = -1, sy0 = 0, sy1 = -1;
+    if (valid) {
+      sx0 = R.minX / kSuperTile; sx1 = (R.maxX - 1) / kSuperTile;
+      sy0 = R.minY / kSuperTile; sy1 = (R.maxY - 1) / kSuperTile;
+      atomicMin(&s_rect[0], sx0); atomicMax(&s_rect[1], sx1);
+      atomicMin(&s_rect[2], sy0); atomicMax(&s_rect[3], sy1);
+    }
+    __syncthreads();
+    // super-tile lists in submission order: per super-tile of the chunk's union
+    // rectangle, one ballot per warp, then a prefix over the 8 warps
+    const int ux0 = s_rect[0], ux1 = s_rect[1], uy0 = s_rect[2], uy1 = s_rect[3];
+    const int uw = ux1 - ux0 + 1;
+    const int nu = ux1 >= ux0 ? uw * (uy1 - uy0 + 1) : 0;
+    uint32_t* s_bal = s_dyn;                    // [nu][8]
+    uint32_t* s_pre = s_dyn + (size_t)nu * 8;   // [nu][8]
+    for (int u = 0; u < nu; ++u) {
+      const int sx = ux0 + u % uw, sy = uy0 + u / uw;
+      const bool flag = valid && sx >= sx0 && sx <= sx1 && sy >= sy0 && sy <= sy1;
+      const uint32_t bal = __ballot_sync(0xFFFFFFFFu, flag);
+      if (lane == 0) s_bal[u * 8 + warp] = bal;
+    }
+    __syncthreads();
+    for (int u = tid; u < nu; u += kChunk) {
+      uint32_t acc = 0;
+#pragma unroll
+      for (int w = 0; w < 8; ++w) {
+        s_pre[u * 8 + w] = acc;
+        acc += __popc(s_bal[u * 8 + w]);
       }
-  }
-  // rows of this chunk's quads -> (quad, row) entries for the row walk
-  if (valid) {
-    const uint32_t rowG = P.viewBase[ch.view].rows + P.chunkBase[c].rows + s_rowLocal[tid];
-    const uint32_t rows = (uint32_t)(R.maxY - R.minY);
-    for (uint32_t i = 0; i < rows; ++i) P.rowOwner[rowG + i] = make_uint2(q, i);
+    }
+    __syncthreads();
+    if (valid) {
+      const uint32_t lt = (1u << lane) - 1u;
+      const uint4 entry = make_uint4(q, (uint32_t)R.minX | ((uint32_t)R.minY << 16),
+                                     (uint32_t)R.maxX | ((uint32_t)R.maxY << 16), (uint32_t)R.maxZ);
+      for (int sy = sy0; sy <= sy1; ++sy)
+        for (int sx = sx0; sx <= sx1; ++sx) {
+          const int u = (sy - uy0) * uw + (sx - ux0);
+          const uint32_t rank = s_pre[u * 8 + warp] + __popc(s_bal[u * 8 + warp] & lt);
+          const uint32_t st = (uint32_t)sy * V.stX + (uint32_t)sx;
+          P.stList[P.stStart[V.stBase + st] + P.mat[V.matBase + st * V.chunkCount + ch.localIndex] + rank] = entry;
+        }
+    }
+    // rows of this chunk's quads -> (quad, row) entries for the row walk
+    if (valid) {
+      const uint32_t rowG = P.viewBase[ch.view].rows + P.chunkBase[c].rows + s_rowLocal[tid];
+      const uint32_t rows = (uint32_t)(R.maxY - R.minY);
+      for (uint32_t i = 0; i < rows; ++i) P.rowOwner[rowG + i] = make_uint2(q, i);
+    }
+    __syncthreads();  // shared arrays are reused by the next chunk
   }
 }
 
@@ -755,6 +808,7 @@ __global__ void __launch_bounds__(256) k_walk(FrameParams P)
 // max-merge (Rasterizer.cpp:1148-1290).
 
 constexpr int kRasterThreads = 256;
+constexpr int kRasterMinBlocks = 4;  // resident CTAs per SM the register budget is sized for
 constexpr int kLocalCap = 768;   // overlapping quads buffered per tile
 constexpr int kFragStride = 33;  // words per fragment slot (padding: conflict-free banks)
 constexpr int kScanPerRound = 512;
@@ -985,20 +1039,71 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
   }
 }
 
-template <bool kWins>
-__global__ void __launch_bounds__(kRasterThreads, 2) k_raster(FrameParams P)
+// ---- k_tile_prep ----------------------------------------------------------------------
+// One warp per warp-tile (8x4 blocks, one lane per block): applies the view's
+// clear (hiZ := 1, Rasterizer.cpp:107-121) to every block, then either queues
+// the tile for k_raster (its super-tile has a quad list) or finishes it here:
+// no quad touches it, so its per-tile hiZ minimum is final.
+
+__device__ __forceinline__ uint32_t view_of_tile(const FrameParams& P, uint32_t wt)
 {
-  __shared__ RasterSmem S;
-  if (P.header->overflow) return;
-  const uint32_t tid = threadIdx.x, lane = tid & 31;
-  const uint32_t wt = blockIdx.x;
-  if (wt >= P.numTiles) return;
   uint32_t lo = 0, hi = P.numViews - 1;
   while (lo < hi) {
     const uint32_t mid = (lo + hi + 1) >> 1;
     if (P.views[mid].tileStart <= wt) lo = mid; else hi = mid - 1;
   }
-  const uint32_t v = lo;
+  return lo;
+}
+
+__global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
+{
+  __shared__ uint32_t s_n, s_base;
+  if (P.header->overflow) return;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t wt = blockIdx.x * 8 + warp;
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  bool queue = false;
+  uint32_t slot = 0;
+  if (wt < P.numTiles) {
+    const ViewDesc& V = P.views[view_of_tile(P, wt)];
+    const uint32_t lt = wt - V.tileStart;
+    const uint32_t tx0 = (lt % V.tilesX) * kTileW, ty0 = (lt / V.tilesX) * kTileH;
+    const uint32_t bx = tx0 + (lane & 7), by = ty0 + (lane >> 3);
+    const bool inView = bx < V.blocksX && by < V.blocksY;
+    const uint32_t blk = inView ? by * V.blocksX + bx : 0;
+    const bool clearing = (V.flags & kViewClear) != 0;
+    if (clearing) {
+      if (inView) V.hiz[blk] = 1;
+      if (lt == 0 && lane < 8) V.hiz[V.blocksX * V.blocksY + lane] = 1;  // padding entries
+    }
+    const uint32_t s = V.stBase + (ty0 / kSuperTile) * V.stX + (tx0 / kSuperTile);
+    queue = V.cmdCount && P.stLen[s] != 0;
+    if (!queue) {
+      uint32_t tmin = inView ? (clearing ? 1u : (uint32_t)V.hiz[blk]) : 0xFFFFu;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) tmin = ::min(tmin, __shfl_xor_sync(0xFFFFFFFFu, tmin, o));
+      if (lane == 0) V.tileHiz[lt] = (uint16_t)tmin;
+    } else if (lane == 0) {
+      slot = atomicAdd(&s_n, 1u);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_n) s_base = atomicAdd(&P.header->activeTiles, s_n);
+  __syncthreads();
+  if (queue && lane == 0) P.activeTileList[s_base + slot] = make_uint2(wt, view_of_tile(P, wt));
+}
+
+// ---- k_raster -------------------------------------------------------------------------
+// Persistent CTAs of kRasterThreads threads take queued warp-tiles one at a
+// time (dynamic, heavy tiles vary a lot): per tile, the super-tile list is
+// filtered to the quads that reach the tile and are not already hidden, then
+// rasterised in list order (raster_local_list) and the tile's blocks written back.
+
+template <bool kWins>
+__device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S, uint32_t wt, uint32_t v)
+{
+  const uint32_t tid = threadIdx.x, lane = tid & 31;
   const ViewDesc& V = P.views[v];
   const uint32_t lt = wt - V.tileStart;
   const uint32_t tx = lt % V.tilesX, ty = lt / V.tilesX;
@@ -1074,7 +1179,6 @@ __global__ void __launch_bounds__(kRasterThreads, 2) k_raster(FrameParams P)
     if ((clearing || have) && py == 0) V.hiz[blk] = (uint16_t)hiz;
     if (have) *reinterpret_cast<uint4*>(V.depth + (size_t)blk * 64 + 8 * py) = make_uint4(row[0], row[1], row[2], row[3]);
   }
-  if (clearing && lt == 0 && tid < 8) V.hiz[V.blocksX * V.blocksY + tid] = 1;  // padding entries
   if (kWins) {
     // a pixel is won by the command whose fragment set its final value (the
     // fast-clear overwrite or a strictly larger max-merge); one atomic per
@@ -1097,6 +1201,27 @@ __global__ void __launch_bounds__(kRasterThreads, 2) k_raster(FrameParams P)
 #pragma unroll
     for (int w = 1; w < kRasterThreads / 32; ++w) m = ::min(m, S.scan[w]);
     V.tileHiz[lt] = (uint16_t)m;
+  }
+}
+
+template <bool kWins>
+__global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) k_raster(FrameParams P)
+{
+  __shared__ RasterSmem S;
+  __shared__ uint32_t s_next;
+  if (P.header->overflow) return;
+  const uint32_t nActive = P.header->activeTiles;
+  if (threadIdx.x == 0) s_next = atomicAdd(&P.header->tileCursor, 1u);
+  __syncthreads();
+  uint32_t i = s_next;
+  while (i < nActive) {
+    const uint2 t = P.activeTileList[i];
+    uint32_t nxt = 0;
+    if (threadIdx.x == 0) nxt = atomicAdd(&P.header->tileCursor, 1u);  // next tile, fetched ahead
+    raster_tile<kWins>(P, S, t.x, t.y);
+    if (threadIdx.x == 0) s_next = nxt;
+    __syncthreads();  // shared state is reused by the next tile
+    i = s_next;
   }
 }
 
@@ -1210,53 +1335,60 @@ __global__ void __launch_bounds__(256) k_read_back(const uint16_t* depth, const 
 
 // ---- launchers -------------------------------------------------------------------------
 
-cudaError_t launch_flush(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
-                         bool doQuery, cudaStream_t stream)
+// The frame's kernels in order; with `ev`, an event is recorded before the
+// first stage and after each of the six stages (setup, scan, list fill, row
+// walk, raster, query), also for stages that do not run.
+static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
+                                bool doQuery, cudaStream_t stream, cudaEvent_t* ev)
 {
-  if (doRaster && P.numChunks) {
-    const size_t smem = (size_t)maxStPerView * sizeof(uint32_t);
-    k_setup<<<P.numChunks, kChunk, smem, stream>>>(P);
-  }
+  auto mark = [&](int i) {
+    if (ev) cudaEventRecord(ev[i], stream);
+  };
+  mark(0);
   if (doRaster) {
-    k_scan<<<numSt + P.numViews, 256, 0, stream>>>(P, numSt);
+    // activeChunks, activeTiles, tileCursor
+    cudaError_t e = cudaMemsetAsync(&P.header->activeChunks, 0, 3 * sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
     if (P.numChunks) {
-      k_fill<<<P.numChunks, kChunk, (size_t)maxStPerView * 64, stream>>>(P);
-      k_walk<<<g_walkBlocks, 256, 0, stream>>>(P);
-    }
-    if (P.numTiles) {
-      if (P.wins) k_raster<true><<<P.numTiles, kRasterThreads, 0, stream>>>(P);
-      else k_raster<false><<<P.numTiles, kRasterThreads, 0, stream>>>(P);
+      if (P.matSize) {
+        e = cudaMemsetAsync(P.mat, 0, (size_t)P.matSize * sizeof(uint32_t), stream);  // inactive chunks count 0
+        if (e != cudaSuccess) return e;
+      }
+      k_gate<<<(P.numCmds + 255) / 256, 256, 0, stream>>>(P);
+      k_chunk_gate<<<(P.numChunks + 255) / 256, 256, 0, stream>>>(P);
+      k_setup<<<::min(P.numChunks, g_setupBlocks), kChunk, (size_t)maxStPerView * sizeof(uint32_t), stream>>>(P);
     }
   }
+  mark(1);
+  if (doRaster) k_scan<<<numSt + P.numViews, 256, 0, stream>>>(P, numSt);
+  mark(2);
+  if (doRaster && P.numChunks)
+    k_fill<<<::min(P.numChunks, g_fillBlocks), kChunk, (size_t)maxStPerView * 64, stream>>>(P);
+  mark(3);
+  if (doRaster && P.numChunks) k_walk<<<g_walkBlocks, 256, 0, stream>>>(P);
+  mark(4);
+  if (doRaster && P.numTiles) {
+    k_tile_prep<<<(P.numTiles + 7) / 8, 256, 0, stream>>>(P);
+    const uint32_t grid = ::min(P.numTiles, g_rasterBlocks);
+    if (P.wins) k_raster<true><<<grid, kRasterThreads, 0, stream>>>(P);
+    else k_raster<false><<<grid, kRasterThreads, 0, stream>>>(P);
+  }
+  mark(5);
   if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
+  mark(6);
   return cudaGetLastError();
 }
 
-// Same sequence with an event recorded before the first and after every kernel
-// (ev[0..5]); kernels that do not run still get their events.
-// Same sequence with an event recorded before the first and after every kernel
-// (ev[0..6]); kernels that do not run still get their events.
+cudaError_t launch_flush(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
+                         bool doQuery, cudaStream_t stream)
+{
+  return flush_stages(P, numSt, maxStPerView, doRaster, doQuery, stream, nullptr);
+}
+
 cudaError_t launch_flush_timed(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
                                bool doQuery, cudaStream_t stream, cudaEvent_t* ev)
 {
-  cudaEventRecord(ev[0], stream);
-  if (doRaster && P.numChunks)
-    k_setup<<<P.numChunks, kChunk, (size_t)maxStPerView * sizeof(uint32_t), stream>>>(P);
-  cudaEventRecord(ev[1], stream);
-  if (doRaster) k_scan<<<numSt + P.numViews, 256, 0, stream>>>(P, numSt);
-  cudaEventRecord(ev[2], stream);
-  if (doRaster && P.numChunks) k_fill<<<P.numChunks, kChunk, (size_t)maxStPerView * 64, stream>>>(P);
-  cudaEventRecord(ev[3], stream);
-  if (doRaster && P.numChunks) k_walk<<<g_walkBlocks, 256, 0, stream>>>(P);
-  cudaEventRecord(ev[4], stream);
-  if (doRaster && P.numTiles) {
-    if (P.wins) k_raster<true><<<P.numTiles, kRasterThreads, 0, stream>>>(P);
-    else k_raster<false><<<P.numTiles, kRasterThreads, 0, stream>>>(P);
-  }
-  cudaEventRecord(ev[5], stream);
-  if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
-  cudaEventRecord(ev[6], stream);
-  return cudaGetLastError();
+  return flush_stages(P, numSt, maxStPerView, doRaster, doQuery, stream, ev);
 }
 
 cudaError_t launch_read_back(const uint16_t* depth, const uint16_t* hiz, uint32_t width, uint32_t height,
@@ -1289,11 +1421,21 @@ cudaError_t set_kernel_attributes()
 {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
-  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
-    g_walkBlocks = (uint32_t)sms * 8;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+  g_walkBlocks = (uint32_t)sms * 8;
   cudaError_t e = cudaFuncSetAttribute(k_setup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 4));
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 64));
+  e = cudaFuncSetAttribute(k_fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 64));
+  if (e != cudaSuccess) return e;
+  // persistent grids: resident CTAs per SM at the largest dynamic shared memory used
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_setup, kChunk, kMaxStPerView * 4) == cudaSuccess && nb > 0)
+    g_setupBlocks = (uint32_t)(nb * sms);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fill, kChunk, kMaxStPerView * 16) == cudaSuccess && nb > 0)
+    g_fillBlocks = (uint32_t)(nb * sms);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster<true>, kRasterThreads, 0) == cudaSuccess && nb > 0)
+    g_rasterBlocks = (uint32_t)(nb * sms);
+  return cudaSuccess;
 }
 
 // ---- queries without device allocation -------------------------------------------------

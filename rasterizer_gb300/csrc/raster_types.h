@@ -123,11 +123,18 @@ struct FrameHeader {
   uint32_t totalRows, totalCks, totalSt, overflow;
   uint32_t capCks, capSt, viewsDone, sticky;  // sticky: overflow seen since the last check
   uint32_t maxCks, maxSt, pad[2];              // largest totals seen since the last check
+  // reset at the start of every launch
+  uint32_t activeChunks;  // chunks with a drawn command (k_chunk_gate)
+  uint32_t activeTiles;   // warp-tiles whose super-tile has a quad list (k_tile_prep)
+  uint32_t tileCursor;    // next entry of the active tile list (k_raster)
+  uint32_t pad2;
 };
 
 struct FrameParams {
   const ViewDesc* views;
   uint32_t numViews;
+  uint32_t numCmds;
+  uint32_t matSize;      // entries of `mat` over all views
   const Cmd* cmds;
   const Chunk* chunks;
   uint32_t numChunks;
@@ -154,6 +161,8 @@ struct FrameParams {
   uint32_t* visBits;     // one bit per query slot
   uint32_t* ncBits;
   uint32_t* cmdDraw;     // per command: bit0 drawn, bit1 near-clipped (gated result)
+  uint32_t* activeChunkList;  // chunks with a drawn command (header->activeChunks of them)
+  uint2* activeTileList;      // {warp-tile, view} with a non-empty super-tile list (header->activeTiles)
   // learned occluder selection and win counts (all optional)
   float* feat;           // per command: kFeatures features
   float* score;          // per command: MLP score
