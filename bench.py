@@ -1,24 +1,33 @@
-"""Benchmark: views/s of the plain all-occluder path on one GB300.
+"""Benchmark: views/s of the batched + learned path on one GB300, next to the
+plain path and the reference's CPU algorithm.
 
-Workload (the dense-city configuration): a seeded 64x64 grid of extruded
-buildings, 259,534 triangles baked by the library into 386 occluders (129,768
-quads), rendered at 1920x1080 along a seeded 300-frame street-level camera
-path; every frame clears, gates all occluders on the GPU from their bounds
-(queryVisibility on an empty buffer, as the plain loop does), rasterises the
-visible ones and answers 100,000 query boxes (lognormal extents).  One step =
-one frame = one view.  The rasterizer persists across frames (stale depth in
-cleared blocks, as in the reference).
+Scene: a seeded 64x64 grid of extruded buildings, 259,534 triangles baked by
+the library into 386 occluders (129,768 quads); 100,000 query boxes
+(lognormal extents) per view.
 
-  value    device time of the frame's kernels (CUDA events on the library's
-           stream, inputs resident in HBM, L2 flushed between steps);
-  e2e      the same frames through the reference-facing API with host
-           buffers: clear / setModelViewProjection / rasterize (gated) /
-           queryVisibility batch, host->device and device->host copies inside;
-  cpu_baseline  the CPU oracle (portable restatement of the reference) on one
-           host core, on a bounded sample of the same frames.
+  value    (headline) batched + learned: 64 street-level 1920x1080 views
+           (seeded camera paths, each view moving every step) per graph
+           launch; each view draws the selector's top K of its candidate
+           occluders (K = the smallest fraction keeping >= 99% of the
+           occlusion culls on held-out validation views) and answers its
+           queries.  Device time per launch (CUDA events on the library's
+           stream); the selector is trained first, on the GPU, outside the
+           timed region.  Culls kept vs the full frames and false culls are
+           measured on held-out test paths and reported in `config`;
+  e2e      the same launches through the public API with host data: 64
+           matrices from the host, launch, every view's result bits back;
+  plain_single_view  the plain all-occluder loop, one 1080p view per launch
+           along a 300-frame path (L2 flushed between frames), with its
+           per-kernel times, roofline and end-to-end figure;
+  batched  the 256-view mixed-resolution workload, one launch vs one launch per view;
+  learned  training report, K sweep against the nearest-first ordering, and
+           the 256-view workload with learned selection;
+  cpu_baseline  the CPU oracle (portable restatement of the reference) on
+           one host core, plain loop, on a bounded sample of the headline's views.
 
 --impl reference times the reference's CPU algorithm (the oracle port: the
-reference's AVX2 build cannot run on the Arm host) with all host cores.
+reference's AVX2 build cannot run on the Arm host) with all host cores on the
+headline's views, plain all-occluder loop (the reference has no learned selection).
 """
 from __future__ import annotations
 
@@ -41,6 +50,7 @@ W, H = 1920, 1080
 NQ = 100_000
 FRAMES = 300
 L2_FLUSH_BYTES = 256 << 20
+LEARNED_VIEWS = 64  # 1920x1080 street-level views per batched launch
 
 
 def workload():
@@ -108,9 +118,16 @@ class ClockSampler:
 _CPU_STATE = None
 
 
+def headline_views():
+    """(views, frames, 16) matrices of the headline's street-level views."""
+    from rasterizer_gb300 import scenes
+    return np.stack([scenes.camera_path(64, seed=7000 + k)[0] for k in range(LEARNED_VIEWS)])
+
+
 def _cpu_state():
-    """Per-process CPU oracle state: the baked city, the path, the queries and
-    one persistent Oracle rasterizer (built once per process)."""
+    """Per-process CPU oracle state: the baked city, the headline's views, the
+    queries and one persistent Oracle rasterizer per view slot (built once per
+    process)."""
     global _CPU_STATE
     if _CPU_STATE is None:
         sys.path.insert(0, ROOT)
@@ -119,16 +136,15 @@ def _cpu_state():
         from helpers import city_occluders, to_baked
         from rasterizer_gb300 import scenes
         scene = to_baked(city_occluders())
-        mvps, _ = scenes.camera_path(FRAMES, seed=7)
         mins, maxs = scenes.query_boxes(NQ, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
-        _CPU_STATE = (scene, mvps, mins, maxs, Oracle(W, H))
+        _CPU_STATE = (scene, headline_views(), mins, maxs, Oracle(W, H))
     return _CPU_STATE
 
 
 def _cpu_frame(f: int) -> int:
-    """One frame (plain loop + all queries) on the CPU oracle."""
+    """One view (plain loop + all queries) on the CPU oracle: view f % 64 at frame f // 64."""
     scene, mvps, mins, maxs, orc = _cpu_state()
-    orc.frame_plain(scene, mvps[f % FRAMES])
+    orc.frame_plain(scene, mvps[f % LEARNED_VIEWS, (f // LEARNED_VIEWS) % mvps.shape[1]])
     orc.query(mins, maxs)
     return 1
 
@@ -142,9 +158,9 @@ def cpu_baseline(budget_s: float = 12.0, max_frames: int = 60):
         done += 1
     secs = time.perf_counter() - t0
     return {"value": done / secs, "unit": "views/s", "cores": 1, "kind": "port",
-            "sample": f"{done} frames of the same workload (frames 0..{done - 1} of the path, with all "
-                      f"{NQ} queries each), 1 host thread, CPU oracle (portable restatement; the "
-                      f"reference's AVX2 build does not run on the Arm host)"}
+            "sample": f"{done} views of the headline workload (the first {done} of its 64 street views, "
+                      f"plain all-occluder loop, all {NQ} queries each), 1 host thread, CPU oracle (portable "
+                      f"restatement; the reference's AVX2 build does not run on the Arm host)"}
 
 
 def _warm(_):
@@ -174,10 +190,12 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/u16",
             "data": "synthetic",
-            "config": {"workload": "dense city 64x64 buildings (259,534 tris), 1920x1080, 300-frame street path, "
-                                   "100k lognormal query boxes per frame, plain all-occluder loop"},
+            "config": {"workload": f"{LEARNED_VIEWS} street-level 1920x1080 views of the dense city (259,534 "
+                                   f"tris, 386 occluders, seeded paths), {NQ} lognormal query boxes per view; "
+                                   f"the reference's plain all-occluder loop (it has no learned selection)",
+                       "views_per_step": 1},
             "cpu_baseline": {"value": value, "unit": "views/s", "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} frames (one per step, {cores} worker processes, each with "
+                             "sample": f"{args.steps} views (one per step, {cores} worker processes, each with "
                                        f"its own persistent rasterizer); CPU oracle, because the reference's "
                                        f"AVX2 build cannot run on aarch64"},
             "e2e": {"value": value, "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -302,20 +320,18 @@ def _time_launches(ctx, stream, launch, reps, before=None):
     return sum(a.elapsed_time(b) for a, b in evs) / reps
 
 
-def run_learned(ctx_dev: int, occ, steps: int):
+def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
     """Learned occluder selection.  Trains the selector on the GPU (labels from
     the rasteriser over seeded poses), picks per workload the smallest
     candidate fraction K that keeps >= 99% of the occlusion culls on held-out
-    validation views, then reports on held-out test views: culls kept vs the
-    full frames, false culls, the nearest-first ranking at the same K, and
-    views/s of the batched + learned launch against the plain paths."""
+    validation views, reports culls kept vs the full frames, false culls and
+    the nearest-first ranking at the same K on held-out test views, and times
+    the batched + learned launch (the headline) against the plain batched one."""
     import torch
-    from rasterizer_gb300 import api, learned as L, scenes
-    pmin, pmax = scenes.query_boxes(NQ, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    from rasterizer_gb300 import api, learned as L
     centers = np.stack([o.center for o in occ])
     quads = np.array([o.quads for o in occ])
-    ctx = api.Context(ctx_dev)
-    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", ctx_dev))
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     t = L.Timer()
     net, report = L.train_selector(ctx, occ, NQ, log=None)
     out = {"training": dict(report, seconds=t.lap())}
@@ -328,7 +344,7 @@ def run_learned(ctx_dev: int, occ, steps: int):
                 return f
         return 1.0
 
-    # street level, 1920x1080 (the dense-city configuration with learned selection)
+    # ---- street level, 1920x1080 ----
     k_st = pick(L.street_tracks(6, 30, seed0=6000, n_occluders=len(occ), queries=NQ))
     test = L.street_tracks(8, 30, seed0=5000, n_occluders=len(occ), queries=NQ)
     full = L.run_full(ctx, occ, test, pmin, pmax)
@@ -337,37 +353,82 @@ def run_learned(ctx_dev: int, occ, steps: int):
         a = L.evaluate_learned(ctx, occ, test, pmin, pmax, net, f, full)
         b = L.evaluate_heuristic(ctx, occ, test, pmin, pmax, "nearest", f, full)
         sweep[str(f)] = {"learned": a.as_dict(), "nearest_first": b.as_dict()}
-    # throughput: 64 street views at 1080p per launch, moving along their paths
-    paths = L.street_tracks(64, 64, seed0=7000, n_occluders=len(occ), queries=NQ)
+
+    paths = L.street_tracks(LEARNED_VIEWS, 64, seed0=7000, n_occluders=len(occ), queries=NQ)
     views = L._views(ctx, occ, paths, pmin, pmax)
 
-    def mover(b, tracks=paths, frames=64):
+    def mover(bt, tracks, frames):
         def before(i):
             for v, tr in enumerate(tracks):
-                b.setModelViewProjection(v, tr.mvps[i % frames])
+                bt.setModelViewProjection(v, tr.mvps[i % frames])
         return before
 
     plain = api.PreparedBatch(ctx, views)
-    ms_plain = _time_launches(ctx, stream, plain.launch, steps, mover(plain))
+    ms_plain = _time_launches(ctx, stream, plain.launch, 50, mover(plain, paths, 64))
     ok = plain.check()
     plain.close()
+
+    # headline: batched + learned launches, barrier + synchronize around the timed region
     sel = api.PreparedBatch(ctx, views)
     sel.setSelection(net, k_st, trackWins=True)
-    ms_sel = _time_launches(ctx, stream, sel.launch, steps, mover(sel))
+    move = mover(sel, paths, 64)
+    for i in range(args.warmup):
+        move(i)
+        sel.launch()
     ok = sel.check() and ok
-    prof = sel.profile(10)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(dev.index) if rank == 0 else None
+    time.sleep(0.3 if sampler else 0)
+    _barrier(world)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        move(i)
+        starts[i].record(stream)
+        sel.launch()
+        ends[i].record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    _barrier(world)
+    clocks = sampler.stop() if sampler else None
+    ok = sel.check() and ok
+    dev_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(starts, ends)), world, dev)
+    stats = sel.stats()
+    prof = sel.profile(20)
+    kern = dict(zip(["setup", "scan", "fill", "walk", "raster", "query", "selection"], [float(x) for x in prof]))
+    # end to end through the public API: matrices from the host, launch, every view's result bits back
+    e2e_steps = 30
+    t1 = time.perf_counter()
+    for i in range(e2e_steps):
+        move(i)
+        sel.launch()
+        for v in range(LEARNED_VIEWS):
+            sel.results(v)
+    e2e_s = time.perf_counter() - t1
     sel.close()
     for v in views:
         v["raster"].close()
+    blocks = (W // 8) * (H // 8)
+    raster_bytes = LEARNED_VIEWS * (2 * W * H + 4 * blocks)  # depth written once, hiZ cleared + written
     out["street_1080p"] = {
         "k_fraction": k_st, "test_views": f"{len(test)} held-out paths x 30 frames", "sweep": sweep,
-        "at_k": sweep.get(str(k_st)),
-        "batched_plain_views_per_s": 64 / (ms_plain * 1e-3),
-        "batched_learned_views_per_s": 64 / (ms_sel * 1e-3),
-        "learned_kernels_ms_per_launch": dict(zip(["k_setup", "k_scan", "k_fill", "k_walk", "k_raster", "k_query",
-                                                    "selection"], [float(x) for x in prof])),
-        "views_per_launch": 64, "capacity_ok": bool(ok)}
-    # the 256-view workload (mixed resolutions)
+        "at_k": sweep.get(str(k_st)), "views_per_launch": LEARNED_VIEWS,
+        "batched_plain_views_per_s": LEARNED_VIEWS / (ms_plain * 1e-3),
+        "batched_learned_views_per_s": world * LEARNED_VIEWS * args.steps / (dev_ms * 1e-3),
+        "kernels_ms_per_launch": kern, "work_last_launch": stats, "capacity_ok": bool(ok)}
+    headline = {
+        "value": world * LEARNED_VIEWS * args.steps / (dev_ms * 1e-3), "ms_per_step": dev_ms / args.steps,
+        "clocks": clocks, "kernels": kern,
+        "roofline": {"bound": "hbm", "kernel": "k_raster (with k_tile_prep)", "unit": "GB/s",
+                     "achieved": raster_bytes / (kern["raster"] * 1e-3) / 1e9, "algorithmic_bytes": raster_bytes},
+        "e2e": {"value": world * LEARNED_VIEWS * e2e_steps / e2e_s, "unit": "views/s",
+                "h2d_bytes_per_step": stats["table_bytes"],
+                "d2h_bytes_per_step": LEARNED_VIEWS * 2 * 4 * ((NQ + 31) // 32),
+                "path": "PreparedBatch.setModelViewProjection x64 / launch / results x64 (Python mirror -> "
+                        "C ABI), wall clock"},
+        "launches_per_step": 4 + 9}
+    # ---- the 256-view workload (mixed resolutions) ----
     k_mv = pick(L.multiview_tracks(centers, quads, NQ, frames=4, seed=9))
     test = L.multiview_tracks(centers, quads, NQ, frames=4, seed=3)
     full = L.run_full(ctx, occ, test, pmin, pmax)
@@ -375,24 +436,131 @@ def run_learned(ctx_dev: int, occ, steps: int):
     b = L.evaluate_heuristic(ctx, occ, test, pmin, pmax, "nearest", k_mv, full)
     views = L._views(ctx, occ, test, pmin, pmax)
     plain = api.PreparedBatch(ctx, views)
-    ms_plain = _time_launches(ctx, stream, plain.launch, steps, mover(plain, test, 4))
+    ms_plain = _time_launches(ctx, stream, plain.launch, 20, mover(plain, test, 4))
     ok = plain.check()
     plain.close()
     sel = api.PreparedBatch(ctx, views)
     sel.setSelection(net, k_mv, trackWins=True)
-    ms_sel = _time_launches(ctx, stream, sel.launch, steps, mover(sel, test, 4))
+    ms_sel = _time_launches(ctx, stream, sel.launch, 20, mover(sel, test, 4))
     ok = sel.check() and ok
+    kern_mv = dict(zip(["setup", "scan", "fill", "walk", "raster", "query", "selection"],
+                       [float(x) for x in sel.profile(5)]))
     sel.close()
     for v in views:
         v["raster"].close()
     out["multiview_256"] = {"k_fraction": k_mv, "learned": a.as_dict(), "nearest_first": b.as_dict(),
                             "batched_plain_views_per_s": len(test) / (ms_plain * 1e-3),
                             "batched_learned_views_per_s": len(test) / (ms_sel * 1e-3),
-                            "batched_learned_ms_per_launch": ms_sel, "capacity_ok": bool(ok)}
+                            "batched_learned_ms_per_launch": ms_sel, "kernels_ms_per_launch": kern_mv,
+                            "capacity_ok": bool(ok)}
     out["seconds"] = t.lap() + out["training"]["seconds"]
     net.close()
-    ctx.close()
-    return out
+    return out, headline
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_plain(ctx, r, occ, mvps, mins, maxs, world, dev, args):
+    """The plain all-occluder path, one 1920x1080 view per launch along the
+    camera path (L2 flushed between frames), its per-kernel times and the same
+    frames end to end through the reference-facing API."""
+    import torch
+    from rasterizer_gb300 import api
+    flags = np.full(len(occ), 2, np.uint8)  # OCC_GATED
+    batch = api.PreparedBatch(ctx, [dict(raster=r, mvp=mvps[0], clear=True, occluders=occ, flags=flags,
+                                         mins=mins, maxs=maxs)])
+    for attempt in range(3):  # size the scratch for every frame of the path
+        for f in range(FRAMES):
+            batch.setModelViewProjection(0, mvps[f])
+            batch.launch()
+        if batch.check():
+            break
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+
+    def flush_l2(i):
+        with torch.cuda.stream(stream):
+            flush.fill_(i)
+
+    steps = min(args.steps, 3000)
+    for i in range(args.warmup):
+        batch.setModelViewProjection(0, mvps[i % FRAMES])
+        batch.launch()
+        flush_l2(i)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    _barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(steps):
+        batch.setModelViewProjection(0, mvps[i % FRAMES])
+        starts[i].record(stream)
+        batch.launch()
+        ends[i].record(stream)
+        flush_l2(i)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    _barrier(world)
+    ok = batch.check()
+    dev_ms = max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(starts, ends)), world, dev)
+    prof = batch.profile(min(steps, 300))
+    names = ["k_setup", "k_scan", "k_fill", "k_walk", "k_raster", "k_query"]
+    kern = {n: float(v) for n, v in zip(names, prof)}
+    top = max(kern, key=kern.get)
+    q_setup = sum(o.quads for o in occ)
+    alg = algorithmic_bytes(q_setup, NQ)
+    peak, peak_note = hbm_peak()
+    traffic = load_traffic()
+    roof_kernel = top if top in alg else "k_query"
+    achieved = alg[roof_kernel] / (kern[roof_kernel] * 1e-3) / 1e9
+    frame_ms = sum(kern.values())
+    # end to end through the reference-facing API with host buffers
+    e2e_steps = max(10, min(steps // 10, 100))
+    for i in range(3):
+        r.clear()
+        r.setModelViewProjection(mvps[i])
+        r.rasterizeMany(occ, flags)
+        r.queryVisibilityBatch(mins, maxs)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for i in range(e2e_steps):
+        r.clear()
+        r.setModelViewProjection(mvps[i % FRAMES])
+        r.rasterizeMany(occ, flags)
+        r.queryVisibilityBatch(mins, maxs)
+    e2e_s = time.perf_counter() - t1
+    h2d = NQ * 32 + 216 + 96 * len(occ) + 32 * ((q_setup + 255) // 256) + 12
+    d2h = 2 * 4 * ((NQ + 31) // 32) + 4 * len(occ) + 48
+    batch.close()
+    return {
+        "value": views_per_s(steps, world, dev_ms), "unit": "views/s", "steps": steps,
+        "ms_per_step": dev_ms / steps, "queries_per_s": views_per_s(steps, world, dev_ms) * NQ,
+        "wall_views_per_s": world * steps / wall, "kernels_ms": kern,
+        "l2": "flushed between steps (256 MB write, outside the timed events)",
+        "roofline": {"bound": "hbm", "kernel": roof_kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_note, "traffic": traffic.get(roof_kernel),
+                     "algorithmic_bytes": alg[roof_kernel],
+                     "frame_achieved": alg["frame"] / (frame_ms * 1e-3) / 1e9},
+        "e2e": {"value": world * e2e_steps / e2e_s, "unit": "views/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "path": "Rasterizer.clear/setModelViewProjection/rasterizeMany(gated)/queryVisibilityBatch "
+                        "(Python mirror -> C ABI), host numpy buffers, wall clock"},
+        "capacity_ok": bool(ok)}
+
+
+def hbm_peak():
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
 
 
 def run_gpu(args):
@@ -415,117 +583,38 @@ def run_gpu(args):
     occ = api.bake_scene(mesh.vertices, mesh.indices)
     ctx = api.Context(local)
     r = api.Rasterizer(ctx, W, H)
-    flags = np.full(len(occ), 2, np.uint8)  # OCC_GATED
-    batch = api.PreparedBatch(ctx, [dict(raster=r, mvp=mvps[0], clear=True, occluders=occ, flags=flags,
-                                         mins=mins, maxs=maxs)])
-    # size the scratch for every frame of the path
-    for attempt in range(3):
-        for f in range(FRAMES):
-            batch.setModelViewProjection(0, mvps[f])
-            batch.launch()
-        if batch.check():
-            break
-    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
-
-    def flush_l2(i):
-        with torch.cuda.stream(stream):
-            flush.fill_(i)
-
-    for i in range(args.warmup):
-        batch.setModelViewProjection(0, mvps[i % FRAMES])
-        batch.launch()
-        flush_l2(i)
-    ctx.synchronize()
-    torch.cuda.synchronize()
-
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    sampler = ClockSampler(local) if rank == 0 else None
-    time.sleep(0.3 if sampler else 0)
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for i in range(args.steps):
-        batch.setModelViewProjection(0, mvps[i % FRAMES])
-        starts[i].record(stream)
-        batch.launch()
-        ends[i].record(stream)
-        flush_l2(i)
-    ctx.synchronize()
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    if world > 1:
-        dist.barrier()
-    clocks = sampler.stop() if sampler else None
-    ok = batch.check()
-    dev_ms = max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(starts, ends)), world, dev)
-
-    # per-kernel device times (kernel by kernel, events in between, same stream)
-    prof = batch.profile(min(args.steps, 300))
-    names = ["k_setup", "k_scan", "k_fill", "k_walk", "k_raster", "k_query"]
-    kern = {n: float(v) for n, v in zip(names, prof)}
-    top = max(kern, key=kern.get)
-    q_setup = sum(o.quads for o in occ)
-    alg = algorithmic_bytes(q_setup, NQ)
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    peak, peak_note = 6800.0, "fallback"
-    if os.path.exists(peaks_path):
-        with open(peaks_path) as f:
-            peak, peak_note = float(json.load(f)["hbm_gbs"]), "measured"
-    traffic = load_traffic()
-    roof_kernel = top if top in alg else "k_query"
-    achieved = alg[roof_kernel] / (kern[roof_kernel] * 1e-3) / 1e9
-    frame_ms = sum(kern.values())
-
-    # end to end through the reference-facing API with host buffers
-    e2e_steps = max(10, min(args.steps // 10, 100))
-    for i in range(3):
-        r.clear()
-        r.setModelViewProjection(mvps[i])
-        r.rasterizeMany(occ, flags)
-        r.queryVisibilityBatch(mins, maxs)
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    for i in range(e2e_steps):
-        r.clear()
-        r.setModelViewProjection(mvps[i % FRAMES])
-        r.rasterizeMany(occ, flags)
-        r.queryVisibilityBatch(mins, maxs)
-    e2e_s = time.perf_counter() - t1
-    n_chunks = sum((o.quads + 255) // 256 for o in occ)  # upper bound of the chunk table
-    h2d = NQ * 32 + 216 + 96 * len(occ) + 32 * ((q_setup + 255) // 256) + 12
-    d2h = 2 * 4 * ((NQ + 31) // 32) + 4 * len(occ) + 48
-    del n_chunks
-
-    value = views_per_s(args.steps, world, dev_ms)
+    plain = run_plain(ctx, r, occ, mvps, mins, maxs, world, dev, args)
     batched = run_batched(local, occ, steps=5) if not args.no_batched else None
-    learned = run_learned(local, occ, steps=20) if not args.no_learned else None
+    learned, head = (None, None) if args.no_learned else run_learned(ctx, occ, mins, maxs, world, rank, dev, args)
+    peak, peak_note = hbm_peak()
+    traffic = load_traffic()
 
-    line = {
-        "metric": METRIC, "value": value, "unit": "views/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32/u16", "data": "synthetic",
-        "config": {"workload": workload_desc(mesh, occ), "resolution": f"{W}x{H}", "queries_per_view": NQ,
-                   "occluders": len(occ), "quads": q_setup, "l2": "flushed between steps (256 MB write, outside "
-                   "the timed events)", "timing": "CUDA events on the library stream around each frame's graph "
-                   "launch; max over ranks", "parallelism": f"replicas x{world}"},
-        "queries_per_s": value * NQ,
-        "wall_views_per_s": world * args.steps / wall,
-        "kernels_ms": kern,
-        "roofline": {"bound": "hbm", "kernel": roof_kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_note,
-                     "traffic": traffic.get(roof_kernel), "algorithmic_bytes": alg[roof_kernel],
-                     "frame_achieved": alg["frame"] / (frame_ms * 1e-3) / 1e9},
-        "e2e": {"value": world * e2e_steps / e2e_s, "unit": "views/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h,
-                "path": "Rasterizer.clear/setModelViewProjection/rasterizeMany(gated)/queryVisibilityBatch "
-                        "(Python mirror -> C ABI), host numpy buffers, wall clock"},
-        "gpu_launches": 6 * args.steps,
-        "clocks": clocks,
-        "capacity_ok": bool(ok),
-    }
+    line = {"metric": METRIC, "n_gpus": world, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32/u16", "data": "synthetic"}
+    if head is not None:
+        k = learned["street_1080p"]["k_fraction"]
+        at_k = learned["street_1080p"]["at_k"] or {}
+        roof = dict(head["roofline"], peak=peak, peak_source=peak_note,
+                    frac=head["roofline"]["achieved"] / peak, traffic=traffic.get("k_raster_batched"))
+        line.update({
+            "value": head["value"], "unit": "views/s", "steps": args.steps, "ms_per_step": head["ms_per_step"],
+            "config": {"workload": f"batched + learned: {LEARNED_VIEWS} street-level 1920x1080 views of the dense "
+                                   f"city per launch (seeded paths, {len(occ)} occluders, {NQ} lognormal query "
+                                   f"boxes per view), the selector's top {k:.0%} of each view's candidates",
+                       "culls_kept_vs_full": at_k.get("learned", {}).get("culls_retained"),
+                       "false_culls": at_k.get("learned", {}).get("false_culls"),
+                       "resolution": f"{W}x{H}", "views_per_step": LEARNED_VIEWS,
+                       "l2": f"inputs larger than L2 ({LEARNED_VIEWS} depth buffers of 4 MB per launch)",
+                       "timing": "CUDA events on the library stream around each batched graph launch; max over "
+                                 "ranks", "parallelism": f"replicas x{world}"},
+            "roofline": roof, "e2e": head["e2e"], "clocks": head["clocks"],
+            "gpu_launches": head["launches_per_step"] * args.steps, "kernels_ms": head["kernels"]})
+    else:
+        line.update({"value": plain["value"], "unit": "views/s", "steps": plain["steps"],
+                     "ms_per_step": plain["ms_per_step"], "roofline": plain["roofline"], "e2e": plain["e2e"],
+                     "gpu_launches": 9 * plain["steps"], "kernels_ms": plain["kernels_ms"],
+                     "config": {"workload": workload_desc(mesh, occ), "parallelism": f"replicas x{world}"}})
+    line["plain_single_view"] = dict(plain, workload=workload_desc(mesh, occ))
     if batched is not None:
         line["batched"] = batched
     if learned is not None:
@@ -537,7 +626,6 @@ def run_gpu(args):
         line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line), flush=True)
-    batch.close()
     r.close()
     ctx.close()
     if world > 1:

@@ -181,8 +181,9 @@ int occ_batch_set_selection(occ_batch b, occ_mlp mlp, float fraction, int trackW
 int occ_batch_set_zero_depth(occ_batch b, int enable);
 /* Work counts of the last launch (syncs): block rows walked, row-walk
  * checkpoints, super-tile list entries, chunks with a drawn occluder, warp-tiles
- * rasterised (the others only cleared), and the batch's chunk count. */
-int occ_batch_stats(occ_batch b, uint32_t out[6]);
+ * rasterised (the others only cleared), the batch's chunk count, and the
+ * bytes of tables each launch copies from the host. */
+int occ_batch_stats(occ_batch b, uint32_t out[7]);
 /* Per occluder of the view, after the last launch: its features, pixel wins,
  * candidate flag (passes the visibility test), selected flag and score. */
 int occ_batch_read_selection(occ_batch b, uint32_t view, float* features, uint32_t* wins, uint8_t* candidate,

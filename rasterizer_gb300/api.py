@@ -421,9 +421,9 @@ class PreparedBatch:
 
     def stats(self) -> dict:
         """Work counts of the last launch."""
-        out = np.zeros(6, np.uint32)
+        out = np.zeros(7, np.uint32)
         check(lib().occ_batch_stats(self.handle, _ptr(out)), "occ_batch_stats")
-        keys = ("rows", "checkpoints", "list_entries", "active_chunks", "active_tiles", "chunks")
+        keys = ("rows", "checkpoints", "list_entries", "active_chunks", "active_tiles", "chunks", "table_bytes")
         return {k: int(v) for k, v in zip(keys, out)}
 
     def setZeroDepth(self, enable: bool) -> None:

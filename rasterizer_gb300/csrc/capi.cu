@@ -1231,7 +1231,7 @@ int occ_batch_set_selection(occ_batch b, occ_mlp mlp, float fraction, int trackW
   return capture(b);
 }
 
-int occ_batch_stats(occ_batch b, uint32_t out[6])
+int occ_batch_stats(occ_batch b, uint32_t out[7])
 {
   if (!b || !out) return fail(OCC_ERR_INVALID_ARG, "null argument");
   FrameHeader H;
@@ -1243,6 +1243,7 @@ int occ_batch_stats(occ_batch b, uint32_t out[6])
   out[3] = H.activeChunks;
   out[4] = H.activeTiles;
   out[5] = (uint32_t)b->L.chunks.size();
+  out[6] = (uint32_t)b->tablesBytes;  // host->device bytes per launch (view, command and chunk tables)
   return OCC_OK;
 }
 
