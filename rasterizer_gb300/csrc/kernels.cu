@@ -917,6 +917,51 @@ __device__ __forceinline__ bool make_fragment(const FrameParams& P, const QuadRa
   return true;
 }
 
+// Merges fragment slot `slot` into this thread's pixel row of its block: the
+// reference's hiZ test, fast-clear overwrite or max-merge with memory, and the
+// block's new hiZ (minimum over its eight threads, `groupMask`).  With kWins,
+// own[x] tracks the command (+1) that produced pixel x's value.
+template <bool kWins>
+__device__ __forceinline__ void merge_slot(const ViewDesc& V, const RasterSmem& S, uint32_t slot, uint32_t py,
+                                           uint32_t blk, uint32_t groupMask, uint32_t (&row)[4], uint32_t& hiz,
+                                           bool& have, uint32_t (&own)[8])
+{
+  const uint32_t mz = S.meta[slot] >> 16;
+  if (hiz >= mz) return;  // the reference's hiZ test (Rasterizer.cpp:1148-1152)
+  const uint32_t* src = S.frag + slot * kFragStride + 4 * py;
+  if (hiz == 1) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (kWins) {
+        const uint32_t c1 = S.fcmd[slot] + 1;
+        own[2 * i] = (src[i] & 0xFFFFu) ? c1 : 0u;
+        own[2 * i + 1] = (src[i] >> 16) ? c1 : 0u;
+      }
+      row[i] = src[i];
+    }
+  } else {
+    if (!have) {
+      const uint4 a = *reinterpret_cast<const uint4*>(V.depth + (size_t)blk * 64 + 8 * py);
+      row[0] = a.x; row[1] = a.y; row[2] = a.z; row[3] = a.w;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (kWins) {
+        const uint32_t c1 = S.fcmd[slot] + 1;
+        if ((src[i] & 0xFFFFu) > (row[i] & 0xFFFFu)) own[2 * i] = c1;
+        if ((src[i] >> 16) > (row[i] >> 16)) own[2 * i + 1] = c1;
+      }
+      row[i] = vmax_u16x2(row[i], src[i]);
+    }
+  }
+  have = true;
+  uint32_t mn = vmin_u16x2(vmin_u16x2(row[0], row[1]), vmin_u16x2(row[2], row[3]));
+  mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 1));
+  mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 2));
+  mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 4));
+  hiz = ::min(mn & 0xFFFFu, mn >> 16);
+}
+
 // Runs the buffered local list: fragments in order, kRasterThreads at a time.
 // With kWins, own[x] tracks the command (+1) that produced pixel x's value.
 template <bool kWins>
@@ -997,40 +1042,7 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
         while (mine) {
           const uint32_t slot = 32u * wd + __ffs(mine) - 1;
           mine &= mine - 1;
-          const uint32_t mz = S.meta[slot] >> 16;
-          if (hiz >= mz) continue;  // the reference's hiZ test (Rasterizer.cpp:1148-1152)
-          const uint32_t* src = S.frag + slot * kFragStride + 4 * py;
-          if (hiz == 1) {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-              if (kWins) {
-                const uint32_t c1 = S.fcmd[slot] + 1;
-                own[2 * i] = (src[i] & 0xFFFFu) ? c1 : 0u;
-                own[2 * i + 1] = (src[i] >> 16) ? c1 : 0u;
-              }
-              row[i] = src[i];
-            }
-          } else {
-            if (!have) {
-              const uint4 a = *reinterpret_cast<const uint4*>(V.depth + (size_t)blk * 64 + 8 * py);
-              row[0] = a.x; row[1] = a.y; row[2] = a.z; row[3] = a.w;
-            }
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-              if (kWins) {
-                const uint32_t c1 = S.fcmd[slot] + 1;
-                if ((src[i] & 0xFFFFu) > (row[i] & 0xFFFFu)) own[2 * i] = c1;
-                if ((src[i] >> 16) > (row[i] >> 16)) own[2 * i + 1] = c1;
-              }
-              row[i] = vmax_u16x2(row[i], src[i]);
-            }
-          }
-          have = true;
-          uint32_t mn = vmin_u16x2(vmin_u16x2(row[0], row[1]), vmin_u16x2(row[2], row[3]));
-          mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 1));
-          mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 2));
-          mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 4));
-          hiz = ::min(mn & 0xFFFFu, mn >> 16);
+          merge_slot<kWins>(V, S, slot, py, blk, groupMask, row, hiz, have, own);
         }
       }
       if (py == 0) S.hiz[myBlock] = hiz;
@@ -1042,8 +1054,9 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
 // ---- k_tile_prep ----------------------------------------------------------------------
 // One warp per warp-tile (8x4 blocks, one lane per block): applies the view's
 // clear (hiZ := 1, Rasterizer.cpp:107-121) to every block, then either queues
-// the tile for k_raster (its super-tile has a quad list) or finishes it here:
-// no quad touches it, so its per-tile hiZ minimum is final.
+// the tile for k_raster (a quad of its super-tile list reaches it; long lists
+// are not checked) or finishes it here: no quad touches it, so its per-tile
+// hiZ minimum is final.
 
 __device__ __forceinline__ uint32_t view_of_tile(const FrameParams& P, uint32_t wt)
 {
@@ -1054,6 +1067,8 @@ __device__ __forceinline__ uint32_t view_of_tile(const FrameParams& P, uint32_t 
   }
   return lo;
 }
+
+constexpr uint32_t kPrepScanMax = 256;  // lists up to this length are checked against the tile
 
 __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
 {
@@ -1078,7 +1093,23 @@ __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
       if (lt == 0 && lane < 8) V.hiz[V.blocksX * V.blocksY + lane] = 1;  // padding entries
     }
     const uint32_t s = V.stBase + (ty0 / kSuperTile) * V.stX + (tx0 / kSuperTile);
-    queue = V.cmdCount && P.stLen[s] != 0;
+    const uint32_t len = V.cmdCount ? P.stLen[s] : 0u;
+    queue = len != 0;
+    if (queue && len <= kPrepScanMax) {
+      // queue the tile only if a quad of the super-tile list reaches it
+      const uint4* list = P.stList + P.stStart[s];
+      bool any = false;
+      for (uint32_t i0 = 0; i0 < len && !any; i0 += 32) {
+        bool o = false;
+        if (i0 + lane < len) {
+          const uint4 e = __ldg(list + i0 + lane);
+          o = (e.y & 0xFFFFu) < tx0 + kTileW && (e.z & 0xFFFFu) > tx0 && (e.y >> 16) < ty0 + kTileH &&
+              (e.z >> 16) > ty0;
+        }
+        any = __any_sync(0xFFFFFFFFu, o);
+      }
+      queue = any;
+    }
     if (!queue) {
       uint32_t tmin = inView ? (clearing ? 1u : (uint32_t)V.hiz[blk]) : 0xFFFFu;
 #pragma unroll
@@ -1117,12 +1148,11 @@ __device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S,
   bool have = false;
   uint32_t row[4] = {0, 0, 0, 0};
   uint32_t own[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (py == 0) S.hiz[myBlock] = hiz;
-  __syncthreads();
-
   const uint32_t s = V.stBase + (ty0 / kSuperTile) * V.stX + (tx0 / kSuperTile);
   const uint32_t listLen = V.cmdCount ? P.stLen[s] : 0;
   const uint4* list = P.stList + (V.cmdCount ? P.stStart[s] : 0);
+  if (py == 0) S.hiz[myBlock] = hiz;
+  __syncthreads();
   uint32_t n = 0;
   // kScanPerRound list entries per round (two per thread), appended to the
   // local list in list order unless already hidden in every block they touch
