@@ -654,6 +654,37 @@ def run_profile_frames(frames: int, start: int = 0):
     ctx.close()
 
 
+def run_profile_learned(frames: int, views: int, train_steps: int):
+    """A short GPU-only run for profilers: the headline's batched + learned
+    launch (first `views` street views, untrained selector at K = 10 %, the
+    same kernels and the same number of drawn occluders per view), `frames`
+    graph launches, then `train_steps` training steps on random rows."""
+    from rasterizer_gb300 import api, learned as L, scenes
+    mesh = scenes.city_scene()
+    occ = api.bake_scene(mesh.vertices, mesh.indices)
+    pmin, pmax = scenes.query_boxes(NQ, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    ctx = api.Context(0)
+    net = api.OccluderSelector(ctx, seed=0)
+    paths = L.street_tracks(views, 64, seed0=7000, n_occluders=len(occ), queries=NQ)
+    vs = L._views(ctx, occ, paths, pmin, pmax)
+    b = api.PreparedBatch(ctx, vs)
+    b.setSelection(net, 0.1, trackWins=True)
+    for f in range(frames):
+        for v, tr in enumerate(paths):
+            b.setModelViewProjection(v, tr.mvps[f % 64])
+        b.launch()
+    ok = b.check()
+    rng = np.random.default_rng(0)
+    x = rng.uniform(0, 1, (4096, 16)).astype(np.float32)
+    y = rng.uniform(0, 1, 4096).astype(np.float32)
+    for _ in range(train_steps):
+        net.trainStep(x, y, 1e-3)
+    print(json.dumps({"frames": frames, "views": views, "capacity_ok": ok, "stats": b.stats()}), flush=True)
+    b.close()
+    net.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile-run", type=int, default=0, metavar="FRAMES",
@@ -665,10 +696,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-view batched leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-selection leg (training included)")
+    ap.add_argument("--profile-learned", type=int, default=0, metavar="FRAMES",
+                    help="only launch the batched + learned frame FRAMES times (for ncu); prints a status line")
+    ap.add_argument("--profile-views", type=int, default=LEARNED_VIEWS, help="views per launch for --profile-learned")
+    ap.add_argument("--profile-train", type=int, default=0, help="training steps after --profile-learned")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.profile_run:
+    if args.profile_learned:
+        run_profile_learned(args.profile_learned, args.profile_views, args.profile_train)
+    elif args.profile_run:
         run_profile_frames(args.profile_run)
     elif args.impl == "reference":
         run_reference(args)

@@ -30,7 +30,8 @@ cudaError_t launch_mlp_forward(const float* feat, uint32_t M, const MlpDevice* m
                                float* xb, cudaStream_t stream);
 cudaError_t launch_mlp_backward(const float* score, const float* target, uint32_t B, const MlpDevice* mlp,
                                 const float* xb, const float* h1, const float* h2, float* ds, float* dh1, float* dh2,
-                                float* err2, float* grad, cudaStream_t stream);
+                                float* err2, float* partial, float* grad, cudaStream_t stream);
+uint32_t mlp_grad_blocks(uint32_t B);
 cudaError_t launch_mlp_publish(const float* params, MlpDevice* mlp, cudaStream_t stream);
 cudaError_t launch_adam(float* params, const float* grad, float* m, float* v, float lr, uint32_t step,
                         cudaStream_t stream);
@@ -881,6 +882,7 @@ struct occ_mlp_s {
   DevBuf<float> params, m, v, grad;  // fp32 master weights, Adam moments, gradient (+ loss)
   DevBuf<MlpDevice> dev;             // the kernels' copy (bf16 matrices)
   DevBuf<float> feat, target, score, xb, h1, h2, ds, dh1, dh2, err2;  // training batch
+  DevBuf<float> partial;  // per row block partial gradients
   uint32_t step = 0;
 };
 
@@ -1403,6 +1405,7 @@ static int mlp_batch(occ_mlp m, uint32_t n, const float* features, const float* 
   OCC_CHECK(m->dh1.reserve((size_t)n * kHidden));
   OCC_CHECK(m->dh2.reserve((size_t)n * kHidden));
   OCC_CHECK(m->err2.reserve(n));
+  OCC_CHECK(m->partial.reserve((size_t)mlp_grad_blocks(n) * (mlp_param_count() + 1)));
   cudaStream_t st = m->ctx->stream;
   OCC_CUDA(cudaMemcpyAsync(m->feat.p, features, (size_t)n * kFeatures * 4, cudaMemcpyHostToDevice, st));
   if (targets) OCC_CUDA(cudaMemcpyAsync(m->target.p, targets, (size_t)n * 4, cudaMemcpyHostToDevice, st));
@@ -1428,7 +1431,7 @@ int occ_mlp_gradients(occ_mlp m, uint32_t n, const float* features, const float*
   cudaStream_t st = m->ctx->stream;
   OCC_CUDA(launch_mlp_forward(m->feat.p, n, m->dev.p, m->score.p, m->h1.p, m->h2.p, m->xb.p, st));
   OCC_CUDA(launch_mlp_backward(m->score.p, m->target.p, n, m->dev.p, m->xb.p, m->h1.p, m->h2.p, m->ds.p, m->dh1.p,
-                               m->dh2.p, m->err2.p, m->grad.p, st));
+                               m->dh2.p, m->err2.p, m->partial.p, m->grad.p, st));
   const int np = mlp_param_count();
   if (grads) OCC_CUDA(cudaMemcpyAsync(grads, m->grad.p, (size_t)np * 4, cudaMemcpyDeviceToHost, st));
   if (loss) OCC_CUDA(cudaMemcpyAsync(loss, m->grad.p + np, 4, cudaMemcpyDeviceToHost, st));
@@ -1443,7 +1446,7 @@ int occ_mlp_train_step(occ_mlp m, uint32_t n, const float* features, const float
   cudaStream_t st = m->ctx->stream;
   OCC_CUDA(launch_mlp_forward(m->feat.p, n, m->dev.p, m->score.p, m->h1.p, m->h2.p, m->xb.p, st));
   OCC_CUDA(launch_mlp_backward(m->score.p, m->target.p, n, m->dev.p, m->xb.p, m->h1.p, m->h2.p, m->ds.p, m->dh1.p,
-                               m->dh2.p, m->err2.p, m->grad.p, st));
+                               m->dh2.p, m->err2.p, m->partial.p, m->grad.p, st));
   OCC_CUDA(launch_adam(m->params.p, m->grad.p, m->m.p, m->v.p, lr, ++m->step, st));
   OCC_CUDA(launch_mlp_publish(m->params.p, m->dev.p, st));
   if (loss) OCC_CUDA(cudaMemcpyAsync(loss, m->grad.p + mlp_param_count(), 4, cudaMemcpyDeviceToHost, st));

@@ -398,39 +398,51 @@ __global__ void __launch_bounds__(128) k_mlp_backward_rows(const float* __restri
   }
 }
 
-// Gradient of every parameter (and the loss in slot kParams), summed over the
-// batch in row order (deterministic).
-__global__ void __launch_bounds__(128) k_mlp_grad_reduce(uint32_t B, const float* __restrict__ xb,
-                                                         const float* __restrict__ h1, const float* __restrict__ h2,
-                                                         const float* __restrict__ ds, const float* __restrict__ dh1,
-                                                         const float* __restrict__ dh2, const float* __restrict__ err2,
-                                                         float* grad)
+// Gradient of every parameter (and the squared errors in slot kParams), summed
+// over the rows of one row block [r0, r1) in row order: partial[rb][p].
+__device__ __forceinline__ float grad_term(uint32_t p, uint32_t r, const float* __restrict__ xb,
+                                           const float* __restrict__ h1, const float* __restrict__ h2,
+                                           const float* __restrict__ ds, const float* __restrict__ dh1,
+                                           const float* __restrict__ dh2, const float* __restrict__ err2)
+{
+  if (p < (uint32_t)kOffB1) {
+    const uint32_t n = p / kFeatures, k = p % kFeatures;
+    return dh1[(size_t)r * kHidden + n] * xb[(size_t)r * kFeatures + k];
+  }
+  if (p < (uint32_t)kOffW2) return dh1[(size_t)r * kHidden + (p - kOffB1)];
+  if (p < (uint32_t)kOffB2) {
+    const uint32_t q = p - kOffW2, n = q / kHidden, k = q % kHidden;
+    return dh2[(size_t)r * kHidden + n] * h1[(size_t)r * kHidden + k];
+  }
+  if (p < (uint32_t)kOffW3) return dh2[(size_t)r * kHidden + (p - kOffB2)];
+  if (p < (uint32_t)kOffB3) return ds[r] * h2[(size_t)r * kHidden + (p - kOffW3)];
+  if (p == (uint32_t)kOffB3) return ds[r];
+  return err2[r];
+}
+
+__global__ void __launch_bounds__(128) k_mlp_grad_partial(uint32_t B, uint32_t rowsPerBlock,
+                                                          const float* __restrict__ xb, const float* __restrict__ h1,
+                                                          const float* __restrict__ h2, const float* __restrict__ ds,
+                                                          const float* __restrict__ dh1, const float* __restrict__ dh2,
+                                                          const float* __restrict__ err2, float* partial)
+{
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > (uint32_t)kParams) return;
+  const uint32_t r0 = blockIdx.y * rowsPerBlock, r1 = ::min(B, r0 + rowsPerBlock);
+  float acc = 0.0f;
+  for (uint32_t r = r0; r < r1; ++r) acc += grad_term(p, r, xb, h1, h2, ds, dh1, dh2, err2);
+  partial[(size_t)blockIdx.y * (kParams + 1) + p] = acc;
+}
+
+// Sums the row blocks in order (deterministic); slot kParams becomes the loss.
+__global__ void __launch_bounds__(128) k_mlp_grad_final(uint32_t B, uint32_t blocks, const float* __restrict__ partial,
+                                                        float* grad)
 {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p > (uint32_t)kParams) return;
   float acc = 0.0f;
-  if (p < (uint32_t)kOffB1) {
-    const uint32_t n = p / kFeatures, k = p % kFeatures;
-    for (uint32_t r = 0; r < B; ++r) acc += dh1[(size_t)r * kHidden + n] * xb[(size_t)r * kFeatures + k];
-  } else if (p < (uint32_t)kOffW2) {
-    const uint32_t n = p - kOffB1;
-    for (uint32_t r = 0; r < B; ++r) acc += dh1[(size_t)r * kHidden + n];
-  } else if (p < (uint32_t)kOffB2) {
-    const uint32_t q = p - kOffW2, n = q / kHidden, k = q % kHidden;
-    for (uint32_t r = 0; r < B; ++r) acc += dh2[(size_t)r * kHidden + n] * h1[(size_t)r * kHidden + k];
-  } else if (p < (uint32_t)kOffW3) {
-    const uint32_t n = p - kOffB2;
-    for (uint32_t r = 0; r < B; ++r) acc += dh2[(size_t)r * kHidden + n];
-  } else if (p < (uint32_t)kOffB3) {
-    const uint32_t k = p - kOffW3;
-    for (uint32_t r = 0; r < B; ++r) acc += ds[r] * h2[(size_t)r * kHidden + k];
-  } else if (p == (uint32_t)kOffB3) {
-    for (uint32_t r = 0; r < B; ++r) acc += ds[r];
-  } else {
-    for (uint32_t r = 0; r < B; ++r) acc += err2[r];
-    acc /= (float)B;  // loss
-  }
-  grad[p] = acc;
+  for (uint32_t b = 0; b < blocks; ++b) acc += partial[(size_t)b * (kParams + 1) + p];
+  grad[p] = p == (uint32_t)kParams ? acc / (float)B : acc;
 }
 
 // Writes the kernels' copy of the weights (bf16 matrices) from the fp32 master.
@@ -486,12 +498,17 @@ cudaError_t launch_mlp_forward(const float* feat, uint32_t M, const MlpDevice* m
   return cudaGetLastError();
 }
 
+uint32_t mlp_grad_blocks(uint32_t B) { return ::min(64u, (B + 63) / 64); }
+
 cudaError_t launch_mlp_backward(const float* score, const float* target, uint32_t B, const MlpDevice* mlp,
                                 const float* xb, const float* h1, const float* h2, float* ds, float* dh1, float* dh2,
-                                float* err2, float* grad, cudaStream_t stream)
+                                float* err2, float* partial, float* grad, cudaStream_t stream)
 {
   k_mlp_backward_rows<<<(B + 127) / 128, 128, 0, stream>>>(score, target, B, mlp, h1, h2, ds, dh1, dh2, err2);
-  k_mlp_grad_reduce<<<(kParams + 1 + 127) / 128, 128, 0, stream>>>(B, xb, h1, h2, ds, dh1, dh2, err2, grad);
+  const uint32_t nb = mlp_grad_blocks(B), rows = (B + nb - 1) / nb;
+  const dim3 grid((kParams + 1 + 127) / 128, nb);
+  k_mlp_grad_partial<<<grid, 128, 0, stream>>>(B, rows, xb, h1, h2, ds, dh1, dh2, err2, partial);
+  k_mlp_grad_final<<<(kParams + 1 + 127) / 128, 128, 0, stream>>>(B, nb, partial, grad);
   return cudaGetLastError();
 }
 
