@@ -333,7 +333,7 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
     quads = np.array([o.quads for o in occ])
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     t = L.Timer()
-    net, report = L.train_selector(ctx, occ, NQ, log=None)
+    net, report = L.train_selector(ctx, occ, NQ, log=None, mins=pmin, maxs=pmax)
     out = {"training": dict(report, seconds=t.lap())}
     fracs = (0.05, 0.1, 0.2, 0.35, 0.5)
 

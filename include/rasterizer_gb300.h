@@ -166,6 +166,14 @@ int occ_mlp_gradients(occ_mlp m, uint32_t n, const float* features, const float*
  * floats each; any pointer may be NULL on get) and the Adam step count. */
 int occ_mlp_get_state(occ_mlp m, float* params, float* adamM, float* adamV, uint32_t* step);
 int occ_mlp_set_state(occ_mlp m, const float* params, const float* adamM, const float* adamV, uint32_t step);
+/* Listwise loss: rows form numGroups groups (one view in one frame each),
+ * group g = rows [groupStart[g], groupStart[g+1]), groupStart[numGroups] = n;
+ * targets are a distribution over each group's rows; loss = mean over groups
+ * of the cross-entropy between it and the softmax of the group's scores. */
+int occ_mlp_gradients_listwise(occ_mlp m, uint32_t n, const float* features, const float* targets,
+                               uint32_t numGroups, const uint32_t* groupStart, float* loss, float* grads);
+int occ_mlp_train_step_listwise(occ_mlp m, uint32_t n, const float* features, const float* targets,
+                                uint32_t numGroups, const uint32_t* groupStart, float lr, float* loss);
 /* one Adam step (beta 0.9 / 0.999) on one batch */
 int occ_mlp_train_step(occ_mlp m, uint32_t n, const float* features, const float* targets, float lr, float* loss);
 /* On a prepared batch: mlp != NULL keeps ceil(fraction * candidates) occluders
@@ -184,8 +192,23 @@ int occ_batch_set_zero_depth(occ_batch b, int enable);
  * rasterised (the others only cleared), the batch's chunk count, and the
  * bytes of tables each launch copies from the host. */
 int occ_batch_stats(occ_batch b, uint32_t out[7]);
+/* With enable != 0 (and a network set), each launch runs a second pass after
+ * the top-K one: every other candidate whose bounds are still visible against
+ * the first pass's buffer (queryVisibility, as Main.cpp:192-206 runs it before
+ * each rasterize) is drawn too, without a clear; the queries follow the second
+ * pass.  The frame then differs from the full frame only by drawing order.
+ * A pixel whose value the second pass replaces counts as a win of both
+ * occluders. */
+int occ_batch_set_second_pass(occ_batch b, int enable);
+/* Training labels of the selector (needs trackWins): each launch records the
+ * owner of every pixel's final value and, for every query box culled by
+ * depth (inside the frustum), credits the owners of a 4x4 grid of sample
+ * pixels in its screen rectangle.  Per occluder of the view: its credits. */
+int occ_batch_set_cull_labels(occ_batch b, int enable);
+int occ_batch_read_cull_labels(occ_batch b, uint32_t view, uint32_t* counts);
 /* Per occluder of the view, after the last launch: its features, pixel wins,
- * candidate flag (passes the visibility test), selected flag and score. */
+ * candidate flag (passes the visibility test), selected flag (1 = top-K,
+ * 2 = drawn by the second pass) and score. */
 int occ_batch_read_selection(occ_batch b, uint32_t view, float* features, uint32_t* wins, uint8_t* candidate,
                              uint8_t* selected, float* scores);
 

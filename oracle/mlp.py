@@ -88,3 +88,34 @@ def adam(p, g, m, v, step: int, lr: float, beta1=0.9, beta2=0.999, eps=1e-8):
     bc2 = np.float32(1 - beta2 ** step)
     p = p - np.float32(lr) * (m / bc1) / (np.sqrt(v / bc2) + np.float32(eps))
     return p, m, v
+
+
+def listwise_gradients(p: np.ndarray, x: np.ndarray, t: np.ndarray, group_start: np.ndarray):
+    """Listwise loss: per group, cross-entropy between the target distribution
+    t and the softmax of the scores; mean over groups.  (loss, gradient)."""
+    W1, b1, W2, b2, w3, b3 = unpack(p)
+    s, a = forward(p, x, keep=True)
+    t = np.asarray(t, np.float64)
+    G = len(group_start) - 1
+    ds = np.zeros_like(s)
+    loss = 0.0
+    for g in range(G):
+        lo, hi = int(group_start[g]), int(group_start[g + 1])
+        if hi <= lo:
+            continue
+        z = s[lo:hi] - s[lo:hi].max()
+        lp = z - np.log(np.exp(z).sum())
+        loss += -(t[lo:hi] * lp).sum()
+        ds[lo:hi] = np.exp(lp) - t[lo:hi]
+    ds /= G
+    loss /= G
+    g = np.zeros(PARAMS)
+    g[5248:5312] = a["h2"].T @ ds
+    g[5312] = ds.sum()
+    dz2 = np.outer(ds, w3.astype(np.float64)) * (a["z2"] > 0)
+    g[1088:5184] = (dz2.T @ a["h1b"]).ravel()
+    g[5184:5248] = dz2.sum(axis=0)
+    dz1 = (dz2 @ bf16(W2).astype(np.float64)) * (a["z1"] > 0)
+    g[0:1024] = (dz1.T @ a["xb"]).ravel()
+    g[1024:1088] = dz1.sum(axis=0)
+    return loss, g

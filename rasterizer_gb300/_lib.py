@@ -64,6 +64,9 @@ SIGNATURES = {
     "occ_batch_set_selection": (I32, [P, P, C.c_float, I32]),
     "occ_batch_read_selection": (I32, [P, U32, P, P, P, P, P]),
     "occ_batch_set_zero_depth": (I32, [P, I32]),
+    "occ_batch_set_second_pass": (I32, [P, I32]),
+    "occ_batch_set_cull_labels": (I32, [P, I32]),
+    "occ_batch_read_cull_labels": (I32, [P, U32, P]),
     "occ_batch_stats": (I32, [P, P]),
     "occ_mlp_param_count": (I32, []),
     "occ_mlp_create": (I32, [P, U32, C.POINTER(P)]),
@@ -75,6 +78,8 @@ SIGNATURES = {
     "occ_mlp_forward": (I32, [P, U32, P, P]),
     "occ_mlp_gradients": (I32, [P, U32, P, P, C.POINTER(C.c_float), P]),
     "occ_mlp_train_step": (I32, [P, U32, P, P, C.c_float, C.POINTER(C.c_float)]),
+    "occ_mlp_gradients_listwise": (I32, [P, U32, P, P, U32, P, C.POINTER(C.c_float), P]),
+    "occ_mlp_train_step_listwise": (I32, [P, U32, P, P, U32, P, C.c_float, C.POINTER(C.c_float)]),
     "occ_quad_decompose": (I32, [P, U32, P, U32, P, C.POINTER(U32)]),
     "occ_sah_generate_batches": (I32, [P, U32, U32, U32, P, P, C.POINTER(U32)]),
     "occ_occluder_bake": (I32, [P, U32, P, P, P, C.POINTER(U32), P, P, P]),

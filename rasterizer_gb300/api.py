@@ -426,6 +426,23 @@ class PreparedBatch:
         keys = ("rows", "checkpoints", "list_entries", "active_chunks", "active_tiles", "chunks", "table_bytes")
         return {k: int(v) for k, v in zip(keys, out)}
 
+    def setSecondPass(self, enable: bool) -> None:
+        """After the top-K pass, also draw every other candidate whose bounds
+        are still visible against that pass's buffer (needs a selector)."""
+        check(lib().occ_batch_set_second_pass(self.handle, int(bool(enable))), "occ_batch_set_second_pass")
+
+    def setCullLabels(self, enable: bool) -> None:
+        """Per launch, credit each occluder with the sample pixels it owns in
+        the screen rectangles of the boxes culled by depth (needs trackWins)."""
+        check(lib().occ_batch_set_cull_labels(self.handle, int(bool(enable))), "occ_batch_set_cull_labels")
+
+    def cullLabels(self, view: int) -> np.ndarray:
+        n = self.ws.ncmd[view]
+        out = np.zeros(n, np.uint32)
+        if n:
+            check(lib().occ_batch_read_cull_labels(self.handle, view, _ptr(out)), "occ_batch_read_cull_labels")
+        return out
+
     def setZeroDepth(self, enable: bool) -> None:
         """Zero each cleared view's depth at the start of every launch, so a
         frame's queries do not see depth left by earlier frames in cleared
@@ -434,7 +451,8 @@ class PreparedBatch:
 
     def selection(self, view: int) -> dict:
         """Per occluder of `view` after the last launch: features (n x 16, the
-        previous-launch wins among them), wins, candidate, selected, score."""
+        previous-launch wins among them), wins, candidate, selected (drawn by
+        either pass), second_pass (drawn by the second pass), score."""
         n = self.ws.ncmd[view]
         out = dict(features=np.zeros((n, 16), np.float32), wins=np.zeros(n, np.uint32),
                    candidate=np.zeros(n, np.uint8), selected=np.zeros(n, np.uint8), score=np.zeros(n, np.float32))
@@ -443,7 +461,8 @@ class PreparedBatch:
                                                  _ptr(out["candidate"]), _ptr(out["selected"]), _ptr(out["score"])),
                   "occ_batch_read_selection")
         out["candidate"] = out["candidate"].astype(bool)
-        out["selected"] = out["selected"].astype(bool)
+        out["second_pass"] = out["selected"] == 2
+        out["selected"] = out["selected"] != 0
         return out
 
     def results(self, view: int):
@@ -528,6 +547,27 @@ class OccluderSelector:
         check(lib().occ_mlp_gradients(self.handle, len(x), _ptr(x), _ptr(t), C.byref(loss), _ptr(g)),
               "occ_mlp_gradients")
         return float(loss.value), g
+
+    def gradientsListwise(self, features, targets, group_start):
+        x = _f32(features).reshape(-1, self.FEATURES)
+        t = _f32(targets).reshape(len(x))
+        gs = np.ascontiguousarray(group_start, np.uint32)
+        g = np.zeros(self.nparams, np.float32)
+        loss = C.c_float()
+        check(lib().occ_mlp_gradients_listwise(self.handle, len(x), _ptr(x), _ptr(t), len(gs) - 1, _ptr(gs),
+                                               C.byref(loss), _ptr(g)), "occ_mlp_gradients_listwise")
+        return float(loss.value), g
+
+    def trainStepListwise(self, features, targets, group_start, lr: float = 1e-3) -> float:
+        """One Adam step on the listwise loss: rows in groups (group_start[g]
+        .. group_start[g+1]), targets a distribution within each group."""
+        x = _f32(features).reshape(-1, self.FEATURES)
+        t = _f32(targets).reshape(len(x))
+        gs = np.ascontiguousarray(group_start, np.uint32)
+        loss = C.c_float()
+        check(lib().occ_mlp_train_step_listwise(self.handle, len(x), _ptr(x), _ptr(t), len(gs) - 1, _ptr(gs),
+                                                float(lr), C.byref(loss)), "occ_mlp_train_step_listwise")
+        return float(loss.value)
 
     def trainStep(self, features, targets, lr: float = 1e-3) -> float:
         x = _f32(features).reshape(-1, self.FEATURES)

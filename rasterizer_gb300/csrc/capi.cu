@@ -30,9 +30,11 @@ cudaError_t launch_mlp_forward(const float* feat, uint32_t M, const MlpDevice* m
                                float* xb, cudaStream_t stream);
 cudaError_t launch_mlp_backward(const float* score, const float* target, uint32_t B, const MlpDevice* mlp,
                                 const float* xb, const float* h1, const float* h2, float* ds, float* dh1, float* dh2,
-                                float* err2, float* partial, float* grad, cudaStream_t stream);
+                                float* err2, float* partial, float* grad, cudaStream_t stream,
+                                const uint32_t* groupStart = nullptr, uint32_t groups = 0);
 uint32_t mlp_grad_blocks(uint32_t B);
 cudaError_t launch_mlp_publish(const float* params, MlpDevice* mlp, cudaStream_t stream);
+cudaError_t launch_cull_labels(const FrameParams& P, cudaStream_t stream);
 cudaError_t launch_adam(float* params, const float* grad, float* m, float* v, float lr, uint32_t step,
                         cudaStream_t stream);
 int mlp_param_count();
@@ -176,6 +178,7 @@ struct occ_raster_s {
   occ_ctx_s* ctx = nullptr;
   uint32_t width = 0, height = 0, blocksX = 0, blocksY = 0;
   DevBuf<uint16_t> depth, hiz, tileHiz;
+  DevBuf<uint32_t> owner;  // per pixel: command + 1 of its final value (cull labels only)
   float cols[16] = {};
   float rows[16] = {};
   bool clearPending = false;
@@ -883,6 +886,7 @@ struct occ_mlp_s {
   DevBuf<MlpDevice> dev;             // the kernels' copy (bf16 matrices)
   DevBuf<float> feat, target, score, xb, h1, h2, ds, dh1, dh2, err2;  // training batch
   DevBuf<float> partial;  // per row block partial gradients
+  DevBuf<uint32_t> groups;  // listwise loss: first row of each group, then the row count
   uint32_t step = 0;
 };
 
@@ -911,6 +915,9 @@ struct occ_batch_s {
   float selectFrac = 1.0f;
   bool trackWins = false, features = false;
   bool zeroDepth = false;  // zero every view's depth at the start of each launch
+  bool secondPass = false; // after the top-K pass, draw the other candidates still visible
+  bool cullLabels = false; // per-pixel owners and per-command cull counts (training labels)
+  DevBuf<uint32_t> cullCount;
   DevBuf<float> feat, score;
   DevBuf<uint8_t> cand, select;
   DevBuf<uint32_t> wins;
@@ -1000,6 +1007,8 @@ int capture(occ_batch_s* b)
       P.selectFrac = b->selectFrac;
     }
   }
+  const bool labels = b->cullLabels && b->features && b->trackWins;
+  if (labels) P.cullCount = b->cullCount.p;
   b->params = P;
   b->anyRaster = anyRaster;
 
@@ -1009,8 +1018,22 @@ int capture(occ_batch_s* b)
     for (auto& J : b->jobs)
       if (e1 == cudaSuccess && J.clear)
         e1 = cudaMemsetAsync(J.r->depth.p, 0, (size_t)J.r->width * J.r->height * sizeof(uint16_t), ctx->stream);
+  if (labels) {
+    for (auto& J : b->jobs)
+      if (e1 == cudaSuccess)
+        e1 = cudaMemsetAsync(J.r->owner.p, 0, (size_t)J.r->width * J.r->height * sizeof(uint32_t), ctx->stream);
+    if (e1 == cudaSuccess && numCmds) e1 = cudaMemsetAsync(b->cullCount.p, 0, (size_t)numCmds * 4, ctx->stream);
+  }
   cudaError_t e2 = b->features ? launch_selection(P, numCmds, b->mlp != nullptr, ctx->stream) : cudaSuccess;
-  if (e2 == cudaSuccess) e2 = launch_flush(P, b->L.numSt, b->L.maxStPerView, anyRaster, b->L.querySlots > 0, ctx->stream);
+  const bool two = b->secondPass && b->mlp != nullptr;
+  if (e2 == cudaSuccess)
+    e2 = launch_flush(P, b->L.numSt, b->L.maxStPerView, anyRaster, !two && b->L.querySlots > 0, ctx->stream);
+  if (e2 == cudaSuccess && two) {
+    FrameParams P2 = P;
+    P2.phase = 1;
+    e2 = launch_flush(P2, b->L.numSt, b->L.maxStPerView, anyRaster, b->L.querySlots > 0, ctx->stream);
+  }
+  if (e2 == cudaSuccess && labels) e2 = launch_cull_labels(P, ctx->stream);
   cudaGraph_t g = nullptr;
   cudaError_t e3 = cudaStreamEndCapture(ctx->stream, &g);
   if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
@@ -1189,8 +1212,24 @@ int occ_batch_profile(occ_batch b, uint32_t iterations, float* msPerKernel)
     cudaEventRecord(ev[7], ctx->stream);
     cudaError_t e = b->features ? launch_selection(b->params, (uint32_t)b->L.cmds.size(), b->mlp != nullptr, ctx->stream)
                                 : cudaSuccess;
+    const bool two = b->secondPass && b->mlp != nullptr;
     if (e == cudaSuccess) e = launch_flush_timed(b->params, b->L.numSt, b->L.maxStPerView, b->anyRaster,
-                                       b->L.querySlots > 0, ctx->stream, ev);
+                                                 !two && b->L.querySlots > 0, ctx->stream, ev);
+    if (e == cudaSuccess && cudaEventSynchronize(ev[6]) == cudaSuccess) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[7], ev[0]);
+      msPerKernel[6] += ms / (float)iterations;
+      if (two) {  // the second pass is timed into the same stages
+        for (int k = 0; k < 6; ++k) {
+          cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+          msPerKernel[k] += ms / (float)iterations;
+        }
+        FrameParams P2 = b->params;
+        P2.phase = 1;
+        e = launch_flush_timed(P2, b->L.numSt, b->L.maxStPerView, b->anyRaster, b->L.querySlots > 0, ctx->stream,
+                               ev);
+      }
+    }
     cudaEventRecord(b->ringEv[b->cur], ctx->stream);
     if (e != cudaSuccess) status = fail(OCC_ERR_CUDA, std::string("profile launch: ") + cudaGetErrorString(e));
     if (cudaEventSynchronize(ev[6]) != cudaSuccess) status = fail(OCC_ERR_CUDA, "profile sync");
@@ -1198,11 +1237,6 @@ int occ_batch_profile(occ_batch b, uint32_t iterations, float* msPerKernel)
       float ms = 0;
       cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
       msPerKernel[k] += ms / (float)iterations;
-    }
-    if (status == OCC_OK) {
-      float ms = 0;
-      cudaEventElapsedTime(&ms, ev[7], ev[0]);
-      msPerKernel[6] += ms / (float)iterations;
     }
   }
   for (auto& e : ev) cudaEventDestroy(e);
@@ -1249,6 +1283,45 @@ int occ_batch_stats(occ_batch b, uint32_t out[7])
   return OCC_OK;
 }
 
+int occ_batch_set_cull_labels(occ_batch b, int enable)
+{
+  if (!b) return fail(OCC_ERR_INVALID_ARG, "null batch");
+  if (enable && !(b->features && b->trackWins))
+    return fail(OCC_ERR_INVALID_ARG, "cull labels need win counting (occ_batch_set_selection with trackWins)");
+  b->cullLabels = enable != 0;
+  if (b->cullLabels) {
+    OCC_CHECK(b->cullCount.reserve(std::max<size_t>(b->L.cmds.size(), 1)));
+    for (size_t v = 0; v < b->jobs.size(); ++v) {
+      occ_raster_s* r = b->jobs[v].r;
+      OCC_CHECK(r->owner.reserve((size_t)r->width * r->height));
+      b->L.views[v].owner = r->owner.p;
+    }
+  } else {
+    for (auto& V : b->L.views) V.owner = nullptr;
+  }
+  b->dirty = true;  // the next launch uploads the view table with the owner buffers
+  return capture(b);
+}
+
+int occ_batch_read_cull_labels(occ_batch b, uint32_t view, uint32_t* counts)
+{
+  if (!b || !counts || view >= b->L.views.size()) return fail(OCC_ERR_INVALID_ARG, "bad argument");
+  if (!b->cullLabels) return fail(OCC_ERR_INVALID_ARG, "cull labels are not enabled on this batch");
+  const ViewDesc& V = b->L.views[view];
+  if (V.cmdCount)
+    OCC_CUDA(cudaMemcpyAsync(counts, b->cullCount.p + V.cmdStart, (size_t)V.cmdCount * 4, cudaMemcpyDeviceToHost,
+                             b->ctx->stream));
+  OCC_CUDA(cudaStreamSynchronize(b->ctx->stream));
+  return OCC_OK;
+}
+
+int occ_batch_set_second_pass(occ_batch b, int enable)
+{
+  if (!b) return fail(OCC_ERR_INVALID_ARG, "null batch");
+  b->secondPass = enable != 0;
+  return capture(b);
+}
+
 int occ_batch_set_zero_depth(occ_batch b, int enable)
 {
   if (!b) return fail(OCC_ERR_INVALID_ARG, "null batch");
@@ -1271,6 +1344,13 @@ int occ_batch_read_selection(occ_batch b, uint32_t view, float* features, uint32
     if (selected) {
       if (b->mlp) OCC_CUDA(cudaMemcpyAsync(selected, b->select.p + c0, n, cudaMemcpyDeviceToHost, st));
       else OCC_CUDA(cudaMemcpyAsync(selected, b->cand.p + c0, n, cudaMemcpyDeviceToHost, st));
+      if (b->mlp && b->secondPass) {
+        std::vector<uint32_t> draw(n);
+        OCC_CUDA(cudaMemcpyAsync(draw.data(), b->S.cmdDraw.p + c0, n * 4, cudaMemcpyDeviceToHost, st));
+        OCC_CUDA(cudaStreamSynchronize(st));
+        for (size_t i = 0; i < n; ++i)
+          if (!selected[i] && (draw[i] & 1u)) selected[i] = 2;  // drawn by the second pass
+      }
     }
     if (scores) OCC_CUDA(cudaMemcpyAsync(scores, b->score.p + c0, n * 4, cudaMemcpyDeviceToHost, st));
   }
@@ -1435,6 +1515,52 @@ int occ_mlp_gradients(occ_mlp m, uint32_t n, const float* features, const float*
   const int np = mlp_param_count();
   if (grads) OCC_CUDA(cudaMemcpyAsync(grads, m->grad.p, (size_t)np * 4, cudaMemcpyDeviceToHost, st));
   if (loss) OCC_CUDA(cudaMemcpyAsync(loss, m->grad.p + np, 4, cudaMemcpyDeviceToHost, st));
+  OCC_CUDA(cudaStreamSynchronize(st));
+  return OCC_OK;
+}
+
+static int mlp_groups(occ_mlp m, uint32_t n, uint32_t numGroups, const uint32_t* groupStart)
+{
+  if (!groupStart || !numGroups || groupStart[0] != 0 || groupStart[numGroups] != n)
+    return fail(OCC_ERR_INVALID_ARG, "group starts must run from 0 to n");
+  for (uint32_t g = 0; g < numGroups; ++g)
+    if (groupStart[g + 1] < groupStart[g]) return fail(OCC_ERR_INVALID_ARG, "group starts must not decrease");
+  OCC_CHECK(m->groups.reserve(numGroups + 1));
+  OCC_CUDA(cudaMemcpyAsync(m->groups.p, groupStart, (size_t)(numGroups + 1) * 4, cudaMemcpyHostToDevice,
+                           m->ctx->stream));
+  return OCC_OK;
+}
+
+int occ_mlp_gradients_listwise(occ_mlp m, uint32_t n, const float* features, const float* targets,
+                               uint32_t numGroups, const uint32_t* groupStart, float* loss, float* grads)
+{
+  if (!m || !n || !features || !targets) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  OCC_CHECK(mlp_groups(m, n, numGroups, groupStart));
+  OCC_CHECK(mlp_batch(m, n, features, targets));
+  cudaStream_t st = m->ctx->stream;
+  OCC_CUDA(launch_mlp_forward(m->feat.p, n, m->dev.p, m->score.p, m->h1.p, m->h2.p, m->xb.p, st));
+  OCC_CUDA(launch_mlp_backward(m->score.p, m->target.p, n, m->dev.p, m->xb.p, m->h1.p, m->h2.p, m->ds.p, m->dh1.p,
+                               m->dh2.p, m->err2.p, m->partial.p, m->grad.p, st, m->groups.p, numGroups));
+  const int np = mlp_param_count();
+  if (grads) OCC_CUDA(cudaMemcpyAsync(grads, m->grad.p, (size_t)np * 4, cudaMemcpyDeviceToHost, st));
+  if (loss) OCC_CUDA(cudaMemcpyAsync(loss, m->grad.p + np, 4, cudaMemcpyDeviceToHost, st));
+  OCC_CUDA(cudaStreamSynchronize(st));
+  return OCC_OK;
+}
+
+int occ_mlp_train_step_listwise(occ_mlp m, uint32_t n, const float* features, const float* targets,
+                                uint32_t numGroups, const uint32_t* groupStart, float lr, float* loss)
+{
+  if (!m || !n || !features || !targets) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  OCC_CHECK(mlp_groups(m, n, numGroups, groupStart));
+  OCC_CHECK(mlp_batch(m, n, features, targets));
+  cudaStream_t st = m->ctx->stream;
+  OCC_CUDA(launch_mlp_forward(m->feat.p, n, m->dev.p, m->score.p, m->h1.p, m->h2.p, m->xb.p, st));
+  OCC_CUDA(launch_mlp_backward(m->score.p, m->target.p, n, m->dev.p, m->xb.p, m->h1.p, m->h2.p, m->ds.p, m->dh1.p,
+                               m->dh2.p, m->err2.p, m->partial.p, m->grad.p, st, m->groups.p, numGroups));
+  OCC_CUDA(launch_adam(m->params.p, m->grad.p, m->m.p, m->v.p, lr, ++m->step, st));
+  OCC_CUDA(launch_mlp_publish(m->params.p, m->dev.p, st));
+  if (loss) OCC_CUDA(cudaMemcpyAsync(loss, m->grad.p + mlp_param_count(), 4, cudaMemcpyDeviceToHost, st));
   OCC_CUDA(cudaStreamSynchronize(st));
   return OCC_OK;
 }

@@ -468,15 +468,56 @@ __global__ void __launch_bounds__(256) k_gate(FrameParams P)
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= P.numCmds) return;
   const Cmd& cmd = P.cmds[c];
+  const ViewDesc& V = P.views[cmd.view];
   uint32_t draw = 1, nc = (cmd.flags & kCmdNearClip) ? 1u : 0u;
   if (cmd.flags & kCmdGated) {
     uint32_t rect[4], maxZ = 0;
-    const int st = query_front(P.views[cmd.view], cmd.boundsMin, cmd.boundsMax, rect, &maxZ);
+    const int st = query_front(V, cmd.boundsMin, cmd.boundsMax, rect, &maxZ);
     draw = (st == 1 || (st == 2 && maxZ > 0)) ? 1u : 0u;
     nc = st == 1 ? 1u : 0u;
   }
   if (P.select && !P.select[c]) draw = 0;  // not among the view's top-K
   P.cmdDraw[c] = draw | (nc << 1);
+}
+
+// Second pass of a selection, one warp per command: a candidate left out of
+// the top-K is drawn if its bounds are still visible against the first pass's
+// buffer (queryVisibility, as the reference's loop runs it before each
+// rasterize, Main.cpp:192-206).  The lanes share the query2D over warp-tiles.
+__global__ void __launch_bounds__(256) k_gate_second(FrameParams P)
+{
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t c = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (c >= P.numCmds) return;  // whole warp
+  const uint32_t first = P.cmdDraw[c] & 1u;
+  uint32_t draw = 0, nc = 0;
+  if (!first && P.cand[c]) {
+    const Cmd& cmd = P.cmds[c];
+    const ViewDesc& V = P.views[cmd.view];
+    uint32_t rect[4], maxZ = 0;
+    const int st = query_front(V, cmd.boundsMin, cmd.boundsMax, rect, &maxZ);  // same on every lane
+    if (st == 1) {
+      draw = nc = 1;
+    } else if (st == 2) {
+      const uint32_t tilesX = (V.blocksX + kTileW - 1) / kTileW;
+      const uint32_t tx0 = (rect[0] >> 3) / kTileW, tx1 = (rect[1] >> 3) / kTileW;
+      const uint32_t ty0 = (rect[2] >> 3) / kTileH, ty1 = (rect[3] >> 3) / kTileH;
+      const uint32_t ntx = tx1 - tx0 + 1, nt = ntx * (ty1 - ty0 + 1);
+      bool found = false;
+      for (uint32_t t0 = 0; t0 < nt && !found; t0 += 32) {
+        const uint32_t t = t0 + lane;
+        bool hit = false;
+        if (t < nt) {
+          const uint32_t tx = tx0 + t % ntx, ty = ty0 + t / ntx;
+          if (maxZ > (uint32_t)V.tileHiz[ty * tilesX + tx])
+            hit = query2d_tile(V, tx, ty, rect[0], rect[1], rect[2], rect[3], maxZ);
+        }
+        found = __ballot_sync(0xFFFFFFFFu, hit) != 0;
+      }
+      draw = found ? 1u : 0u;
+    }
+  }
+  if (lane == 0) P.cmdDraw[c] = draw | (nc << 1) | (first << 2);
 }
 
 // One thread per chunk: chunks with a drawn command go to the active list (in
@@ -750,48 +791,67 @@ __global__ void __launch_bounds__(kChunk) k_fill(FrameParams P)
 // incremental adds along the row (Rasterizer.cpp:1125-1146), storing the edge
 // offsets and depth lanes at the quad's first column and every 8 block columns.
 
+// Plain IEEE add where the quad's depth cannot overflow (x86-exact there),
+// else the x86 rules; chosen per quad, outside the inner loops.
+template <bool kSafe>
+__device__ __forceinline__ float zadd(float a, float b)
+{
+  return kSafe ? x86::radd(a, b) : x86::xadd(a, b);
+}
+template <bool kSafe>
+__device__ __forceinline__ float zfma(float a, float b, float c)
+{
+  return kSafe ? x86::rfma(a, b, c) : x86::xfmadd(a, b, c);
+}
+
+template <bool kSafe>
+__device__ __forceinline__ void walk_row(const FrameParams& P, const QuadRaster& Q, const QuadWalk& Wk, uint32_t qq,
+                                         uint32_t r)
+{
+  const float dsp = -0.4375f;  // -0.5f + 1.0f / 16.0f
+  float depth[8], off[4];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const float lx = dsp + 0.125f * (float)(k & 3);
+    const float ly = dsp + 0.125f * (float)(k >> 2);
+    depth[k] = x86::xfmadd(Q.Dx, lx, x86::xfmadd(Q.Dy, ly, Wk.plane0));
+  }
+#pragma unroll
+  for (int e = 0; e < 4; ++e) off[e] = Wk.off[e];
+  for (uint32_t i = 0; i < r; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) depth[k] = zadd<kSafe>(depth[k], Q.Dy);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) off[e] = x86::radd(off[e], Wk.ny[e]);
+  }
+  const uint32_t nck = nck_of(Q);
+  float4* out = reinterpret_cast<float4*>(P.ck + (size_t)kCkFloats * (P.ckBase[qq] + r * nck));
+  const uint32_t lastCk = ::max((uint32_t)Q.minX, (uint32_t)(Q.maxX - 1) & ~7u);
+  for (uint32_t bx = Q.minX;; ++bx) {
+    if (bx == Q.minX || (bx & 7u) == 0) {
+      out[0] = make_float4(off[0], off[1], off[2], off[3]);
+      out[1] = make_float4(depth[0], depth[1], depth[2], depth[3]);
+      out[2] = make_float4(depth[4], depth[5], depth[6], depth[7]);
+      out += 3;
+    }
+    if (bx == lastCk) break;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) depth[k] = zadd<kSafe>(Q.Dx, depth[k]);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) off[e] = x86::radd(Q.nx[e], off[e]);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_walk(FrameParams P)
 {
   if (P.header->overflow) return;
   const uint32_t total = P.header->totalRows;
-  const float dsp = -0.4375f;  // -0.5f + 1.0f / 16.0f
   for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < total; row += gridDim.x * blockDim.x) {
     const uint2 own = P.rowOwner[row];
-    const uint32_t qq = own.x, r = own.y;
-    const QuadRaster Q = P.rec[qq];
-    const QuadWalk Wk = P.walk[qq];
-    const bool safe = (Q.flags & kQuadSafe) != 0;
-    float depth[8], off[4];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const float lx = dsp + 0.125f * (float)(k & 3);
-      const float ly = dsp + 0.125f * (float)(k >> 2);
-      depth[k] = x86::xfmadd(Q.Dx, lx, x86::xfmadd(Q.Dy, ly, Wk.plane0));
-    }
-#pragma unroll
-    for (int e = 0; e < 4; ++e) off[e] = Wk.off[e];
-    for (uint32_t i = 0; i < r; ++i) {
-#pragma unroll
-      for (int k = 0; k < 8; ++k) depth[k] = safe ? x86::radd(depth[k], Q.Dy) : x86::xadd(depth[k], Q.Dy);
-#pragma unroll
-      for (int e = 0; e < 4; ++e) off[e] = x86::radd(off[e], Wk.ny[e]);
-    }
-    const uint32_t nck = nck_of(Q);
-    float4* out = reinterpret_cast<float4*>(P.ck + (size_t)kCkFloats * (P.ckBase[qq] + r * nck));
-    const uint32_t lastCk = ::max((uint32_t)Q.minX, (uint32_t)(Q.maxX - 1) & ~7u);
-    for (uint32_t bx = Q.minX;; ++bx) {
-      if (bx == Q.minX || (bx & 7u) == 0) {
-        out[0] = make_float4(off[0], off[1], off[2], off[3]);
-        out[1] = make_float4(depth[0], depth[1], depth[2], depth[3]);
-        out[2] = make_float4(depth[4], depth[5], depth[6], depth[7]);
-        out += 3;
-      }
-      if (bx == lastCk) break;
-#pragma unroll
-      for (int k = 0; k < 8; ++k) depth[k] = safe ? x86::radd(Q.Dx, depth[k]) : x86::xadd(Q.Dx, depth[k]);
-#pragma unroll
-      for (int e = 0; e < 4; ++e) off[e] = x86::radd(Q.nx[e], off[e]);
-    }
+    const QuadRaster Q = P.rec[own.x];
+    const QuadWalk Wk = P.walk[own.x];
+    if (Q.flags & kQuadSafe) walk_row<true>(P, Q, Wk, own.x, own.y);
+    else walk_row<false>(P, Q, Wk, own.x, own.y);
   }
 }
 
@@ -829,8 +889,9 @@ struct RasterSmem {
 // Fragment of quad Q at block (bx, by): packed depth rows with the coverage
 // mask applied.  Returns false if the reference would skip the block (convex
 // quad outside the offset range, or an empty mask).
-__device__ __forceinline__ bool make_fragment(const FrameParams& P, const QuadRaster& Q, uint32_t ckq,
-                                              uint32_t bx, uint32_t by, uint32_t tx0, uint32_t (&r)[10][4])
+template <bool kSafe>
+__device__ __forceinline__ bool make_fragment_t(const FrameParams& P, const QuadRaster& Q, uint32_t ckq,
+                                                uint32_t bx, uint32_t by, uint32_t tx0, uint32_t (&r)[10][4])
 {
   const uint32_t cx = ::max((uint32_t)Q.minX, tx0);
   const uint32_t kk = (cx >> 3) - ((uint32_t)Q.minX >> 3);
@@ -839,10 +900,9 @@ __device__ __forceinline__ bool make_fragment(const FrameParams& P, const QuadRa
   const float4 o = __ldg(ck), d0 = __ldg(ck + 1), d1 = __ldg(ck + 2);
   float off[4] = {o.x, o.y, o.z, o.w};
   float depth[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
-  const bool safe = (Q.flags & kQuadSafe) != 0;
   for (uint32_t i = cx; i < bx; ++i) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) depth[k] = safe ? x86::radd(Q.Dx, depth[k]) : x86::xadd(Q.Dx, depth[k]);
+    for (int k = 0; k < 8; ++k) depth[k] = zadd<kSafe>(Q.Dx, depth[k]);
 #pragma unroll
     for (int e = 0; e < 4; ++e) off[e] = x86::radd(Q.nx[e], off[e]);
   }
@@ -881,9 +941,9 @@ __device__ __forceinline__ bool make_fragment(const FrameParams& P, const QuadRa
   float d1v[8], d8[8], d9[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    d1v[k] = safe ? x86::rfma(Dx, 0.5f, depth[k]) : x86::xfmadd(Dx, 0.5f, depth[k]);
-    d8[k] = safe ? x86::radd(Dy, depth[k]) : x86::xadd(Dy, depth[k]);
-    d9[k] = safe ? x86::radd(Dy, d1v[k]) : x86::xadd(Dy, d1v[k]);
+    d1v[k] = zfma<kSafe>(Dx, 0.5f, depth[k]);
+    d8[k] = zadd<kSafe>(Dy, depth[k]);
+    d9[k] = zadd<kSafe>(Dy, d1v[k]);
   }
   r[0][0] = pack2(depth[0], depth[1]); r[0][1] = pack2(depth[2], depth[3]);
   r[0][2] = pack2(d1v[0], d1v[1]);     r[0][3] = pack2(d1v[2], d1v[3]);
@@ -915,6 +975,36 @@ __device__ __forceinline__ bool make_fragment(const FrameParams& P, const QuadRa
     }
   }
   return true;
+}
+
+// Computes the fragment and, if the reference would draw it, stores its 8
+// rows of 4 packed words at dst (a fragment slot in shared memory).
+template <bool kSafe>
+__device__ __forceinline__ bool fragment_to(const FrameParams& P, const QuadRaster& Q, uint32_t ckq, uint32_t bx,
+                                            uint32_t by, uint32_t tx0, uint32_t* dst)
+{
+  uint32_t r[10][4];
+  if (!make_fragment_t<kSafe>(P, Q, ckq, bx, by, tx0, r)) return false;
+#pragma unroll
+  for (int y = 0; y < 8; ++y)
+#pragma unroll
+    for (int w = 0; w < 4; ++w) dst[4 * y + w] = r[y][w];
+  return true;
+}
+
+// Quads whose depth may overflow are rare: their copy stays out of line so
+// that the common path keeps its registers.
+static __device__ __noinline__ bool fragment_to_unsafe(const FrameParams& P, const QuadRaster& Q, uint32_t ckq,
+                                                       uint32_t bx, uint32_t by, uint32_t tx0, uint32_t* dst)
+{
+  return fragment_to<false>(P, Q, ckq, bx, by, tx0, dst);
+}
+
+__device__ __forceinline__ bool make_fragment(const FrameParams& P, const QuadRaster& Q, uint32_t ckq, uint32_t bx,
+                                              uint32_t by, uint32_t tx0, uint32_t* dst)
+{
+  if (Q.flags & kQuadSafe) return fragment_to<true>(P, Q, ckq, bx, by, tx0, dst);
+  return fragment_to_unsafe(P, Q, ckq, bx, by, tx0, dst);
 }
 
 // Merges fragment slot `slot` into this thread's pixel row of its block: the
@@ -1020,13 +1110,7 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
       // so a block with hiZ >= maxZ now still has it when this fragment's
       // turn comes, unless hiZ == 1 and maxZ == 1.
       const bool skip = ownerHiz >= Q.maxZ && !(ownerHiz == 1 && Q.maxZ == 1);
-      uint32_t r[10][4];
-      if (!skip && make_fragment(P, Q, ckq, bx, by, tx0, r)) {
-        uint32_t* dst = S.frag + tid * kFragStride;
-#pragma unroll
-        for (int y = 0; y < 8; ++y)
-#pragma unroll
-          for (int w = 0; w < 4; ++w) dst[4 * y + w] = r[y][w];
+      if (!skip && make_fragment(P, Q, ckq, bx, by, tx0, S.frag + tid * kFragStride)) {
         meta = ((uint32_t)Q.maxZ << 16) | 32u | target;
         if (kWins) S.fcmd[tid] = P.walk[q].pad[0];
         atomicOr(&S.bmask[target][tid >> 5], 1u << lane);
@@ -1087,7 +1171,7 @@ __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
     const uint32_t bx = tx0 + (lane & 7), by = ty0 + (lane >> 3);
     const bool inView = bx < V.blocksX && by < V.blocksY;
     const uint32_t blk = inView ? by * V.blocksX + bx : 0;
-    const bool clearing = (V.flags & kViewClear) != 0;
+    const bool clearing = (V.flags & kViewClear) != 0 && P.phase == 0;
     if (clearing) {
       if (inView) V.hiz[blk] = 1;
       if (lt == 0 && lane < 8) V.hiz[V.blocksX * V.blocksY + lane] = 1;  // padding entries
@@ -1143,7 +1227,7 @@ __device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S,
   const uint32_t bx = tx0 + (myBlock & 7), by = ty0 + (myBlock >> 3);
   const bool inView = bx < V.blocksX && by < V.blocksY;
   const uint32_t blk = inView ? by * V.blocksX + bx : 0;
-  const bool clearing = (V.flags & kViewClear) != 0;
+  const bool clearing = (V.flags & kViewClear) != 0 && P.phase == 0;
   uint32_t hiz = clearing ? 1u : (inView ? (uint32_t)V.hiz[blk] : 0xFFFFu);
   bool have = false;
   uint32_t row[4] = {0, 0, 0, 0};
@@ -1218,6 +1302,17 @@ __device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S,
       const uint32_t key = inView ? own[x] : 0u;
       const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
       if (key && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&P.wins[key - 1], (uint32_t)__popc(peers));
+    }
+    if (V.owner && inView) {
+      uint32_t* o = V.owner + (size_t)blk * 64 + 8 * py;
+      if (P.phase == 0) {
+        reinterpret_cast<uint4*>(o)[0] = make_uint4(own[0], own[1], own[2], own[3]);
+        reinterpret_cast<uint4*>(o)[1] = make_uint4(own[4], own[5], own[6], own[7]);
+      } else {
+#pragma unroll
+        for (int x = 0; x < 8; ++x)
+          if (own[x]) o[x] = own[x];  // pixels the second pass changed
+      }
     }
   }
   // per-tile minimum hiZ for the queries
@@ -1384,7 +1479,8 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
         e = cudaMemsetAsync(P.mat, 0, (size_t)P.matSize * sizeof(uint32_t), stream);  // inactive chunks count 0
         if (e != cudaSuccess) return e;
       }
-      k_gate<<<(P.numCmds + 255) / 256, 256, 0, stream>>>(P);
+      if (P.phase) k_gate_second<<<(P.numCmds + 7) / 8, 256, 0, stream>>>(P);
+      else k_gate<<<(P.numCmds + 255) / 256, 256, 0, stream>>>(P);
       k_chunk_gate<<<(P.numChunks + 255) / 256, 256, 0, stream>>>(P);
       k_setup<<<::min(P.numChunks, g_setupBlocks), kChunk, (size_t)maxStPerView * sizeof(uint32_t), stream>>>(P);
     }
@@ -1466,6 +1562,44 @@ cudaError_t set_kernel_attributes()
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster<true>, kRasterThreads, 0) == cudaSuccess && nb > 0)
     g_rasterBlocks = (uint32_t)(nb * sms);
   return cudaSuccess;
+}
+
+// ---- cull labels ---------------------------------------------------------------------------
+// One thread per query slot, after k_query: a box with a screen rectangle that
+// the frame culls (an occlusion cull) credits the owners of a 4x4 grid of
+// sample pixels in its rectangle, one count each (training labels of the
+// occluder selector: how many culled boxes an occluder's pixels hide).
+
+__global__ void __launch_bounds__(256) k_cull_labels(FrameParams P)
+{
+  const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= P.numQuerySlots) return;
+  uint32_t lo = 0, hi = P.numViews - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (P.views[mid].queryStart <= slot) lo = mid; else hi = mid - 1;
+  }
+  const ViewDesc& V = P.views[lo];
+  if (!V.owner || slot - V.queryStart >= V.queryCount) return;
+  if ((P.visBits[slot >> 5] >> (slot & 31)) & 1u) return;  // visible
+  const float4 a = P.qmin[slot], b = P.qmax[slot];
+  const float bmin[4] = {a.x, a.y, a.z, a.w}, bmax[4] = {b.x, b.y, b.z, b.w};
+  uint32_t rect[4], maxZ = 0;
+  if (query_front(V, bmin, bmax, rect, &maxZ) != 2) return;  // outside the frustum: not an occlusion cull
+  for (uint32_t j = 0; j < 4; ++j) {
+    const uint32_t y = rect[2] + (uint32_t)(((uint64_t)(rect[3] - rect[2]) * (2 * j + 1)) / 8);
+    for (uint32_t i = 0; i < 4; ++i) {
+      const uint32_t x = rect[0] + (uint32_t)(((uint64_t)(rect[1] - rect[0]) * (2 * i + 1)) / 8);
+      const uint32_t o = V.owner[(size_t)((y >> 3) * V.blocksX + (x >> 3)) * 64 + 8 * (y & 7) + (x & 7)];
+      if (o) atomicAdd(&P.cullCount[o - 1], 1u);
+    }
+  }
+}
+
+cudaError_t launch_cull_labels(const FrameParams& P, cudaStream_t stream)
+{
+  if (P.numQuerySlots) k_cull_labels<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
+  return cudaGetLastError();
 }
 
 // ---- queries without device allocation -------------------------------------------------

@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(256) k_features(FrameParams P, uint32_t numCmd
   f[11] = 0.0f;  // k_view_norm
   f[12] = 0.0f;
   f[13] = log2f(1.0f + (float)prev) / lwh;
-  f[14] = (P.cmdDraw[c] & 1u) ? 1.0f : 0.0f;  // written by the previous launch's k_setup
+  f[14] = (P.cmdDraw[c] & 5u) ? 1.0f : 0.0f;  // drawn by either pass of the previous launch (k_gate)
   f[15] = 1.0f;
   P.cand[c] = cand ? 1 : 0;
 }
@@ -369,19 +369,52 @@ __global__ void __launch_bounds__(256) k_topk(FrameParams P)
 
 // ---- training: backward and Adam ---------------------------------------------------------------
 
-// Per row: ds = 2 (s - t) / B, dh2 = ds w3 (h2 > 0), dh1 = (dh2 W2) (h1 > 0).
+// Listwise loss, one warp per group of rows (one view in one frame): the
+// scores' softmax over the group against the target distribution t of the
+// group; loss = -sum_groups sum_i t_i log p_i / G, ds_i = (p_i - t_i) / G.
+// err2 receives each row's loss term scaled by B / G, so that the common
+// reduction (sum / B) yields the loss.
+__global__ void __launch_bounds__(256) k_listwise_ds(const float* __restrict__ score, const float* __restrict__ target,
+                                                     const uint32_t* __restrict__ groupStart, uint32_t G, uint32_t B,
+                                                     float* ds, float* err2)
+{
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t g = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (g >= G) return;
+  const uint32_t a = groupStart[g], b = groupStart[g + 1];
+  float mx = -3.0e38f;
+  for (uint32_t i = a + lane; i < b; i += 32) mx = fmaxf(mx, score[i]);
+  for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+  float z = 0.0f;
+  for (uint32_t i = a + lane; i < b; i += 32) z += expf(score[i] - mx);
+  for (int o = 16; o; o >>= 1) z += __shfl_xor_sync(0xFFFFFFFFu, z, o);
+  const float lz = logf(z), invG = 1.0f / (float)G;
+  for (uint32_t i = a + lane; i < b; i += 32) {
+    const float lp = score[i] - mx - lz;
+    ds[i] = (expf(lp) - target[i]) * invG;
+    err2[i] = -target[i] * lp * ((float)B * invG);
+  }
+}
+
+// Per row: ds = 2 (s - t) / B (mean squared error; with haveDs, ds is given),
+// dh2 = ds w3 (h2 > 0), dh1 = (dh2 W2) (h1 > 0).
 __global__ void __launch_bounds__(128) k_mlp_backward_rows(const float* __restrict__ score,
                                                            const float* __restrict__ target, uint32_t B,
                                                            const MlpDevice* __restrict__ mlp,
                                                            const float* __restrict__ h1, const float* __restrict__ h2,
-                                                           float* ds, float* dh1, float* dh2, float* err2)
+                                                           float* ds, float* dh1, float* dh2, float* err2, bool haveDs)
 {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= B) return;
-  const float e = score[r] - target[r];
-  const float d = 2.0f * e / (float)B;
-  ds[r] = d;
-  err2[r] = e * e;
+  float d;
+  if (haveDs) {
+    d = ds[r];
+  } else {
+    const float e = score[r] - target[r];
+    d = 2.0f * e / (float)B;
+    ds[r] = d;
+    err2[r] = e * e;
+  }
   float g2[kHidden];
 #pragma unroll 8
   for (int n = 0; n < kHidden; ++n) {
@@ -502,9 +535,12 @@ uint32_t mlp_grad_blocks(uint32_t B) { return ::min(64u, (B + 63) / 64); }
 
 cudaError_t launch_mlp_backward(const float* score, const float* target, uint32_t B, const MlpDevice* mlp,
                                 const float* xb, const float* h1, const float* h2, float* ds, float* dh1, float* dh2,
-                                float* err2, float* partial, float* grad, cudaStream_t stream)
+                                float* err2, float* partial, float* grad, cudaStream_t stream,
+                                const uint32_t* groupStart, uint32_t groups)
 {
-  k_mlp_backward_rows<<<(B + 127) / 128, 128, 0, stream>>>(score, target, B, mlp, h1, h2, ds, dh1, dh2, err2);
+  if (groupStart) k_listwise_ds<<<(groups + 7) / 8, 256, 0, stream>>>(score, target, groupStart, groups, B, ds, err2);
+  k_mlp_backward_rows<<<(B + 127) / 128, 128, 0, stream>>>(score, target, B, mlp, h1, h2, ds, dh1, dh2, err2,
+                                                           groupStart != nullptr);
   const uint32_t nb = mlp_grad_blocks(B), rows = (B + nb - 1) / nb;
   const dim3 grid((kParams + 1 + 127) / 128, nb);
   k_mlp_grad_partial<<<grid, 128, 0, stream>>>(B, rows, xb, h1, h2, ds, dh1, dh2, err2, partial);

@@ -57,6 +57,8 @@ struct ViewDesc {
   uint32_t matBase;                     // count matrix base: stX*stY*chunkCount entries
   uint32_t queryStart, queryCount;      // query slots; queryStart is a multiple of 32
   uint32_t flags;
+  uint32_t* owner;   // optional, width*height (depth layout): command + 1 that produced each
+                     // pixel's final value this launch, 0 if none (cull labels of the selector)
 };
 
 struct Cmd {
@@ -135,6 +137,8 @@ struct FrameParams {
   uint32_t numViews;
   uint32_t numCmds;
   uint32_t matSize;      // entries of `mat` over all views
+  uint32_t phase;        // 0: the frame (or the top-K pass); 1: the second pass of a
+                         // selection (no clear; draws the remaining candidates still visible)
   const Cmd* cmds;
   const Chunk* chunks;
   uint32_t numChunks;
@@ -160,7 +164,8 @@ struct FrameParams {
   const float4* qmax;
   uint32_t* visBits;     // one bit per query slot
   uint32_t* ncBits;
-  uint32_t* cmdDraw;     // per command: bit0 drawn, bit1 near-clipped (gated result)
+  uint32_t* cmdDraw;     // per command: bit0 drawn (this pass), bit1 near-clipped, bit2 drawn by
+                         // the first pass of this launch (second pass only)
   uint32_t* activeChunkList;  // chunks with a drawn command (header->activeChunks of them)
   uint2* activeTileList;      // {warp-tile, view} with a non-empty super-tile list (header->activeTiles)
   // learned occluder selection and win counts (all optional)
@@ -172,6 +177,7 @@ struct FrameParams {
                          // previous frame's wins by the feature kernel, then reset)
   const MlpDevice* mlp;
   float selectFrac;      // fraction of each view's candidates kept
+  uint32_t* cullCount;   // per command: samples of occlusion-culled boxes it owns (labels; optional)
 };
 
 }  // namespace occ

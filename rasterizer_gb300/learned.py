@@ -77,23 +77,27 @@ def _launch(b: api.PreparedBatch, tracks, f: int) -> None:
 
 
 def collect_labels(ctx, occluders, tracks: list[Track], group: int = 64, selector=None,
-                   fraction: float = 0.2) -> dict:
+                   fraction: float = 0.2, mins=None, maxs=None) -> dict:
     """Runs the tracks with every occluder drawn and win counting on.  For
     every candidate occluder of every frame: features (N, 16), wins (N,),
-    the view's pixel count, and a group id per (view, frame).  With a
+    the view's pixel count, and a group id per (view, frame); with query
+    boxes (`mins`, `maxs`, each track's range), also its cull credits (N,):
+    samples of the boxes culled by depth whose pixels it owns.  With a
     `selector`, the features come from the same tracks run under that
     selector at `fraction` (its own previous-frame wins and draw flags, as
     it will see them), the wins from the full frames.  Tracks of a group of
     `group` views must have equal frame counts."""
-    X, wins, wh, gid = [], [], [], []
+    X, wins, wh, gid, culls = [], [], [], [], []
     g = 0
     for g0 in range(0, len(tracks), group):
         ts = tracks[g0:g0 + group]
         frames = len(ts[0].mvps)
         assert all(len(t.mvps) == frames for t in ts)
-        views = _views(ctx, occluders, ts)
+        views = _views(ctx, occluders, ts, mins, maxs)
         b = api.PreparedBatch(ctx, views)
         b.setSelection(None, trackWins=True)
+        if mins is not None:
+            b.setCullLabels(True)
         batches = [b]
         if selector is not None:
             sviews = _views(ctx, occluders, ts)
@@ -111,6 +115,8 @@ def collect_labels(ctx, occluders, tracks: list[Track], group: int = 64, selecto
                 n = int(c.sum())
                 X.append(feats[c])
                 wins.append(s["wins"][c])
+                if mins is not None:
+                    culls.append(b.cullLabels(i)[c])
                 wh.append(np.full(n, t.width * t.height, np.int64))
                 gid.append(np.full(n, g, np.int64))
                 g += 1
@@ -118,7 +124,10 @@ def collect_labels(ctx, occluders, tracks: list[Track], group: int = 64, selecto
             x.close()
         for v in views:
             v["raster"].close()
-    return dict(X=np.concatenate(X), wins=np.concatenate(wins), wh=np.concatenate(wh), group=np.concatenate(gid))
+    out = dict(X=np.concatenate(X), wins=np.concatenate(wins), wh=np.concatenate(wh), group=np.concatenate(gid))
+    if mins is not None:
+        out["culls"] = np.concatenate(culls)
+    return out
 
 
 def concat_labels(parts: list[dict]) -> dict:
@@ -132,13 +141,18 @@ def concat_labels(parts: list[dict]) -> dict:
 
 
 def targets(labels: dict, kind: str = "log_view") -> np.ndarray:
-    """Regression targets from pixel wins.  "log_view": log2(1 + wins) /
+    """Regression targets.  "culls": log2(1 + cull credits) / 21; "mix": the
+    mean of "culls" and "log_view"; "log_view": log2(1 + wins) /
     log2(1 + pixels of the view); "log_max": log2(1 + wins) / log2(1 + the
     largest wins of the same view and frame); "rank": the occluder's rank among
     the candidates of its view and frame, 1 for the most wins, 0 for none."""
     w = labels["wins"].astype(np.float64)
     if kind == "log_view":
         return (np.log2(1.0 + w) / np.log2(1.0 + labels["wh"])).astype(np.float32)
+    if kind == "culls":  # cull credits: 16 samples per culled box, up to 100k boxes per view
+        return (np.log2(1.0 + labels["culls"].astype(np.float64)) / 21.0).astype(np.float32)
+    if kind == "mix":
+        return (0.5 * targets(labels, "log_view") + 0.5 * targets(labels, "culls")).astype(np.float32)
     g = labels["group"]
     ng = int(g.max()) + 1 if len(g) else 0
     if kind == "log_max":
@@ -189,6 +203,62 @@ def train(selector: api.OccluderSelector, X: np.ndarray, y: np.ndarray, steps: i
             xb[m, 14] = 0.0
         step_lr = lr * (0.5 * (1.0 + math.cos(math.pi * it / steps)) * 0.9 + 0.1)
         losses.append(selector.trainStep(xb, y[idx], lr=step_lr))
+        if log_every and (it + 1) % log_every == 0:
+            print(f"  step {it + 1}: loss {np.mean(losses[-log_every:]):.5f}", flush=True)
+    return np.asarray(losses)
+
+
+def group_distribution(labels: dict, key: str = "culls") -> np.ndarray:
+    """Per row, its share of the group's total `key` (cull credits by
+    default); groups with no credit at all fall back to pixel wins."""
+    g = labels["group"]
+    ng = int(g.max()) + 1 if len(g) else 0
+    out = np.zeros(len(g))
+    for k in (key, "wins"):
+        v = labels[k].astype(np.float64)
+        tot = np.zeros(ng)
+        np.add.at(tot, g, v)
+        use = (out == 0) & (tot[g] > 0)
+        if k != key:
+            have = np.zeros(ng, bool)
+            np.logical_or.at(have, g, out > 0)
+            use &= ~have[g]
+        out[use] = v[use] / tot[g][use]
+    return out.astype(np.float32)
+
+
+def train_listwise(selector: api.OccluderSelector, labels: dict, dist: np.ndarray, source: np.ndarray,
+                   steps: int = 6000, groups_per_step: int = 256, lr: float = 2e-3, seed: int = 0,
+                   drop_prev: float = 0.3, log_every: int = 0):
+    """Adam on the listwise loss: each step takes `groups_per_step` (view,
+    frame) groups, half from street rows and half from multi-view rows
+    (`source` 0/1 per row), and fits the softmax of each group's scores to the
+    group's target distribution `dist`.  Returns the loss history."""
+    rng = np.random.default_rng(seed)
+    g = labels["group"]
+    ng = int(g.max()) + 1
+    starts = np.searchsorted(g, np.arange(ng + 1))
+    sizes = starts[1:] - starts[:-1]
+    gsrc = source[starts[:-1]]
+    tot = np.zeros(ng)
+    np.add.at(tot, g, dist)
+    ok = (sizes > 1) & (tot > 0)
+    pools = [np.nonzero(ok & (gsrc == k))[0] for k in (0, 1)]
+    pools = [p for p in pools if len(p)]
+    X = labels["X"]
+    losses = []
+    for it in range(steps):
+        per = groups_per_step // len(pools)
+        gs = np.concatenate([p[rng.integers(0, len(p), per)] for p in pools])
+        idx = np.concatenate([np.arange(starts[k], starts[k + 1]) for k in gs])
+        gstart = np.concatenate([[0], np.cumsum(sizes[gs])]).astype(np.uint32)
+        xb = X[idx].copy()
+        if drop_prev > 0:
+            m = rng.random(len(idx)) < drop_prev
+            xb[m, 13] = 0.0
+            xb[m, 14] = 0.0
+        step_lr = lr * (0.5 * (1.0 + math.cos(math.pi * it / steps)) * 0.9 + 0.1)
+        losses.append(selector.trainStepListwise(xb, dist[idx], gstart, lr=step_lr))
         if log_every and (it + 1) % log_every == 0:
             print(f"  step {it + 1}: loss {np.mean(losses[-log_every:]):.5f}", flush=True)
     return np.asarray(losses)
@@ -275,13 +345,16 @@ def _quads(occluders, ids):
 
 
 def evaluate_learned(ctx, occluders, tracks, mins, maxs, selector, fraction: float, full,
-                     use_prev: bool = True) -> CullStats:
+                     use_prev: bool = True, second_pass: bool = False) -> CullStats:
     """The selector's frames (top `fraction` of each view's candidates, the
     previous-frame wins of the selected frames feeding the next unless
-    `use_prev` is off) against `full`."""
+    `use_prev` is off; with `second_pass`, plus the other candidates still
+    visible after the top-K pass) against `full`."""
     views = _views(ctx, occluders, tracks, mins, maxs)
     b = api.PreparedBatch(ctx, views)
     b.setSelection(selector, fraction, trackWins=use_prev)
+    if second_pass:
+        b.setSecondPass(True)
     b.setZeroDepth(True)
     st = CullStats()
     qs = [_quads(occluders, t.occluders) for t in tracks]
@@ -387,11 +460,13 @@ class Recipe:
     multiview_seeds: tuple = (101, 102, 103, 104, 105, 106, 107, 108)
     multiview_frames: int = 8
     rounds: tuple = ((0.15, 20, 120, (201, 202, 203, 204)), (0.3, 20, 120, (301, 302, 303, 304)))
-    steps0: int = 8000
-    steps: int = 10000
-    batch: int = 4096
+    steps0: int = 6000
+    steps: int = 6000
+    batch: int = 4096          # rows per step (mean squared error)
+    groups_per_step: int = 256  # (view, frame) groups per step (listwise)
     lr: float = 2e-3
-    target: str = "log_view"
+    objective: str = "listwise"  # or "mse" on `target`
+    target: str = "culls"        # listwise: distribution of cull credits; mse: a `targets` kind
     seed: int = 0
 
     def poses(self) -> int:
@@ -402,53 +477,64 @@ class Recipe:
 
 
 def _recipe_data(ctx, occluders, centers, quads, n_query_pool, street_paths, street_frames, seed0, mseeds, mframes,
-                 selector=None, fraction=0.2):
+                 selector=None, fraction=0.2, mins=None, maxs=None):
+    nq = n_query_pool if mins is not None else 0
     parts = [collect_labels(ctx, occluders, street_tracks(street_paths, street_frames, seed0,
-                                                          n_occluders=len(occluders)),
-                            group=40, selector=selector, fraction=fraction)]
+                                                          n_occluders=len(occluders), queries=nq),
+                            group=40, selector=selector, fraction=fraction, mins=mins, maxs=maxs)]
     n_street = len(parts[0]["wins"])
     for sd in mseeds:
         parts.append(collect_labels(ctx, occluders, multiview_tracks(centers, quads, n_query_pool, mframes, sd),
-                                    group=64, selector=selector, fraction=fraction))
+                                    group=64, selector=selector, fraction=fraction, mins=mins, maxs=maxs))
     lab = concat_labels(parts)
     src = np.zeros(len(lab["wins"]), np.int8)
     src[n_street:] = 1
     return lab, src
 
 
-def train_selector(ctx, occluders, n_query_pool: int = 100_000, recipe: Recipe | None = None, log=print):
+def train_selector(ctx, occluders, n_query_pool: int = 100_000, recipe: Recipe | None = None, log=print,
+                   mins=None, maxs=None):
     """Trains a selector for the city scene's occluders end to end on the GPU:
     labels from the rasteriser, forward/backward/Adam on the device.  Street
-    rows and multi-view rows are sampled half and half.  Returns (selector,
-    report)."""
+    and multi-view data are sampled half and half.  With the query pool
+    (`mins`, `maxs`) the labels are cull credits, else pixel wins.  The
+    default objective is listwise: per view and frame, the softmax of the
+    scores is fitted to the distribution of the labels, which is what a top-K
+    choice needs.  Returns (selector, report)."""
     rc = recipe or Recipe()
     centers = np.stack([o.center for o in occluders])
     quads = np.array([o.quads for o in occluders])
     t = Timer()
     lab, src = _recipe_data(ctx, occluders, centers, quads, n_query_pool, rc.street_paths, rc.street_frames, 1000,
-                            rc.multiview_seeds, rc.multiview_frames)
+                            rc.multiview_seeds, rc.multiview_frames, mins=mins, maxs=maxs)
     labs, srcs = [lab], [src]
     report = dict(poses=rc.poses(), label_seconds=t.lap())
 
     def weights(s):
         return np.where(s == 0, 0.5 / max(int((s == 0).sum()), 1), 0.5 / max(int((s == 1).sum()), 1))
 
+    def fit(net, lab, src, steps, seed, drop):
+        if rc.objective == "listwise":
+            dist = group_distribution(lab, rc.target if rc.target in lab else "wins")
+            return train_listwise(net, lab, dist, src, steps=steps, groups_per_step=rc.groups_per_step, lr=rc.lr,
+                                  seed=seed, drop_prev=drop)
+        return train(net, lab["X"], targets(lab, rc.target), steps=steps, batch=rc.batch, lr=rc.lr, seed=seed,
+                     drop_prev=drop, weights=weights(src))
+
     net = api.OccluderSelector(ctx, seed=rc.seed)
-    losses = train(net, lab["X"], targets(lab, rc.target), steps=rc.steps0, batch=rc.batch, lr=rc.lr,
-                   seed=rc.seed, drop_prev=0.3, weights=weights(src))
+    losses = fit(net, lab, src, rc.steps0, rc.seed, 0.3)
     report["rounds"] = [dict(rows=int(len(lab["wins"])), final_loss=float(losses[-200:].mean()),
                              train_seconds=t.lap())]
     for k, (frac, sp, sf, ms) in enumerate(rc.rounds):
         lab, src = _recipe_data(ctx, occluders, centers, quads, n_query_pool, sp, sf, 2000 + 1000 * k, ms,
-                                rc.multiview_frames, selector=net, fraction=frac)
+                                rc.multiview_frames, selector=net, fraction=frac, mins=mins, maxs=maxs)
         labs.append(lab)
         srcs.append(src)
         allab = concat_labels(labs)
         alsrc = np.concatenate(srcs)
         label_s = t.lap()
         nxt = api.OccluderSelector(ctx, seed=rc.seed + k + 1)
-        losses = train(nxt, allab["X"], targets(allab, rc.target), steps=rc.steps, batch=rc.batch, lr=rc.lr,
-                       seed=rc.seed + k + 1, drop_prev=0.15, weights=weights(alsrc))
+        losses = fit(nxt, allab, alsrc, rc.steps, rc.seed + k + 1, 0.15)
         net.close()
         net = nxt
         report["rounds"].append(dict(rows=int(len(allab["wins"])), on_policy_fraction=frac, label_seconds=label_s,

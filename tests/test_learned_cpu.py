@@ -56,3 +56,33 @@ def test_reference_gradient_matches_finite_differences():
             assert abs((fp - fm) / (2 * h) - g[i]) < 2e-3 * max(1.0, abs(g[i])), i
     finally:
         ref.bf16 = saved
+
+
+def test_group_distribution_and_listwise_reference():
+    lab = dict(wins=np.array([0, 5, 10, 0, 3, 3, 100, 4, 4]), culls=np.array([0, 2, 2, 0, 0, 0, 0, 0, 0]),
+               wh=np.full(9, 100), group=np.array([0, 0, 0, 1, 1, 1, 1, 2, 2]))
+    d = L.group_distribution(lab)
+    assert np.allclose(d[:3], [0, 0.5, 0.5]) and np.allclose(d[3:7], np.array([0, 3, 3, 100]) / 106)
+    assert np.allclose(d[7:], [0.5, 0.5])
+    # listwise reference gradient against central differences (bf16 roundings off)
+    rng = np.random.default_rng(1)
+    p = rng.normal(0, 0.3, ref.PARAMS).astype(np.float32)
+    x = rng.uniform(0, 1, (30, 16)).astype(np.float32)
+    gs = np.array([0, 7, 19, 30])
+    t = rng.uniform(0, 1, 30)
+    for a, b in zip(gs[:-1], gs[1:]):
+        t[a:b] /= t[a:b].sum()
+    saved = ref.bf16
+    ref.bf16 = lambda a: np.asarray(a, np.float32)
+    try:
+        _, g = ref.listwise_gradients(p, x, t, gs)
+        for i in rng.choice(ref.PARAMS, 20, replace=False):
+            h = 1e-3
+            pp, pm = p.astype(np.float64).copy(), p.astype(np.float64).copy()
+            pp[i] += h
+            pm[i] -= h
+            fp, _ = ref.listwise_gradients(pp.astype(np.float32), x, t, gs)
+            fm, _ = ref.listwise_gradients(pm.astype(np.float32), x, t, gs)
+            assert abs((fp - fm) / (2 * h) - g[i]) < 2e-3 * max(1.0, abs(g[i])), i
+    finally:
+        ref.bf16 = saved
