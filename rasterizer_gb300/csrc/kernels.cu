@@ -1052,33 +1052,20 @@ __device__ __forceinline__ void merge_slot(const ViewDesc& V, const RasterSmem& 
   hiz = ::min(mn & 0xFFFFu, mn >> 16);
 }
 
-// Runs the buffered local list: fragments in order, kRasterThreads at a time.
-// With kWins, own[x] tracks the command (+1) that produced pixel x's value.
+// Runs the buffered local list (n quads, F fragments): fragments in order,
+// kRasterThreads at a time.  With kWins, own[x] tracks the command (+1) that
+// produced pixel x's value.
 template <bool kWins>
 __device__ __forceinline__ void raster_local_list(const FrameParams& P, const ViewDesc& V, RasterSmem& S, uint32_t n,
-                                                  uint32_t tx0, uint32_t ty0, uint32_t tid, uint32_t blk, bool inView,
-                                                  uint32_t (&row)[4], uint32_t& hiz, bool& have, uint32_t (&own)[8])
+                                                  uint32_t F, uint32_t tx0, uint32_t ty0, uint32_t tid, uint32_t blk,
+                                                  bool inView, uint32_t (&row)[4], uint32_t& hiz, bool& have,
+                                                  uint32_t (&own)[8])
 {
   const uint32_t lane = tid & 31;
   const uint32_t py = tid & 7;  // pixel row owned by this thread
   const uint32_t myBlock = tid >> 3;
   const uint32_t groupMask = 0xFFu << (lane & ~7u);
-  // exclusive prefix of fragment counts over the local list
-  uint32_t carry = 0;
-  for (uint32_t i0 = 0; i0 < n; i0 += kRasterThreads) {
-    const uint32_t i = i0 + tid;
-    uint32_t c = 0;
-    if (i < n) {
-      const uint32_t rc = S.lrect[i];
-      c = ((rc >> 5) & 15u) * ((rc >> 9) & 7u);
-    }
-    uint32_t tot;
-    const uint32_t ex = block_exclusive_scan<kRasterThreads>(c, tot, S.scan);
-    if (i < n) S.loff[i] = carry + ex;
-    carry += tot;
-  }
-  const uint32_t F = carry;
-  __syncthreads();
+  // S.loff holds each local quad's first fragment, F the fragment count
   for (uint32_t f0 = 0; f0 < F; f0 += kRasterThreads) {
     (&S.bmask[0][0])[tid] = 0;  // 32 blocks x (kRasterThreads / 32) words == kRasterThreads
     const uint32_t f = f0 + tid;
@@ -1237,16 +1224,17 @@ __device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S,
   const uint4* list = P.stList + (V.cmdCount ? P.stStart[s] : 0);
   if (py == 0) S.hiz[myBlock] = hiz;
   __syncthreads();
-  uint32_t n = 0;
-  // kScanPerRound list entries per round (two per thread), appended to the
-  // local list in list order unless already hidden in every block they touch
+  uint32_t n = 0, F = 0;
+  // kScanPerRound list entries per round (two consecutive ones per thread),
+  // appended to the local list in list order unless already hidden in every
+  // block they touch; one scan of (fragments << 16 | quads) places both
   for (uint32_t base = 0; base < listLen; base += kScanPerRound) {
     uint4 e[2];
     bool ov[2];
     uint32_t rect[2];
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-      const uint32_t idx = base + kRasterThreads * k + tid;
+      const uint32_t idx = base + 2 * tid + k;
       e[k] = idx < listLen ? __ldg(list + idx) : make_uint4(0, 0, 0, 0);
     }
 #pragma unroll
@@ -1273,20 +1261,29 @@ __device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S,
       ov[k] = o;
       rect[k] = (x0 - tx0) | ((y0 - ty0) << 3) | ((x1 - x0) << 5) | ((y1 - y0) << 9);
     }
+    uint32_t fr[2];
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      uint32_t tot;
-      const uint32_t pos = n + block_exclusive_scan<kRasterThreads>(ov[k] ? 1u : 0u, tot, S.scan);
+    for (int k = 0; k < 2; ++k) fr[k] = ov[k] ? ((rect[k] >> 5) & 15u) * ((rect[k] >> 9) & 7u) : 0u;
+    const uint32_t cnt = (ov[0] ? 1u : 0u) + (ov[1] ? 1u : 0u);
+    uint32_t tot;  // per round at most 512 quads and 16,384 fragments: the halves do not carry
+    const uint32_t ex = block_exclusive_scan<kRasterThreads>(cnt | ((fr[0] + fr[1]) << 16), tot, S.scan);
+    uint32_t pos = n + (ex & 0xFFFFu), fpos = F + (ex >> 16);
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
       if (ov[k]) {
         S.lq[pos] = e[k].x;
         S.lrect[pos] = rect[k];
+        S.loff[pos] = fpos;
+        ++pos;
+        fpos += fr[k];
       }
-      n += tot;
-    }
+    n += tot & 0xFFFFu;
+    F += tot >> 16;
     __syncthreads();
     if (n > (uint32_t)(kLocalCap - kScanPerRound) || (base + kScanPerRound >= listLen && n > 0)) {
-      raster_local_list<kWins>(P, V, S, n, tx0, ty0, tid, blk, inView, row, hiz, have, own);
+      raster_local_list<kWins>(P, V, S, n, F, tx0, ty0, tid, blk, inView, row, hiz, have, own);
       n = 0;
+      F = 0;
     }
   }
   if (inView) {
