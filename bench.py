@@ -376,6 +376,7 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
         move(i)
         sel.launch()
     ok = sel.check() and ok
+    tuning = sel.autotune(5)  # launch shapes for this batch, picked before the timed region
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     sampler = ClockSampler(dev.index) if rank == 0 else None
@@ -416,7 +417,7 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
         "at_k": sweep.get(str(k_st)), "views_per_launch": LEARNED_VIEWS,
         "batched_plain_views_per_s": LEARNED_VIEWS / (ms_plain * 1e-3),
         "batched_learned_views_per_s": world * LEARNED_VIEWS * args.steps / (dev_ms * 1e-3),
-        "kernels_ms_per_launch": kern, "work_last_launch": stats, "capacity_ok": bool(ok)}
+        "kernels_ms_per_launch": kern, "work_last_launch": stats, "autotune": tuning, "capacity_ok": bool(ok)}
     headline = {
         "value": world * LEARNED_VIEWS * args.steps / (dev_ms * 1e-3), "ms_per_step": dev_ms / args.steps,
         "clocks": clocks, "kernels": kern,
@@ -441,6 +442,9 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
     plain.close()
     sel = api.PreparedBatch(ctx, views)
     sel.setSelection(net, k_mv, trackWins=True)
+    sel.launch()
+    sel.check()
+    tuning_mv = sel.autotune(3)
     ms_sel = _time_launches(ctx, stream, sel.launch, 20, mover(sel, test, 4))
     ok = sel.check() and ok
     kern_mv = dict(zip(["setup", "scan", "fill", "walk", "raster", "query", "selection"],
@@ -452,6 +456,7 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
                             "batched_plain_views_per_s": len(test) / (ms_plain * 1e-3),
                             "batched_learned_views_per_s": len(test) / (ms_sel * 1e-3),
                             "batched_learned_ms_per_launch": ms_sel, "kernels_ms_per_launch": kern_mv,
+                            "autotune": tuning_mv,
                             "capacity_ok": bool(ok)}
     out["seconds"] = t.lap() + out["training"]["seconds"]
     net.close()

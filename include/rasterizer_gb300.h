@@ -187,6 +187,13 @@ int occ_batch_set_selection(occ_batch b, occ_mlp mlp, float fraction, int trackW
  * on the frames before it; zeroed depth makes each frame stand alone (used to
  * compare a selected subset against the full frame).  No reference counterpart. */
 int occ_batch_set_zero_depth(occ_batch b, int enable);
+/* Autotuner: times the batch's frame stage by stage (occ_batch_profile) over
+ * launch shapes -- resident CTAs per SM of the persistent setup, list-fill and
+ * raster kernels, row-walk CTAs per SM, tiles per raster queue fetch -- and
+ * keeps, per stage, the fastest; the graph is captured again with them.
+ * tuned[5] = {setup, fill, walk, raster CTAs per SM, tiles per fetch};
+ * msBefore/msAfter[7] as occ_batch_profile (either may be NULL). */
+int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[5], float msBefore[7], float msAfter[7]);
 /* Work counts of the last launch (syncs): block rows walked, row-walk
  * checkpoints, super-tile list entries, chunks with a drawn occluder, warp-tiles
  * rasterised (the others only cleared), the batch's chunk count, and the

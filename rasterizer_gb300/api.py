@@ -419,6 +419,22 @@ class PreparedBatch:
                                             int(bool(trackWins))), "occ_batch_set_selection")
         self._selector = mlp  # the captured launch reads the network's weights
 
+    def autotune(self, iterations: int = 5) -> dict:
+        """Picks the launch shapes of the persistent kernels by timing the
+        batch's own frame stage by stage; returns the choice and the stage
+        times before and after."""
+        tuned = np.zeros(5, np.uint32)
+        before = np.zeros(7, np.float32)
+        after = np.zeros(7, np.float32)
+        check(lib().occ_batch_autotune(self.handle, iterations, _ptr(tuned), _ptr(before), _ptr(after)),
+              "occ_batch_autotune")
+        keys = ("setup_ctas_per_sm", "fill_ctas_per_sm", "walk_ctas_per_sm", "raster_ctas_per_sm",
+                "raster_tiles_per_fetch")
+        names = ("setup", "scan", "fill", "walk", "raster", "query", "selection")
+        return {"tuned": {k: int(v) for k, v in zip(keys, tuned)},
+                "ms_before": {k: float(v) for k, v in zip(names, before)},
+                "ms_after": {k: float(v) for k, v in zip(names, after)}}
+
     def stats(self) -> dict:
         """Work counts of the last launch."""
         out = np.zeros(7, np.uint32)

@@ -35,6 +35,7 @@ cudaError_t launch_mlp_backward(const float* score, const float* target, uint32_
 uint32_t mlp_grad_blocks(uint32_t B);
 cudaError_t launch_mlp_publish(const float* params, MlpDevice* mlp, cudaStream_t stream);
 cudaError_t launch_cull_labels(const FrameParams& P, cudaStream_t stream);
+void tuning_limits(uint32_t out[4]);
 cudaError_t launch_adam(float* params, const float* grad, float* m, float* v, float lr, uint32_t step,
                         cudaStream_t stream);
 int mlp_param_count();
@@ -917,6 +918,7 @@ struct occ_batch_s {
   bool zeroDepth = false;  // zero every view's depth at the start of each launch
   bool secondPass = false; // after the top-K pass, draw the other candidates still visible
   bool cullLabels = false; // per-pixel owners and per-command cull counts (training labels)
+  LaunchTuning tune{};     // launch shapes (occ_batch_autotune)
   DevBuf<uint32_t> cullCount;
   DevBuf<float> feat, score;
   DevBuf<uint8_t> cand, select;
@@ -1007,6 +1009,7 @@ int capture(occ_batch_s* b)
       P.selectFrac = b->selectFrac;
     }
   }
+  P.tune = b->tune;
   const bool labels = b->cullLabels && b->features && b->trackWins;
   if (labels) P.cullCount = b->cullCount.p;
   b->params = P;
@@ -1280,6 +1283,64 @@ int occ_batch_stats(occ_batch b, uint32_t out[7])
   out[4] = H.activeTiles;
   out[5] = (uint32_t)b->L.chunks.size();
   out[6] = (uint32_t)b->tablesBytes;  // host->device bytes per launch (view, command and chunk tables)
+  return OCC_OK;
+}
+
+// Mean per-stage milliseconds of `iterations` frames with launch shape `t`.
+static int profile_with(occ_batch b, const LaunchTuning& t, uint32_t iterations, float ms[7])
+{
+  const LaunchTuning saved = b->params.tune;
+  b->params.tune = t;
+  const int st = occ_batch_profile(b, iterations, ms);
+  b->params.tune = saved;
+  return st;
+}
+
+int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[5], float msBefore[7], float msAfter[7])
+{
+  if (!b || !iterations) return fail(OCC_ERR_INVALID_ARG, "bad argument");
+  uint32_t lim[4];
+  tuning_limits(lim);
+  LaunchTuning best = b->tune;
+  float ms[7], base[7];
+  OCC_CHECK(profile_with(b, best, iterations, base));
+  if (msBefore) std::memcpy(msBefore, base, sizeof(base));
+  // each parameter moves one stage's time only: search them one at a time
+  auto search = [&](uint32_t LaunchTuning::*field, int stage, std::vector<uint32_t> cands) -> int {
+    float bestMs = 3.0e38f;
+    uint32_t bestV = best.*field;
+    for (uint32_t v : cands) {
+      LaunchTuning t = best;
+      t.*field = v;
+      OCC_CHECK(profile_with(b, t, iterations, ms));
+      if (ms[stage] < bestMs) {
+        bestMs = ms[stage];
+        bestV = v;
+      }
+    }
+    best.*field = bestV;
+    return OCC_OK;
+  };
+  auto upTo = [](uint32_t n) {
+    std::vector<uint32_t> v;
+    for (uint32_t i = 1; i <= n; ++i) v.push_back(i);
+    return v;
+  };
+  OCC_CHECK(search(&LaunchTuning::setupPerSm, 0, upTo(lim[0])));
+  OCC_CHECK(search(&LaunchTuning::fillPerSm, 2, upTo(lim[1])));
+  OCC_CHECK(search(&LaunchTuning::walkPerSm, 3, {2, 4, 8, 16}));
+  OCC_CHECK(search(&LaunchTuning::rasterPerSm, 4, upTo(lim[2])));
+  OCC_CHECK(search(&LaunchTuning::rasterChunk, 4, {1, 2, 4, 8, 16}));
+  b->tune = best;
+  OCC_CHECK(capture(b));
+  if (msAfter) OCC_CHECK(occ_batch_profile(b, iterations, msAfter));
+  if (tuned) {
+    tuned[0] = best.setupPerSm;
+    tuned[1] = best.fillPerSm;
+    tuned[2] = best.walkPerSm;
+    tuned[3] = best.rasterPerSm;
+    tuned[4] = best.rasterChunk;
+  }
   return OCC_OK;
 }
 

@@ -48,9 +48,14 @@ __device__ const unsigned long long kDevCoverage[4096] = {OCC_COVERAGE_TABLE_VAL
 static uint32_t g_walkBlocks = 152 * 8;
 // Persistent grids of the setup / list-fill / raster kernels (resident CTAs x SMs),
 // looping over the launch's active chunks and tiles.
-static uint32_t g_setupBlocks = 152 * 4;
-static uint32_t g_fillBlocks = 152 * 4;
-static uint32_t g_rasterBlocks = 152 * 2;
+static uint32_t g_sms = 152;
+static uint32_t g_setupPerSm = 4, g_fillPerSm = 4, g_rasterPerSm = 4;  // occupancy limits
+
+static uint32_t grid_of(uint32_t tuned, uint32_t limit, uint32_t work)
+{
+  const uint32_t perSm = tuned ? ::min(tuned, limit) : limit;
+  return ::max(1u, ::min(work, perSm * g_sms));
+}
 
 // Primitive mode for the 8-bit configuration (area signs | W signs << 4),
 // the classification of Rasterizer.cpp:30-64.
@@ -1333,16 +1338,21 @@ __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) k_raster(Fra
   __shared__ uint32_t s_next;
   if (P.header->overflow) return;
   const uint32_t nActive = P.header->activeTiles;
-  if (threadIdx.x == 0) s_next = atomicAdd(&P.header->tileCursor, 1u);
+  const uint32_t chunk = P.tune.rasterChunk ? P.tune.rasterChunk : 1u;  // tiles per fetch
+  if (threadIdx.x == 0) s_next = atomicAdd(&P.header->tileCursor, chunk);
   __syncthreads();
   uint32_t i = s_next;
   while (i < nActive) {
-    const uint2 t = P.activeTileList[i];
     uint32_t nxt = 0;
-    if (threadIdx.x == 0) nxt = atomicAdd(&P.header->tileCursor, 1u);  // next tile, fetched ahead
-    raster_tile<kWins>(P, S, t.x, t.y);
+    if (threadIdx.x == 0) nxt = atomicAdd(&P.header->tileCursor, chunk);  // next fetch, ahead of time
+    const uint32_t end = ::min(i + chunk, nActive);
+    for (uint32_t j = i; j < end; ++j) {
+      const uint2 t = P.activeTileList[j];
+      raster_tile<kWins>(P, S, t.x, t.y);
+      __syncthreads();  // shared state is reused by the next tile
+    }
     if (threadIdx.x == 0) s_next = nxt;
-    __syncthreads();  // shared state is reused by the next tile
+    __syncthreads();
     i = s_next;
   }
 }
@@ -1479,20 +1489,22 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
       if (P.phase) k_gate_second<<<(P.numCmds + 7) / 8, 256, 0, stream>>>(P);
       else k_gate<<<(P.numCmds + 255) / 256, 256, 0, stream>>>(P);
       k_chunk_gate<<<(P.numChunks + 255) / 256, 256, 0, stream>>>(P);
-      k_setup<<<::min(P.numChunks, g_setupBlocks), kChunk, (size_t)maxStPerView * sizeof(uint32_t), stream>>>(P);
+      k_setup<<<grid_of(P.tune.setupPerSm, g_setupPerSm, P.numChunks), kChunk,
+                (size_t)maxStPerView * sizeof(uint32_t), stream>>>(P);
     }
   }
   mark(1);
   if (doRaster) k_scan<<<numSt + P.numViews, 256, 0, stream>>>(P, numSt);
   mark(2);
   if (doRaster && P.numChunks)
-    k_fill<<<::min(P.numChunks, g_fillBlocks), kChunk, (size_t)maxStPerView * 64, stream>>>(P);
+    k_fill<<<grid_of(P.tune.fillPerSm, g_fillPerSm, P.numChunks), kChunk, (size_t)maxStPerView * 64, stream>>>(P);
   mark(3);
-  if (doRaster && P.numChunks) k_walk<<<g_walkBlocks, 256, 0, stream>>>(P);
+  if (doRaster && P.numChunks)
+    k_walk<<<P.tune.walkPerSm ? P.tune.walkPerSm * g_sms : g_walkBlocks, 256, 0, stream>>>(P);
   mark(4);
   if (doRaster && P.numTiles) {
     k_tile_prep<<<(P.numTiles + 7) / 8, 256, 0, stream>>>(P);
-    const uint32_t grid = ::min(P.numTiles, g_rasterBlocks);
+    const uint32_t grid = grid_of(P.tune.rasterPerSm, g_rasterPerSm, P.numTiles);
     if (P.wins) k_raster<true><<<grid, kRasterThreads, 0, stream>>>(P);
     else k_raster<false><<<grid, kRasterThreads, 0, stream>>>(P);
   }
@@ -1545,6 +1557,7 @@ cudaError_t set_kernel_attributes()
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+  g_sms = (uint32_t)sms;
   g_walkBlocks = (uint32_t)sms * 8;
   cudaError_t e = cudaFuncSetAttribute(k_setup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 4));
   if (e != cudaSuccess) return e;
@@ -1553,12 +1566,21 @@ cudaError_t set_kernel_attributes()
   // persistent grids: resident CTAs per SM at the largest dynamic shared memory used
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_setup, kChunk, kMaxStPerView * 4) == cudaSuccess && nb > 0)
-    g_setupBlocks = (uint32_t)(nb * sms);
+    g_setupPerSm = (uint32_t)nb;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fill, kChunk, kMaxStPerView * 16) == cudaSuccess && nb > 0)
-    g_fillBlocks = (uint32_t)(nb * sms);
+    g_fillPerSm = (uint32_t)nb;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster<true>, kRasterThreads, 0) == cudaSuccess && nb > 0)
-    g_rasterBlocks = (uint32_t)(nb * sms);
+    g_rasterPerSm = (uint32_t)nb;
   return cudaSuccess;
+}
+
+// Occupancy limits (resident CTAs per SM) of the persistent kernels, and the SM count.
+void tuning_limits(uint32_t out[4])
+{
+  out[0] = g_setupPerSm;
+  out[1] = g_fillPerSm;
+  out[2] = g_rasterPerSm;
+  out[3] = g_sms;
 }
 
 // ---- cull labels ---------------------------------------------------------------------------

@@ -132,11 +132,19 @@ struct FrameHeader {
   uint32_t pad2;
 };
 
+// Launch shape of one flush (0 = the default: as many resident CTAs per SM
+// as the kernel's registers and shared memory allow; one tile per fetch).
+// Chosen per batch by occ_batch_autotune.
+struct LaunchTuning {
+  uint32_t setupPerSm, fillPerSm, walkPerSm, rasterPerSm, rasterChunk, pad[3];
+};
+
 struct FrameParams {
   const ViewDesc* views;
   uint32_t numViews;
   uint32_t numCmds;
   uint32_t matSize;      // entries of `mat` over all views
+  LaunchTuning tune;
   uint32_t phase;        // 0: the frame (or the top-K pass); 1: the second pass of a
                          // selection (no clear; draws the remaining candidates still visible)
   const Cmd* cmds;

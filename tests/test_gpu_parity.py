@@ -243,3 +243,30 @@ def test_multiview_workload_subset(ctx):
         _compare(v["raster"], orc, ("depth", "hiz"))
         assert np.array_equal(vis.astype(np.uint8), ovis), s.kind
         assert np.array_equal(nc.astype(np.uint8), onc), s.kind
+
+
+def test_autotuned_launch_shapes_keep_results(ctx):
+    """Launch shapes picked by the autotuner (CTAs per SM, tiles per fetch)
+    change timing only: the batch still reproduces the oracle."""
+    occ = city_occluders()
+    scene = to_baked(occ)
+    w, h = 960, 544
+    mvps, _ = scenes.camera_path(30, seed=29, width=w, height_px=h)
+    mins, maxs = scenes.query_boxes(20000, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    r = api.Rasterizer(ctx, w, h)
+    b = api.PreparedBatch(ctx, [dict(raster=r, mvp=mvps[0], clear=True, occluders=occ,
+                                     flags=np.full(len(occ), 2, np.uint8), mins=mins, maxs=maxs)])
+    rep = b.autotune(2)
+    assert all(v >= 1 for v in rep["tuned"].values())
+    orc = Oracle(w, h)
+    orc.frame_plain(scene, mvps[0])  # the preparing frame
+    for f in (5, 17):
+        b.setModelViewProjection(0, mvps[f])
+        b.launch()
+        assert b.check()
+        orc.frame_plain(scene, mvps[f])
+        vis, _ = b.results(0)
+        ovis, _ = orc.query(mins, maxs)
+        assert np.array_equal(vis.astype(np.uint8), ovis)
+        _compare(r, orc, ("depth", "hiz"))
+    b.close()
