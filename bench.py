@@ -458,9 +458,74 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
                             "batched_learned_ms_per_launch": ms_sel, "kernels_ms_per_launch": kern_mv,
                             "autotune": tuning_mv,
                             "capacity_ok": bool(ok)}
+    if not args.no_large:
+        out["large_4k_plus_63"] = run_large(ctx, net, dev)
     out["seconds"] = t.lap() + out["training"]["seconds"]
     net.close()
     return out, headline
+
+
+LARGE_NQ = 1_000_000
+
+
+def run_large(ctx, net, dev):
+    """The large combined workload: a seeded 2M-triangle city (128x128
+    buildings), one 3840x2160 main view plus 63 mixed-resolution views in one
+    launch, 1M query boxes; K chosen for >= 99 % of the occlusion culls on a
+    validation variant; culls kept against the plain all-occluder frames, and
+    views/s and queries/s of the plain and the learned launch (autotuned)."""
+    import torch
+    from rasterizer_gb300 import api, learned as L, scenes
+    t = L.Timer()
+    mesh = scenes.city_scene(grid=128, target_tris=2_000_000)
+    occ = api.bake_scene(mesh.vertices, mesh.indices)
+    bake_s = t.lap()
+    centers = np.stack([o.center for o in occ])
+    quads = np.array([o.quads for o in occ])
+    pmin, pmax = scenes.query_boxes(LARGE_NQ, seed=45, footprint=600.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    val = L.large_tracks(centers, quads, LARGE_NQ, frames=2, seed=6)
+    fval = L.run_full(ctx, occ, val, pmin, pmax)
+    k = 1.0
+    for f in (0.05, 0.1, 0.2, 0.35, 0.5):
+        if L.evaluate_learned(ctx, occ, val, pmin, pmax, net, f, fval).retained >= 0.99:
+            k = f
+            break
+    test = L.large_tracks(centers, quads, LARGE_NQ, frames=2, seed=5)
+    full = L.run_full(ctx, occ, test, pmin, pmax)
+    a = L.evaluate_learned(ctx, occ, test, pmin, pmax, net, k, full)
+    b = L.evaluate_heuristic(ctx, occ, test, pmin, pmax, "nearest", k, full)
+    views = L._views(ctx, occ, test, pmin, pmax)
+    nq = sum(tr.query_count for tr in test)
+
+    def mover(bt):
+        def before(i):
+            for v, tr in enumerate(test):
+                bt.setModelViewProjection(v, tr.mvps[i % 2])
+        return before
+
+    out = {}
+    for name, frac in (("plain", None), ("learned", k)):
+        bt = api.PreparedBatch(ctx, views)
+        if frac is not None:
+            bt.setSelection(net, frac, trackWins=True)
+        bt.launch()
+        bt.check()
+        tuned = bt.autotune(3)["tuned"]
+        ms = _time_launches(ctx, stream, bt.launch, 20, mover(bt))
+        ok = bt.check()
+        out[name] = {"ms_per_launch": ms, "views_per_s": len(test) / (ms * 1e-3),
+                     "queries_per_s": nq / (ms * 1e-3), "autotune": tuned, "capacity_ok": bool(ok)}
+        bt.close()
+    for v in views:
+        v["raster"].close()
+    return {"workload": f"2M-triangle city ({mesh.triangles} tris -> {int(quads.sum())} quads in {len(occ)} "
+                        f"occluders), one 3840x2160 main view + 63 mixed views per launch, {nq} query boxes "
+                        f"per launch ({LARGE_NQ} pool)",
+            "bake_seconds": bake_s, "k_fraction": k, "learned": a.as_dict(), "nearest_first": b.as_dict(),
+            "plain": out["plain"], "batched_learned": out["learned"],
+            "speedup_vs_plain_batched": out["learned"]["views_per_s"] / out["plain"]["views_per_s"],
+            "seconds": t.lap() + bake_s}
 
 
 def _barrier(world):
@@ -701,6 +766,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-view batched leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-selection leg (training included)")
+    ap.add_argument("--no-large", action="store_true", help="skip the 2M-triangle 4K + 63-view leg")
     ap.add_argument("--profile-learned", type=int, default=0, metavar="FRAMES",
                     help="only launch the batched + learned frame FRAMES times (for ncu); prints a status line")
     ap.add_argument("--profile-views", type=int, default=LEARNED_VIEWS, help="views per launch for --profile-learned")

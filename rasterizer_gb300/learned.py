@@ -450,6 +450,16 @@ def multiview_tracks(centers, quads, n_query_pool: int, frames: int, seed: int, 
                   s.query_start, s.query_count, s.kind) for j, s in enumerate(specs)]
 
 
+def large_tracks(centers, quads, n_query_pool: int, frames: int, seed: int, grid: int = 128, speed: float = 0.6):
+    """The large combined workload as tracks: the 3840x2160 main view (every
+    occluder, the whole query pool) first, then its 63 auxiliary views drifting."""
+    from . import scenes
+    mvps, aux = scenes.large_workload(centers, quads, n_query_pool, seed=seed, frames=frames, grid=grid)
+    main = Track(3840, 2160, np.arange(len(centers)), mvps, 0, n_query_pool, "main")
+    return [main] + [Track(s.width, s.height, s.occluders, scenes.view_track(s, frames, seed * 1000 + j, speed),
+                           s.query_start, s.query_count, s.kind) for j, s in enumerate(aux)]
+
+
 @dataclass
 class Recipe:
     """Training set-up: seeded street paths and multi-view workloads

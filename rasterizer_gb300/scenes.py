@@ -352,3 +352,16 @@ def multiview_workload(centers: np.ndarray, quads: np.ndarray, n_query_pool: int
         s, n = queries()
         views.append(ViewSpec("probe", w, h, mvp, eye, _pick_occluders(centers, tris, eye, budget), s, n, cam))
     return views
+
+
+def large_workload(centers: np.ndarray, quads: np.ndarray, n_query_pool: int, seed: int = 5, frames: int = 1,
+                   grid: int = 128, cell: float = 16.0):
+    """The large combined workload over a grid x grid city: a 3840x2160
+    street-level main view (a seeded camera path, `frames` frames) drawing
+    every occluder and querying the whole pool, plus 63 auxiliary views of
+    mixed resolution (16 cascades 1024x1024, 24 cube faces 512x512, 23 probe
+    views) as in `multiview_workload`.  Returns (main mvps (frames, 16),
+    auxiliary ViewSpecs)."""
+    mvps, _ = camera_path(frames, seed=seed, grid=grid, cell=cell, width=3840, height_px=2160)
+    aux = multiview_workload(centers, quads, n_query_pool, seed=seed, grid=grid, cell=cell, counts=(16, 24, 23))
+    return mvps, aux

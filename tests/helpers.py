@@ -34,6 +34,12 @@ def city_occluders(grid: int = 64, target: int = 260_000):
     return api.bake_scene(m.vertices, m.indices)
 
 
+@functools.lru_cache(maxsize=None)
+def large_city_occluders():
+    """The 2M-triangle city (128 x 128 buildings)."""
+    return city_occluders(grid=128, target=2_000_000)
+
+
 def canonical_depth(depth: np.ndarray, hiz: np.ndarray, blocks: int) -> np.ndarray:
     """Depth with cleared blocks (hiZ == 1) read as 0, as readBackDepth does."""
     d = depth.reshape(blocks, 64).copy()

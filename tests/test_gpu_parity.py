@@ -270,3 +270,25 @@ def test_autotuned_launch_shapes_keep_results(ctx):
         assert np.array_equal(vis.astype(np.uint8), ovis)
         _compare(r, orc, ("depth", "hiz"))
     b.close()
+
+
+def test_large_city_4k_main_view(ctx):
+    """The 2M-triangle city's 3840x2160 main view (129,600 blocks, full 32-bit
+    block index) with every occluder gated, and 200k boxes, against the oracle."""
+    from helpers import large_city_occluders
+    occ = large_city_occluders()
+    scene = to_baked(occ)
+    mvps, _ = scenes.camera_path(3, seed=5, grid=128, width=3840, height_px=2160)
+    mins, maxs = scenes.query_boxes(200_000, seed=45, footprint=600.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    r = api.Rasterizer(ctx, 3840, 2160)
+    orc = Oracle(3840, 2160)
+    orc.set_block_index_wrap(False)
+    for f in (0, 2):
+        flags = gpu_plain_frame(r, occ, mvps[f])
+        oflags = orc.frame_plain(scene, mvps[f])
+        assert np.array_equal(flags, oflags)
+        _compare(r, orc, ("depth", "hiz"))
+        vis, nc = r.queryVisibilityBatch(mins, maxs)
+        ovis, onc = orc.query(mins, maxs)
+        assert np.array_equal(vis.astype(np.uint8), ovis) and np.array_equal(nc.astype(np.uint8), onc)
+        assert (flags & 1).sum() > 100
