@@ -14,7 +14,8 @@ namespace occ {
 // ExactOps applies the x86 NaN rules to every result.  FastOps uses plain IEEE
 // operations and only records whether any result was NaN: without a NaN the
 // two are bit-identical, so callers run FastOps and fall back to ExactOps for
-// the rare inputs that produce one.
+// the rare inputs that produce one.  LazyOps (below) records NaN only where
+// the caller asks.
 
 struct ExactOps {
   __device__ __forceinline__ float add(float a, float b) { return x86::xadd(a, b); }
@@ -26,6 +27,31 @@ struct ExactOps {
   __device__ __forceinline__ float fnmadd(float a, float b, float c) { return x86::xfnmadd(a, b, c); }
   __device__ __forceinline__ float round(float a) { return x86::round_even(a); }
   __device__ __forceinline__ float floor(float a) { return x86::floor_(a); }
+  __device__ __forceinline__ float dp4(const float* a, const float* b)
+  {
+    return add(add(mul(a[0], b[0]), mul(a[1], b[1])), add(mul(a[2], b[2]), mul(a[3], b[3])));
+  }
+  __device__ __forceinline__ float chk(float r) { return r; }
+};
+
+// Plain IEEE operations without per-result checks; the caller checks with
+// chk() every value that reaches an operation which does not propagate NaN
+// (comparisons, min/max, sign and bit extraction, the reciprocal table).  Any
+// NaN produced earlier reaches one of those through IEEE add/multiply/fma,
+// which propagate NaN, so a clean flag still means no NaN anywhere.
+struct LazyOps {
+  bool nan = false;
+  __device__ __forceinline__ float chk(float r)
+  {
+    nan |= r != r;
+    return r;
+  }
+  __device__ __forceinline__ float add(float a, float b) { return x86::radd(a, b); }
+  __device__ __forceinline__ float sub(float a, float b) { return x86::rsub(a, b); }
+  __device__ __forceinline__ float mul(float a, float b) { return x86::rmul(a, b); }
+  __device__ __forceinline__ float div(float a, float b) { return x86::rdiv(a, b); }
+  __device__ __forceinline__ float fmadd(float a, float b, float c) { return x86::rfma(a, b, c); }
+  __device__ __forceinline__ float floor(float a) { return floorf(a); }
   __device__ __forceinline__ float dp4(const float* a, const float* b)
   {
     return add(add(mul(a[0], b[0]), mul(a[1], b[1])), add(mul(a[2], b[2]), mul(a[3], b[3])));
@@ -80,7 +106,7 @@ __device__ __forceinline__ int query_front_t(Ops& o, const ViewDesc& V, const fl
       plane[i] = (p & 1) ? o.sub(row3[i], rr[i]) : o.add(row3[i], rr[i]);
       offs[i] = o.add(ctr[i], fxor(ext[i], sign(plane[i])));
     }
-    signs |= fu(o.dp4(plane, offs));
+    signs |= fu(o.chk(o.dp4(plane, offs)));  // the box's values and the planes all reach this sum
   }
   if (signs & 0x80000000u) return 0;
 
@@ -107,16 +133,16 @@ __device__ __forceinline__ int query_front_t(Ops& o, const ViewDesc& V, const fl
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     float eps = o.mul(me[i], 0.001f);
-    close |= (c[i][3] < eps) || (c[4 + i][3] < eps);
+    close |= (o.chk(c[i][3]) < eps) || (o.chk(c[4 + i][3]) < eps);
   }
   if (close) return 1;
   float X[8], Y[8], Z[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     float iw = rcp(c[k][3]);
-    X[k] = o.mul(c[k][0], iw);
-    Y[k] = o.mul(c[k][1], iw);
-    Z[k] = o.mul(c[k][2], iw);
+    X[k] = o.chk(o.mul(c[k][0], iw));
+    Y[k] = o.chk(o.mul(c[k][1], iw));
+    Z[k] = o.chk(o.mul(c[k][2], iw));
   }
   float mnX[4], mxX[4], mnY[4], mxY[4];
 #pragma unroll
@@ -170,7 +196,7 @@ static __device__ __noinline__ int query_front_exact(const ViewDesc& V, const fl
 __device__ __forceinline__ int query_front(const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect,
                                            uint32_t* maxZOut, uint32_t* minZOut = nullptr)
 {
-  FastOps f;
+  LazyOps f;
   const int st = query_front_t(f, V, bmin, bmax, rect, maxZOut, minZOut);
   if (!f.nan) return st;
   return query_front_exact(V, bmin, bmax, rect, maxZOut, minZOut);

@@ -63,3 +63,21 @@ def mismatch_report(name, a, b) -> str:
         return ""
     i = bad[0]
     return f"{name}: {bad.size} mismatches, first at {i}: gpu {a[i]} oracle {b[i]}"
+
+
+def special_boxes(n: int, seed: int, footprint: float = 100.0, nan: bool = True):
+    """n query boxes, about half of them with one or two coordinates replaced
+    by NaN (unless `nan` is off), infinities, huge, tiny or signed-zero values
+    (and a few with w != 1): the x86 NaN and overflow rules of queryVisibility."""
+    rng = np.random.default_rng(seed)
+    mins, maxs = scenes.query_boxes(n, seed=seed, footprint=footprint)
+    special = [np.inf, -np.inf, 1e30, -1e30, 3.4e38, -3.4e38, 1e-40, -0.0, 0.0, 2.0] + ([np.nan] if nan else [])
+    special = np.array(special, np.float32)
+    for i in range(n):
+        if rng.random() < 0.5:
+            for _ in range(int(rng.integers(1, 3))):
+                which = mins if rng.random() < 0.5 else maxs
+                which[i, int(rng.integers(0, 3))] = special[int(rng.integers(0, len(special)))]
+        if rng.random() < 0.03:
+            (mins if rng.random() < 0.5 else maxs)[i, 3] = special[int(rng.integers(0, len(special)))]
+    return mins, maxs

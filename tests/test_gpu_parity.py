@@ -292,3 +292,22 @@ def test_large_city_4k_main_view(ctx):
         ovis, onc = orc.query(mins, maxs)
         assert np.array_equal(vis.astype(np.uint8), ovis) and np.array_equal(nc.astype(np.uint8), onc)
         assert (flags & 1).sum() > 100
+
+
+def test_query_special_values(ctx):
+    """Boxes with NaN, infinite, huge, tiny and signed-zero coordinates: the
+    x86 NaN and overflow rules of queryVisibility, bit for bit."""
+    from helpers import special_boxes
+    occ = boxes_occluders()
+    scene = to_baked(occ)
+    mvp = scenes.view_projection((3.0, 2.0, -50.0), (0.0, -0.05, 1.0), aspect=640 / 360)
+    r = api.Rasterizer(ctx, 640, 360)
+    orc = Oracle(640, 360)
+    gpu_plain_frame(r, occ, mvp)
+    orc.frame_plain(scene, mvp)
+    mins, maxs = special_boxes(8192, seed=61)
+    vis, nc = r.queryVisibilityBatch(mins, maxs)
+    ovis, onc = orc.query(mins, maxs)
+    assert not mismatch_report("visible", vis.astype(np.uint8), ovis)
+    assert not mismatch_report("needsClipping", nc.astype(np.uint8), onc)
+    assert vis.sum() > 0 and (~vis).sum() > 0
