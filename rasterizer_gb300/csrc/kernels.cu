@@ -171,6 +171,7 @@ __device__ bool query2d_tile(const ViewDesc& V, uint32_t tx, uint32_t ty, uint32
   const uint32_t bx0 = minX >> 3, bx1 = maxX >> 3, by0 = minY >> 3, by1 = maxY >> 3;
   const uint32_t ya = ::max(by0, ty * kTileH), yb = ::min(by1, ty * kTileH + kTileH - 1);
   const uint32_t xa = ::max(bx0, tx * kTileW), xb = ::min(bx1, tx * kTileW + kTileW - 1);
+  const uint32_t mz2 = maxZ | (maxZ << 16);  // maxZ is a packed 16-bit depth
   for (uint32_t by = ya; by <= yb; ++by) {
     int32_t sy = (int32_t)(minY - 8 * by);
     sy = sy < 0 ? 0 : sy;
@@ -185,15 +186,18 @@ __device__ bool query2d_tile(const ViewDesc& V, uint32_t tx, uint32_t ty, uint32
       int32_t ex = (int32_t)(maxX - bx * 8);
       ex = ex > 7 ? 7 : ex;
       if (interiorLine && sx == 0 && ex == 7) return true;
+      // the reference's rowSelector as 16-bit lanes of the 4 row words
+      uint32_t cm[4];
+#pragma unroll
+      for (int w = 0; w < 4; ++w)
+        cm[w] = ((2 * w >= sx && 2 * w <= ex) ? 0x0000FFFFu : 0u) | ((2 * w + 1 >= sx && 2 * w + 1 <= ex) ? 0xFFFF0000u : 0u);
       const uint16_t* d = V.depth + (size_t)blk * 64;
       for (int32_t y = sy; y <= ey; ++y) {
         const uint4 row = *reinterpret_cast<const uint4*>(d + 8 * y);
-        const uint32_t w[4] = {row.x, row.y, row.z, row.w};
-#pragma unroll
-        for (int x = 0; x < 8; ++x) {
-          const uint32_t v = (w[x >> 1] >> ((x & 1) * 16)) & 0xFFFFu;
-          if (x >= sx && x <= ex && v < maxZ) return true;
-        }
+        // a pixel is visible where its depth < maxZ (Rasterizer.cpp:333-336)
+        if ((__vcmpltu2(row.x, mz2) & cm[0]) | (__vcmpltu2(row.y, mz2) & cm[1]) | (__vcmpltu2(row.z, mz2) & cm[2]) |
+            (__vcmpltu2(row.w, mz2) & cm[3]))
+          return true;
       }
     }
   }
@@ -677,14 +681,16 @@ __global__ void __launch_bounds__(256) k_scan(FrameParams P, uint32_t numSt)
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  uint32_t carry = 0;
-  for (uint32_t i0 = 0; i0 < numSt; i0 += 256) {
-    const uint32_t i = i0 + tid;
-    const uint32_t v = i < numSt ? __ldcg(&P.stLen[i]) : 0;
-    uint32_t tot;
-    const uint32_t ex = block_exclusive_scan<256>(v, tot, s_scan);
-    if (i < numSt) P.stStart[i] = carry + ex;
-    carry += tot;
+  // list starts: each thread sums a contiguous run of super-tiles, one block
+  // scan of the run totals, then each thread writes its run's prefixes
+  const uint32_t per = (numSt + 255) / 256, a0 = ::min(numSt, tid * per), a1 = ::min(numSt, a0 + per);
+  uint32_t run = 0;
+  for (uint32_t i = a0; i < a1; ++i) run += __ldcg(&P.stLen[i]);
+  uint32_t carry;
+  uint32_t pre = block_exclusive_scan<256>(run, carry, s_scan);
+  for (uint32_t i = a0; i < a1; ++i) {
+    P.stStart[i] = pre;
+    pre += __ldcg(&P.stLen[i]);
   }
   uint32_t carryR = 0, carryC = 0;
   for (uint32_t i0 = 0; i0 < P.numViews; i0 += 256) {
@@ -1374,7 +1380,7 @@ __global__ void __launch_bounds__(128) k_tile_hiz(const uint16_t* hiz, uint16_t*
 
 // ---- k_query -------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(256) k_query(FrameParams P)
+__global__ void __launch_bounds__(256, 6) k_query(FrameParams P)
 {
   if (P.header->overflow) return;
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;

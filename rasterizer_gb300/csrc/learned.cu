@@ -309,9 +309,32 @@ __device__ __forceinline__ uint32_t block_count(bool p, uint32_t* sm)
   return total;
 }
 
+__device__ __forceinline__ uint32_t block_exclusive_scan256(uint32_t v, uint32_t& total, uint32_t* sm /* 8 */)
+{
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= (uint32_t)o) x += t;
+  }
+  if (lane == 31) sm[warp] = x;
+  __syncthreads();
+  uint32_t prefix = 0;
+  total = 0;
+  for (uint32_t w = 0; w < 8; ++w) {
+    if (w < warp) prefix += sm[w];
+    total += sm[w];
+  }
+  __syncthreads();
+  return prefix + x - v;
+}
+
 __global__ void __launch_bounds__(256) k_topk(FrameParams P)
 {
   __shared__ uint32_t s_red[8];
+  __shared__ uint32_t s_hist[256];
+  __shared__ uint32_t s_pick[2];
   const ViewDesc& V = P.views[blockIdx.x];
   const uint32_t c0 = V.cmdStart, n = V.cmdCount;
   uint32_t ncand = 0;
@@ -325,22 +348,37 @@ __global__ void __launch_bounds__(256) k_topk(FrameParams P)
   }
   uint32_t K = (uint32_t)ceilf(P.selectFrac * (float)ncand);
   K = K < 1 ? 1 : (K > ncand ? ncand : K);
-  // largest T with |{key >= T}| >= K, bit by bit from the top
-  uint32_t T = 0;
-  for (int bit = 31; bit >= 0; --bit) {
-    const uint32_t trial = T | (1u << bit);
-    uint32_t cnt = 0;
-    for (uint32_t i0 = 0; i0 < n; i0 += 256) {
-      const uint32_t i = i0 + threadIdx.x;
-      cnt += block_count(i < n && P.cand[c0 + i] && score_key(P.score[c0 + i]) >= trial, s_red);
+  // radix select, 8 bits at a time from the top: T = the K-th largest key
+  uint32_t T = 0, above = 0;  // keys > the current prefix range already counted
+  for (int shift = 24; shift >= 0; shift -= 8) {
+    s_hist[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t hiMask = shift == 24 ? 0u : (0xFFFFFFFFu << (shift + 8));
+    for (uint32_t i = threadIdx.x; i < n; i += 256)
+      if (P.cand[c0 + i]) {
+        const uint32_t key = score_key(P.score[c0 + i]);
+        if ((key & hiMask) == (T & hiMask)) atomicAdd(&s_hist[(key >> shift) & 255u], 1u);
+      }
+    __syncthreads();
+    // largest digit d with above + count(digits >= d) >= K: thread t holds
+    // digit 255 - t, an inclusive scan over t counts the digits >= it
+    if (threadIdx.x == 0) {
+      s_pick[0] = 0;
+      s_pick[1] = above;
     }
-    if (cnt >= K) T = trial;
+    const uint32_t v = s_hist[255 - threadIdx.x];
+    uint32_t tot;
+    const uint32_t incl = block_exclusive_scan256(v, tot, s_red) + v;
+    if (above + incl >= K && above + incl - v < K) {
+      s_pick[0] = 255 - threadIdx.x;
+      s_pick[1] = above + incl - v;  // keys above this digit (within the prefix) plus the earlier ones
+    }
+    __syncthreads();
+    T |= s_pick[0] << shift;
+    above = s_pick[1];
+    __syncthreads();
   }
-  uint32_t above = 0;
-  for (uint32_t i0 = 0; i0 < n; i0 += 256) {
-    const uint32_t i = i0 + threadIdx.x;
-    above += block_count(i < n && P.cand[c0 + i] && score_key(P.score[c0 + i]) > T, s_red);
-  }
+  // `above` keys are > T; the remaining K - above come from the ties at T, in command order
   uint32_t needEq = K - above, seenEq = 0;
   for (uint32_t i0 = 0; i0 < n; i0 += 256) {
     const uint32_t i = i0 + threadIdx.x;
