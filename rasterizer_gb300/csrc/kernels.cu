@@ -1304,12 +1304,22 @@ __device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S,
   if (kWins) {
     // a pixel is won by the command whose fragment set its final value (the
     // fast-clear overwrite or a strictly larger max-merge); one atomic per
-    // distinct command per warp and pixel column
+    // distinct command per warp (rows won by one command: the common case)
+    // or per warp and pixel column
+    bool same = true;
 #pragma unroll
-    for (int x = 0; x < 8; ++x) {
-      const uint32_t key = inView ? own[x] : 0u;
+    for (int x = 1; x < 8; ++x) same &= own[x] == own[0];
+    if (__all_sync(0xFFFFFFFFu, same)) {
+      const uint32_t key = inView ? own[0] : 0u;
       const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
-      if (key && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&P.wins[key - 1], (uint32_t)__popc(peers));
+      if (key && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&P.wins[key - 1], 8u * (uint32_t)__popc(peers));
+    } else {
+#pragma unroll
+      for (int x = 0; x < 8; ++x) {
+        const uint32_t key = inView ? own[x] : 0u;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+        if (key && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&P.wins[key - 1], (uint32_t)__popc(peers));
+      }
     }
     if (V.owner && inView) {
       uint32_t* o = V.owner + (size_t)blk * 64 + 8 * py;
