@@ -724,11 +724,13 @@ def run_profile_frames(frames: int, start: int = 0):
     ctx.close()
 
 
-def run_profile_learned(frames: int, views: int, train_steps: int):
+def run_profile_learned(frames: int, views: int, train_steps: int, extras: bool = False):
     """A short GPU-only run for profilers: the headline's batched + learned
     launch (first `views` street views, untrained selector at K = 10 %, the
     same kernels and the same number of drawn occluders per view), `frames`
-    graph launches, then `train_steps` training steps on random rows."""
+    graph launches, then `train_steps` listwise training steps on random rows.
+    With `extras`, the first launch also runs the second pass and the cull
+    labels (every kernel of the library then runs at least once)."""
     from rasterizer_gb300 import api, learned as L, scenes
     mesh = scenes.city_scene()
     occ = api.bake_scene(mesh.vertices, mesh.indices)
@@ -739,6 +741,12 @@ def run_profile_learned(frames: int, views: int, train_steps: int):
     vs = L._views(ctx, occ, paths, pmin, pmax)
     b = api.PreparedBatch(ctx, vs)
     b.setSelection(net, 0.1, trackWins=True)
+    if extras:
+        b.setSecondPass(True)
+        b.setCullLabels(True)
+        b.launch()
+        b.setSecondPass(False)
+        b.setCullLabels(False)
     for f in range(frames):
         for v, tr in enumerate(paths):
             b.setModelViewProjection(v, tr.mvps[f % 64])
@@ -747,8 +755,11 @@ def run_profile_learned(frames: int, views: int, train_steps: int):
     rng = np.random.default_rng(0)
     x = rng.uniform(0, 1, (4096, 16)).astype(np.float32)
     y = rng.uniform(0, 1, 4096).astype(np.float32)
+    gs = np.arange(0, 4097, 64, dtype=np.uint32)  # 64 groups of 64 rows
+    for a, b_ in zip(gs[:-1], gs[1:]):
+        y[a:b_] /= y[a:b_].sum()
     for _ in range(train_steps):
-        net.trainStep(x, y, 1e-3)
+        net.trainStepListwise(x, y, gs, 1e-3)
     print(json.dumps({"frames": frames, "views": views, "capacity_ok": ok, "stats": b.stats()}), flush=True)
     b.close()
     net.close()
@@ -771,11 +782,13 @@ def main():
                     help="only launch the batched + learned frame FRAMES times (for ncu); prints a status line")
     ap.add_argument("--profile-views", type=int, default=LEARNED_VIEWS, help="views per launch for --profile-learned")
     ap.add_argument("--profile-train", type=int, default=0, help="training steps after --profile-learned")
+    ap.add_argument("--profile-extras", action="store_true",
+                    help="--profile-learned: first launch with the second pass and the cull labels")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.profile_learned:
-        run_profile_learned(args.profile_learned, args.profile_views, args.profile_train)
+        run_profile_learned(args.profile_learned, args.profile_views, args.profile_train, args.profile_extras)
     elif args.profile_run:
         run_profile_frames(args.profile_run)
     elif args.impl == "reference":
