@@ -897,12 +897,31 @@ struct RasterSmem {
   uint32_t n;
 };
 
+// Row y of a fragment, masked by the coverage mask, into its slot.
+__device__ __forceinline__ void put_row(uint32_t* dst, int y, uint64_t mask, uint32_t w0, uint32_t w1, uint32_t w2,
+                                        uint32_t w3)
+{
+  if (mask != ~0ull) {
+    const int bitpos = (y & 1) ? (y >> 1) : 4 + (y >> 1);
+    const uint64_t bits = (mask >> bitpos) & 0x0101010101010101ull;
+    const uint32_t lo = (uint32_t)bits * 0xFFu, hi = (uint32_t)(bits >> 32) * 0xFFu;
+    w0 &= __byte_perm(lo, 0, 0x1100);
+    w1 &= __byte_perm(lo, 0, 0x3322);
+    w2 &= __byte_perm(hi, 0, 0x1100);
+    w3 &= __byte_perm(hi, 0, 0x3322);
+  }
+  dst[4 * y + 0] = w0;
+  dst[4 * y + 1] = w1;
+  dst[4 * y + 2] = w2;
+  dst[4 * y + 3] = w3;
+}
+
 // Fragment of quad Q at block (bx, by): packed depth rows with the coverage
-// mask applied.  Returns false if the reference would skip the block (convex
-// quad outside the offset range, or an empty mask).
+// mask applied, written to dst.  Returns false if the reference would skip
+// the block (convex quad outside the offset range, or an empty mask).
 template <bool kSafe>
 __device__ __forceinline__ bool make_fragment_t(const FrameParams& P, const QuadRaster& Q, uint32_t ckq,
-                                                uint32_t bx, uint32_t by, uint32_t tx0, uint32_t (&r)[10][4])
+                                                uint32_t bx, uint32_t by, uint32_t tx0, uint32_t* dst)
 {
   const uint32_t cx = ::max((uint32_t)Q.minX, tx0);
   const uint32_t kk = (cx >> 3) - ((uint32_t)Q.minX >> 3);
@@ -947,44 +966,43 @@ __device__ __forceinline__ bool make_fragment_t(const FrameParams& P, const Quad
     if (!mask) return false;
   }
   // depth rows (Rasterizer.cpp:1241-1268): rows 0/1 from (depth, d1), rows 8/9
-  // from (d8, d9), rows 2-7 by rounding averages of packed values
+  // from (d8, d9), rows 2-7 by rounding averages of packed values; rows are
+  // written to the slot as soon as they are known, to keep few registers live
   const float Dx = Q.Dx, Dy = Q.Dy;
-  float d1v[8], d8[8], d9[8];
+  uint32_t r0[4], r1[4], r8[4], r9[4];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    d1v[k] = zfma<kSafe>(Dx, 0.5f, depth[k]);
-    d8[k] = zadd<kSafe>(Dy, depth[k]);
-    d9[k] = zadd<kSafe>(Dy, d1v[k]);
+  for (int h = 0; h < 2; ++h) {  // depth lanes 0-3 give rows 0 and 8, lanes 4-7 rows 1 and 9
+    float a[4], b[4], c[4], e[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      a[k] = depth[4 * h + k];
+      b[k] = zfma<kSafe>(Dx, 0.5f, a[k]);
+      c[k] = zadd<kSafe>(Dy, a[k]);
+      e[k] = zadd<kSafe>(Dy, b[k]);
+    }
+    uint32_t* ra = h ? r1 : r0;
+    uint32_t* rb = h ? r9 : r8;
+    ra[0] = pack2(a[0], a[1]); ra[1] = pack2(a[2], a[3]); ra[2] = pack2(b[0], b[1]); ra[3] = pack2(b[2], b[3]);
+    rb[0] = pack2(c[0], c[1]); rb[1] = pack2(c[2], c[3]); rb[2] = pack2(e[0], e[1]); rb[3] = pack2(e[2], e[3]);
   }
-  r[0][0] = pack2(depth[0], depth[1]); r[0][1] = pack2(depth[2], depth[3]);
-  r[0][2] = pack2(d1v[0], d1v[1]);     r[0][3] = pack2(d1v[2], d1v[3]);
-  r[1][0] = pack2(depth[4], depth[5]); r[1][1] = pack2(depth[6], depth[7]);
-  r[1][2] = pack2(d1v[4], d1v[5]);     r[1][3] = pack2(d1v[6], d1v[7]);
-  r[8][0] = pack2(d8[0], d8[1]);       r[8][1] = pack2(d8[2], d8[3]);
-  r[8][2] = pack2(d9[0], d9[1]);       r[8][3] = pack2(d9[2], d9[3]);
-  r[9][0] = pack2(d8[4], d8[5]);       r[9][1] = pack2(d8[6], d8[7]);
-  r[9][2] = pack2(d9[4], d9[5]);       r[9][3] = pack2(d9[6], d9[7]);
+  uint32_t r4[4], r5[4];
 #pragma unroll
   for (int w = 0; w < 4; ++w) {
-    r[4][w] = avg_u16x2(r[0][w], r[8][w]);
-    r[5][w] = avg_u16x2(r[1][w], r[9][w]);
-    r[2][w] = avg_u16x2(r[0][w], r[4][w]);
-    r[3][w] = avg_u16x2(r[1][w], r[5][w]);
-    r[6][w] = avg_u16x2(r[4][w], r[8][w]);
-    r[7][w] = avg_u16x2(r[5][w], r[9][w]);
+    r4[w] = avg_u16x2(r0[w], r8[w]);
+    r5[w] = avg_u16x2(r1[w], r9[w]);
   }
-  if (mask != ~0ull) {
-#pragma unroll
-    for (int y = 0; y < 8; ++y) {
-      const int bitpos = (y & 1) ? (y >> 1) : 4 + (y >> 1);
-      const uint64_t bits = (mask >> bitpos) & 0x0101010101010101ull;
-      const uint32_t lo = (uint32_t)bits * 0xFFu, hi = (uint32_t)(bits >> 32) * 0xFFu;
-      r[y][0] &= __byte_perm(lo, 0, 0x1100);
-      r[y][1] &= __byte_perm(lo, 0, 0x3322);
-      r[y][2] &= __byte_perm(hi, 0, 0x1100);
-      r[y][3] &= __byte_perm(hi, 0, 0x3322);
-    }
-  }
+  put_row(dst, 2, mask, avg_u16x2(r0[0], r4[0]), avg_u16x2(r0[1], r4[1]), avg_u16x2(r0[2], r4[2]),
+          avg_u16x2(r0[3], r4[3]));
+  put_row(dst, 3, mask, avg_u16x2(r1[0], r5[0]), avg_u16x2(r1[1], r5[1]), avg_u16x2(r1[2], r5[2]),
+          avg_u16x2(r1[3], r5[3]));
+  put_row(dst, 0, mask, r0[0], r0[1], r0[2], r0[3]);
+  put_row(dst, 1, mask, r1[0], r1[1], r1[2], r1[3]);
+  put_row(dst, 6, mask, avg_u16x2(r4[0], r8[0]), avg_u16x2(r4[1], r8[1]), avg_u16x2(r4[2], r8[2]),
+          avg_u16x2(r4[3], r8[3]));
+  put_row(dst, 7, mask, avg_u16x2(r5[0], r9[0]), avg_u16x2(r5[1], r9[1]), avg_u16x2(r5[2], r9[2]),
+          avg_u16x2(r5[3], r9[3]));
+  put_row(dst, 4, mask, r4[0], r4[1], r4[2], r4[3]);
+  put_row(dst, 5, mask, r5[0], r5[1], r5[2], r5[3]);
   return true;
 }
 
@@ -994,13 +1012,7 @@ template <bool kSafe>
 __device__ __forceinline__ bool fragment_to(const FrameParams& P, const QuadRaster& Q, uint32_t ckq, uint32_t bx,
                                             uint32_t by, uint32_t tx0, uint32_t* dst)
 {
-  uint32_t r[10][4];
-  if (!make_fragment_t<kSafe>(P, Q, ckq, bx, by, tx0, r)) return false;
-#pragma unroll
-  for (int y = 0; y < 8; ++y)
-#pragma unroll
-    for (int w = 0; w < 4; ++w) dst[4 * y + w] = r[y][w];
-  return true;
+  return make_fragment_t<kSafe>(P, Q, ckq, bx, by, tx0, dst);
 }
 
 // Quads whose depth may overflow are rare: their copy stays out of line so
