@@ -157,6 +157,110 @@ class Rasterizer {
   uint32_t w_, h_;
 };
 
+// The learned occluder selector (replaces the distance-sorted loop of
+// Main.cpp:184-206): an MLP scoring each occluder of a view.
+class OccluderSelector {
+ public:
+  explicit OccluderSelector(Context& ctx, uint32_t seed = 0) { check(occ_mlp_create(ctx.handle(), seed, &m_), "occ_mlp_create"); }
+  ~OccluderSelector() { occ_mlp_destroy(m_); }
+  OccluderSelector(const OccluderSelector&) = delete;
+  OccluderSelector& operator=(const OccluderSelector&) = delete;
+  static uint32_t paramCount() { return (uint32_t)occ_mlp_param_count(); }
+  std::vector<float> params() const
+  {
+    std::vector<float> p(paramCount());
+    check(occ_mlp_get_params(m_, p.data()), "occ_mlp_get_params");
+    return p;
+  }
+  void setParams(const std::vector<float>& p) { check(occ_mlp_set_params(m_, p.data()), "occ_mlp_set_params"); }
+  // one listwise Adam step: rows in groups [groupStart[g], groupStart[g+1])
+  float trainStepListwise(uint32_t n, const float* features, const float* targets, const std::vector<uint32_t>& groupStart,
+                          float lr)
+  {
+    float loss = 0;
+    check(occ_mlp_train_step_listwise(m_, n, features, targets, (uint32_t)groupStart.size() - 1, groupStart.data(), lr,
+                                      &loss),
+          "occ_mlp_train_step_listwise");
+    return loss;
+  }
+  occ_mlp handle() const { return m_; }
+
+ private:
+  occ_mlp m_ = nullptr;
+};
+
+// Many views prepared once and launched as one CUDA graph per frame.
+class Batch {
+ public:
+  struct View {
+    Rasterizer* raster;
+    const float* mvp;                          // float[16]
+    std::vector<const Occluder*> occluders;
+    std::vector<uint8_t> flags;                // OCC_GATED / OCC_NEAR_CLIP per occluder (empty: all 0)
+    std::vector<Vec4> queryMins, queryMaxs;
+  };
+
+  Batch(Context& ctx, const std::vector<View>& views) : views_(views.size())
+  {
+    std::vector<occ_view_work> w(views.size());
+    for (size_t i = 0; i < views.size(); ++i) {
+      const View& v = views[i];
+      std::vector<occ_occluder>& ids = ids_.emplace_back();
+      for (const Occluder* o : v.occluders) ids.push_back(o->upload(ctx));
+      occ_view_work& x = w[i];
+      std::memset(&x, 0, sizeof(x));
+      x.raster = v.raster->handle();
+      x.mvp = v.mvp;
+      x.clear = 1;
+      x.numOccluders = (uint32_t)ids.size();
+      x.occluders = ids.data();
+      x.flags = v.flags.empty() ? nullptr : v.flags.data();
+      x.numQueries = (uint32_t)v.queryMins.size();
+      x.queryMins = x.numQueries ? &v.queryMins[0].v[0] : nullptr;
+      x.queryMaxs = x.numQueries ? &v.queryMaxs[0].v[0] : nullptr;
+      queries_.push_back(x.numQueries);
+    }
+    check(occ_batch_prepare(ctx.handle(), (uint32_t)w.size(), w.data(), &b_), "occ_batch_prepare");
+  }
+  ~Batch() { occ_batch_destroy(b_); }
+  Batch(const Batch&) = delete;
+  Batch& operator=(const Batch&) = delete;
+
+  void setModelViewProjection(uint32_t view, const float* m) { check(occ_batch_set_mvp(b_, view, m), "occ_batch_set_mvp"); }
+  // top `fraction` of each view's candidates by the selector's score
+  void setSelection(OccluderSelector* selector, float fraction, bool trackWins = true)
+  {
+    check(occ_batch_set_selection(b_, selector ? selector->handle() : nullptr, fraction, trackWins ? 1 : 0),
+          "occ_batch_set_selection");
+  }
+  void setSecondPass(bool enable) { check(occ_batch_set_second_pass(b_, enable ? 1 : 0), "occ_batch_set_second_pass"); }
+  void autotune(uint32_t iterations = 5) { check(occ_batch_autotune(b_, iterations, nullptr, nullptr, nullptr), "occ_batch_autotune"); }
+  void launch() { check(occ_batch_launch(b_), "occ_batch_launch"); }
+  // false if a launch since the last check outgrew the scratch (grown now: run the frame again)
+  bool check_capacity()
+  {
+    const int s = occ_batch_check(b_);
+    if (s == OCC_ERR_CAPACITY) return false;
+    check(s, "occ_batch_check");
+    return true;
+  }
+  // visibility bits of one view's boxes (bit i%32 of word i/32)
+  void results(uint32_t view, std::vector<uint32_t>& visibleBits, std::vector<uint32_t>& needsClippingBits)
+  {
+    const size_t nw = (queries_.at(view) + 31) / 32;
+    visibleBits.resize(nw);
+    needsClippingBits.resize(nw);
+    check(occ_batch_results(b_, view, visibleBits.data(), needsClippingBits.data()), "occ_batch_results");
+  }
+  occ_batch handle() const { return b_; }
+
+ private:
+  occ_batch b_ = nullptr;
+  size_t views_;
+  std::vector<std::vector<occ_occluder>> ids_;
+  std::vector<uint32_t> queries_;
+};
+
 struct QuadDecomposition {
   static std::vector<uint32_t> decompose(const std::vector<uint32_t>& indices, const std::vector<Vec4>& vertices)
   {

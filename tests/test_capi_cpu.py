@@ -75,3 +75,50 @@ def test_cpp_facade_compiles():
         p = os.path.join(d, "t.cpp")
         open(p, "w").write(src)
         subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I" + os.path.join(ROOT, "include"), p], check=True)
+
+
+FACADE_PROGRAM = r"""
+#include "rasterizer_gb300/Rasterizer.hpp"
+// The demo's frame loop with the learned selector, through the facade only
+// (built and linked here; it needs a GPU to run).
+int run(int argc) {
+  gb300::Context ctx(0);
+  gb300::Rasterizer raster(ctx, 1920, 1080);
+  std::vector<gb300::Vec4> verts(16, gb300::Vec4{{0, 0, 0, 1}});
+  auto occ = gb300::Occluder::bake(verts, gb300::Vec4{{0, 0, 0, 1}}, gb300::Vec4{{1, 1, 1, 1}});
+  float mvp[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 1, 0, 0, 0, 0};
+  gb300::Batch::View v{&raster, mvp, {occ.get()}, {OCC_GATED}, {gb300::Vec4{{0, 0, 5, 1}}}, {gb300::Vec4{{1, 1, 6, 1}}}};
+  gb300::Batch batch(ctx, {v});
+  gb300::OccluderSelector sel(ctx, 1);
+  batch.setSelection(&sel, 0.35f);
+  batch.autotune(2);
+  batch.launch();
+  std::vector<uint32_t> vis, nc;
+  batch.check_capacity();
+  batch.results(0, vis, nc);
+  raster.clear();
+  raster.setModelViewProjection(mvp);
+  bool needsClipping = false;
+  if (raster.queryVisibility(occ->m_boundsMin, occ->m_boundsMax, needsClipping))
+    needsClipping ? raster.rasterize<true>(*occ) : raster.rasterize<false>(*occ);
+  return (int)vis.size() + argc;
+}
+int main(int argc, char**) { return argc > 100 ? run(argc) : 0; }
+"""
+
+
+def test_cpp_facade_links_against_the_library():
+    """A program using the facade (batch, selector, the reference's calls)
+    compiles and links against librasterizer_gb300; run with no argument it
+    does not touch a GPU."""
+    import rasterizer_gb300._lib as L
+    so = L.lib_path() if hasattr(L, "lib_path") else os.path.join(ROOT, "rasterizer_gb300", "lib", "librasterizer_gb300.so")
+    if not os.path.exists(so):
+        pytest.skip("library not built")
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "t.cpp")
+        exe = os.path.join(d, "t")
+        open(p, "w").write(FACADE_PROGRAM)
+        subprocess.run(["g++", "-std=c++17", "-O0", "-I" + os.path.join(ROOT, "include"), p, "-o", exe, so,
+                        "-Wl,-rpath," + os.path.dirname(so)], check=True)
+        assert subprocess.run([exe]).returncode == 0
