@@ -358,9 +358,10 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
     views = L._views(ctx, occ, paths, pmin, pmax)
 
     def mover(bt, tracks, frames):
+        stacked = np.stack([tr.mvps[:frames] for tr in tracks], axis=1)  # (frames, views, 16)
+
         def before(i):
-            for v, tr in enumerate(tracks):
-                bt.setModelViewProjection(v, tr.mvps[i % frames])
+            bt.setModelViewProjections(stacked[i % frames])
         return before
 
     plain = api.PreparedBatch(ctx, views)
@@ -398,14 +399,15 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
     stats = sel.stats()
     prof = sel.profile(20)
     kern = dict(zip(["setup", "scan", "fill", "walk", "raster", "query", "selection"], [float(x) for x in prof]))
-    # end to end through the public API: matrices from the host, launch, every view's result bits back
-    e2e_steps = 30
+    # end to end through the public API: the step's 64 matrices from the host,
+    # launch, every view's result bits back to the host
+    e2e_steps = 50
+    sel.resultsAll()
     t1 = time.perf_counter()
     for i in range(e2e_steps):
         move(i)
         sel.launch()
-        for v in range(LEARNED_VIEWS):
-            sel.results(v)
+        vis_words, nc_words, _ = sel.resultsAll()
     e2e_s = time.perf_counter() - t1
     sel.close()
     for v in views:
@@ -424,10 +426,9 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
         "roofline": {"bound": "hbm", "kernel": "k_raster (with k_tile_prep)", "unit": "GB/s",
                      "achieved": raster_bytes / (kern["raster"] * 1e-3) / 1e9, "algorithmic_bytes": raster_bytes},
         "e2e": {"value": world * LEARNED_VIEWS * e2e_steps / e2e_s, "unit": "views/s",
-                "h2d_bytes_per_step": stats["table_bytes"],
-                "d2h_bytes_per_step": LEARNED_VIEWS * 2 * 4 * ((NQ + 31) // 32),
-                "path": "PreparedBatch.setModelViewProjection x64 / launch / results x64 (Python mirror -> "
-                        "C ABI), wall clock"},
+                "h2d_bytes_per_step": stats["table_bytes"], "d2h_bytes_per_step": int(vis_words.nbytes + nc_words.nbytes),
+                "path": "PreparedBatch.setModelViewProjections (64 matrices) / launch / resultsAll (every view's "
+                        "bits, one copy) through the Python mirror of the C ABI, wall clock"},
         "launches_per_step": 4 + 9}
     # ---- the 256-view workload (mixed resolutions) ----
     k_mv = pick(L.multiview_tracks(centers, quads, NQ, frames=4, seed=9))
@@ -498,10 +499,11 @@ def run_large(ctx, net, dev):
     views = L._views(ctx, occ, test, pmin, pmax)
     nq = sum(tr.query_count for tr in test)
 
+    stacked = np.stack([tr.mvps[:2] for tr in test], axis=1)
+
     def mover(bt):
         def before(i):
-            for v, tr in enumerate(test):
-                bt.setModelViewProjection(v, tr.mvps[i % 2])
+            bt.setModelViewProjections(stacked[i % 2])
         return before
 
     out = {}

@@ -136,6 +136,12 @@ typedef struct occ_batch_s* occ_batch;
 int occ_batch_prepare(occ_ctx ctx, uint32_t numViews, const occ_view_work* views, occ_batch* out);
 int occ_batch_set_mvp(occ_batch b, uint32_t view, const float matrix[16]);
 int occ_batch_launch(occ_batch b);
+/* Matrices of views first .. first+count-1 in one call (count float[16]). */
+int occ_batch_set_mvps(occ_batch b, uint32_t first, uint32_t count, const float* matrices);
+/* All views' result bits in one copy (syncs): `words` = occ_batch_result_words
+ * words per array; view v's bits start at word firstWord[v] (numViews entries). */
+int occ_batch_result_words(occ_batch b, uint32_t* words);
+int occ_batch_results_all(occ_batch b, uint32_t* visibleBits, uint32_t* needsClippingBits, uint32_t* firstWord);
 int occ_batch_results(occ_batch b, uint32_t view, uint32_t* visibleBits, uint32_t* needsClippingBits);
 int occ_batch_check(occ_batch b); /* syncs; OCC_ERR_CAPACITY if a launch overflowed */
 /* Runs the frame `iterations` times kernel by kernel with CUDA events between

@@ -68,6 +68,9 @@ SIGNATURES = {
     "occ_batch_set_cull_labels": (I32, [P, I32]),
     "occ_batch_read_cull_labels": (I32, [P, U32, P]),
     "occ_batch_stats": (I32, [P, P]),
+    "occ_batch_set_mvps": (I32, [P, U32, U32, P]),
+    "occ_batch_result_words": (I32, [P, C.POINTER(U32)]),
+    "occ_batch_results_all": (I32, [P, P, P, P]),
     "occ_batch_autotune": (I32, [P, U32, P, P, P]),
     "occ_mlp_param_count": (I32, []),
     "occ_mlp_create": (I32, [P, U32, C.POINTER(P)]),

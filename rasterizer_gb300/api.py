@@ -388,8 +388,35 @@ class PreparedBatch:
         m = _f32(matrix).reshape(16)
         check(lib().occ_batch_set_mvp(self.handle, view, _ptr(m)), "occ_batch_set_mvp")
 
+    def setModelViewProjections(self, matrices, first: int = 0) -> None:
+        """Matrices of views first, first+1, ... in one call ((n, 16) floats)."""
+        m = _f32(matrices).reshape(-1, 16)
+        check(lib().occ_batch_set_mvps(self.handle, first, len(m), _ptr(m)), "occ_batch_set_mvps")
+
     def launch(self) -> None:
         check(lib().occ_batch_launch(self.handle), "occ_batch_launch")
+
+    def resultsAll(self, unpack: bool = False):
+        """Every view's result bits in one copy: (visible words, needs-clipping
+        words, first word of each view); with `unpack`, a list of per-view
+        (visible, needsClipping) bool arrays."""
+        if not hasattr(self, "_words"):
+            w = C.c_uint32()
+            check(lib().occ_batch_result_words(self.handle, C.byref(w)), "occ_batch_result_words")
+            self._words = w.value
+            self._vis = np.zeros(max(w.value, 1), np.uint32)
+            self._nc = np.zeros(max(w.value, 1), np.uint32)
+            self._first = np.zeros(len(self.ws.nq), np.uint32)
+        check(lib().occ_batch_results_all(self.handle, _ptr(self._vis), _ptr(self._nc), _ptr(self._first)),
+              "occ_batch_results_all")
+        if not unpack:
+            return self._vis, self._nc, self._first
+        out = []
+        for v, n in enumerate(self.ws.nq):
+            a = int(self._first[v])
+            nw = (n + 31) // 32
+            out.append((unpack_bits(self._vis[a:a + nw], n), unpack_bits(self._nc[a:a + nw], n)))
+        return out
 
     def check(self) -> bool:
         """True if every launch since the last check fitted the scratch; on

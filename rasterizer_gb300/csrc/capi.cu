@@ -1142,6 +1142,43 @@ int occ_batch_set_mvp(occ_batch b, uint32_t view, const float matrix[16])
   return OCC_OK;
 }
 
+int occ_batch_set_mvps(occ_batch b, uint32_t first, uint32_t count, const float* matrices)
+{
+  if (!b || (count && !matrices) || first > b->L.views.size() || count > b->L.views.size() - first)
+    return fail(OCC_ERR_INVALID_ARG, "bad argument");
+  for (uint32_t i = 0; i < count; ++i) {
+    occ_raster_s* r = b->jobs[first + i].r;
+    bake_mvp(matrices + 16 * (size_t)i, r->width, r->height, r->cols, r->rows);
+    std::memcpy(b->L.views[first + i].cols, r->cols, sizeof(r->cols));
+    std::memcpy(b->L.views[first + i].rows, r->rows, sizeof(r->rows));
+  }
+  b->dirty = true;
+  return OCC_OK;
+}
+
+int occ_batch_results_all(occ_batch b, uint32_t* visibleBits, uint32_t* needsClippingBits, uint32_t* firstWord)
+{
+  if (!b) return fail(OCC_ERR_INVALID_ARG, "null batch");
+  const size_t nw = b->L.querySlots / 32;  // every view's range starts on a word
+  if (firstWord)
+    for (size_t v = 0; v < b->L.views.size(); ++v) firstWord[v] = b->L.views[v].queryStart / 32;
+  if (nw) {
+    if (visibleBits)
+      OCC_CUDA(cudaMemcpyAsync(visibleBits, b->vis.p, nw * 4, cudaMemcpyDeviceToHost, b->ctx->stream));
+    if (needsClippingBits)
+      OCC_CUDA(cudaMemcpyAsync(needsClippingBits, b->nc.p, nw * 4, cudaMemcpyDeviceToHost, b->ctx->stream));
+  }
+  OCC_CUDA(cudaStreamSynchronize(b->ctx->stream));
+  return OCC_OK;
+}
+
+int occ_batch_result_words(occ_batch b, uint32_t* words)
+{
+  if (!b || !words) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  *words = b->L.querySlots / 32;
+  return OCC_OK;
+}
+
 int occ_batch_launch(occ_batch b)
 {
   if (!b) return fail(OCC_ERR_INVALID_ARG, "null batch");

@@ -311,3 +311,34 @@ def test_query_special_values(ctx):
     assert not mismatch_report("visible", vis.astype(np.uint8), ovis)
     assert not mismatch_report("needsClipping", nc.astype(np.uint8), onc)
     assert vis.sum() > 0 and (~vis).sum() > 0
+
+
+def test_bulk_matrices_and_results(ctx):
+    """Matrices of many views in one call and every view's bits in one copy
+    give what the per-view calls give."""
+    occ = boxes_occluders()
+    sizes = [(640, 360), (320, 200), (512, 512)]
+    views, mvps = [], []
+    for i, (w, h) in enumerate(sizes):
+        mvps.append(scenes.view_projection((5.0 * i, 2.0, -40.0), (0.0, -0.05, 1.0), aspect=w / h))
+        mins, maxs = scenes.query_boxes(700 + 100 * i, seed=70 + i)
+        views.append(dict(raster=api.Rasterizer(ctx, w, h), mvp=mvps[-1], clear=True, occluders=occ,
+                          flags=np.full(len(occ), 2, np.uint8), mins=mins, maxs=maxs))
+    b = api.PreparedBatch(ctx, views)
+    moved = [scenes.view_projection((5.0 * i + 3, 2.5, -38.0), (0.05, -0.05, 1.0), aspect=w / h)
+             for i, (w, h) in enumerate(sizes)]
+    b.setModelViewProjections(np.stack(moved))
+    b.launch()
+    assert b.check()
+    bulk = b.resultsAll(unpack=True)
+    single = [b.results(v) for v in range(len(views))]
+    for (bv, bn), (sv, sn) in zip(bulk, single):
+        assert np.array_equal(bv, sv) and np.array_equal(bn, sn)
+    for v, m in enumerate(moved):
+        b.setModelViewProjection(v, m)
+    b.launch()
+    assert b.check()
+    for v, (sv, sn) in enumerate(single):
+        vv, nn = b.results(v)
+        assert np.array_equal(vv, sv) and np.array_equal(nn, sn)
+    b.close()
