@@ -371,7 +371,7 @@ int run_batch(occ_ctx_s* ctx, FrameScratch& S, std::vector<ViewJob>& jobs, bool 
   OCC_CHECK(S.stLen.reserve(L.numSt));
   OCC_CHECK(S.cmdDraw.reserve(L.cmds.size()));
   OCC_CHECK(S.activeChunks.reserve(L.chunks.size()));
-  OCC_CHECK(S.activeTiles.reserve(L.numTiles));
+  OCC_CHECK(S.activeTiles.reserve((size_t)L.numTiles * kUnitsPerTile));
   if (S.header.n == 0) {
     OCC_CHECK(S.header.reserve(1));
     OCC_CUDA(cudaMemsetAsync(S.header.p, 0, sizeof(FrameHeader), ctx->stream));

@@ -868,31 +868,35 @@ __global__ void __launch_bounds__(256) k_walk(FrameParams P)
 
 // ---- k_raster ------------------------------------------------------------------------
 //
-// One CTA of 256 threads per 8x4-block tile.  Thread t owns pixel row t%8 of
-// block t/8 (4 packed words in registers); the eight threads of a block keep
-// its hiZ in step.  The CTA walks its super-tile's
-// quad list in order, keeps the quads that overlap the tile and are not
-// already hidden in an ordered local list, and turns them into (quad, block)
-// fragments, 256 at a time: every thread computes one fragment (coverage mask,
-// packed depth rows), then each block's eight threads merge the fragments aimed
-// at it in list order with the reference's hiZ test, fast-clear overwrite and
-// max-merge (Rasterizer.cpp:1148-1290).
+// One CTA of 128 threads per raster unit of 8 x kRasterRows blocks (half a
+// warp-tile).  Thread t owns pixel row t%8 of block t/8 (4 packed words in
+// registers); the eight threads of a block keep its hiZ in step.  The CTA
+// walks its super-tile's quad list in order, keeps the quads that overlap the
+// unit and are not already hidden in an ordered local list, and turns them
+// into (quad, block) fragments, 128 at a time: every thread computes one
+// fragment (coverage mask, packed depth rows), then each block's eight threads
+// merge the fragments aimed at it in list order with the reference's hiZ
+// test, fast-clear overwrite and max-merge (Rasterizer.cpp:1148-1290).  A unit
+// is mostly latency (record loads, fragment arithmetic, the ordered merge):
+// small units let eight CTAs per SM overlap eight of them.
 
-constexpr int kRasterThreads = 256;
-constexpr int kRasterMinBlocks = 4;  // resident CTAs per SM the register budget is sized for
-constexpr int kLocalCap = 768;   // overlapping quads buffered per tile
+constexpr int kUnitBlocks = kTileW * kRasterRows;       // 16 blocks
+constexpr int kRasterThreads = 8 * kUnitBlocks;          // one thread per block row: 128
+constexpr int kRasterMinBlocks = 8;  // resident CTAs per SM the register budget is sized for
+constexpr int kLocalCap = 512;   // overlapping quads buffered per unit
 constexpr int kFragStride = 33;  // words per fragment slot (padding: conflict-free banks)
-constexpr int kScanPerRound = 512;
+constexpr int kScanPerRound = 2 * kRasterThreads;
+constexpr int kMaskWords = kRasterThreads / 32;
 
 struct RasterSmem {
   uint32_t lq[kLocalCap];        // quad index
-  uint32_t lrect[kLocalCap];     // quad rect within the tile: x0 | y0 << 3 | w << 5 | h << 9
+  uint32_t lrect[kLocalCap];     // quad rect within the unit: x0 | y0 << 3 | w << 5 | h << 9
   uint32_t loff[kLocalCap];      // first fragment of each local quad
   uint32_t frag[kRasterThreads * kFragStride];
   uint32_t meta[kRasterThreads]; // per fragment slot: maxZ << 16 | valid << 5 | target block
   uint32_t fcmd[kRasterThreads]; // per fragment slot: command (win counting only)
-  uint32_t bmask[32][kRasterThreads / 32];  // per block: fragment slots aimed at it
-  uint32_t hiz[32];              // per block: current hiZ
+  uint32_t bmask[kUnitBlocks][kMaskWords];  // per block: fragment slots aimed at it
+  uint32_t hiz[kUnitBlocks];     // per block: current hiZ
   uint32_t scan[kRasterThreads / 32];
   uint32_t n;
 };
@@ -1090,7 +1094,7 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
   const uint32_t groupMask = 0xFFu << (lane & ~7u);
   // S.loff holds each local quad's first fragment, F the fragment count
   for (uint32_t f0 = 0; f0 < F; f0 += kRasterThreads) {
-    (&S.bmask[0][0])[tid] = 0;  // 32 blocks x (kRasterThreads / 32) words == kRasterThreads
+    if (tid < kUnitBlocks * kMaskWords) (&S.bmask[0][0])[tid] = 0;
     const uint32_t f = f0 + tid;
     uint32_t target = 0, q = 0, bx = 0, by = 0;
     const bool haveF = f < F;
@@ -1131,7 +1135,7 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
     // merge, in slot order, the fragments aimed at this thread's block
     if (inView) {
 #pragma unroll 1
-      for (int wd = 0; wd < kRasterThreads / 32; ++wd) {
+      for (int wd = 0; wd < kMaskWords; ++wd) {
         uint32_t mine = S.bmask[myBlock][wd];
         while (mine) {
           const uint32_t slot = 32u * wd + __ffs(mine) - 1;
@@ -1172,10 +1176,10 @@ __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
   const uint32_t wt = blockIdx.x * 8 + warp;
   if (threadIdx.x == 0) s_n = 0;
   __syncthreads();
-  bool queue = false;
-  uint32_t slot = 0;
+  uint32_t queue = 0, slot = 0, v = 0;  // queue: bit u = raster unit u of the tile
   if (wt < P.numTiles) {
-    const ViewDesc& V = P.views[view_of_tile(P, wt)];
+    v = view_of_tile(P, wt);
+    const ViewDesc& V = P.views[v];
     const uint32_t lt = wt - V.tileStart;
     const uint32_t tx0 = (lt % V.tilesX) * kTileW, ty0 = (lt / V.tilesX) * kTileH;
     const uint32_t bx = tx0 + (lane & 7), by = ty0 + (lane >> 3);
@@ -1188,51 +1192,67 @@ __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
     }
     const uint32_t s = V.stBase + (ty0 / kSuperTile) * V.stX + (tx0 / kSuperTile);
     const uint32_t len = V.cmdCount ? P.stLen[s] : 0u;
-    queue = len != 0;
-    if (queue && len <= kPrepScanMax) {
-      // queue the tile only if a quad of the super-tile list reaches it
+    if (len > kPrepScanMax) {
+      queue = (1u << kUnitsPerTile) - 1u;
+    } else if (len) {
+      // queue a unit only if a quad of the super-tile list reaches it
       const uint4* list = P.stList + P.stStart[s];
-      bool any = false;
-      for (uint32_t i0 = 0; i0 < len && !any; i0 += 32) {
-        bool o = false;
+      for (uint32_t i0 = 0; i0 < len && queue != (1u << kUnitsPerTile) - 1u; i0 += 32) {
+        uint32_t hit = 0;
         if (i0 + lane < len) {
           const uint4 e = __ldg(list + i0 + lane);
-          o = (e.y & 0xFFFFu) < tx0 + kTileW && (e.z & 0xFFFFu) > tx0 && (e.y >> 16) < ty0 + kTileH &&
-              (e.z >> 16) > ty0;
+          if ((e.y & 0xFFFFu) < tx0 + kTileW && (e.z & 0xFFFFu) > tx0)
+            for (uint32_t u = 0; u < (uint32_t)kUnitsPerTile; ++u) {
+              const uint32_t uy0 = ty0 + u * kRasterRows;
+              if ((e.y >> 16) < uy0 + kRasterRows && (e.z >> 16) > uy0) hit |= 1u << u;
+            }
         }
-        any = __any_sync(0xFFFFFFFFu, o);
+        queue |= __reduce_or_sync(0xFFFFFFFFu, hit);
       }
-      queue = any;
     }
-    if (!queue) {
-      uint32_t tmin = inView ? (clearing ? 1u : (uint32_t)V.hiz[blk]) : 0xFFFFu;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) tmin = ::min(tmin, __shfl_xor_sync(0xFFFFFFFFu, tmin, o));
-      if (lane == 0) V.tileHiz[lt] = (uint16_t)tmin;
-    } else if (lane == 0) {
-      slot = atomicAdd(&s_n, 1u);
-    }
+    if (lane == 0 && queue) slot = atomicAdd(&s_n, (uint32_t)__popc(queue));
   }
   __syncthreads();
   if (threadIdx.x == 0 && s_n) s_base = atomicAdd(&P.header->activeTiles, s_n);
   __syncthreads();
-  if (queue && lane == 0) P.activeTileList[s_base + slot] = make_uint2(wt, view_of_tile(P, wt));
+  if (lane == 0 && queue) {
+    uint32_t k = s_base + slot;
+    for (uint32_t u = 0; u < (uint32_t)kUnitsPerTile; ++u)
+      if (queue & (1u << u)) P.activeTileList[k++] = make_uint2(wt * kUnitsPerTile + u, v);
+  }
+}
+
+// Per warp-tile minimum hiZ of every view (after rasterisation; the queries
+// skip a tile whose minimum is >= their depth).  One warp per tile.
+__global__ void __launch_bounds__(256) k_tile_min(FrameParams P)
+{
+  if (P.header->overflow) return;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t wt = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (wt >= P.numTiles) return;
+  const ViewDesc& V = P.views[view_of_tile(P, wt)];
+  const uint32_t lt = wt - V.tileStart;
+  const uint32_t bx = (lt % V.tilesX) * kTileW + (lane & 7), by = (lt / V.tilesX) * kTileH + (lane >> 3);
+  uint32_t m = (bx < V.blocksX && by < V.blocksY) ? (uint32_t)V.hiz[by * V.blocksX + bx] : 0xFFFFu;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = ::min(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+  if (lane == 0) V.tileHiz[lt] = (uint16_t)m;
 }
 
 // ---- k_raster -------------------------------------------------------------------------
-// Persistent CTAs of kRasterThreads threads take queued warp-tiles one at a
-// time (dynamic, heavy tiles vary a lot): per tile, the super-tile list is
-// filtered to the quads that reach the tile and are not already hidden, then
-// rasterised in list order (raster_local_list) and the tile's blocks written back.
+// Persistent CTAs of kRasterThreads threads take queued raster units a few at
+// a time (dynamic, heavy units vary a lot): per unit, the super-tile list is
+// filtered to the quads that reach the unit and are not already hidden, then
+// rasterised in list order (raster_local_list) and the unit's blocks written back.
 
 template <bool kWins>
-__device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S, uint32_t wt, uint32_t v)
+__device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S, uint32_t unit, uint32_t v)
 {
   const uint32_t tid = threadIdx.x, lane = tid & 31;
   const ViewDesc& V = P.views[v];
-  const uint32_t lt = wt - V.tileStart;
+  const uint32_t lt = unit / kUnitsPerTile - V.tileStart;  // the warp-tile holding the unit
   const uint32_t tx = lt % V.tilesX, ty = lt / V.tilesX;
-  const uint32_t tx0 = tx * kTileW, ty0 = ty * kTileH;
+  const uint32_t tx0 = tx * kTileW, ty0 = ty * kTileH + (unit % kUnitsPerTile) * kRasterRows;
   const uint32_t myBlock = tid >> 3, py = tid & 7;
   const uint32_t bx = tx0 + (myBlock & 7), by = ty0 + (myBlock >> 3);
   const bool inView = bx < V.blocksX && by < V.blocksY;
@@ -1264,7 +1284,7 @@ __device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S,
     for (int k = 0; k < 2; ++k) {
       const uint32_t qx0 = e[k].y & 0xFFFFu, qy0 = e[k].y >> 16, qx1 = e[k].z & 0xFFFFu, qy1 = e[k].z >> 16;
       const uint32_t x0 = ::max(qx0, tx0), x1 = ::min(qx1, tx0 + kTileW);
-      const uint32_t y0 = ::max(qy0, ty0), y1 = ::min(qy1, ty0 + kTileH);
+      const uint32_t y0 = ::max(qy0, ty0), y1 = ::min(qy1, ty0 + kRasterRows);
       bool o = x0 < x1 && y0 < y1;  // padding entries have an empty box
       if (o) {
         // hidden if every block it touches here already has hiZ >= its maxZ
@@ -1288,7 +1308,7 @@ __device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S,
 #pragma unroll
     for (int k = 0; k < 2; ++k) fr[k] = ov[k] ? ((rect[k] >> 5) & 15u) * ((rect[k] >> 9) & 7u) : 0u;
     const uint32_t cnt = (ov[0] ? 1u : 0u) + (ov[1] ? 1u : 0u);
-    uint32_t tot;  // per round at most 512 quads and 16,384 fragments: the halves do not carry
+    uint32_t tot;  // per round at most 256 quads and 4,096 fragments: the halves do not carry
     const uint32_t ex = block_exclusive_scan<kRasterThreads>(cnt | ((fr[0] + fr[1]) << 16), tot, S.scan);
     uint32_t pos = n + (ex & 0xFFFFu), fpos = F + (ex >> 16);
 #pragma unroll
@@ -1344,18 +1364,6 @@ __device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S,
           if (own[x]) o[x] = own[x];  // pixels the second pass changed
       }
     }
-  }
-  // per-tile minimum hiZ for the queries
-  uint32_t tmin = (inView && py == 0) ? hiz : 0xFFFFu;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) tmin = ::min(tmin, __shfl_xor_sync(0xFFFFFFFFu, tmin, o));
-  if (lane == 0) S.scan[tid >> 5] = tmin;
-  __syncthreads();
-  if (tid == 0) {
-    uint32_t m = S.scan[0];
-#pragma unroll
-    for (int w = 1; w < kRasterThreads / 32; ++w) m = ::min(m, S.scan[w]);
-    V.tileHiz[lt] = (uint16_t)m;
   }
 }
 
@@ -1532,9 +1540,10 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
   mark(4);
   if (doRaster && P.numTiles) {
     k_tile_prep<<<(P.numTiles + 7) / 8, 256, 0, stream>>>(P);
-    const uint32_t grid = grid_of(P.tune.rasterPerSm, g_rasterPerSm, P.numTiles);
+    const uint32_t grid = grid_of(P.tune.rasterPerSm, g_rasterPerSm, P.numTiles * kUnitsPerTile);
     if (P.wins) k_raster<true><<<grid, kRasterThreads, 0, stream>>>(P);
     else k_raster<false><<<grid, kRasterThreads, 0, stream>>>(P);
+    k_tile_min<<<(P.numTiles + 7) / 8, 256, 0, stream>>>(P);
   }
   mark(5);
   if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);

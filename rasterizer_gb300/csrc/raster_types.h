@@ -19,6 +19,8 @@ constexpr int kSuperTile = 16;            // binning super-tile edge, in 8x8 blo
 constexpr int kTileW = 8;                 // warp-tile: 8 x 4 blocks, one lane per block
 constexpr int kTileH = 4;
 constexpr int kCkSpan = 8;                // row-walk checkpoint every 8 block columns (== kTileW)
+constexpr int kRasterRows = 2;            // raster unit: 8 x kRasterRows blocks (a part of a warp-tile)
+constexpr int kUnitsPerTile = kTileH / kRasterRows;
 constexpr int kMaxCmdPerChunk = 40;       // commands are >= 8 quads, so <= 33 per chunk
 constexpr int kCkFloats = 12;             // 4 edge offsets + 8 depth lanes
 constexpr int kMaxStPerView = 3072;       // super-tiles per view (e.g. 12288 x 6144 pixels)
