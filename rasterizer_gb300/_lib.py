@@ -72,6 +72,7 @@ SIGNATURES = {
     "occ_batch_result_words": (I32, [P, C.POINTER(U32)]),
     "occ_batch_results_all": (I32, [P, P, P, P]),
     "occ_batch_autotune": (I32, [P, U32, P, P, P]),
+    "occ_batch_set_tuning": (I32, [P, P]),
     "occ_mlp_param_count": (I32, []),
     "occ_mlp_create": (I32, [P, U32, C.POINTER(P)]),
     "occ_mlp_destroy": (I32, [P]),

@@ -450,17 +450,25 @@ class PreparedBatch:
         """Picks the launch shapes of the persistent kernels by timing the
         batch's own frame stage by stage; returns the choice and the stage
         times before and after."""
-        tuned = np.zeros(5, np.uint32)
+        tuned = np.zeros(6, np.uint32)
         before = np.zeros(7, np.float32)
         after = np.zeros(7, np.float32)
         check(lib().occ_batch_autotune(self.handle, iterations, _ptr(tuned), _ptr(before), _ptr(after)),
               "occ_batch_autotune")
         keys = ("setup_ctas_per_sm", "fill_ctas_per_sm", "walk_ctas_per_sm", "raster_ctas_per_sm",
-                "raster_tiles_per_fetch")
+                "raster_tiles_per_fetch", "query_rounds")
         names = ("setup", "scan", "fill", "walk", "raster", "query", "selection")
         return {"tuned": {k: int(v) for k, v in zip(keys, tuned)},
                 "ms_before": {k: float(v) for k, v in zip(names, before)},
                 "ms_after": {k: float(v) for k, v in zip(names, after)}}
+
+    def setTuning(self, tuned: dict) -> None:
+        """Sets launch shapes directly (keys as `autotune()["tuned"]`; missing
+        keys or 0: the default)."""
+        keys = ("setup_ctas_per_sm", "fill_ctas_per_sm", "walk_ctas_per_sm", "raster_ctas_per_sm",
+                "raster_tiles_per_fetch", "query_rounds")
+        t = np.array([int(tuned.get(k, 0)) for k in keys], np.uint32)
+        check(lib().occ_batch_set_tuning(self.handle, _ptr(t)), "occ_batch_set_tuning")
 
     def stats(self) -> dict:
         """Work counts of the last launch."""

@@ -1333,7 +1333,7 @@ static int profile_with(occ_batch b, const LaunchTuning& t, uint32_t iterations,
   return st;
 }
 
-int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[5], float msBefore[7], float msAfter[7])
+int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[6], float msBefore[7], float msAfter[7])
 {
   if (!b || !iterations) return fail(OCC_ERR_INVALID_ARG, "bad argument");
   uint32_t lim[4];
@@ -1368,6 +1368,7 @@ int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[5], floa
   OCC_CHECK(search(&LaunchTuning::walkPerSm, 3, {2, 4, 8, 16}));
   OCC_CHECK(search(&LaunchTuning::rasterPerSm, 4, upTo(lim[2])));
   OCC_CHECK(search(&LaunchTuning::rasterChunk, 4, {1, 2, 4, 8, 16}));
+  OCC_CHECK(search(&LaunchTuning::queryRounds, 5, {kQueryPerThread, 1, 2, 3, 4}));
   b->tune = best;
   OCC_CHECK(capture(b));
   if (msAfter) OCC_CHECK(occ_batch_profile(b, iterations, msAfter));
@@ -1377,6 +1378,7 @@ int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[5], floa
     tuned[2] = best.walkPerSm;
     tuned[3] = best.rasterPerSm;
     tuned[4] = best.rasterChunk;
+    tuned[5] = best.queryRounds;
   }
   return OCC_OK;
 }
@@ -1417,6 +1419,23 @@ int occ_batch_set_second_pass(occ_batch b, int enable)
 {
   if (!b) return fail(OCC_ERR_INVALID_ARG, "null batch");
   b->secondPass = enable != 0;
+  return capture(b);
+}
+
+int occ_batch_set_tuning(occ_batch b, const uint32_t tune[6])
+{
+  if (!b || !tune) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  for (int i = 0; i < 5; ++i)
+    if (tune[i] > 64) return fail(OCC_ERR_INVALID_ARG, "launch shape out of range (at most 64)");
+  if (tune[5] > kQueryRounds && tune[5] != kQueryPerThread) return fail(OCC_ERR_INVALID_ARG, "unknown query form");
+  LaunchTuning t{};
+  t.setupPerSm = tune[0];
+  t.fillPerSm = tune[1];
+  t.walkPerSm = tune[2];
+  t.rasterPerSm = tune[3];
+  t.rasterChunk = tune[4];
+  t.queryRounds = tune[5];
+  b->tune = t;
   return capture(b);
 }
 

@@ -17,9 +17,11 @@
 //               filters its super-tile's list into the quads overlapping the
 //               tile, computes (quad, block) fragments 128 at a time and merges
 //               them per block in list order (Rasterizer.cpp:1098-1292).
-//   k_query     one thread per query box (Rasterizer.cpp:123-349); boxes over
-//               more than two tiles are tested by the whole warp; result bits
-//               gathered with ballots.
+//   k_query     queryVisibility + query2D (Rasterizer.cpp:123-349): frustum test
+//               per box, survivors compacted per CTA and projected by full
+//               warps (k_query_thread: one box per thread in place, for few
+//               boxes); boxes over more than two tiles are tested by the whole
+//               warp.
 //
 // Exactness: every float operation follows the reference's order and
 // rounding (x86_emu.cuh); the block loop sees each quad's primitives in
@@ -1410,38 +1412,27 @@ __global__ void __launch_bounds__(128) k_tile_hiz(const uint16_t* hiz, uint16_t*
 
 // ---- k_query -------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(256, 6) k_query(FrameParams P)
+// Front-end status -> visibility for boxes with small rectangles (query2D per
+// thread); `big` marks the ones left to query_big_boxes.
+__device__ __forceinline__ void query_resolve(const ViewDesc& V, int st, const uint32_t* rect, uint32_t maxZ, bool& vis,
+                                              bool& nc, bool& big)
 {
-  if (P.header->overflow) return;
-  const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t lane = threadIdx.x & 31;
-  bool vis = false, nc = false, big = false;
-  uint32_t rect[4] = {0, 0, 0, 0}, maxZ = 0, view = 0;
-  if (slot < P.numQuerySlots) {
-    uint32_t lo = 0, hi = P.numViews - 1;
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi + 1) >> 1;
-      if (P.views[mid].queryStart <= slot) lo = mid; else hi = mid - 1;
-    }
-    view = lo;
-    const ViewDesc& V = P.views[lo];
-    if (slot - V.queryStart < V.queryCount) {
-      const float4 a = P.qmin[slot], b = P.qmax[slot];
-      const float bmin[4] = {a.x, a.y, a.z, a.w}, bmax[4] = {b.x, b.y, b.z, b.w};
-      const int st = query_front(V, bmin, bmax, rect, &maxZ);
-      if (st == 1) {
-        vis = true;
-        nc = true;
-      } else if (st == 2) {
-        const uint32_t ntx = (rect[1] >> 3) / kTileW - (rect[0] >> 3) / kTileW + 1;
-        const uint32_t nty = (rect[3] >> 3) / kTileH - (rect[2] >> 3) / kTileH + 1;
-        big = ntx * nty > 2;
-        if (!big) vis = query2d(V, rect[0], rect[1], rect[2], rect[3], maxZ);
-      }
-    }
+  if (st == 1) {
+    vis = true;
+    nc = true;
+  } else if (st == 2) {
+    const uint32_t ntx = (rect[1] >> 3) / kTileW - (rect[0] >> 3) / kTileW + 1;
+    const uint32_t nty = (rect[3] >> 3) / kTileH - (rect[2] >> 3) / kTileH + 1;
+    big = ntx * nty > 2;
+    if (!big) vis = query2d(V, rect[0], rect[1], rect[2], rect[3], maxZ);
   }
-  // boxes spanning more than two warp-tiles: the whole warp tests one box at a
-  // time, one tile per lane
+}
+
+// Boxes spanning more than two warp-tiles: the whole warp tests one box at a
+// time, one tile per lane.  Called by all 32 lanes.
+__device__ __forceinline__ void query_big_boxes(const FrameParams& P, bool big, const uint32_t* rect, uint32_t maxZ,
+                                                uint32_t view, uint32_t lane, bool& vis)
+{
   uint32_t bigMask = __ballot_sync(0xFFFFFFFFu, big);
   while (bigMask) {
     const int j = __ffs(bigMask) - 1;
@@ -1466,10 +1457,128 @@ __global__ void __launch_bounds__(256, 6) k_query(FrameParams P)
     }
     if ((int)lane == j) vis = found;
   }
+}
+
+// The view owning query slot `slot`, searched in [lo, hi].
+__device__ __forceinline__ uint32_t query_view(const FrameParams& P, uint32_t slot, uint32_t lo, uint32_t hi)
+{
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (P.views[mid].queryStart <= slot) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// One thread per query slot, the whole front end and query2D in place: the
+// fastest form when there are too few slots to keep the GPU busy after
+// compaction (a single view's 100k boxes).
+__global__ void __launch_bounds__(256, 6) k_query_thread(FrameParams P)
+{
+  if (P.header->overflow) return;
+  const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31;
+  bool vis = false, nc = false, big = false;
+  uint32_t rect[4] = {0, 0, 0, 0}, maxZ = 0, view = 0;
+  if (slot < P.numQuerySlots) {
+    view = query_view(P, slot, 0, P.numViews - 1);
+    const ViewDesc& V = P.views[view];
+    if (slot - V.queryStart < V.queryCount) {
+      const float4 a = P.qmin[slot], b = P.qmax[slot];
+      const float bmin[4] = {a.x, a.y, a.z, a.w}, bmax[4] = {b.x, b.y, b.z, b.w};
+      const int st = query_front(V, bmin, bmax, rect, &maxZ);
+      query_resolve(V, st, rect, maxZ, vis, nc, big);
+    }
+  }
+  query_big_boxes(P, big, rect, maxZ, view, lane, vis);
   const uint32_t vb = __ballot_sync(0xFFFFFFFFu, vis), nb = __ballot_sync(0xFFFFFFFFu, nc);
   if (lane == 0 && slot < P.numQuerySlots) {
     P.visBits[slot >> 5] = vb;
     P.ncBits[slot >> 5] = nb;
+  }
+}
+
+// One CTA per `rounds` x 256 query slots, in two phases.  Every thread tests
+// its boxes against the six frustum planes; the boxes inside (and those whose
+// arithmetic met a NaN) are compacted in shared memory, and then all warps
+// project them and run query2D with their lanes full (most boxes of a view
+// are outside its frustum: without compaction most lanes idle through the
+// projection).  Each slot's bits land in shared words, written out once.
+__global__ void __launch_bounds__(256, 6) k_query(FrameParams P, uint32_t rounds)
+{
+  __shared__ uint32_t s_slot[256 * kQueryRounds], s_view[256 * kQueryRounds];
+  __shared__ uint32_t s_vis[8 * kQueryRounds], s_nc[8 * kQueryRounds];
+  __shared__ uint32_t s_n, s_range[2];
+  if (P.header->overflow) return;
+  const uint32_t tid = threadIdx.x, lane = tid & 31;
+  const uint32_t first = blockIdx.x * 256 * rounds;
+  if (tid < 8 * rounds) {
+    s_vis[tid] = 0;
+    s_nc[tid] = 0;
+  }
+  if (tid == 0) s_n = 0;
+  if (tid < 2)  // views of the CTA's first and last slot: the threads' searches start there
+    s_range[tid] = query_view(P, ::min(first + (tid ? 256 * rounds - 1 : 0), P.numQuerySlots - 1), 0, P.numViews - 1);
+  __syncthreads();
+  for (uint32_t r = 0; r < rounds; ++r) {
+    const uint32_t slot = first + 256 * r + tid;
+    bool keep = false, exact = false;
+    uint32_t view = 0;
+    if (slot < P.numQuerySlots) {
+      view = query_view(P, slot, s_range[0], s_range[1]);
+      const ViewDesc& V = P.views[view];
+      if (slot - V.queryStart < V.queryCount) {
+        const float4 a = P.qmin[slot], b = P.qmax[slot];
+        const float bmin[4] = {a.x, a.y, a.z, a.w}, bmax[4] = {b.x, b.y, b.z, b.w};
+        LazyOps f;
+        const bool outside = query_outside_t(f, V, bmin, bmax);
+        exact = f.nan;  // redone in full under the x86 NaN rules
+        keep = !outside || exact;
+      }
+    }
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, keep);
+    uint32_t at = 0;
+    if (lane == 0 && m) at = atomicAdd(&s_n, (uint32_t)__popc(m));
+    at = __shfl_sync(0xFFFFFFFFu, at, 0) + (uint32_t)__popc(m & ((1u << lane) - 1u));
+    if (keep) {
+      s_slot[at] = slot;
+      s_view[at] = view | (exact ? 0x80000000u : 0u);
+    }
+  }
+  __syncthreads();
+  const uint32_t n = s_n;
+  for (uint32_t base = tid & ~31u; base < n; base += 256) {  // warp-uniform: query_big_boxes is cooperative
+    const uint32_t k = base + lane;
+    bool vis = false, nc = false, big = false;
+    uint32_t rect[4] = {0, 0, 0, 0}, maxZ = 0, v = 0, sl = 0;
+    if (k < n) {
+      sl = s_slot[k];
+      const uint32_t e = s_view[k];
+      v = e & 0x7FFFFFFFu;
+      const ViewDesc& V = P.views[v];
+      const float4 a = P.qmin[sl], b = P.qmax[sl];
+      const float bmin[4] = {a.x, a.y, a.z, a.w}, bmax[4] = {b.x, b.y, b.z, b.w};
+      int st;
+      if (e >> 31) {
+        st = query_front_exact(V, bmin, bmax, rect, &maxZ, nullptr);
+      } else {
+        LazyOps g;
+        st = query_project_t(g, V, bmin, bmax, rect, &maxZ);
+        if (g.nan) st = query_front_exact(V, bmin, bmax, rect, &maxZ, nullptr);
+      }
+      query_resolve(V, st, rect, maxZ, vis, nc, big);
+    }
+    query_big_boxes(P, big, rect, maxZ, v, lane, vis);
+    const uint32_t w = (sl - first) >> 5, bit = 1u << (sl & 31u);
+    if (vis) atomicOr(&s_vis[w], bit);
+    if (nc) atomicOr(&s_nc[w], bit);
+  }
+  __syncthreads();
+  if (tid < 8 * rounds) {
+    const uint32_t w = (first >> 5) + tid;
+    if (32 * w < P.numQuerySlots) {
+      P.visBits[w] = s_vis[tid];
+      P.ncBits[w] = s_nc[tid];
+    }
   }
 }
 
@@ -1546,7 +1655,16 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
     k_tile_min<<<(P.numTiles + 7) / 8, 256, 0, stream>>>(P);
   }
   mark(5);
-  if (doQuery && P.numQuerySlots) k_query<<<(P.numQuerySlots + 255) / 256, 256, 0, stream>>>(P);
+  if (doQuery && P.numQuerySlots) {
+    const uint32_t ctas = (P.numQuerySlots + 255) / 256, wave = g_sms * 6;
+    uint32_t rounds = P.tune.queryRounds;
+    if (rounds == 0)  // by slot count: compaction pays once the slots fill the GPU a few times over
+      rounds = ctas < 4 * wave ? kQueryPerThread : ::min(kQueryRounds, ctas / wave);
+    if (rounds == kQueryPerThread || rounds > kQueryRounds)
+      k_query_thread<<<ctas, 256, 0, stream>>>(P);
+    else
+      k_query<<<(ctas + rounds - 1) / rounds, 256, 0, stream>>>(P, rounds);
+  }
   mark(6);
   return cudaGetLastError();
 }

@@ -82,13 +82,12 @@ struct FastOps {
 
 // ---- queryVisibility front end (Rasterizer.cpp:123-273) ------------------------------
 
-// Returns 0 (not visible), 1 (visible, needs clipping) or 2 (rect + maxZ for query2D).
+// The frustum half of the front end (Rasterizer.cpp:125-167): true when the
+// box is outside one of the six planes.
 template <class Ops>
-__device__ __forceinline__ int query_front_t(Ops& o, const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect, uint32_t* maxZOut,
-                                             uint32_t* minZOut = nullptr)
+__device__ __forceinline__ bool query_outside_t(Ops& o, const ViewDesc& V, const float* bmin, const float* bmax)
 {
-  using x86::xmin; using x86::xmax; using x86::fxor; using x86::fabs_; using x86::sign; using x86::fu;
-  using x86::cvtt; using x86::i2f; using x86::rcp; using x86::pack_depth; using x86::radd; using x86::rmul;
+  using x86::fxor; using x86::sign; using x86::fu;
   float ext[4], ctr[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
@@ -108,8 +107,22 @@ __device__ __forceinline__ int query_front_t(Ops& o, const ViewDesc& V, const fl
     }
     signs |= fu(o.chk(o.dp4(plane, offs)));  // the box's values and the planes all reach this sum
   }
-  if (signs & 0x80000000u) return 0;
+  return (signs & 0x80000000u) != 0;
+}
 
+// The projection half (Rasterizer.cpp:169-273) for a box inside the frustum:
+// 1 (visible, needs clipping) or 2 (screen rectangle + maxZ for query2D), 0
+// for an empty rectangle.  minZOut (optional) receives the smallest packed
+// corner depth.
+template <class Ops>
+__device__ __forceinline__ int query_project_t(Ops& o, const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect,
+                                               uint32_t* maxZOut, uint32_t* minZOut = nullptr)
+{
+  using x86::xmin; using x86::xmax; using x86::fxor; using x86::fu;
+  using x86::cvtt; using x86::i2f; using x86::rcp; using x86::pack_depth;
+  float ext[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) ext[i] = o.sub(bmax[i], bmin[i]);
   const float* col0 = V.cols;
   const float* col1 = V.cols + 4;
   const float* col2 = V.cols + 8;
@@ -182,6 +195,15 @@ __device__ __forceinline__ int query_front_t(Ops& o, const ViewDesc& V, const fl
   rect[3] = (uint32_t)b[3];
   *maxZOut = maxZ;
   return 2;
+}
+
+// Returns 0 (not visible), 1 (visible, needs clipping) or 2 (rect + maxZ for query2D).
+template <class Ops>
+__device__ __forceinline__ int query_front_t(Ops& o, const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect,
+                                             uint32_t* maxZOut, uint32_t* minZOut = nullptr)
+{
+  if (query_outside_t(o, V, bmin, bmax)) return 0;
+  return query_project_t(o, V, bmin, bmax, rect, maxZOut, minZOut);
 }
 
 static __device__ __noinline__ int query_front_exact(const ViewDesc& V, const float* bmin, const float* bmax, uint32_t* rect,

@@ -134,11 +134,18 @@ struct FrameHeader {
   uint32_t pad2;
 };
 
+// k_query forms: kQueryPerThread runs one box per thread in place; 1..kQueryRounds
+// are the compacting CTAs with that many rounds of 256 slots each.
+constexpr uint32_t kQueryRounds = 4;
+constexpr uint32_t kQueryPerThread = 255;
+
 // Launch shape of one flush (0 = the default: as many resident CTAs per SM
 // as the kernel's registers and shared memory allow; one tile per fetch).
 // Chosen per batch by occ_batch_autotune.
 struct LaunchTuning {
-  uint32_t setupPerSm, fillPerSm, walkPerSm, rasterPerSm, rasterChunk, pad[3];
+  uint32_t setupPerSm, fillPerSm, walkPerSm, rasterPerSm, rasterChunk;
+  uint32_t queryRounds;  // 0: chosen by slot count; else a k_query form (above)
+  uint32_t pad[2];
 };
 
 struct FrameParams {

@@ -313,6 +313,48 @@ def test_query_special_values(ctx):
     assert vis.sum() > 0 and (~vis).sum() > 0
 
 
+@pytest.mark.parametrize("form", [255, 1, 2, 3, 4])
+def test_query_forms(ctx, form):
+    """Both query kernels -- one box per thread, and frustum survivors
+    compacted per CTA over 1-4 rounds of 256 slots -- give the oracle's bits,
+    special values (NaN, infinities, huge and signed-zero coordinates) included,
+    over views whose slot ranges share CTAs (one view without boxes)."""
+    from helpers import special_boxes
+    occ = boxes_occluders()
+    scene = to_baked(occ)
+    sizes = [(640, 360), (320, 200), (512, 512), (64, 64), (256, 128)]
+    counts = [5000, 3000, 0, 90, 700]
+    views, orcs = [], []
+    for i, ((w, h), n) in enumerate(zip(sizes, counts)):
+        mvp = scenes.view_projection((3.0 + 4 * i, 2.0, -50.0), (0.0, -0.05, 1.0), aspect=w / h)
+        if i == 1:
+            mins, maxs = special_boxes(n, seed=61)
+        elif n:
+            mins, maxs = scenes.query_boxes(n, seed=80 + i)
+        else:
+            mins = maxs = None
+        views.append(dict(raster=api.Rasterizer(ctx, w, h), mvp=mvp, clear=True, occluders=occ,
+                          flags=np.full(len(occ), 2, np.uint8), mins=mins, maxs=maxs))
+        orc = Oracle(w, h)
+        orc.frame_plain(scene, mvp)
+        orcs.append(orc)
+    b = api.PreparedBatch(ctx, views)  # runs the frame once to prepare
+    b.setTuning({"query_rounds": form})
+    b.launch()
+    assert b.check()
+    for v, (view, orc) in enumerate(zip(views, orcs)):
+        orc.frame_plain(scene, view["mvp"])  # the same frame again: the launch
+        vis, nc = b.results(v)
+        if view["mins"] is None:
+            assert len(vis) == 0
+            continue
+        ovis, onc = orc.query(view["mins"], view["maxs"])
+        assert not mismatch_report(f"visible view {v}", vis.astype(np.uint8), ovis)
+        assert not mismatch_report(f"needsClipping view {v}", nc.astype(np.uint8), onc)
+        _compare(view["raster"], orc, ("depth", "hiz"))
+    b.close()
+
+
 def test_bulk_matrices_and_results(ctx):
     """Matrices of many views in one call and every view's bits in one copy
     give what the per-view calls give."""
