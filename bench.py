@@ -481,6 +481,19 @@ def run_large(ctx, net, dev):
     mesh = scenes.city_scene(grid=128, target_tris=2_000_000)
     occ = api.bake_scene(mesh.vertices, mesh.indices)
     bake_s = t.lap()
+    # the baked occluder file: save once, then time a load against the bake
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "city2m.occ")
+        api.save_occluders(path, occ)
+        t0 = time.perf_counter()
+        loaded = api.load_occluders(path)
+        load_s = time.perf_counter() - t0
+        file_bytes = os.path.getsize(path)
+    same = len(loaded) == len(occ) and all(
+        a.packetCount == b.packetCount and np.array_equal(a.packed[:8 * a.packetCount], b.packed)
+        for a, b in zip(occ, loaded))
+    del loaded
+    t.lap()
     centers = np.stack([o.center for o in occ])
     quads = np.array([o.quads for o in occ])
     pmin, pmax = scenes.query_boxes(LARGE_NQ, seed=45, footprint=600.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
@@ -524,7 +537,10 @@ def run_large(ctx, net, dev):
     return {"workload": f"2M-triangle city ({mesh.triangles} tris -> {int(quads.sum())} quads in {len(occ)} "
                         f"occluders), one 3840x2160 main view + 63 mixed views per launch, {nq} query boxes "
                         f"per launch ({LARGE_NQ} pool)",
-            "bake_seconds": bake_s, "k_fraction": k, "learned": a.as_dict(), "nearest_first": b.as_dict(),
+            "bake_seconds": bake_s,
+            "baked_file": {"load_seconds": load_s, "bytes": file_bytes, "identical": bool(same),
+                           "speedup_vs_bake": bake_s / max(load_s, 1e-9)},
+            "k_fraction": k, "learned": a.as_dict(), "nearest_first": b.as_dict(),
             "plain": out["plain"], "batched_learned": out["learned"],
             "speedup_vs_plain_batched": out["learned"]["views_per_s"] / out["plain"]["views_per_s"],
             "seconds": t.lap() + bake_s}

@@ -29,6 +29,7 @@ extern "C" {
 #define OCC_ERR_CUDA (-3)
 #define OCC_ERR_CAPACITY (-4)
 #define OCC_ERR_UNSUPPORTED (-5)
+#define OCC_ERR_IO (-6)          /* a file could not be read or written, or is not valid */
 
 typedef struct occ_ctx_s* occ_ctx;
 typedef struct occ_raster_s* occ_raster;
@@ -105,6 +106,16 @@ int occ_raster_query2d(occ_raster r, uint32_t minX, uint32_t maxX, uint32_t minY
                        int* visible);
 /* Rasterizer::readBackDepth (Rasterizer.cpp:351-399): width*height RGBA8. */
 int occ_raster_read_back_depth(occ_raster r, void* rgba);
+/* readBackDepth and the values it computes on the way to its bytes, for
+ * debugging and visualisation: width*height row-major elements; blocks with
+ * hiZ == 1 (cleared) give 0 in every format, as the reference's bytes do. */
+enum {
+  OCC_READBACK_RGBA8 = 0,      /* the reference's bytes, as occ_raster_read_back_depth */
+  OCC_READBACK_LINEAR_F32 = 1, /* float linDepth = 0.5 / (1000.25 - (1 - depth) * 999.75) (:381) */
+  OCC_READBACK_DEPTH_F32 = 2,  /* float depth = float bits (u16 << 12) * 3.9623753e28 (:378-379) */
+  OCC_READBACK_PACKED_U16 = 3  /* the packed 16-bit depth itself, block layout undone */
+};
+int occ_raster_read_back(occ_raster r, int format, void* out);
 /* Raw buffers in the reference's layout: depth width*height u16 (8x8 blocks,
  * block-major, 8 rows of 8 pixels), hiZ blocks+8 u16. */
 int occ_raster_read_depth_raw(occ_raster r, uint16_t* out);
@@ -248,6 +259,28 @@ int occ_sah_generate_batches(const float* aabbs, uint32_t n, uint32_t targetSize
 int occ_occluder_bake(const float* vertices, uint32_t nVertices, const float refMin[4], const float refMax[4],
                       uint32_t* packedOut, uint32_t* packetCount, float boundsMin[4], float boundsMax[4],
                       float center[4]);
+
+/* ---- files (host) ----------------------------------------------------------------
+ * The reference demo's mesh files (Main.cpp:56-84): VertexBuffer.bin, raw
+ * float4 vertices; IndexBuffer.bin, raw u32 triangle indices.  With vertices
+ * and indices NULL only the counts are returned; otherwise *numVertices and
+ * *numIndices give the buffers' capacities on input and the counts on output. */
+int occ_mesh_load_bin(const char* vertexPath, const char* indexPath, float* vertices, uint32_t* numVertices,
+                      uint32_t* indices, uint32_t* numIndices);
+/* Baked occluders of a scene in one file (versioned, hashed; no reference
+ * counterpart: the demo bakes at every start, Main.cpp:86-128).  Occluder k:
+ * packetCounts[k] 32-byte vectors at packed[k] (Occluder.h:19-20) and
+ * bounds[20k..20k+19] = refMin, refMax, boundsMin, boundsMax, center (4 floats
+ * each, Occluder.h:12-16).  Written to path + ".part", then renamed. */
+int occ_occluders_save(const char* path, uint32_t count, const uint32_t* packetCounts, const uint32_t* const* packed,
+                       const float* bounds);
+/* Occluder count and packed words (sum of 8 * packetCount) of a baked file. */
+int occ_occluders_file_info(const char* path, uint32_t* count, uint64_t* words);
+/* Loads a baked file into caller buffers sized by occ_occluders_file_info:
+ * packetCounts[count], packed[words] (occluders back to back), bounds[20 * count]. */
+int occ_occluders_load(const char* path, uint32_t capacityCount, uint64_t capacityWords, uint32_t* packetCounts,
+                       uint32_t* packed, float* bounds);
+
 /* The coverage-mask table as the reference builds it on this host
  * (Rasterizer.cpp:547-604) and the table the GPU uses (generated on x86-64). */
 int occ_build_coverage_table(int64_t* out4096);

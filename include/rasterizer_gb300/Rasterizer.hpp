@@ -94,6 +94,58 @@ struct Occluder {
   mutable occ_occluder m_id = 0;
 };
 
+// The reference demo's mesh files (Main.cpp:56-84): dir/VertexBuffer.bin and
+// dir/IndexBuffer.bin.
+inline void loadMeshBin(const std::string& dir, std::vector<Vec4>& vertices, std::vector<uint32_t>& indices)
+{
+  const std::string vp = dir + "/VertexBuffer.bin", ip = dir + "/IndexBuffer.bin";
+  uint32_t nv = 0, ni = 0;
+  check(occ_mesh_load_bin(vp.c_str(), ip.c_str(), nullptr, &nv, nullptr, &ni), "occ_mesh_load_bin");
+  vertices.resize(nv ? nv : 1);
+  indices.resize(ni ? ni : 1);
+  check(occ_mesh_load_bin(vp.c_str(), ip.c_str(), &vertices[0].v[0], &nv, indices.data(), &ni), "occ_mesh_load_bin");
+  vertices.resize(nv);
+  indices.resize(ni);
+}
+
+// Baked occluders of a scene in one file, and back.
+inline void saveOccluders(const std::string& path, const std::vector<std::unique_ptr<Occluder>>& occluders)
+{
+  std::vector<uint32_t> counts;
+  std::vector<const uint32_t*> packed;
+  std::vector<float> bounds;
+  for (const auto& o : occluders) {
+    counts.push_back(o->m_packetCount);
+    packed.push_back(o->m_vertexData.data());
+    for (const Vec4* b : {&o->m_refMin, &o->m_refMax, &o->m_boundsMin, &o->m_boundsMax, &o->m_center})
+      bounds.insert(bounds.end(), b->v, b->v + 4);
+  }
+  check(occ_occluders_save(path.c_str(), (uint32_t)occluders.size(), counts.data(), packed.data(), bounds.data()),
+        "occ_occluders_save");
+}
+
+inline std::vector<std::unique_ptr<Occluder>> loadOccluders(const std::string& path)
+{
+  uint32_t n = 0;
+  uint64_t words = 0;
+  check(occ_occluders_file_info(path.c_str(), &n, &words), "occ_occluders_file_info");
+  std::vector<uint32_t> counts(n ? n : 1), packed(words ? words : 1);
+  std::vector<float> bounds(20 * (size_t)(n ? n : 1));
+  check(occ_occluders_load(path.c_str(), n, words, counts.data(), packed.data(), bounds.data()), "occ_occluders_load");
+  std::vector<std::unique_ptr<Occluder>> out;
+  size_t pos = 0;
+  for (uint32_t k = 0; k < n; ++k) {
+    auto o = std::make_unique<Occluder>();
+    o->m_packetCount = counts[k];
+    o->m_vertexData.assign(packed.begin() + pos, packed.begin() + pos + 8 * (size_t)counts[k]);
+    pos += 8 * (size_t)counts[k];
+    Vec4* dst[5] = {&o->m_refMin, &o->m_refMax, &o->m_boundsMin, &o->m_boundsMax, &o->m_center};
+    for (int j = 0; j < 5; ++j) std::memcpy(dst[j]->v, &bounds[20 * (size_t)k + 4 * j], 16);
+    out.push_back(std::move(o));
+  }
+  return out;
+}
+
 class Rasterizer {
  public:
   Rasterizer(Context& ctx, uint32_t width, uint32_t height) : ctx_(ctx), w_(width), h_(height)
@@ -139,6 +191,8 @@ class Rasterizer {
   }
 
   void readBackDepth(void* target) const { check(occ_raster_read_back_depth(r_, target), "occ_raster_read_back_depth"); }
+  // OCC_READBACK_* format: width*height elements of 4 (RGBA8, float) or 2 (u16) bytes
+  void readBack(int format, void* target) const { check(occ_raster_read_back(r_, format, target), "occ_raster_read_back"); }
 
   // Batch form of queryVisibility: one bit per box (bit i%32 of word i/32).
   void queryVisibilityBatch(uint32_t n, const Vec4* mins, const Vec4* maxs, uint32_t* visibleBits,

@@ -63,6 +63,7 @@ def oracle_lib():
         lib.orc_query2d.argtypes = [P, U32, U32, U32, U32, U32]
         lib.orc_query_batch.argtypes = [P, U32, P, P, P, P]
         lib.orc_read_back.argtypes = [P, P]
+        lib.orc_read_back_values.argtypes = [P, C.c_int, P]
         lib.orc_read_depth.argtypes = [P, P]
         lib.orc_read_hiz.argtypes = [P, P]
         lib.orc_read_hiz.restype = U32
@@ -208,6 +209,14 @@ class Oracle:
     def read_back(self):
         out = np.zeros(self.width * self.height * 4, np.uint8)
         self.lib.orc_read_back(self.h, _ptr(out))
+        return out
+
+    def read_back_values(self, format: str):
+        """(height, width) float linDepth ("linear"), float depth ("depth") or
+        u16 packed depth ("packed"), row-major; 0 in cleared blocks."""
+        code, dt = {"linear": (1, np.float32), "depth": (2, np.float32), "packed": (3, np.uint16)}[format]
+        out = np.zeros((self.height, self.width), dt)
+        self.lib.orc_read_back_values(self.h, code, _ptr(out))
         return out
 
     def write_depth(self, d):

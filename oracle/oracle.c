@@ -770,6 +770,25 @@ void orc_read_back(const orc_raster* r, uint8_t* rgba)
     }
 }
 
+/* The values readBackDepth computes on the way to its bytes (:378-381), row-major,
+   0 in cleared blocks: format 1 float linDepth, 2 float depth, 3 u16 packed depth. */
+void orc_read_back_values(const orc_raster* r, int format, void* out)
+{
+  const float invBias = 3.9623753e+28f;
+  for (uint32_t y = 0; y < r->height; ++y)
+    for (uint32_t x = 0; x < r->width; ++x) {
+      const uint32_t blk = (y >> 3) * r->blocksX + (x >> 3);
+      const size_t o = (size_t)y * r->width + x;
+      const int cleared = r->hiz[blk] == 1;
+      const uint32_t v = cleared ? 0u : r->depth[(size_t)blk * 64 + 8 * (y & 7) + (x & 7)];
+      const float depth = xmul(uf(v << 12), invBias);
+      const float lin = xdiv(2 * 0.25f, xsub(0.25f + 1000.0f, xmul(xsub(1.0f, depth), 1000.0f - 0.25f)));
+      if (format == 3) ((uint16_t*)out)[o] = (uint16_t)v;
+      else if (format == 2) ((float*)out)[o] = cleared ? 0.0f : depth;
+      else ((float*)out)[o] = cleared ? 0.0f : lin;
+    }
+}
+
 void orc_read_depth(const orc_raster* r, uint16_t* out) { memcpy(out, r->depth, (size_t)r->width * r->height * 2); }
 uint32_t orc_read_hiz(const orc_raster* r, uint16_t* out)
 {

@@ -50,6 +50,7 @@ void orc_query_batch(orc_raster* r, uint32_t n, const float* mins, const float* 
                      uint8_t* visible, uint8_t* needsClipping);
 
 void orc_read_back(const orc_raster* r, uint8_t* rgba);     /* :351-399 */
+void orc_read_back_values(const orc_raster* r, int format, void* out); /* :378-381 */
 void orc_read_depth(const orc_raster* r, uint16_t* out);    /* width*height u16, block-major */
 uint32_t orc_read_hiz(const orc_raster* r, uint16_t* out);  /* blocks+8 u16; returns count */
 void orc_read_table(const orc_raster* r, int64_t* out);     /* 4096 masks */

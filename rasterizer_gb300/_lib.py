@@ -48,6 +48,7 @@ SIGNATURES = {
     "occ_raster_query_batch_noalloc": (I32, [P, U32, P, P, P, P]),
     "occ_raster_query2d": (I32, [P, U32, U32, U32, U32, U32, C.POINTER(I32)]),
     "occ_raster_read_back_depth": (I32, [P, P]),
+    "occ_raster_read_back": (I32, [P, I32, P]),
     "occ_raster_read_depth_raw": (I32, [P, P]),
     "occ_raster_read_hiz": (I32, [P, P, C.POINTER(U32)]),
     "occ_raster_write_depth_raw": (I32, [P, P]),
@@ -88,6 +89,10 @@ SIGNATURES = {
     "occ_quad_decompose": (I32, [P, U32, P, U32, P, C.POINTER(U32)]),
     "occ_sah_generate_batches": (I32, [P, U32, U32, U32, P, P, C.POINTER(U32)]),
     "occ_occluder_bake": (I32, [P, U32, P, P, P, C.POINTER(U32), P, P, P]),
+    "occ_mesh_load_bin": (I32, [C.c_char_p, C.c_char_p, P, C.POINTER(U32), P, C.POINTER(U32)]),
+    "occ_occluders_save": (I32, [C.c_char_p, U32, P, P, P]),
+    "occ_occluders_file_info": (I32, [C.c_char_p, C.POINTER(U32), C.POINTER(C.c_uint64)]),
+    "occ_occluders_load": (I32, [C.c_char_p, U32, C.c_uint64, P, P, P]),
     "occ_build_coverage_table": (I32, [P]),
     "occ_coverage_table": (I32, [P]),
 }

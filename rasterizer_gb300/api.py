@@ -8,6 +8,7 @@ asserts become ValueError; GPU or allocation failures raise OccError.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import itertools
 import weakref
 from dataclasses import dataclass, field
@@ -162,6 +163,59 @@ def bake_scene(vertices, indices, targetSize: int = 512, splitGranularity: int =
     return [Occluder.bake(corners[b].reshape(-1, 4), refMin, refMax) for b in batches]
 
 
+def load_mesh_bin(directory: str | None = None, vertex_path: str | None = None, index_path: str | None = None):
+    """The reference demo's mesh files (Main.cpp:56-84): VertexBuffer.bin
+    (float4 vertices) and IndexBuffer.bin (u32 triangle indices) in
+    `directory`, or at the two paths given.  Returns (vertices (n, 4) float32,
+    indices uint32)."""
+    if directory is not None:
+        vertex_path = vertex_path or os.path.join(directory, "VertexBuffer.bin")
+        index_path = index_path or os.path.join(directory, "IndexBuffer.bin")
+    if not vertex_path or not index_path:
+        raise ValueError("give a directory or both file paths")
+    vp, ip = os.fsencode(vertex_path), os.fsencode(index_path)
+    nv, ni = C.c_uint32(), C.c_uint32()
+    check(lib().occ_mesh_load_bin(vp, ip, None, C.byref(nv), None, C.byref(ni)), "occ_mesh_load_bin")
+    v = np.zeros((max(nv.value, 1), 4), np.float32)
+    i = np.zeros(max(ni.value, 1), np.uint32)
+    check(lib().occ_mesh_load_bin(vp, ip, _ptr(v), C.byref(nv), _ptr(i), C.byref(ni)), "occ_mesh_load_bin")
+    return v[:nv.value].copy(), i[:ni.value].copy()
+
+
+def save_occluders(path: str, occluders: list[Occluder]) -> None:
+    """Writes baked occluders to one file (versioned, hashed), so that a
+    program can load them instead of baking again."""
+    n = len(occluders)
+    counts = np.array([o.packetCount for o in occluders], np.uint32)
+    bufs = [np.ascontiguousarray(o.packed[:8 * o.packetCount], np.uint32) for o in occluders]
+    ptrs = (C.c_void_p * max(n, 1))(*[b.ctypes.data for b in bufs])
+    bounds = np.zeros((max(n, 1), 20), np.float32)
+    for k, o in enumerate(occluders):
+        bounds[k] = np.concatenate([o.refMin, o.refMax, o.boundsMin, o.boundsMax, o.center])
+    check(lib().occ_occluders_save(os.fsencode(path), n, _ptr(counts), C.cast(ptrs, C.c_void_p), _ptr(bounds)),
+          "occ_occluders_save")
+
+
+def load_occluders(path: str) -> list[Occluder]:
+    """Occluders written by save_occluders, in the same order."""
+    p = os.fsencode(path)
+    n, w = C.c_uint32(), C.c_uint64()
+    check(lib().occ_occluders_file_info(p, C.byref(n), C.byref(w)), "occ_occluders_file_info")
+    counts = np.zeros(max(n.value, 1), np.uint32)
+    packed = np.zeros(max(w.value, 1), np.uint32)
+    bounds = np.zeros((max(n.value, 1), 20), np.float32)
+    check(lib().occ_occluders_load(p, n.value, w.value, _ptr(counts), _ptr(packed), _ptr(bounds)),
+          "occ_occluders_load")
+    out, pos = [], 0
+    for k in range(n.value):
+        c = int(counts[k])
+        b = bounds[k]
+        out.append(Occluder(packed[pos:pos + 8 * c].copy(), c, b[0:4].copy(), b[4:8].copy(), b[8:12].copy(),
+                            b[12:16].copy(), b[16:20].copy()))
+        pos += 8 * c
+    return out
+
+
 def _xmin(a, b):  # minps: the second operand unless a < b
     return np.where(a < b, a, b)
 
@@ -280,6 +334,20 @@ class Rasterizer:
         """Rasterizer::readBackDepth -> (height, width, 4) uint8."""
         out = np.zeros((self.height, self.width, 4), np.uint8)
         check(lib().occ_raster_read_back_depth(self.handle, _ptr(out)), "occ_raster_read_back_depth")
+        return out
+
+    def readBack(self, format: str = "rgba8") -> np.ndarray:
+        """readBackDepth and its intermediate values, (height, width[, 4]):
+        "rgba8" (the reference's bytes), "linear" (float linDepth), "depth"
+        (float depth), "packed" (the u16 packed depth, block layout undone).
+        Cleared blocks are 0."""
+        kinds = {"rgba8": (0, np.uint8, 4), "linear": (1, np.float32, 1), "depth": (2, np.float32, 1),
+                 "packed": (3, np.uint16, 1)}
+        if format not in kinds:
+            raise ValueError(f"unknown read-back format {format!r}")
+        code, dt, ch = kinds[format]
+        out = np.zeros((self.height, self.width, ch) if ch > 1 else (self.height, self.width), dt)
+        check(lib().occ_raster_read_back(self.handle, code, _ptr(out)), "occ_raster_read_back")
         return out
 
     def readDepthRaw(self) -> np.ndarray:

@@ -23,7 +23,7 @@ NVCC_FLAGS = ARCH + ["-O3", "--fmad=false", "-ftz=false", "-prec-div=true", "-pr
 CXX_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c++17", "-I" + CSRC, "-I" + INCLUDE]
 
 CU_SOURCES = ["kernels.cu", "learned.cu", "capi.cu"]
-CXX_SOURCES = ["bake.cpp"]
+CXX_SOURCES = ["bake.cpp", "files.cpp"]
 
 
 def _nvcc() -> str:

@@ -21,7 +21,7 @@ namespace occ {
 cudaError_t launch_flush(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
                          bool doQuery, cudaStream_t stream);
 cudaError_t launch_read_back(const uint16_t* depth, const uint16_t* hiz, uint32_t width, uint32_t height,
-                             uchar4* out, cudaStream_t stream);
+                             int format, void* out, cudaStream_t stream);
 cudaError_t launch_flush_timed(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
                                bool doQuery, cudaStream_t stream, cudaEvent_t* ev);
 cudaError_t set_kernel_attributes();
@@ -45,6 +45,7 @@ cudaError_t launch_tile_hiz(const uint16_t* hiz, uint16_t* tileHiz, uint32_t blo
                             cudaStream_t stream);
 cudaError_t launch_query2d(const ViewDesc* view, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY,
                            uint32_t maxZ, uint32_t* out, cudaStream_t stream);
+int set_error(int code, const char* msg);
 }  // namespace occ
 
 using namespace occ;
@@ -58,6 +59,16 @@ int fail(int code, const std::string& msg)
   g_error = msg;
   return code;
 }
+
+}  // namespace
+
+// The message occ_last_error returns, for the host-only sources (files.cpp).
+int occ::set_error(int code, const char* msg)
+{
+  return fail(code, msg);
+}
+
+namespace {
 
 #define OCC_CUDA(call)                                                                      \
   do {                                                                                      \
@@ -775,18 +786,26 @@ int occ_raster_query2d(occ_raster r, uint32_t minX, uint32_t maxX, uint32_t minY
   return OCC_OK;
 }
 
-int occ_raster_read_back_depth(occ_raster r, void* rgba)
+static_assert(kReadBackRgba8 == OCC_READBACK_RGBA8 && kReadBackLinearF32 == OCC_READBACK_LINEAR_F32 &&
+                  kReadBackDepthF32 == OCC_READBACK_DEPTH_F32 && kReadBackPackedU16 == OCC_READBACK_PACKED_U16,
+              "read-back format codes");
+
+int occ_raster_read_back(occ_raster r, int format, void* out)
 {
-  if (!r || !rgba) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (!r || !out) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (format < OCC_READBACK_RGBA8 || format > OCC_READBACK_PACKED_U16) return fail(OCC_ERR_INVALID_ARG, "unknown format");
   OCC_CHECK(flush_raster(r, nullptr));
   occ_ctx_s* ctx = r->ctx;
-  DevBuf<uchar4> out;
-  OCC_CHECK(out.reserve((size_t)r->width * r->height));
-  OCC_CUDA(launch_read_back(r->depth.p, r->hiz.p, r->width, r->height, out.p, ctx->stream));
-  OCC_CUDA(cudaMemcpyAsync(rgba, out.p, (size_t)r->width * r->height * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  const size_t bytes = (size_t)r->width * r->height * (format == OCC_READBACK_PACKED_U16 ? 2 : 4);
+  DevBuf<uint8_t> dev;
+  OCC_CHECK(dev.reserve(bytes));
+  OCC_CUDA(launch_read_back(r->depth.p, r->hiz.p, r->width, r->height, format, dev.p, ctx->stream));
+  OCC_CUDA(cudaMemcpyAsync(out, dev.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   OCC_CUDA(cudaStreamSynchronize(ctx->stream));
   return OCC_OK;
 }
+
+int occ_raster_read_back_depth(occ_raster r, void* rgba) { return occ_raster_read_back(r, OCC_READBACK_RGBA8, rgba); }
 
 int occ_raster_read_depth_raw(occ_raster r, uint16_t* out)
 {

@@ -1590,24 +1590,41 @@ __global__ void k_query2d(const ViewDesc* V, uint32_t minX, uint32_t maxX, uint3
 
 // ---- readBackDepth (Rasterizer.cpp:351-399) ---------------------------------------------
 
+// readBackDepth (Rasterizer.cpp:351-399) and the values it computes on the way
+// to its RGBA bytes, one pixel per thread, row-major output; cleared blocks
+// (hiZ == 1) give zero in every format.
 __global__ void __launch_bounds__(256) k_read_back(const uint16_t* depth, const uint16_t* hiz, uint32_t width,
-                                                   uint32_t height, uint32_t blocksX, uchar4* out)
+                                                   uint32_t height, uint32_t blocksX, int format, void* out)
 {
   const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t py = blockIdx.y;
   if (px >= width || py >= height) return;
   const uint32_t bx = px >> 3, by = py >> 3, blk = by * blocksX + bx;
+  const size_t o = (size_t)py * width + px;
+  const bool cleared = hiz[blk] == 1;
+  const uint32_t v = cleared ? 0u : depth[(size_t)blk * 64 + 8 * (py & 7) + (px & 7)];
+  if (format == kReadBackPackedU16) {
+    static_cast<uint16_t*>(out)[o] = (uint16_t)v;
+    return;
+  }
+  const float d = x86::rmul(__uint_as_float(v << 12), 3.9623753e+28f);  // :378-379
+  if (format == kReadBackDepthF32) {
+    static_cast<float*>(out)[o] = cleared ? 0.0f : d;
+    return;
+  }
+  const float lin = x86::rdiv(0.5f, x86::rsub(1000.25f, x86::rmul(x86::rsub(1.0f, d), 999.75f)));  // :381
+  if (format == kReadBackLinearF32) {
+    static_cast<float*>(out)[o] = cleared ? 0.0f : lin;
+    return;
+  }
   uchar4 res = make_uchar4(0, 0, 0, 0);
-  if (hiz[blk] != 1) {
-    const uint32_t v = depth[(size_t)blk * 64 + 8 * (py & 7) + (px & 7)];
-    const float d = x86::rmul(__uint_as_float(v << 12), 3.9623753e+28f);
-    const float lin = x86::rdiv(0.5f, x86::rsub(1000.25f, x86::rmul(x86::rsub(1.0f, d), 999.75f)));
+  if (!cleared) {
     const float s = x86::rmul(25600.0f, lin);
     // static_cast<uint32_t>(float) on x86-64: 64-bit truncation, low 32 bits
     const uint32_t di = (s > -9.2233720e18f && s < 9.2233720e18f) ? (uint32_t)(unsigned long long)__float2ll_rz(s) : 0u;
     res = make_uchar4((unsigned char)(di / 100), (unsigned char)(di % 256), 0, 255);
   }
-  out[(size_t)py * width + px] = res;
+  static_cast<uchar4*>(out)[o] = res;
 }
 
 // ---- launchers -------------------------------------------------------------------------
@@ -1682,10 +1699,10 @@ cudaError_t launch_flush_timed(const FrameParams& P, uint32_t numSt, uint32_t ma
 }
 
 cudaError_t launch_read_back(const uint16_t* depth, const uint16_t* hiz, uint32_t width, uint32_t height,
-                             uchar4* out, cudaStream_t stream)
+                             int format, void* out, cudaStream_t stream)
 {
   dim3 grid((width + 255) / 256, height);
-  k_read_back<<<grid, 256, 0, stream>>>(depth, hiz, width, height, width / 8, out);
+  k_read_back<<<grid, 256, 0, stream>>>(depth, hiz, width, height, width / 8, format, out);
   return cudaGetLastError();
 }
 

@@ -134,6 +134,9 @@ struct FrameHeader {
   uint32_t pad2;
 };
 
+// readBack formats (the OCC_READBACK_* values of the C ABI).
+constexpr int kReadBackRgba8 = 0, kReadBackLinearF32 = 1, kReadBackDepthF32 = 2, kReadBackPackedU16 = 3;
+
 // k_query forms: kQueryPerThread runs one box per thread in place; 1..kQueryRounds
 // are the compacting CTAs with that many rounds of 256 slots each.
 constexpr uint32_t kQueryRounds = 4;

@@ -81,3 +81,37 @@ def special_boxes(n: int, seed: int, footprint: float = 100.0, nan: bool = True)
         if rng.random() < 0.03:
             (mins if rng.random() < 0.5 else maxs)[i, 3] = special[int(rng.integers(0, len(special)))]
     return mins, maxs
+
+
+def encode_linear(lin: np.ndarray) -> np.ndarray:
+    """readBackDepth's bytes from its linear depth (Rasterizer.cpp:383-395):
+    d = uint(25600 * lin), RGBA = (d / 100, d % 256, 0, 255); cleared pixels
+    (packed depth 0 from a cleared block) are all zero.  (height, width, 4)."""
+    s = np.float32(100 * 256) * lin.astype(np.float32)
+    d = s.astype(np.uint64).astype(np.uint32)
+    out = np.zeros(lin.shape + (4,), np.uint8)
+    out[..., 0] = (d // 100).astype(np.uint8)
+    out[..., 1] = (d % 256).astype(np.uint8)
+    out[..., 3] = 255
+    return out
+
+
+def read_back_consistent(rgba: np.ndarray, lin: np.ndarray, depth: np.ndarray, packed: np.ndarray,
+                         cleared: np.ndarray) -> list[str]:
+    """The read-back formats agree with each other: bytes from linDepth,
+    linDepth from depth, depth from the packed value; cleared pixels zero."""
+    errs = []
+    enc = encode_linear(lin)
+    enc[cleared] = 0
+    if not np.array_equal(enc, rgba.reshape(enc.shape)):
+        errs.append("rgba8 != encode(linear)")
+    d = (packed.astype(np.uint32) << 12).view(np.float32) * np.float32(3.9623753e+28)
+    d[cleared] = 0
+    if not np.array_equal(d, depth):
+        errs.append("depth != packed << 12 * 1/bias")
+    one, a, b, half = np.float32(1.0), np.float32(1000.25), np.float32(999.75), np.float32(0.5)
+    l = half / (a - (one - depth) * b)
+    l[cleared] = 0
+    if not np.array_equal(l, lin):
+        errs.append("linear != 0.5 / (1000.25 - (1 - depth) * 999.75)")
+    return errs

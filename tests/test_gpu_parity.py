@@ -355,6 +355,26 @@ def test_query_forms(ctx, form):
     b.close()
 
 
+def test_read_back_formats(ctx):
+    """Every read-back format (the reference's RGBA bytes, float linDepth,
+    float depth, packed u16) == the oracle's, after a city frame with stale
+    and cleared blocks."""
+    occ = city_occluders()
+    scene = to_baked(occ)
+    w, h = 960, 544
+    mvps, _ = scenes.camera_path(10, seed=33, width=w, height_px=h)
+    r = api.Rasterizer(ctx, w, h)
+    orc = Oracle(w, h)
+    for f in (0, 7):
+        gpu_plain_frame(r, occ, mvps[f])
+        orc.frame_plain(scene, mvps[f])
+    assert not mismatch_report("rgba8", r.readBack("rgba8").ravel(), orc.read_back())
+    for k in ("linear", "depth", "packed"):
+        got, want = r.readBack(k), orc.read_back_values(k)
+        assert not mismatch_report(k, got.view(np.uint32 if got.dtype == np.float32 else np.uint16),
+                                   want.view(np.uint32 if want.dtype == np.float32 else np.uint16))
+
+
 def test_bulk_matrices_and_results(ctx):
     """Matrices of many views in one call and every view's bits in one copy
     give what the per-view calls give."""

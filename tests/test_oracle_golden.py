@@ -55,6 +55,22 @@ def test_small_frame_raw():
     assert np.array_equal(orc.read_back(), SMALL["readback"])
 
 
+def test_read_back_formats_consistent():
+    """The oracle's read-back values (float linDepth, float depth, packed u16)
+    reproduce its readBackDepth bytes, which are pinned to the reference."""
+    from helpers import read_back_consistent
+    sc = to_baked(boxes_occluders())
+    orc = Oracle(320, 200)
+    orc.frame_plain(sc, SMALL["mvp"])
+    hiz = orc.hiz()[:40 * 25].reshape(25, 40)
+    cleared = np.repeat(np.repeat(hiz == 1, 8, axis=0), 8, axis=1)
+    lin, depth, packed = (orc.read_back_values(k) for k in ("linear", "depth", "packed"))
+    assert cleared.any() and (~cleared).any()
+    assert not read_back_consistent(orc.read_back(), lin, depth, packed, cleared)
+    raw = orc.depth().reshape(25, 40, 8, 8).transpose(0, 2, 1, 3).reshape(200, 320)
+    assert np.array_equal(np.where(cleared, 0, raw), packed)
+
+
 def _check_frame(orc, flags, vis, nc, g):
     got = {"flags": digest(flags), "depth": digest(orc.depth()), "hiz": digest(orc.hiz()),
            "visible": digest(vis), "needsClipping": digest(nc), "readback": digest(orc.read_back())}

@@ -31,6 +31,15 @@ def _mesh(name):
     return v, i
 
 
+def test_mesh_loader_reads_the_reference_meshes():
+    """load_mesh_bin reads the reference's own mesh files (Main.cpp:56-84) as
+    the demo does: whole files, float4 vertices, u32 indices."""
+    for name in MESHES:
+        v, i = api.load_mesh_bin(os.path.join(bindings.REF_SOURCES, name))
+        rv, ri = _mesh(name)
+        assert np.array_equal(v.view(np.uint32), rv.view(np.uint32)) and np.array_equal(i, ri)
+
+
 @pytest.fixture(scope="module", params=list(MESHES))
 def mesh(request):
     v, i = _mesh(request.param)
