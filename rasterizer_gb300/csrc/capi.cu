@@ -159,7 +159,7 @@ struct FrameScratch {
   DevBuf<QuadWalk> walk;
   DevBuf<Totals> chunkTot, chunkBase, viewTot, viewBase;
   DevBuf<uint32_t> mat, stStart, stLen, cmdDraw, ckBase, activeChunks;
-  DevBuf<uint2> activeTiles;
+  DevBuf<uint4> activeTiles;
   DevBuf<uint4> stList;
   DevBuf<float> ck;
   DevBuf<uint2> rowOwner;  // sized like the checkpoints (a row has at least one)

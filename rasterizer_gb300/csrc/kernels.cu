@@ -1179,6 +1179,7 @@ __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
   if (threadIdx.x == 0) s_n = 0;
   __syncthreads();
   uint32_t queue = 0, slot = 0, v = 0;  // queue: bit u = raster unit u of the tile
+  uint32_t listStart = 0, listLen = 0;
   if (wt < P.numTiles) {
     v = view_of_tile(P, wt);
     const ViewDesc& V = P.views[v];
@@ -1194,6 +1195,8 @@ __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
     }
     const uint32_t s = V.stBase + (ty0 / kSuperTile) * V.stX + (tx0 / kSuperTile);
     const uint32_t len = V.cmdCount ? P.stLen[s] : 0u;
+    listLen = len;
+    listStart = len ? P.stStart[s] : 0u;
     if (len > kPrepScanMax) {
       queue = (1u << kUnitsPerTile) - 1u;
     } else if (len) {
@@ -1220,7 +1223,7 @@ __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
   if (lane == 0 && queue) {
     uint32_t k = s_base + slot;
     for (uint32_t u = 0; u < (uint32_t)kUnitsPerTile; ++u)
-      if (queue & (1u << u)) P.activeTileList[k++] = make_uint2(wt * kUnitsPerTile + u, v);
+      if (queue & (1u << u)) P.activeTileList[k++] = make_uint4(wt * kUnitsPerTile + u, v, listStart, listLen);
   }
 }
 
@@ -1248,8 +1251,9 @@ __global__ void __launch_bounds__(256) k_tile_min(FrameParams P)
 // rasterised in list order (raster_local_list) and the unit's blocks written back.
 
 template <bool kWins>
-__device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S, uint32_t unit, uint32_t v)
+__device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S, const uint4 rec)
 {
+  const uint32_t unit = rec.x, v = rec.y;
   const uint32_t tid = threadIdx.x, lane = tid & 31;
   const ViewDesc& V = P.views[v];
   const uint32_t lt = unit / kUnitsPerTile - V.tileStart;  // the warp-tile holding the unit
@@ -1264,9 +1268,8 @@ __device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S,
   bool have = false;
   uint32_t row[4] = {0, 0, 0, 0};
   uint32_t own[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  const uint32_t s = V.stBase + (ty0 / kSuperTile) * V.stX + (tx0 / kSuperTile);
-  const uint32_t listLen = V.cmdCount ? P.stLen[s] : 0;
-  const uint4* list = P.stList + (V.cmdCount ? P.stStart[s] : 0);
+  const uint32_t listLen = rec.w;  // the unit's super-tile list, from k_tile_prep
+  const uint4* list = P.stList + rec.z;
   if (py == 0) S.hiz[myBlock] = hiz;
   __syncthreads();
   uint32_t n = 0, F = 0;
@@ -1374,20 +1377,37 @@ __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) k_raster(Fra
 {
   __shared__ RasterSmem S;
   __shared__ uint32_t s_next;
+  __shared__ __align__(16) uint4 s_rec[2];  // this unit's queue record and the next one's
   if (P.header->overflow) return;
   const uint32_t nActive = P.header->activeTiles;
-  const uint32_t chunk = P.tune.rasterChunk ? P.tune.rasterChunk : 1u;  // tiles per fetch
-  if (threadIdx.x == 0) s_next = atomicAdd(&P.header->tileCursor, chunk);
+  const uint32_t chunk = P.tune.rasterChunk ? P.tune.rasterChunk : 1u;  // units per fetch
+  if (threadIdx.x == 0) {
+    const uint32_t i0 = atomicAdd(&P.header->tileCursor, chunk);
+    s_next = i0;
+    if (i0 < nActive) s_rec[0] = P.activeTileList[i0];
+  }
   __syncthreads();
-  uint32_t i = s_next;
+  uint32_t i = s_next, buf = 0;
   while (i < nActive) {
     uint32_t nxt = 0;
     if (threadIdx.x == 0) nxt = atomicAdd(&P.header->tileCursor, chunk);  // next fetch, ahead of time
     const uint32_t end = ::min(i + chunk, nActive);
     for (uint32_t j = i; j < end; ++j) {
-      const uint2 t = P.activeTileList[j];
-      raster_tile<kWins>(P, S, t.x, t.y);
-      __syncthreads();  // shared state is reused by the next tile
+      const uint4 rec = s_rec[buf];
+      if (threadIdx.x == 0) {
+        // the next unit's record, copied while this one is rasterised (the
+        // buffer it lands in was last read before the previous unit's barrier)
+        const uint32_t k = j + 1 < end ? j + 1 : nxt;
+        if (k < nActive) {
+          const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&s_rec[buf ^ 1u]);
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(P.activeTileList + k) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+      }
+      raster_tile<kWins>(P, S, rec);
+      if (threadIdx.x == 0) asm volatile("cp.async.wait_all;" ::: "memory");
+      __syncthreads();  // shared state is reused by the next unit; the next record has landed
+      buf ^= 1u;
     }
     if (threadIdx.x == 0) s_next = nxt;
     __syncthreads();

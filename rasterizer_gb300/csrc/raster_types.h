@@ -187,7 +187,8 @@ struct FrameParams {
   uint32_t* cmdDraw;     // per command: bit0 drawn (this pass), bit1 near-clipped, bit2 drawn by
                          // the first pass of this launch (second pass only)
   uint32_t* activeChunkList;  // chunks with a drawn command (header->activeChunks of them)
-  uint2* activeTileList;      // {warp-tile, view} with a non-empty super-tile list (header->activeTiles)
+  uint4* activeTileList;      // queued raster units (header->activeTiles): {unit, view, first entry and
+                              // length of the unit's super-tile list}
   // learned occluder selection and win counts (all optional)
   float* feat;           // per command: kFeatures features
   float* score;          // per command: MLP score
