@@ -254,7 +254,8 @@ int occ_quad_decompose(const uint32_t* indices, uint32_t nIndices, const float* 
  * batched quad indices (n entries), offsets numBatches+1 entries (room for n+1). */
 int occ_sah_generate_batches(const float* aabbs, uint32_t n, uint32_t targetSize, uint32_t splitGranularity,
                              uint32_t* flat, uint32_t* offsets, uint32_t* numBatches);
-/* Occluder::bake: vertices nVertices float4 (multiple of 16, quads of 4);
+/* Occluder::bake: vertices nVertices float4 (quads of 4, a multiple of 32: whole
+ * packets of 8 quads; the reference asserts 16 but reads 32 at a time);
  * packedOut nVertices words; returns the packet count (32-byte vectors). */
 int occ_occluder_bake(const float* vertices, uint32_t nVertices, const float refMin[4], const float refMax[4],
                       uint32_t* packedOut, uint32_t* packetCount, float boundsMin[4], float boundsMax[4],

@@ -91,10 +91,12 @@ class Occluder:
 
     @staticmethod
     def bake(vertices, refMin, refMax) -> "Occluder":
-        """Occluder::bake (Occluder.cpp:7-181): vertices (4 per quad, a multiple of 16)."""
+        """Occluder::bake (Occluder.cpp:7-181): vertices (4 per quad, a multiple
+        of 32: whole packets of 8 quads; the reference asserts a multiple of 16
+        at :9 but packs 32 at a time at :108-122, reading past its array)."""
         v = _f32(vertices).reshape(-1, 4)
-        if len(v) == 0 or len(v) % 16:
-            raise ValueError("vertex count must be a positive multiple of 16 (Occluder.cpp:9)")
+        if len(v) == 0 or len(v) % 32:
+            raise ValueError("vertex count must be a positive multiple of 32 (8 quads per packet)")
         rmin, rmax = _f32(refMin, (4,)), _f32(refMax, (4,))
         packed = np.zeros(len(v), np.uint32)
         pc = C.c_uint32()

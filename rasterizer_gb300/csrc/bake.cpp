@@ -466,7 +466,10 @@ int occ_occluder_bake(const float* vertices, uint32_t nVertices, const float ref
 {
   if (!vertices || !refMin || !refMax || !packedOut || !packetCount || !boundsMin || !boundsMax || !center)
     return OCC_ERR_INVALID_ARG;
-  if (nVertices == 0 || nVertices % 16 != 0) return OCC_ERR_INVALID_ARG;  // Occluder.cpp:9 (8 quads per packet)
+  // whole packets of 8 quads: the reference asserts a multiple of 16 vertices
+  // (Occluder.cpp:9) but packs 32 at a time (:108-122) and reads past its
+  // array for the other half of those counts
+  if (nVertices == 0 || nVertices % 32 != 0) return OCC_ERR_INVALID_ARG;
   const uint32_t nq = nVertices / 4;
   auto vtx = [&](uint32_t i) { return load4(vertices + 4 * (size_t)i); };
 

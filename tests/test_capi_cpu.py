@@ -53,6 +53,13 @@ def test_bake_argument_validation():
     assert lib.occ_quad_decompose(idx3.ctypes.data, 3, v.ctypes.data, 4, out.ctypes.data, C.byref(n)) == -1
     with pytest.raises(ValueError):
         api.Occluder.bake(np.zeros((15, 4), np.float32), np.zeros(4), np.ones(4))
+    # 16 vertices pass the reference's assert but its packing reads 32
+    with pytest.raises(ValueError):
+        api.Occluder.bake(np.zeros((16, 4), np.float32), np.zeros(4), np.ones(4))
+    packed, pc = np.zeros(16, np.uint32), C.c_uint32()
+    z, o = np.zeros(4, np.float32), np.ones(4, np.float32)
+    assert lib.occ_occluder_bake(np.zeros((16, 4), np.float32).ctypes.data, 16, z.ctypes.data, o.ctypes.data,
+                                 packed.ctypes.data, C.byref(pc), z.ctypes.data, z.ctypes.data, z.ctypes.data) == -1
 
 
 def test_sah_small_inputs_form_one_batch():
@@ -84,7 +91,7 @@ FACADE_PROGRAM = r"""
 int run(int argc) {
   gb300::Context ctx(0);
   gb300::Rasterizer raster(ctx, 1920, 1080);
-  std::vector<gb300::Vec4> verts(16, gb300::Vec4{{0, 0, 0, 1}});
+  std::vector<gb300::Vec4> verts(32, gb300::Vec4{{0, 0, 0, 1}});
   auto occ = gb300::Occluder::bake(verts, gb300::Vec4{{0, 0, 0, 1}}, gb300::Vec4{{1, 1, 1, 1}});
   float mvp[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 1, 0, 0, 0, 0};
   gb300::Batch::View v{&raster, mvp, {occ.get()}, {OCC_GATED}, {gb300::Vec4{{0, 0, 5, 1}}}, {gb300::Vec4{{1, 1, 6, 1}}}};
