@@ -469,6 +469,46 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
 LARGE_NQ = 1_000_000
 
 
+def _gpu_bake_timing(ctx, sets, lo, hi, host_occ, reps: int = 5) -> dict:
+    """Occluder::bake of every occluder in one GPU launch
+    (occ_occluders_bake_device), device time with CUDA events on the
+    library's stream, inputs already on the device; checked byte for byte
+    against the host bake."""
+    import torch
+    from rasterizer_gb300 import api
+    from rasterizer_gb300._lib import check, lib
+    n = len(sets)
+    starts = np.zeros(n + 1, np.uint32)
+    starts[1:] = np.cumsum([len(s) for s in sets])
+    boxes = np.tile(np.concatenate([lo, hi]), (n, 1)).astype(np.float32)
+    dev = torch.device("cuda", ctx.device)
+    dv = torch.from_numpy(np.concatenate(sets).astype(np.float32)).to(dev)
+    dp = torch.empty(int(starts[-1]), dtype=torch.int32, device=dev)
+    db = torch.empty(20 * n, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    call = lambda: check(lib().occ_occluders_bake_device(ctx.handle, n, dv.data_ptr(), starts.ctypes.data,
+                                                         boxes.ctypes.data, dp.data_ptr(), db.data_ptr()), "bake")
+    call()  # warm-up (scratch allocation)
+    ctx.synchronize()
+    times = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        call()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    packed = dp.cpu().numpy().view(np.uint32)
+    bounds = db.cpu().numpy().reshape(n, 20)
+    same = all(np.array_equal(packed[starts[k]:starts[k + 1]], o.packed[:8 * o.packetCount])
+               and np.array_equal(bounds[k, 8:20].view(np.uint32),
+                                  np.concatenate([o.boundsMin, o.boundsMax, o.center]).view(np.uint32))
+               for k, o in enumerate(host_occ))
+    return {"occluders": n, "quads": int(starts[-1]) // 4, "seconds": statistics.median(times),
+            "identical_to_host": bool(same), "launches": 1}
+
+
 def run_large(ctx, net, dev):
     """The large combined workload: a seeded 2M-triangle city (128x128
     buildings), one 3840x2160 main view plus 63 mixed-resolution views in one
@@ -479,8 +519,13 @@ def run_large(ctx, net, dev):
     from rasterizer_gb300 import api, learned as L, scenes
     t = L.Timer()
     mesh = scenes.city_scene(grid=128, target_tris=2_000_000)
-    occ = api.bake_scene(mesh.vertices, mesh.indices)
-    bake_s = t.lap()
+    sets, ref_lo, ref_hi = api.scene_batches(mesh.vertices, mesh.indices)  # quads and SAH batches (host)
+    prep_s = t.lap()
+    occ = [api.Occluder.bake(s, ref_lo, ref_hi) for s in sets]              # Occluder::bake per batch (host)
+    host_bake_s = t.lap()
+    bake_s = prep_s + host_bake_s
+    gpu_bake = _gpu_bake_timing(ctx, sets, ref_lo, ref_hi, occ)
+    t.lap()
     # the baked occluder file: save once, then time a load against the bake
     with tempfile.TemporaryDirectory() as d:
         path = os.path.join(d, "city2m.occ")
@@ -538,6 +583,8 @@ def run_large(ctx, net, dev):
                         f"occluders), one 3840x2160 main view + 63 mixed views per launch, {nq} query boxes "
                         f"per launch ({LARGE_NQ} pool)",
             "bake_seconds": bake_s,
+            "bake_steps_seconds": {"decompose_and_sah": prep_s, "occluder_bake_host": host_bake_s},
+            "gpu_bake": gpu_bake,
             "baked_file": {"load_seconds": load_s, "bytes": file_bytes, "identical": bool(same),
                            "speedup_vs_bake": bake_s / max(load_s, 1e-9)},
             "k_fraction": k, "learned": a.as_dict(), "nearest_first": b.as_dict(),

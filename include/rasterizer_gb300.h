@@ -57,6 +57,21 @@ void* occ_ctx_stream(occ_ctx ctx); /* the context's cudaStream_t */
 int occ_occluder_upload(occ_ctx ctx, const uint32_t* packed, uint32_t packetCount, const float refMin[4],
                         const float refMax[4], const float boundsMin[4], const float boundsMax[4],
                         occ_occluder* out);
+/* Occluder::bake (Occluder.cpp:7-181) on the GPU for `count` occluders in one
+ * launch, asynchronous on the context's stream; the bytes equal
+ * occ_occluder_bake's.  Device pointers: vertices (float4, vertexStart[count]
+ * of them), packed (out, one word per vertex, occluder k's words at
+ * vertexStart[k]), bounds (out, 20 floats per occluder: refMin, refMax,
+ * boundsMin, boundsMax, center).  Host arrays: vertexStart (count + 1,
+ * vertexStart[0] = 0, each occluder a positive multiple of 32 vertices),
+ * refBoxes (8 floats per occluder: refMin, refMax). */
+int occ_occluders_bake_device(occ_ctx ctx, uint32_t count, const float* vertices, const uint32_t* vertexStart,
+                              const float* refBoxes, uint32_t* packed, float* bounds);
+/* occ_occluder_upload from device memory (e.g. occ_occluders_bake_device's
+ * output): packed is a device pointer, bounds a host copy of the 20 floats
+ * (refMin, refMax, boundsMin, boundsMax, center). */
+int occ_occluder_upload_device(occ_ctx ctx, const uint32_t* packed, uint32_t packetCount, const float bounds[20],
+                               occ_occluder* out);
 int occ_occluder_count(occ_ctx ctx, uint32_t* count);
 
 /* ---- rasterizer (Rasterizer.h:13-26) ----------------------------------------- */

@@ -48,6 +48,7 @@ class Context:
         h = P()
         check(lib().occ_ctx_create(device, C.byref(h)), "occ_ctx_create")
         self.handle = h.value
+        self.device = device
         self.serial = next(_context_serial)  # never reused, unlike the handle's address
         self._children = weakref.WeakSet()
 
@@ -149,10 +150,11 @@ class SurfaceAreaHeuristic:
         return [flat[offs[i]:offs[i + 1]].copy() for i in range(nb.value)]
 
 
-def bake_scene(vertices, indices, targetSize: int = 512, splitGranularity: int = 8) -> list[Occluder]:
-    """The demo's scene preparation (Main.cpp:86-128): quads, padding to a
-    multiple of 8 quads, per-quad boxes, SAH batches, one occluder per batch
-    quantised in the box of all vertices."""
+def scene_batches(vertices, indices, targetSize: int = 512, splitGranularity: int = 8):
+    """The demo's scene preparation up to the bake (Main.cpp:86-128): quads,
+    padding to a multiple of 8 quads, per-quad boxes, SAH batches.  Returns
+    (per-occluder vertex arrays, 4 per quad; refMin; refMax = the box of all
+    vertices)."""
     v = _f32(vertices).reshape(-1, 4)
     q = QuadDecomposition.decompose(indices, v)
     pad = (-q.size) % 32
@@ -162,7 +164,46 @@ def bake_scene(vertices, indices, targetSize: int = 512, splitGranularity: int =
     aabbs = _quad_boxes(corners)
     batches = SurfaceAreaHeuristic.generateBatches(aabbs, targetSize, splitGranularity)
     refMin, refMax = _box_of(v)
-    return [Occluder.bake(corners[b].reshape(-1, 4), refMin, refMax) for b in batches]
+    return [np.ascontiguousarray(corners[b].reshape(-1, 4)) for b in batches], refMin, refMax
+
+
+def bake_scene(vertices, indices, targetSize: int = 512, splitGranularity: int = 8) -> list[Occluder]:
+    """The demo's scene preparation (Main.cpp:86-128): scene_batches, then one
+    occluder per batch quantised in the box of all vertices."""
+    sets, refMin, refMax = scene_batches(vertices, indices, targetSize, splitGranularity)
+    return [Occluder.bake(s, refMin, refMax) for s in sets]
+
+
+def bake_on_gpu(ctx: Context, vertex_sets, refMin, refMax) -> list[Occluder]:
+    """Occluder::bake for every vertex array of `vertex_sets` in one GPU
+    launch (occ_occluders_bake_device; the same bytes as Occluder.bake), all
+    quantised in [refMin, refMax]; returns host copies.  Device buffers come
+    from PyTorch."""
+    import torch
+    n = len(vertex_sets)
+    if n == 0:
+        return []
+    sets = [_f32(s).reshape(-1, 4) for s in vertex_sets]
+    starts = np.zeros(n + 1, np.uint32)
+    starts[1:] = np.cumsum([len(s) for s in sets])
+    boxes = np.tile(np.concatenate([_f32(refMin, (4,)), _f32(refMax, (4,))]), (n, 1)).astype(np.float32)
+    dev = torch.device("cuda", ctx.device)
+    dv = torch.from_numpy(np.concatenate(sets)).to(dev)
+    dp = torch.empty(int(starts[-1]), dtype=torch.int32, device=dev)
+    db = torch.empty(20 * n, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize(dev)  # the uploads run on torch's stream, the bake on the context's
+    check(lib().occ_occluders_bake_device(ctx.handle, n, dv.data_ptr(), _ptr(starts), _ptr(boxes), dp.data_ptr(),
+                                          db.data_ptr()), "occ_occluders_bake_device")
+    ctx.synchronize()
+    packed = dp.cpu().numpy().view(np.uint32)
+    bounds = db.cpu().numpy().reshape(n, 20)
+    out = []
+    for k in range(n):
+        words = packed[starts[k]:starts[k + 1]].copy()
+        b = bounds[k]
+        out.append(Occluder(words, len(words) // 8, b[0:4].copy(), b[4:8].copy(), b[8:12].copy(), b[12:16].copy(),
+                            b[16:20].copy()))
+    return out
 
 
 def load_mesh_bin(directory: str | None = None, vertex_path: str | None = None, index_path: str | None = None):

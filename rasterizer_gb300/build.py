@@ -22,7 +22,7 @@ NVCC_FLAGS = ARCH + ["-O3", "--fmad=false", "-ftz=false", "-prec-div=true", "-pr
                      "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I" + CSRC, "-I" + INCLUDE]
 CXX_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c++17", "-I" + CSRC, "-I" + INCLUDE]
 
-CU_SOURCES = ["kernels.cu", "learned.cu", "capi.cu"]
+CU_SOURCES = ["kernels.cu", "learned.cu", "capi.cu", "bake_gpu.cu"]
 CXX_SOURCES = ["bake.cpp", "files.cpp"]
 
 

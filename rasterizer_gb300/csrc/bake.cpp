@@ -19,56 +19,21 @@
 #include <vector>
 
 #include "../../include/rasterizer_gb300.h"
+#include "bake_math.cuh"
 #include "x86_emu.cuh"
 
 namespace {
 
 using namespace x86;
-
-struct V4 {
-  float v[4];
-};
+using bake::V4;
+using bake::vadd;
+using bake::vsub;
+using bake::normalize;
 
 V4 load4(const float* p)
 {
   V4 r;
   std::memcpy(r.v, p, 16);
-  return r;
-}
-
-V4 vsub(const V4& a, const V4& b)
-{
-  V4 r;
-  for (int i = 0; i < 4; ++i) r.v[i] = xsub(a.v[i], b.v[i]);
-  return r;
-}
-
-V4 vadd(const V4& a, const V4& b)
-{
-  V4 r;
-  for (int i = 0; i < 4; ++i) r.v[i] = xadd(a.v[i], b.v[i]);
-  return r;
-}
-
-// cross product of the xyz lanes, w = a.w*b.w - a.w*b.w (VectorMath.h:6-12)
-V4 cross(const V4& a, const V4& b)
-{
-  V4 r;
-  r.v[0] = xsub(xmul(a.v[1], b.v[2]), xmul(a.v[2], b.v[1]));
-  r.v[1] = xsub(xmul(a.v[2], b.v[0]), xmul(a.v[0], b.v[2]));
-  r.v[2] = xsub(xmul(a.v[0], b.v[1]), xmul(a.v[1], b.v[0]));
-  r.v[3] = xsub(xmul(a.v[3], b.v[3]), xmul(a.v[3], b.v[3]));
-  return r;
-}
-
-V4 tri_normal(const V4& a, const V4& b, const V4& c) { return cross(vsub(b, a), vsub(c, a)); }
-
-// v * RSQRTPS(dot3(v, v)) on all four lanes (VectorMath.h:20-23)
-V4 normalize(const V4& v)
-{
-  const float s = rsqrt_host(dp3(v.v, v.v));
-  V4 r;
-  for (int i = 0; i < 4; ++i) r.v[i] = xmul(v.v[i], s);
   return r;
 }
 
@@ -475,11 +440,9 @@ int occ_occluder_bake(const float* vertices, uint32_t nVertices, const float ref
 
   // k-means of the quad normals around the six axis directions (Occluder.cpp:11-78)
   std::vector<V4> normals(nq);
-  for (uint32_t q = 0; q < nq; ++q) {
-    const V4 v0 = vtx(4 * q), v1 = vtx(4 * q + 1), v2 = vtx(4 * q + 2), v3 = vtx(4 * q + 3);
-    normals[q] = normalize(vadd(tri_normal(v0, v1, v2), tri_normal(v0, v2, v3)));
-  }
-  V4 centroid[6] = {{{1, 0, 0, 0}}, {{0, 1, 0, 0}}, {{0, 0, 1, 0}}, {{0, -1, 0, 0}}, {{0, 0, -1, 0}}, {{-1, 0, 0, 0}}};
+  for (uint32_t q = 0; q < nq; ++q) normals[q] = bake::quad_normal(vtx(4 * q), vtx(4 * q + 1), vtx(4 * q + 2), vtx(4 * q + 3));
+  V4 centroid[6];
+  for (int k = 0; k < 6; ++k) centroid[k] = bake::seed_centroid(k);
   std::vector<uint32_t> cluster(nq, 0);
   bool changed = true;
   for (int iter = 0; iter < 10 && changed; ++iter) {
@@ -516,15 +479,8 @@ int occ_occluder_bake(const float* vertices, uint32_t nVertices, const float ref
   uint32_t packets = 0;
   for (uint32_t g = 0; g < nq; g += 8) {
     for (uint32_t j = 0; j < 4; ++j) {
-      for (uint32_t l = 0; l < 8; ++l) {
-        const V4 p = vtx(4 * order[g + l] + j);
-        float r[3];
-        for (int a = 0; a < 3; ++a) r[a] = xmul(xsub(p.v[a], lo.v[a]), inv.v[a]);
-        const int32_t X = cvtt(xfmadd(r[0], 2047.0f, 0.5f)) - 1024;
-        const int32_t Y = cvtt(xfmadd(r[1], 2047.0f, 0.5f));
-        const int32_t Z = cvtt(xfmadd(r[2], 1023.0f, 0.5f));
-        packedOut[(size_t)packets * 8 + 8 * j + l] = ((uint32_t)X << 21) | ((uint32_t)Y << 10) | (uint32_t)Z;
-      }
+      for (uint32_t l = 0; l < 8; ++l)
+        packedOut[(size_t)packets * 8 + 8 * j + l] = bake::pack_vertex(vtx(4 * order[g + l] + j), lo, inv);
     }
     packets += 4;
   }

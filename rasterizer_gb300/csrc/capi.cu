@@ -46,6 +46,8 @@ cudaError_t launch_tile_hiz(const uint16_t* hiz, uint16_t* tileHiz, uint32_t blo
 cudaError_t launch_query2d(const ViewDesc* view, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY,
                            uint32_t maxZ, uint32_t* out, cudaStream_t stream);
 int set_error(int code, const char* msg);
+cudaError_t launch_bake(const BakeJob* jobs, uint32_t count, const float4* vertices, float4* normals,
+                        uint32_t* cluster, uint32_t* order, uint32_t* packed, float* bounds, cudaStream_t stream);
 }  // namespace occ
 
 using namespace occ;
@@ -184,6 +186,10 @@ struct occ_ctx_s {
   PinBuf<uint8_t> readback;
   cudaEvent_t stageFree = nullptr;  // signalled when the last upload from `stage` finished
   DevBuf<int64_t> table;
+  // GPU bake: job table and per-quad scratch (normals, cluster, order)
+  DevBuf<BakeJob> bakeJobs;
+  DevBuf<float4> bakeNormals;
+  DevBuf<uint32_t> bakeCluster, bakeOrder;
 };
 
 struct occ_raster_s {
@@ -595,6 +601,67 @@ int occ_occluder_upload(occ_ctx ctx, const uint32_t* packed, uint32_t packetCoun
   std::memcpy(rec.refMax, refMax, 16);
   std::memcpy(rec.boundsMin, boundsMin, 16);
   std::memcpy(rec.boundsMax, boundsMax, 16);
+  ctx->poolWords += words;
+  ctx->occluders.push_back(rec);
+  *out = (occ_occluder)(ctx->occluders.size() - 1);
+  return OCC_OK;
+}
+
+int occ_occluders_bake_device(occ_ctx ctx, uint32_t count, const float* vertices, const uint32_t* vertexStart,
+                              const float* refBoxes, uint32_t* packed, float* bounds)
+{
+  if (!ctx || (count && (!vertices || !vertexStart || !refBoxes || !packed || !bounds)))
+    return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (!count) return OCC_OK;
+  if (vertexStart[0] != 0) return fail(OCC_ERR_INVALID_ARG, "vertexStart[0] must be 0");
+  std::vector<BakeJob> jobs(count);
+  for (uint32_t k = 0; k < count; ++k) {
+    if (vertexStart[k + 1] <= vertexStart[k] || (vertexStart[k + 1] - vertexStart[k]) % 32 != 0)
+      return fail(OCC_ERR_INVALID_ARG, "each occluder needs a positive multiple of 32 vertices (8 quads per packet)");
+    jobs[k].vertexStart = vertexStart[k];
+    jobs[k].vertexCount = vertexStart[k + 1] - vertexStart[k];
+    std::memcpy(jobs[k].refMin, refBoxes + 8 * (size_t)k, 16);
+    std::memcpy(jobs[k].refMax, refBoxes + 8 * (size_t)k + 4, 16);
+  }
+  const size_t quads = vertexStart[count] / 4;
+  OCC_CHECK(ctx->bakeJobs.reserve(count));
+  OCC_CHECK(ctx->bakeNormals.reserve(quads));
+  OCC_CHECK(ctx->bakeCluster.reserve(quads));
+  OCC_CHECK(ctx->bakeOrder.reserve(quads));
+  OCC_CUDA(cudaMemcpyAsync(ctx->bakeJobs.p, jobs.data(), count * sizeof(BakeJob), cudaMemcpyHostToDevice, ctx->stream));
+  OCC_CUDA(launch_bake(ctx->bakeJobs.p, count, reinterpret_cast<const float4*>(vertices), ctx->bakeNormals.p,
+                       ctx->bakeCluster.p, ctx->bakeOrder.p, packed, bounds, ctx->stream));
+  return OCC_OK;
+}
+
+int occ_occluder_upload_device(occ_ctx ctx, const uint32_t* packed, uint32_t packetCount, const float bounds[20],
+                               occ_occluder* out)
+{
+  if (!ctx || !packed || !bounds || !out) return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (packetCount == 0 || packetCount % 4 != 0)
+    return fail(OCC_ERR_INVALID_ARG, "packetCount must be a positive multiple of 4 (8 quads per packet group)");
+  const size_t words = (size_t)packetCount * 8;
+  if (ctx->poolWords + words > 0xFFFFFFFFull) return fail(OCC_ERR_CAPACITY, "occluder pool exceeds 2^32 words");
+  if (ctx->poolWords + words > ctx->pool.n) {
+    size_t cap = std::max<size_t>(ctx->pool.n * 2, ctx->poolWords + words);
+    cap = std::max<size_t>(cap, 1 << 16);
+    uint32_t* np = nullptr;
+    cudaError_t e = cudaMalloc(&np, cap * 4);
+    if (e != cudaSuccess) return fail(OCC_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    if (ctx->poolWords) OCC_CUDA(cudaMemcpyAsync(np, ctx->pool.p, ctx->poolWords * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->pool.release();
+    ctx->pool.p = np;
+    ctx->pool.n = cap;
+  }
+  OCC_CUDA(cudaMemcpyAsync(ctx->pool.p + ctx->poolWords, packed, words * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  OccluderRec rec{};
+  rec.wordOffset = (uint32_t)ctx->poolWords;
+  rec.packetCount = packetCount;
+  std::memcpy(rec.refMin, bounds, 16);
+  std::memcpy(rec.refMax, bounds + 4, 16);
+  std::memcpy(rec.boundsMin, bounds + 8, 16);
+  std::memcpy(rec.boundsMax, bounds + 12, 16);
   ctx->poolWords += words;
   ctx->occluders.push_back(rec);
   *out = (occ_occluder)(ctx->occluders.size() - 1);

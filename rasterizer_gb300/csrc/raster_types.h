@@ -134,6 +134,13 @@ struct FrameHeader {
   uint32_t pad2;
 };
 
+// One occluder of a GPU bake: vertexCount float4 (a multiple of 32) from
+// vertexStart in the launch's vertex array, quantised in [refMin, refMax].
+struct BakeJob {
+  uint32_t vertexStart, vertexCount, pad[2];
+  float refMin[4], refMax[4];
+};
+
 // readBack formats (the OCC_READBACK_* values of the C ABI).
 constexpr int kReadBackRgba8 = 0, kReadBackLinearF32 = 1, kReadBackDepthF32 = 2, kReadBackPackedU16 = 3;
 

@@ -25,9 +25,11 @@
 #include "x86_tables.h"
 
 #if defined(__CUDACC__)
-// Device copy of the RCPPS table, indexed with data-dependent bits (global
-// memory through the read-only path; the constant cache would serialise).
+// Device copies of the RCPPS and RSQRTPS tables, indexed with data-dependent
+// bits (global memory through the read-only path; the constant cache would
+// serialise).
 __device__ const uint32_t kDevRcpTable[2048] = {X86_RCP_TABLE_VALUES};
+__device__ const uint32_t kDevRsqrtTable[4096] = {X86_RSQRT_TABLE_VALUES};
 #endif
 
 namespace x86 {
@@ -189,8 +191,8 @@ X86_HD float rcp(float a)
   return uf(re <= 0 ? s : (s | ((uint32_t)re << 23) | (t & 0x7FFFFFu)));
 }
 
-// RSQRTPS (host bake only; verified for all 2^32 inputs).
-inline float rsqrt_host(float a)
+// RSQRTPS (occluder bake; the host form verified for all 2^32 inputs).
+X86_HD float rsqrt(float a)
 {
   uint32_t x = fu(a), s = x & 0x80000000u, E = (x >> 23) & 0xFF;
   if (E == 255 && (x & 0x7FFFFF)) return uf(x | 0x400000u);
@@ -198,7 +200,11 @@ inline float rsqrt_host(float a)
   if (s) return uf(kDefaultNaN);
   if (E == 255) return 0.0f;
   uint32_t p = E & 1, Eb = p ? 127 : 128;
+#ifdef __CUDA_ARCH__
+  uint32_t t = __ldg(&kDevRsqrtTable[(p << 11) | ((x >> 12) & 0x7FF)]);
+#else
   uint32_t t = kX86RsqrtTable[(p << 11) | ((x >> 12) & 0x7FF)];
+#endif
   int re = (int)((t >> 23) & 0xFF) - ((int)E - (int)Eb) / 2;
   return uf(((uint32_t)re << 23) | (t & 0x7FFFFFu));
 }
