@@ -1454,7 +1454,7 @@ int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[6], floa
   OCC_CHECK(search(&LaunchTuning::walkPerSm, 3, {2, 4, 8, 16}));
   OCC_CHECK(search(&LaunchTuning::rasterPerSm, 4, upTo(lim[2])));
   OCC_CHECK(search(&LaunchTuning::rasterChunk, 4, {1, 2, 4, 8, 16}));
-  OCC_CHECK(search(&LaunchTuning::queryRounds, 5, {kQueryPerThread, 1, 2, 3, 4}));
+  OCC_CHECK(search(&LaunchTuning::queryRounds, 5, {kQueryPerThread, 1, 2, 4, 8}));
   b->tune = best;
   OCC_CHECK(capture(b));
   if (msAfter) OCC_CHECK(occ_batch_profile(b, iterations, msAfter));

@@ -18,10 +18,10 @@
 //               tile, computes (quad, block) fragments 128 at a time and merges
 //               them per block in list order (Rasterizer.cpp:1098-1292).
 //   k_query     queryVisibility + query2D (Rasterizer.cpp:123-349): frustum test
-//               per box, survivors compacted per CTA and projected by full
+//               per box, survivors listed per warp and projected by full
 //               warps (k_query_thread: one box per thread in place, for few
-//               boxes); boxes over more than two tiles are tested by the whole
-//               warp.
+//               boxes); boxes over more than 8 blocks are tested by the whole
+//               warp, a block per lane.
 //
 // Exactness: every float operation follows the reference's order and
 // rounding (x86_emu.cuh); the block loop sees each quad's primitives in
@@ -166,43 +166,50 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t& t
 // skipped as a whole, which skips exactly the same blocks.  The result is the
 // OR over blocks, so tiles and blocks may be visited in any order.
 
-// Blocks of tile (tx, ty) inside the block rectangle [bx0,bx1]x[by0,by1].
+// One block (bx, by) of the rectangle: skipped if maxZ <= its hiZ, visible if
+// the rectangle covers it whole, else any covered pixel with depth < maxZ
+// (Rasterizer.cpp:303-344).
+__device__ __forceinline__ bool query2d_block(const ViewDesc& V, uint32_t bx, uint32_t by, uint32_t minX,
+                                              uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ)
+{
+  const uint32_t blk = by * V.blocksX + bx;
+  if (maxZ <= (uint32_t)V.hiz[blk]) return false;
+  int32_t sy = (int32_t)(minY - 8 * by);
+  sy = sy < 0 ? 0 : sy;
+  int32_t ey = (int32_t)(maxY - 8 * by);
+  ey = ey > 7 ? 7 : ey;
+  int32_t sx = (int32_t)(minX - bx * 8);
+  sx = sx < 0 ? 0 : sx;
+  int32_t ex = (int32_t)(maxX - bx * 8);
+  ex = ex > 7 ? 7 : ex;
+  if (sy == 0 && ey == 7 && sx == 0 && ex == 7) return true;
+  const uint32_t mz2 = maxZ | (maxZ << 16);  // maxZ is a packed 16-bit depth
+  // the reference's rowSelector as 16-bit lanes of the 4 row words
+  uint32_t cm[4];
+#pragma unroll
+  for (int w = 0; w < 4; ++w)
+    cm[w] = ((2 * w >= sx && 2 * w <= ex) ? 0x0000FFFFu : 0u) | ((2 * w + 1 >= sx && 2 * w + 1 <= ex) ? 0xFFFF0000u : 0u);
+  const uint16_t* d = V.depth + (size_t)blk * 64;
+  for (int32_t y = sy; y <= ey; ++y) {
+    const uint4 row = *reinterpret_cast<const uint4*>(d + 8 * y);
+    // a pixel is visible where its depth < maxZ (Rasterizer.cpp:333-336)
+    if ((__vcmpltu2(row.x, mz2) & cm[0]) | (__vcmpltu2(row.y, mz2) & cm[1]) | (__vcmpltu2(row.z, mz2) & cm[2]) |
+        (__vcmpltu2(row.w, mz2) & cm[3]))
+      return true;
+  }
+  return false;
+}
+
+// Blocks of tile (tx, ty) inside the rectangle.
 __device__ bool query2d_tile(const ViewDesc& V, uint32_t tx, uint32_t ty, uint32_t minX, uint32_t maxX,
                              uint32_t minY, uint32_t maxY, uint32_t maxZ)
 {
   const uint32_t bx0 = minX >> 3, bx1 = maxX >> 3, by0 = minY >> 3, by1 = maxY >> 3;
   const uint32_t ya = ::max(by0, ty * kTileH), yb = ::min(by1, ty * kTileH + kTileH - 1);
   const uint32_t xa = ::max(bx0, tx * kTileW), xb = ::min(bx1, tx * kTileW + kTileW - 1);
-  const uint32_t mz2 = maxZ | (maxZ << 16);  // maxZ is a packed 16-bit depth
-  for (uint32_t by = ya; by <= yb; ++by) {
-    int32_t sy = (int32_t)(minY - 8 * by);
-    sy = sy < 0 ? 0 : sy;
-    int32_t ey = (int32_t)(maxY - 8 * by);
-    ey = ey > 7 ? 7 : ey;
-    const bool interiorLine = sy == 0 && ey == 7;
-    for (uint32_t bx = xa; bx <= xb; ++bx) {
-      const uint32_t blk = by * V.blocksX + bx;
-      if (maxZ <= (uint32_t)V.hiz[blk]) continue;
-      int32_t sx = (int32_t)(minX - bx * 8);
-      sx = sx < 0 ? 0 : sx;
-      int32_t ex = (int32_t)(maxX - bx * 8);
-      ex = ex > 7 ? 7 : ex;
-      if (interiorLine && sx == 0 && ex == 7) return true;
-      // the reference's rowSelector as 16-bit lanes of the 4 row words
-      uint32_t cm[4];
-#pragma unroll
-      for (int w = 0; w < 4; ++w)
-        cm[w] = ((2 * w >= sx && 2 * w <= ex) ? 0x0000FFFFu : 0u) | ((2 * w + 1 >= sx && 2 * w + 1 <= ex) ? 0xFFFF0000u : 0u);
-      const uint16_t* d = V.depth + (size_t)blk * 64;
-      for (int32_t y = sy; y <= ey; ++y) {
-        const uint4 row = *reinterpret_cast<const uint4*>(d + 8 * y);
-        // a pixel is visible where its depth < maxZ (Rasterizer.cpp:333-336)
-        if ((__vcmpltu2(row.x, mz2) & cm[0]) | (__vcmpltu2(row.y, mz2) & cm[1]) | (__vcmpltu2(row.z, mz2) & cm[2]) |
-            (__vcmpltu2(row.w, mz2) & cm[3]))
-          return true;
-      }
-    }
-  }
+  for (uint32_t by = ya; by <= yb; ++by)
+    for (uint32_t bx = xa; bx <= xb; ++bx)
+      if (query2d_block(V, bx, by, minX, maxX, minY, maxY, maxZ)) return true;
   return false;
 }
 
@@ -1432,6 +1439,10 @@ __global__ void __launch_bounds__(128) k_tile_hiz(const uint16_t* hiz, uint16_t*
 
 // ---- k_query -------------------------------------------------------------------------
 
+// Boxes whose rectangle covers more than a warp-tile's worth of blocks are
+// tested by the whole warp (query_big_boxes); smaller ones by their own thread.
+constexpr uint32_t kQueryThreadBlocks = 32;
+
 // Front-end status -> visibility for boxes with small rectangles (query2D per
 // thread); `big` marks the ones left to query_big_boxes.
 __device__ __forceinline__ void query_resolve(const ViewDesc& V, int st, const uint32_t* rect, uint32_t maxZ, bool& vis,
@@ -1441,15 +1452,17 @@ __device__ __forceinline__ void query_resolve(const ViewDesc& V, int st, const u
     vis = true;
     nc = true;
   } else if (st == 2) {
-    const uint32_t ntx = (rect[1] >> 3) / kTileW - (rect[0] >> 3) / kTileW + 1;
-    const uint32_t nty = (rect[3] >> 3) / kTileH - (rect[2] >> 3) / kTileH + 1;
-    big = ntx * nty > 2;
+    const uint32_t nb = ((rect[1] >> 3) - (rect[0] >> 3) + 1) * ((rect[3] >> 3) - (rect[2] >> 3) + 1);
+    big = nb > kQueryThreadBlocks;
     if (!big) vis = query2d(V, rect[0], rect[1], rect[2], rect[3], maxZ);
   }
 }
 
-// Boxes spanning more than two warp-tiles: the whole warp tests one box at a
-// time, one tile per lane.  Called by all 32 lanes.
+// Boxes with large rectangles: the whole warp tests one box at a time.  Its
+// warp-tiles are screened 32 at a time, one per lane, against their minimum
+// hiZ (a tile whose minimum is >= maxZ holds no block the reference would
+// read); each remaining tile is then tested one block per lane (a tile has
+// 8 x 4 = 32 blocks).  Called by all 32 lanes.
 __device__ __forceinline__ void query_big_boxes(const FrameParams& P, bool big, const uint32_t* rect, uint32_t maxZ,
                                                 uint32_t view, uint32_t lane, bool& vis)
 {
@@ -1462,18 +1475,27 @@ __device__ __forceinline__ void query_big_boxes(const FrameParams& P, bool big, 
     const uint32_t mz = __shfl_sync(0xFFFFFFFFu, maxZ, j), vj = __shfl_sync(0xFFFFFFFFu, view, j);
     const ViewDesc& V = P.views[vj];
     const uint32_t tilesX = (V.blocksX + kTileW - 1) / kTileW;
-    const uint32_t tx0 = (minX >> 3) / kTileW, tx1 = (maxX >> 3) / kTileW;
-    const uint32_t ty0 = (minY >> 3) / kTileH, ty1 = (maxY >> 3) / kTileH;
-    const uint32_t ntx = tx1 - tx0 + 1, nt = ntx * (ty1 - ty0 + 1);
+    const uint32_t bx0 = minX >> 3, bx1 = maxX >> 3, by0 = minY >> 3, by1 = maxY >> 3;
+    const uint32_t tx0 = bx0 / kTileW, ty0 = by0 / kTileH;
+    const uint32_t ntx = bx1 / kTileW - tx0 + 1, nt = ntx * (by1 / kTileH - ty0 + 1);
     bool found = false;
     for (uint32_t t0 = 0; t0 < nt && !found; t0 += 32) {
       const uint32_t t = t0 + lane;
-      bool hit = false;
+      bool open = false;
       if (t < nt) {
         const uint32_t tx = tx0 + t % ntx, ty = ty0 + t / ntx;
-        if (mz > (uint32_t)V.tileHiz[ty * tilesX + tx]) hit = query2d_tile(V, tx, ty, minX, maxX, minY, maxY, mz);
+        open = mz > (uint32_t)V.tileHiz[ty * tilesX + tx];
       }
-      found = __ballot_sync(0xFFFFFFFFu, hit) != 0;
+      uint32_t openMask = __ballot_sync(0xFFFFFFFFu, open);
+      while (openMask && !found) {
+        const uint32_t tt = t0 + (uint32_t)(__ffs(openMask) - 1);
+        openMask &= openMask - 1;
+        const uint32_t bx = (tx0 + tt % ntx) * kTileW + (lane & (kTileW - 1));
+        const uint32_t by = (ty0 + tt / ntx) * kTileH + lane / kTileW;
+        const bool hit = bx >= bx0 && bx <= bx1 && by >= by0 && by <= by1 &&
+                         query2d_block(V, bx, by, minX, maxX, minY, maxY, mz);
+        found = __ballot_sync(0xFFFFFFFFu, hit) != 0;
+      }
     }
     if ((int)lane == j) vis = found;
   }
@@ -1517,34 +1539,36 @@ __global__ void __launch_bounds__(256, 6) k_query_thread(FrameParams P)
   }
 }
 
-// One CTA per `rounds` x 256 query slots, in two phases.  Every thread tests
-// its boxes against the six frustum planes; the boxes inside (and those whose
-// arithmetic met a NaN) are compacted in shared memory, and then all warps
-// project them and run query2D with their lanes full (most boxes of a view
-// are outside its frustum: without compaction most lanes idle through the
-// projection).  Each slot's bits land in shared words, written out once.
+// Each warp takes `rounds` x 32 consecutive query slots.  It tests every box
+// against the six frustum planes, queues the boxes inside (and those whose
+// arithmetic met a NaN) in its own shared-memory list, then projects them and
+// runs query2D 32 at a time with its lanes full (most boxes of a view are
+// outside its frustum: without the list most lanes would idle through the
+// projection).  Warps never wait for one another.  CTAs run from the last
+// slots to the first: the views rasterised last are the likeliest still in L2.
 __global__ void __launch_bounds__(256, 6) k_query(FrameParams P, uint32_t rounds)
 {
-  __shared__ uint32_t s_slot[256 * kQueryRounds], s_view[256 * kQueryRounds];
-  __shared__ uint32_t s_vis[8 * kQueryRounds], s_nc[8 * kQueryRounds];
-  __shared__ uint32_t s_n, s_range[2];
+  __shared__ uint32_t s_slot[8][32 * kQueryRounds], s_view[8][32 * kQueryRounds];
+  __shared__ uint32_t s_vis[8][kQueryRounds], s_nc[8][kQueryRounds];
   if (P.header->overflow) return;
-  const uint32_t tid = threadIdx.x, lane = tid & 31;
-  const uint32_t first = blockIdx.x * 256 * rounds;
-  if (tid < 8 * rounds) {
-    s_vis[tid] = 0;
-    s_nc[tid] = 0;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t first = ((gridDim.x - 1 - blockIdx.x) * 8 + warp) * 32 * rounds;
+  if (first >= P.numQuerySlots) return;
+  if (lane < rounds) {
+    s_vis[warp][lane] = 0;
+    s_nc[warp][lane] = 0;
   }
-  if (tid == 0) s_n = 0;
-  if (tid < 2)  // views of the CTA's first and last slot: the threads' searches start there
-    s_range[tid] = query_view(P, ::min(first + (tid ? 256 * rounds - 1 : 0), P.numQuerySlots - 1), 0, P.numViews - 1);
-  __syncthreads();
+  // the views of the warp's first and last slot bound every lane's search
+  const uint32_t edge = lane ? ::min(first + 32 * rounds - 1, P.numQuerySlots - 1) : first;
+  const uint32_t ev = lane < 2 ? query_view(P, edge, 0, P.numViews - 1) : 0u;
+  const uint32_t vlo = __shfl_sync(0xFFFFFFFFu, ev, 0), vhi = __shfl_sync(0xFFFFFFFFu, ev, 1);
+  uint32_t n = 0;
   for (uint32_t r = 0; r < rounds; ++r) {
-    const uint32_t slot = first + 256 * r + tid;
+    const uint32_t slot = first + 32 * r + lane;
     bool keep = false, exact = false;
     uint32_t view = 0;
     if (slot < P.numQuerySlots) {
-      view = query_view(P, slot, s_range[0], s_range[1]);
+      view = query_view(P, slot, vlo, vhi);
       const ViewDesc& V = P.views[view];
       if (slot - V.queryStart < V.queryCount) {
         const float4 a = P.qmin[slot], b = P.qmax[slot];
@@ -1556,23 +1580,21 @@ __global__ void __launch_bounds__(256, 6) k_query(FrameParams P, uint32_t rounds
       }
     }
     const uint32_t m = __ballot_sync(0xFFFFFFFFu, keep);
-    uint32_t at = 0;
-    if (lane == 0 && m) at = atomicAdd(&s_n, (uint32_t)__popc(m));
-    at = __shfl_sync(0xFFFFFFFFu, at, 0) + (uint32_t)__popc(m & ((1u << lane) - 1u));
     if (keep) {
-      s_slot[at] = slot;
-      s_view[at] = view | (exact ? 0x80000000u : 0u);
+      const uint32_t at = n + (uint32_t)__popc(m & ((1u << lane) - 1u));
+      s_slot[warp][at] = slot;
+      s_view[warp][at] = view | (exact ? 0x80000000u : 0u);
     }
+    n += (uint32_t)__popc(m);
   }
-  __syncthreads();
-  const uint32_t n = s_n;
-  for (uint32_t base = tid & ~31u; base < n; base += 256) {  // warp-uniform: query_big_boxes is cooperative
+  __syncwarp();
+  for (uint32_t base = 0; base < n; base += 32) {
     const uint32_t k = base + lane;
     bool vis = false, nc = false, big = false;
-    uint32_t rect[4] = {0, 0, 0, 0}, maxZ = 0, v = 0, sl = 0;
+    uint32_t rect[4] = {0, 0, 0, 0}, maxZ = 0, v = 0, sl = first;
     if (k < n) {
-      sl = s_slot[k];
-      const uint32_t e = s_view[k];
+      sl = s_slot[warp][k];
+      const uint32_t e = s_view[warp][k];
       v = e & 0x7FFFFFFFu;
       const ViewDesc& V = P.views[v];
       const float4 a = P.qmin[sl], b = P.qmax[sl];
@@ -1589,15 +1611,15 @@ __global__ void __launch_bounds__(256, 6) k_query(FrameParams P, uint32_t rounds
     }
     query_big_boxes(P, big, rect, maxZ, v, lane, vis);
     const uint32_t w = (sl - first) >> 5, bit = 1u << (sl & 31u);
-    if (vis) atomicOr(&s_vis[w], bit);
-    if (nc) atomicOr(&s_nc[w], bit);
+    if (vis) atomicOr(&s_vis[warp][w], bit);
+    if (nc) atomicOr(&s_nc[warp][w], bit);
   }
-  __syncthreads();
-  if (tid < 8 * rounds) {
-    const uint32_t w = (first >> 5) + tid;
+  __syncwarp();
+  if (lane < rounds) {
+    const uint32_t w = (first >> 5) + lane;
     if (32 * w < P.numQuerySlots) {
-      P.visBits[w] = s_vis[tid];
-      P.ncBits[w] = s_nc[tid];
+      P.visBits[w] = s_vis[warp][lane];
+      P.ncBits[w] = s_nc[warp][lane];
     }
   }
 }
@@ -1695,13 +1717,14 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
   if (doQuery && P.numQuerySlots) {
     const uint32_t ctas = (P.numQuerySlots + 255) / 256, wave = g_sms * 6;
     uint32_t rounds = P.tune.queryRounds;
-    if (rounds == 0)  // by slot count: compaction pays once the slots fill the GPU a few times over
-      rounds = ctas < 4 * wave ? kQueryPerThread : ::min(kQueryRounds, ctas / wave);
+    if (rounds == 0)  // by slot count: the warp lists pay once the slots fill the GPU a few times over
+      rounds = ctas < 4 * wave ? kQueryPerThread : ::min(kQueryRounds, ::max(1u, ctas / (6 * wave)));
     if (rounds == kQueryPerThread || rounds > kQueryRounds)
       k_query_thread<<<ctas, 256, 0, stream>>>(P);
     else
       k_query<<<(ctas + rounds - 1) / rounds, 256, 0, stream>>>(P, rounds);
   }
+
   mark(6);
   return cudaGetLastError();
 }

@@ -145,8 +145,8 @@ struct BakeJob {
 constexpr int kReadBackRgba8 = 0, kReadBackLinearF32 = 1, kReadBackDepthF32 = 2, kReadBackPackedU16 = 3;
 
 // k_query forms: kQueryPerThread runs one box per thread in place; 1..kQueryRounds
-// are the compacting CTAs with that many rounds of 256 slots each.
-constexpr uint32_t kQueryRounds = 4;
+// are the compacting warps with that many rounds of 32 slots each.
+constexpr uint32_t kQueryRounds = 8;
 constexpr uint32_t kQueryPerThread = 255;
 
 // Launch shape of one flush (0 = the default: as many resident CTAs per SM
