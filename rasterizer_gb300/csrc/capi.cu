@@ -160,7 +160,7 @@ struct FrameScratch {
   DevBuf<QuadRaster> rec;
   DevBuf<QuadWalk> walk;
   DevBuf<Totals> chunkTot, chunkBase, viewTot, viewBase;
-  DevBuf<uint32_t> mat, stStart, stLen, cmdDraw, ckBase, activeChunks;
+  DevBuf<uint32_t> mat, stStart, stLen, cmdDraw, ckBase, activeChunks, viewActive, viewActiveCount;
   DevBuf<uint4> activeTiles;
   DevBuf<uint4> stList;
   DevBuf<float> ck;
@@ -388,6 +388,8 @@ int run_batch(occ_ctx_s* ctx, FrameScratch& S, std::vector<ViewJob>& jobs, bool 
   OCC_CHECK(S.stLen.reserve(L.numSt));
   OCC_CHECK(S.cmdDraw.reserve(L.cmds.size()));
   OCC_CHECK(S.activeChunks.reserve(L.chunks.size()));
+  OCC_CHECK(S.viewActive.reserve(L.chunks.size()));
+  OCC_CHECK(S.viewActiveCount.reserve(nv));
   OCC_CHECK(S.activeTiles.reserve((size_t)L.numTiles * kUnitsPerTile));
   if (S.header.n == 0) {
     OCC_CHECK(S.header.reserve(1));
@@ -433,6 +435,8 @@ int run_batch(occ_ctx_s* ctx, FrameScratch& S, std::vector<ViewJob>& jobs, bool 
     P.numCmds = (uint32_t)L.cmds.size();
     P.matSize = L.matSize;
     P.activeChunkList = S.activeChunks.p;
+    P.viewActiveChunks = S.viewActive.p;
+    P.viewActiveCount = S.viewActiveCount.p;
     P.activeTileList = S.activeTiles.p;
     P.cmds = reinterpret_cast<const Cmd*>(S.tables.p + offCmds);
     P.chunks = reinterpret_cast<const Chunk*>(S.tables.p + offChunks);
@@ -1055,6 +1059,8 @@ int capture(occ_batch_s* b)
   P.numCmds = (uint32_t)b->L.cmds.size();
   P.matSize = b->L.matSize;
   P.activeChunkList = S.activeChunks.p;
+    P.viewActiveChunks = S.viewActive.p;
+    P.viewActiveCount = S.viewActiveCount.p;
   P.activeTileList = S.activeTiles.p;
   P.cmds = reinterpret_cast<const Cmd*>(S.tables.p + b->offCmds);
   P.chunks = reinterpret_cast<const Chunk*>(S.tables.p + b->offChunks);

@@ -20,8 +20,8 @@
 //   k_query     queryVisibility + query2D (Rasterizer.cpp:123-349): frustum test
 //               per box, survivors listed per warp and projected by full
 //               warps (k_query_thread: one box per thread in place, for few
-//               boxes); boxes over more than 8 blocks are tested by the whole
-//               warp, a block per lane.
+//               boxes); boxes over more than a warp-tile of blocks (two
+//               warp-tiles in k_query_thread) are tested by the whole warp.
 //
 // Exactness: every float operation follows the reference's order and
 // rounding (x86_emu.cuh); the block loop sees each quad's primitives in
@@ -543,25 +543,31 @@ __global__ void __launch_bounds__(256) k_gate_second(FrameParams P)
 // others contribute no rows, checkpoints or list entries.
 __global__ void __launch_bounds__(256) k_chunk_gate(FrameParams P)
 {
-  __shared__ uint32_t s_n, s_base;
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (threadIdx.x == 0) s_n = 0;
-  __syncthreads();
-  bool active = false;
-  if (c < P.numChunks) {
-    const Chunk ch = P.chunks[c];
-    for (uint32_t k = 0; k < ch.cmdCount && !active; ++k) active = (P.cmdDraw[ch.cmdFirst + k] & 1u) != 0;
-    if (!active) P.chunkTot[c] = Totals{0, 0, 0, 0};
+  __shared__ uint32_t s_scan[8];
+  __shared__ uint32_t s_base;
+  const uint32_t v = blockIdx.x, tid = threadIdx.x;
+  const ViewDesc& V = P.views[v];
+  uint32_t n = 0;
+  for (uint32_t i0 = 0; i0 < V.chunkCount; i0 += 256) {
+    const uint32_t i = i0 + tid, c = V.chunkStart + i;
+    bool active = false;
+    if (i < V.chunkCount) {
+      const Chunk ch = P.chunks[c];
+      for (uint32_t k = 0; k < ch.cmdCount && !active; ++k) active = (P.cmdDraw[ch.cmdFirst + k] & 1u) != 0;
+      if (!active) P.chunkTot[c] = Totals{0, 0, 0, 0};
+    }
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan<256>(active ? 1u : 0u, tot, s_scan);
+    if (tid == 0 && tot) s_base = atomicAdd(&P.header->activeChunks, tot);
+    __syncthreads();
+    if (active) {
+      P.viewActiveChunks[V.chunkStart + n + ex] = i;
+      P.activeChunkList[s_base + ex] = c;
+    }
+    n += tot;
+    __syncthreads();  // s_base is reused by the next round
   }
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t bal = __ballot_sync(0xFFFFFFFFu, active);
-  uint32_t wbase = 0;
-  if (lane == 0 && bal) wbase = atomicAdd(&s_n, (uint32_t)__popc(bal));
-  __syncthreads();
-  if (threadIdx.x == 0 && s_n) s_base = atomicAdd(&P.header->activeChunks, s_n);
-  __syncthreads();
-  wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
-  if (active) P.activeChunkList[s_base + wbase + __popc(bal & ((1u << lane) - 1u))] = c;
+  if (tid == 0) P.viewActiveCount[v] = n;
 }
 
 // ---- k_setup -------------------------------------------------------------------------
@@ -657,14 +663,19 @@ __global__ void __launch_bounds__(256) k_scan(FrameParams P, uint32_t numSt)
       if (P.views[mid].stBase <= b) lo = mid; else hi = mid - 1;
     }
     const ViewDesc& V = P.views[lo];
+    // the row of the count matrix, over the view's active chunks only (in
+    // chunk order; the other entries are never written nor read)
     uint32_t* m = P.mat + V.matBase + (b - V.stBase) * V.chunkCount;
+    const uint32_t* act = P.viewActiveChunks + V.chunkStart;
+    const uint32_t na = V.chunkCount ? P.viewActiveCount[lo] : 0u;
     uint32_t carry = 0;
-    for (uint32_t i0 = 0; i0 < V.chunkCount; i0 += 256) {
+    for (uint32_t i0 = 0; i0 < na; i0 += 256) {
       const uint32_t i = i0 + tid;
-      const uint32_t v = i < V.chunkCount ? m[i] : 0;
+      const uint32_t idx = i < na ? act[i] : 0u;
+      const uint32_t v = i < na ? m[idx] : 0u;
       uint32_t tot;
       const uint32_t ex = block_exclusive_scan<256>(v, tot, s_scan);
-      if (i < V.chunkCount) m[i] = carry + ex;
+      if (i < na) m[idx] = carry + ex;
       carry += tot;
     }
     if (tid == 0) P.stLen[b] = carry;
@@ -1439,12 +1450,11 @@ __global__ void __launch_bounds__(128) k_tile_hiz(const uint16_t* hiz, uint16_t*
 
 // ---- k_query -------------------------------------------------------------------------
 
-// Boxes whose rectangle covers more than a warp-tile's worth of blocks are
-// tested by the whole warp (query_big_boxes); smaller ones by their own thread.
-constexpr uint32_t kQueryThreadBlocks = 32;
-
 // Front-end status -> visibility for boxes with small rectangles (query2D per
-// thread); `big` marks the ones left to query_big_boxes.
+// thread); `big` marks the ones left to query_big_boxes.  Small means at most
+// a warp-tile's worth of blocks where the warp's lanes are full (kFull, the
+// survivor lists of k_query), at most two warp-tiles where many lanes idle.
+template <bool kFull>
 __device__ __forceinline__ void query_resolve(const ViewDesc& V, int st, const uint32_t* rect, uint32_t maxZ, bool& vis,
                                               bool& nc, bool& big)
 {
@@ -1452,8 +1462,14 @@ __device__ __forceinline__ void query_resolve(const ViewDesc& V, int st, const u
     vis = true;
     nc = true;
   } else if (st == 2) {
-    const uint32_t nb = ((rect[1] >> 3) - (rect[0] >> 3) + 1) * ((rect[3] >> 3) - (rect[2] >> 3) + 1);
-    big = nb > kQueryThreadBlocks;
+    if (kFull) {
+      const uint32_t nb = ((rect[1] >> 3) - (rect[0] >> 3) + 1) * ((rect[3] >> 3) - (rect[2] >> 3) + 1);
+      big = nb > (uint32_t)(kTileW * kTileH);
+    } else {
+      const uint32_t ntx = (rect[1] >> 3) / kTileW - (rect[0] >> 3) / kTileW + 1;
+      const uint32_t nty = (rect[3] >> 3) / kTileH - (rect[2] >> 3) / kTileH + 1;
+      big = ntx * nty > 2;
+    }
     if (!big) vis = query2d(V, rect[0], rect[1], rect[2], rect[3], maxZ);
   }
 }
@@ -1528,7 +1544,7 @@ __global__ void __launch_bounds__(256, 6) k_query_thread(FrameParams P)
       const float4 a = P.qmin[slot], b = P.qmax[slot];
       const float bmin[4] = {a.x, a.y, a.z, a.w}, bmax[4] = {b.x, b.y, b.z, b.w};
       const int st = query_front(V, bmin, bmax, rect, &maxZ);
-      query_resolve(V, st, rect, maxZ, vis, nc, big);
+      query_resolve<false>(V, st, rect, maxZ, vis, nc, big);
     }
   }
   query_big_boxes(P, big, rect, maxZ, view, lane, vis);
@@ -1607,7 +1623,7 @@ __global__ void __launch_bounds__(256, 6) k_query(FrameParams P, uint32_t rounds
         st = query_project_t(g, V, bmin, bmax, rect, &maxZ);
         if (g.nan) st = query_front_exact(V, bmin, bmax, rect, &maxZ, nullptr);
       }
-      query_resolve(V, st, rect, maxZ, vis, nc, big);
+      query_resolve<true>(V, st, rect, maxZ, vis, nc, big);
     }
     query_big_boxes(P, big, rect, maxZ, v, lane, vis);
     const uint32_t w = (sl - first) >> 5, bit = 1u << (sl & 31u);
@@ -1686,13 +1702,9 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
     cudaError_t e = cudaMemsetAsync(&P.header->activeChunks, 0, 3 * sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
     if (P.numChunks) {
-      if (P.matSize) {
-        e = cudaMemsetAsync(P.mat, 0, (size_t)P.matSize * sizeof(uint32_t), stream);  // inactive chunks count 0
-        if (e != cudaSuccess) return e;
-      }
       if (P.phase) k_gate_second<<<(P.numCmds + 7) / 8, 256, 0, stream>>>(P);
       else k_gate<<<(P.numCmds + 255) / 256, 256, 0, stream>>>(P);
-      k_chunk_gate<<<(P.numChunks + 255) / 256, 256, 0, stream>>>(P);
+      k_chunk_gate<<<P.numViews, 256, 0, stream>>>(P);
       k_setup<<<grid_of(P.tune.setupPerSm, g_setupPerSm, P.numChunks), kChunk,
                 (size_t)maxStPerView * sizeof(uint32_t), stream>>>(P);
     }

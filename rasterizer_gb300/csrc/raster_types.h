@@ -194,6 +194,8 @@ struct FrameParams {
   uint32_t* cmdDraw;     // per command: bit0 drawn (this pass), bit1 near-clipped, bit2 drawn by
                          // the first pass of this launch (second pass only)
   uint32_t* activeChunkList;  // chunks with a drawn command (header->activeChunks of them)
+  uint32_t* viewActiveChunks; // per view, from its chunkStart: local indices of its active chunks, in order
+  uint32_t* viewActiveCount;  // per view: how many
   uint4* activeTileList;      // queued raster units (header->activeTiles): {unit, view, first entry and
                               // length of the unit's super-tile list}
   // learned occluder selection and win counts (all optional)
