@@ -1031,6 +1031,14 @@ void write_tables(occ_batch_s* b, uint8_t* dst)
   if (!b->L.chunks.empty()) std::memcpy(dst + b->offChunks, b->L.chunks.data(), b->L.chunks.size() * sizeof(Chunk));
 }
 
+// Between launches only the view table changes (matrices, owner buffers): the
+// command and chunk tables are uploaded when the graph is captured, and each
+// launch copies the view table alone (its first offCmds bytes).
+void write_views(occ_batch_s* b, uint8_t* dst)
+{
+  std::memcpy(dst, b->L.views.data(), b->L.views.size() * sizeof(ViewDesc));
+}
+
 // (Re)captures the per-frame sequence: table upload from the current ring slot,
 // then the five kernels.
 int capture(occ_batch_s* b)
@@ -1107,8 +1115,12 @@ int capture(occ_batch_s* b)
   b->params = P;
   b->anyRaster = anyRaster;
 
+  // every table once (every ring slot holds the command and chunk tables),
+  // then the graph copies the view table at each launch
+  OCC_CUDA(cudaMemcpyAsync(S.tables.p, b->ring[b->cur].p, b->tablesBytes, cudaMemcpyHostToDevice, ctx->stream));
+  OCC_CUDA(cudaEventRecord(b->ringEv[b->cur], ctx->stream));
   OCC_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  cudaError_t e1 = cudaMemcpyAsync(S.tables.p, b->ring[b->cur].p, b->tablesBytes, cudaMemcpyHostToDevice, ctx->stream);
+  cudaError_t e1 = cudaMemcpyAsync(S.tables.p, b->ring[b->cur].p, b->offCmds, cudaMemcpyHostToDevice, ctx->stream);
   if (b->zeroDepth)
     for (auto& J : b->jobs)
       if (e1 == cudaSuccess && J.clear)
@@ -1199,7 +1211,7 @@ int occ_batch_prepare(occ_ctx ctx, uint32_t numViews, const occ_view_work* views
     OCC_CUDA(cudaEventCreateWithFlags(&b->ringEv[k], cudaEventDisableTiming));
     OCC_CUDA(cudaEventRecord(b->ringEv[k], ctx->stream));
   }
-  write_tables(b.get(), b->ring[0].p);
+  for (int k = 0; k < kRing; ++k) write_tables(b.get(), b->ring[k].p);
   // query boxes, uploaded once
   const uint32_t slots = b->L.querySlots;
   if (slots) {
@@ -1278,9 +1290,9 @@ int occ_batch_launch(occ_batch b)
   if (b->dirty) {
     const int slot = (b->cur + 1) % kRing;
     OCC_CUDA(cudaEventSynchronize(b->ringEv[slot]));
-    write_tables(b, b->ring[slot].p);
+    write_views(b, b->ring[slot].p);
     OCC_CUDA(cudaGraphExecMemcpyNodeSetParams1D(b->exec, b->copyNode, b->S.tables.p, b->ring[slot].p,
-                                                b->tablesBytes, cudaMemcpyHostToDevice));
+                                                b->offCmds, cudaMemcpyHostToDevice));
     b->cur = slot;
     b->dirty = false;
   }
@@ -1334,13 +1346,13 @@ int occ_batch_profile(occ_batch b, uint32_t iterations, float* msPerKernel)
     if (b->dirty) {
       const int slot = (b->cur + 1) % kRing;
       cudaEventSynchronize(b->ringEv[slot]);
-      write_tables(b, b->ring[slot].p);
+      write_views(b, b->ring[slot].p);
       b->cur = slot;
       b->dirty = false;
       OCC_CUDA(cudaGraphExecMemcpyNodeSetParams1D(b->exec, b->copyNode, b->S.tables.p, b->ring[slot].p,
-                                                  b->tablesBytes, cudaMemcpyHostToDevice));
+                                                  b->offCmds, cudaMemcpyHostToDevice));
     }
-    cudaMemcpyAsync(b->S.tables.p, b->ring[b->cur].p, b->tablesBytes, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(b->S.tables.p, b->ring[b->cur].p, b->offCmds, cudaMemcpyHostToDevice, ctx->stream);
     cudaEventRecord(ev[7], ctx->stream);
     cudaError_t e = b->features ? launch_selection(b->params, (uint32_t)b->L.cmds.size(), b->mlp != nullptr, ctx->stream)
                                 : cudaSuccess;
@@ -1411,7 +1423,7 @@ int occ_batch_stats(occ_batch b, uint32_t out[7])
   out[3] = H.activeChunks;
   out[4] = H.activeTiles;
   out[5] = (uint32_t)b->L.chunks.size();
-  out[6] = (uint32_t)b->tablesBytes;  // host->device bytes per launch (view, command and chunk tables)
+  out[6] = (uint32_t)b->offCmds;  // host->device bytes per launch (the view table)
   return OCC_OK;
 }
 

@@ -1474,11 +1474,14 @@ __device__ __forceinline__ void query_resolve(const ViewDesc& V, int st, const u
   }
 }
 
-// Boxes with large rectangles: the whole warp tests one box at a time.  Its
-// warp-tiles are screened 32 at a time, one per lane, against their minimum
-// hiZ (a tile whose minimum is >= maxZ holds no block the reference would
-// read); each remaining tile is then tested one block per lane (a tile has
-// 8 x 4 = 32 blocks).  Called by all 32 lanes.
+// Boxes with large rectangles: the whole warp tests one box at a time, its
+// warp-tiles 32 at a time, one per lane, after their minimum hiZ (a tile whose
+// minimum is >= maxZ holds no block the reference would read).  kSplit: each
+// tile that passes is then tested one block per lane (a tile has 8 x 4 = 32
+// blocks; best when the lanes are full); otherwise its lane tests the tile's
+// blocks itself (fewer steps in sequence: best when few boxes keep the GPU
+// busy).  Called by all 32 lanes.
+template <bool kSplit>
 __device__ __forceinline__ void query_big_boxes(const FrameParams& P, bool big, const uint32_t* rect, uint32_t maxZ,
                                                 uint32_t view, uint32_t lane, bool& vis)
 {
@@ -1501,6 +1504,11 @@ __device__ __forceinline__ void query_big_boxes(const FrameParams& P, bool big, 
       if (t < nt) {
         const uint32_t tx = tx0 + t % ntx, ty = ty0 + t / ntx;
         open = mz > (uint32_t)V.tileHiz[ty * tilesX + tx];
+        if (!kSplit && open) open = query2d_tile(V, tx, ty, minX, maxX, minY, maxY, mz);
+      }
+      if (!kSplit) {
+        found = __ballot_sync(0xFFFFFFFFu, open) != 0;
+        continue;
       }
       uint32_t openMask = __ballot_sync(0xFFFFFFFFu, open);
       while (openMask && !found) {
@@ -1547,7 +1555,7 @@ __global__ void __launch_bounds__(256, 6) k_query_thread(FrameParams P)
       query_resolve<false>(V, st, rect, maxZ, vis, nc, big);
     }
   }
-  query_big_boxes(P, big, rect, maxZ, view, lane, vis);
+  query_big_boxes<false>(P, big, rect, maxZ, view, lane, vis);
   const uint32_t vb = __ballot_sync(0xFFFFFFFFu, vis), nb = __ballot_sync(0xFFFFFFFFu, nc);
   if (lane == 0 && slot < P.numQuerySlots) {
     P.visBits[slot >> 5] = vb;
@@ -1625,7 +1633,7 @@ __global__ void __launch_bounds__(256, 6) k_query(FrameParams P, uint32_t rounds
       }
       query_resolve<true>(V, st, rect, maxZ, vis, nc, big);
     }
-    query_big_boxes(P, big, rect, maxZ, v, lane, vis);
+    query_big_boxes<true>(P, big, rect, maxZ, v, lane, vis);
     const uint32_t w = (sl - first) >> 5, bit = 1u << (sl & 31u);
     if (vis) atomicOr(&s_vis[warp][w], bit);
     if (nc) atomicOr(&s_nc[warp][w], bit);
