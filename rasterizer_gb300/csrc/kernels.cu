@@ -651,41 +651,32 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
 // to finish lays the super-tile lists and the views' row/checkpoint ranges out
 // back to back and checks the capacities.
 
+// Inclusive prefix sum over the warp's lanes.
+__device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t v, uint32_t lane)
+{
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, v, o);
+    if (lane >= (uint32_t)o) v += u;
+  }
+  return v;
+}
+
 __global__ void __launch_bounds__(256) k_scan(FrameParams P, uint32_t numSt)
 {
   __shared__ uint32_t s_scan[8];
   __shared__ uint32_t s_last;
-  const uint32_t b = blockIdx.x, tid = threadIdx.x;
-  if (b < numSt) {
-    uint32_t lo = 0, hi = P.numViews - 1;  // view owning super-tile b
-    while (lo < hi) {
-      uint32_t mid = (lo + hi + 1) >> 1;
-      if (P.views[mid].stBase <= b) lo = mid; else hi = mid - 1;
-    }
-    const ViewDesc& V = P.views[lo];
-    // the row of the count matrix, over the view's active chunks only (in
-    // chunk order; the other entries are never written nor read)
-    uint32_t* m = P.mat + V.matBase + (b - V.stBase) * V.chunkCount;
-    const uint32_t* act = P.viewActiveChunks + V.chunkStart;
-    const uint32_t na = V.chunkCount ? P.viewActiveCount[lo] : 0u;
-    uint32_t carry = 0;
-    for (uint32_t i0 = 0; i0 < na; i0 += 256) {
-      const uint32_t i = i0 + tid;
-      const uint32_t idx = i < na ? act[i] : 0u;
-      const uint32_t v = i < na ? m[idx] : 0u;
-      uint32_t tot;
-      const uint32_t ex = block_exclusive_scan<256>(v, tot, s_scan);
-      if (i < na) m[idx] = carry + ex;
-      carry += tot;
-    }
-    if (tid == 0) P.stLen[b] = carry;
-  } else {
-    const uint32_t v = b - numSt;
+  const uint32_t tid = threadIdx.x, lane = tid & 31;
+  // the first numViews CTAs: one view each (its chunk totals, block scans);
+  // the others: one warp per super-tile (its row of the count matrix).  Few
+  // CTAs in all, so that few arrive at the counter below.
+  if (blockIdx.x < P.numViews) {
+    const uint32_t v = blockIdx.x;
     const ViewDesc& V = P.views[v];
     uint32_t carryR = 0, carryC = 0;
     for (uint32_t i0 = 0; i0 < V.chunkCount; i0 += 256) {
       const uint32_t i = i0 + tid;
-      Totals t = i < V.chunkCount ? P.chunkTot[V.chunkStart + i] : Totals{0, 0, 0, 0};
+      const Totals t = i < V.chunkCount ? P.chunkTot[V.chunkStart + i] : Totals{0, 0, 0, 0};
       uint32_t totR, totC;
       const uint32_t exR = block_exclusive_scan<256>(t.rows, totR, s_scan);
       const uint32_t exC = block_exclusive_scan<256>(t.cks, totC, s_scan);
@@ -694,6 +685,30 @@ __global__ void __launch_bounds__(256) k_scan(FrameParams P, uint32_t numSt)
       carryC += totC;
     }
     if (tid == 0) P.viewTot[v] = Totals{carryR, carryC, 0, 0};
+  }
+  const uint32_t stride = (gridDim.x - P.numViews) * 8;
+  for (uint32_t b = (blockIdx.x - P.numViews) * 8 + (tid >> 5); blockIdx.x >= P.numViews && b < numSt; b += stride) {
+    uint32_t lo = 0, hi = P.numViews - 1;  // view owning super-tile b
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (P.views[mid].stBase <= b) lo = mid; else hi = mid - 1;
+    }
+    const ViewDesc& V = P.views[lo];
+    // the row over the view's active chunks only, in chunk order (the other
+    // entries are neither written nor read)
+    uint32_t* m = P.mat + V.matBase + (b - V.stBase) * V.chunkCount;
+    const uint32_t* act = P.viewActiveChunks + V.chunkStart;
+    const uint32_t na = V.chunkCount ? P.viewActiveCount[lo] : 0u;
+    uint32_t carry = 0;
+    for (uint32_t i0 = 0; i0 < na; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      const uint32_t idx = i < na ? act[i] : 0u;
+      const uint32_t v = i < na ? m[idx] : 0u;
+      const uint32_t inc = warp_inclusive_scan(v, lane);
+      if (i < na) m[idx] = carry + inc - v;
+      carry += __shfl_sync(0xFFFFFFFFu, inc, 31);
+    }
+    if (lane == 0) P.stLen[b] = carry;
   }
   __threadfence();
   __syncthreads();
@@ -1718,7 +1733,7 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
     }
   }
   mark(1);
-  if (doRaster) k_scan<<<numSt + P.numViews, 256, 0, stream>>>(P, numSt);
+  if (doRaster) k_scan<<<P.numViews + ::max(1u, ::min((numSt + 7) / 8, 4 * g_sms)), 256, 0, stream>>>(P, numSt);
   mark(2);
   if (doRaster && P.numChunks)
     k_fill<<<grid_of(P.tune.fillPerSm, g_fillPerSm, P.numChunks), kChunk, (size_t)maxStPerView * 64, stream>>>(P);
