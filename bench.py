@@ -831,6 +831,40 @@ def run_profile_learned(frames: int, views: int, train_steps: int, extras: bool 
     ctx.close()
 
 
+def run_profile_misc():
+    """A short GPU-only run for profilers: the kernels outside the batched
+    frame -- the GPU bake of a scene's occluders, a plain 1080p frame and its
+    100k queries one box per thread, query2D, the no-allocation query path,
+    a hiZ upload (per-tile minimum) and the four read-back formats."""
+    import ctypes as C
+    from rasterizer_gb300 import api, scenes
+    from rasterizer_gb300._lib import check, lib
+    mesh = scenes.boxes_scene()
+    sets, lo, hi = api.scene_batches(mesh.vertices, mesh.indices)
+    ctx = api.Context(0)
+    occ = api.bake_on_gpu(ctx, sets, lo, hi)
+    r = api.Rasterizer(ctx, W, H)
+    r.clear()
+    r.setModelViewProjection(scenes.boxes_camera(W, H))
+    r.rasterizeMany(occ, np.full(len(occ), 2, np.uint8))
+    r.flush()
+    mins, maxs = scenes.query_boxes(NQ, seed=43)
+    vis, _ = r.queryVisibilityBatch(mins, maxs)
+    seen = r.query2D(0, 255, 0, 127, 40000)
+    n = 4096
+    a, b = np.ascontiguousarray(mins[:n], np.float32), np.ascontiguousarray(maxs[:n], np.float32)
+    vb, nb = np.zeros(n // 32, np.uint32), np.zeros(n // 32, np.uint32)
+    check(lib().occ_raster_query_batch_noalloc(r.handle, n, a.ctypes.data, b.ctypes.data, vb.ctypes.data,
+                                               nb.ctypes.data), "occ_raster_query_batch_noalloc")
+    r.writeHiZ(r.readHiZ())
+    sums = {f: float(np.asarray(r.readBack(f), np.float64).sum()) for f in ("rgba8", "linear", "depth", "packed")}
+    print(json.dumps({"occluders": len(occ), "visible": int(vis.sum()), "query2d": bool(seen),
+                      "noalloc_visible": int(np.unpackbits(vb.view(np.uint8)).sum()), "readback_sums": sums}),
+          flush=True)
+    r.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile-run", type=int, default=0, metavar="FRAMES",
@@ -847,12 +881,16 @@ def main():
                     help="only launch the batched + learned frame FRAMES times (for ncu); prints a status line")
     ap.add_argument("--profile-views", type=int, default=LEARNED_VIEWS, help="views per launch for --profile-learned")
     ap.add_argument("--profile-train", type=int, default=0, help="training steps after --profile-learned")
+    ap.add_argument("--profile-misc", action="store_true",
+                    help="only launch the kernels outside the batched frame once each (for ncu)")
     ap.add_argument("--profile-extras", action="store_true",
                     help="--profile-learned: first launch with the second pass and the cull labels")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.profile_learned:
+    if args.profile_misc:
+        run_profile_misc()
+    elif args.profile_learned:
         run_profile_learned(args.profile_learned, args.profile_views, args.profile_train, args.profile_extras)
     elif args.profile_run:
         run_profile_frames(args.profile_run)
