@@ -1107,6 +1107,9 @@ int capture(occ_batch_s* b)
       P.select = b->select.p;
       P.mlp = mlp_device(b->mlp);
       P.selectFrac = b->selectFrac;
+      uint32_t maxCmds = 0;
+      for (const auto& V : b->L.views) maxCmds = std::max(maxCmds, V.cmdCount);
+      P.fusedSelect = maxCmds <= kFusedSelectMaxCmds ? 1u : 0u;
     }
   }
   P.tune = b->tune;

@@ -1726,7 +1726,7 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
     if (e != cudaSuccess) return e;
     if (P.numChunks) {
       if (P.phase) k_gate_second<<<(P.numCmds + 7) / 8, 256, 0, stream>>>(P);
-      else k_gate<<<(P.numCmds + 255) / 256, 256, 0, stream>>>(P);
+      else if (!P.fusedSelect) k_gate<<<(P.numCmds + 255) / 256, 256, 0, stream>>>(P);  // else k_select_view did
       k_chunk_gate<<<P.numViews, 256, 0, stream>>>(P);
       k_setup<<<grid_of(P.tune.setupPerSm, g_setupPerSm, P.numChunks), kChunk,
                 (size_t)maxStPerView * sizeof(uint32_t), stream>>>(P);

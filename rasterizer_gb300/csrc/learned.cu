@@ -113,11 +113,11 @@ __global__ void __launch_bounds__(256) k_features(FrameParams P, uint32_t numCmd
   P.cand[c] = cand ? 1 : 0;
 }
 
-// One CTA per view: features 11 and 12 from the view's candidates.
-__global__ void __launch_bounds__(256) k_view_norm(FrameParams P)
+// Features 11 and 12 of view v from its candidates (a CTA of 256 threads).
+__device__ __forceinline__ void view_norm(const FrameParams& P, uint32_t v)
 {
   __shared__ float s_red[3][8];
-  const ViewDesc& V = P.views[blockIdx.x];
+  const ViewDesc& V = P.views[v];
   const uint32_t c0 = V.cmdStart, n = V.cmdCount;
   float dmin = 3.0e38f, dmax = -3.0e38f, amax = 0.0f;
   for (uint32_t i = threadIdx.x; i < n; i += 256) {
@@ -157,6 +157,9 @@ __global__ void __launch_bounds__(256) k_view_norm(FrameParams P)
   }
 }
 
+// One CTA per view: features 11 and 12 (win counting without a selector).
+__global__ void __launch_bounds__(256) k_view_norm(FrameParams P) { view_norm(P, blockIdx.x); }
+
 // ---- MLP forward: mma.sync m16n8k16, bf16 x bf16 -> fp32 ------------------------------------
 
 __device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
@@ -176,116 +179,138 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
 
 __device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
-// Scores M rows of kFeatures floats.  One warp per 16-row tile; the warp's
-// lane (g = lane/4, t = lane%4) holds, per the m16n8k16 fragment layout, rows
-// g and g+8 and columns 2t, 2t+1 of every 8-column tile.  Layer 1's fp32
-// accumulators become layer 2's bf16 A fragments in registers.  With h1/h2/xb
-// non-null the activations are saved for the backward pass.
+// The network's weights in shared memory (bf16 pairs for the MMA operands).
+struct MlpSmem {
+  uint32_t w1[kHidden * kFeatures / 2];
+  uint32_t w2[kHidden * kHidden / 2];
+  float b1[kHidden], b2[kHidden], w3[kHidden];
+};
+
+__device__ __forceinline__ void mlp_load(MlpSmem& W, const MlpDevice* __restrict__ mlp)
+{
+  for (int i = threadIdx.x; i < kHidden * kFeatures / 2; i += blockDim.x)
+    W.w1[i] = reinterpret_cast<const uint32_t*>(mlp->w1t)[i];
+  for (int i = threadIdx.x; i < kHidden * kHidden / 2; i += blockDim.x)
+    W.w2[i] = reinterpret_cast<const uint32_t*>(mlp->w2t)[i];
+  for (int i = threadIdx.x; i < kHidden; i += blockDim.x) {
+    W.b1[i] = mlp->b1[i];
+    W.b2[i] = mlp->b2[i];
+    W.w3[i] = mlp->w3[i];
+  }
+}
+
+// Scores rows [tile*16, tile*16+16) of M rows of kFeatures floats (one warp).
+// The warp's lane (g = lane/4, t = lane%4) holds, per the m16n8k16 fragment
+// layout, rows g and g+8 and columns 2t, 2t+1 of every 8-column tile.  Layer
+// 1's fp32 accumulators become layer 2's bf16 A fragments in registers.  With
+// h1/h2/xb non-null the activations are saved for the backward pass.
+__device__ __forceinline__ void mlp_tile(const MlpSmem& W, float b3, uint32_t tile, const float* __restrict__ feat,
+                                         uint32_t M, float* __restrict__ score, float* h1out, float* h2out,
+                                         float* xout)
+{
+  const uint32_t lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const uint32_t* s_w1 = W.w1;
+  const uint32_t* s_w2 = W.w2;
+  const float* s_b1 = W.b1;
+  const float* s_b2 = W.b2;
+  const float* s_w3 = W.w3;
+  const uint32_t r0 = tile * 16 + g, r1 = r0 + 8;
+  auto x = [&](uint32_t r, uint32_t k) -> float { return r < M ? feat[(size_t)r * kFeatures + k] : 0.0f; };
+  uint32_t a[4];
+  a[0] = pack_bf16x2(x(r0, 2 * t), x(r0, 2 * t + 1));
+  a[1] = pack_bf16x2(x(r1, 2 * t), x(r1, 2 * t + 1));
+  a[2] = pack_bf16x2(x(r0, 8 + 2 * t), x(r0, 9 + 2 * t));
+  a[3] = pack_bf16x2(x(r1, 8 + 2 * t), x(r1, 9 + 2 * t));
+  if (xout) {
+    const uint32_t ks[4] = {2 * t, 2 * t + 1, 8 + 2 * t, 9 + 2 * t};
+    for (int i = 0; i < 4; ++i) {
+      if (r0 < M) xout[(size_t)r0 * kFeatures + ks[i]] = bf16_round(x(r0, ks[i]));
+      if (r1 < M) xout[(size_t)r1 * kFeatures + ks[i]] = bf16_round(x(r1, ks[i]));
+    }
+  }
+  // layer 1: 8 column tiles of 8
+  float h1[8][4];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    h1[j][0] = h1[j][1] = h1[j][2] = h1[j][3] = 0.0f;
+    const uint32_t n = 8 * j + g;
+    mma_bf16_16816(h1[j], a, s_w1[(n * kFeatures + 2 * t) / 2], s_w1[(n * kFeatures + 8 + 2 * t) / 2]);
+    const float c0 = s_b1[8 * j + 2 * t], c1 = s_b1[8 * j + 2 * t + 1];
+    h1[j][0] = fmaxf(h1[j][0] + c0, 0.0f);
+    h1[j][1] = fmaxf(h1[j][1] + c1, 0.0f);
+    h1[j][2] = fmaxf(h1[j][2] + c0, 0.0f);
+    h1[j][3] = fmaxf(h1[j][3] + c1, 0.0f);
+  }
+  // layer 2: A fragments from layer 1's accumulators, 4 k-chunks of 16
+  uint32_t a2[4][4];
+#pragma unroll
+  for (int kc = 0; kc < 4; ++kc) {
+    a2[kc][0] = pack_bf16x2(h1[2 * kc][0], h1[2 * kc][1]);
+    a2[kc][1] = pack_bf16x2(h1[2 * kc][2], h1[2 * kc][3]);
+    a2[kc][2] = pack_bf16x2(h1[2 * kc + 1][0], h1[2 * kc + 1][1]);
+    a2[kc][3] = pack_bf16x2(h1[2 * kc + 1][2], h1[2 * kc + 1][3]);
+  }
+  if (h1out) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t col = 8 * j + 2 * t;
+      if (r0 < M) {
+        h1out[(size_t)r0 * kHidden + col] = bf16_round(h1[j][0]);
+        h1out[(size_t)r0 * kHidden + col + 1] = bf16_round(h1[j][1]);
+      }
+      if (r1 < M) {
+        h1out[(size_t)r1 * kHidden + col] = bf16_round(h1[j][2]);
+        h1out[(size_t)r1 * kHidden + col + 1] = bf16_round(h1[j][3]);
+      }
+    }
+  }
+  float p0 = 0.0f, p1 = 0.0f;  // layer 3 partial dot products for rows r0, r1
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const uint32_t n = 8 * j + g;
+#pragma unroll
+    for (int kc = 0; kc < 4; ++kc)
+      mma_bf16_16816(acc, a2[kc], s_w2[(n * kHidden + 16 * kc + 2 * t) / 2],
+                     s_w2[(n * kHidden + 16 * kc + 8 + 2 * t) / 2]);
+    const uint32_t col = 8 * j + 2 * t;
+    const float v0 = fmaxf(acc[0] + s_b2[col], 0.0f), v1 = fmaxf(acc[1] + s_b2[col + 1], 0.0f);
+    const float v2 = fmaxf(acc[2] + s_b2[col], 0.0f), v3 = fmaxf(acc[3] + s_b2[col + 1], 0.0f);
+    p0 += v0 * s_w3[col] + v1 * s_w3[col + 1];
+    p1 += v2 * s_w3[col] + v3 * s_w3[col + 1];
+    if (h2out) {
+      if (r0 < M) {
+        h2out[(size_t)r0 * kHidden + col] = v0;
+        h2out[(size_t)r0 * kHidden + col + 1] = v1;
+      }
+      if (r1 < M) {
+        h2out[(size_t)r1 * kHidden + col] = v2;
+        h2out[(size_t)r1 * kHidden + col + 1] = v3;
+      }
+    }
+  }
+  p0 += __shfl_xor_sync(0xFFFFFFFFu, p0, 1);
+  p0 += __shfl_xor_sync(0xFFFFFFFFu, p0, 2);
+  p1 += __shfl_xor_sync(0xFFFFFFFFu, p1, 1);
+  p1 += __shfl_xor_sync(0xFFFFFFFFu, p1, 2);
+  if (t == 0) {
+    if (r0 < M) score[r0] = p0 + b3;
+    if (r1 < M) score[r1] = p1 + b3;
+  }
+}
+
+// Scores M rows: one warp per 16-row tile.
 __global__ void __launch_bounds__(128) k_mlp_forward(const float* __restrict__ feat, uint32_t M,
                                                      const MlpDevice* __restrict__ mlp, float* __restrict__ score,
                                                      float* h1out, float* h2out, float* xout)
 {
-  __shared__ uint32_t s_w1[kHidden * kFeatures / 2];
-  __shared__ uint32_t s_w2[kHidden * kHidden / 2];
-  __shared__ float s_b1[kHidden], s_b2[kHidden], s_w3[kHidden];
-  for (int i = threadIdx.x; i < kHidden * kFeatures / 2; i += blockDim.x)
-    s_w1[i] = reinterpret_cast<const uint32_t*>(mlp->w1t)[i];
-  for (int i = threadIdx.x; i < kHidden * kHidden / 2; i += blockDim.x)
-    s_w2[i] = reinterpret_cast<const uint32_t*>(mlp->w2t)[i];
-  for (int i = threadIdx.x; i < kHidden; i += blockDim.x) {
-    s_b1[i] = mlp->b1[i];
-    s_b2[i] = mlp->b2[i];
-    s_w3[i] = mlp->w3[i];
-  }
+  __shared__ MlpSmem W;
+  mlp_load(W, mlp);
   __syncthreads();
   const float b3 = mlp->b3;
-  const uint32_t lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const uint32_t warpsTotal = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile * 16 < M; tile += warpsTotal) {
-    const uint32_t r0 = tile * 16 + g, r1 = r0 + 8;
-    auto x = [&](uint32_t r, uint32_t k) -> float { return r < M ? feat[(size_t)r * kFeatures + k] : 0.0f; };
-    uint32_t a[4];
-    a[0] = pack_bf16x2(x(r0, 2 * t), x(r0, 2 * t + 1));
-    a[1] = pack_bf16x2(x(r1, 2 * t), x(r1, 2 * t + 1));
-    a[2] = pack_bf16x2(x(r0, 8 + 2 * t), x(r0, 9 + 2 * t));
-    a[3] = pack_bf16x2(x(r1, 8 + 2 * t), x(r1, 9 + 2 * t));
-    if (xout) {
-      const uint32_t ks[4] = {2 * t, 2 * t + 1, 8 + 2 * t, 9 + 2 * t};
-      for (int i = 0; i < 4; ++i) {
-        if (r0 < M) xout[(size_t)r0 * kFeatures + ks[i]] = bf16_round(x(r0, ks[i]));
-        if (r1 < M) xout[(size_t)r1 * kFeatures + ks[i]] = bf16_round(x(r1, ks[i]));
-      }
-    }
-    // layer 1: 8 column tiles of 8
-    float h1[8][4];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      h1[j][0] = h1[j][1] = h1[j][2] = h1[j][3] = 0.0f;
-      const uint32_t n = 8 * j + g;
-      mma_bf16_16816(h1[j], a, s_w1[(n * kFeatures + 2 * t) / 2], s_w1[(n * kFeatures + 8 + 2 * t) / 2]);
-      const float c0 = s_b1[8 * j + 2 * t], c1 = s_b1[8 * j + 2 * t + 1];
-      h1[j][0] = fmaxf(h1[j][0] + c0, 0.0f);
-      h1[j][1] = fmaxf(h1[j][1] + c1, 0.0f);
-      h1[j][2] = fmaxf(h1[j][2] + c0, 0.0f);
-      h1[j][3] = fmaxf(h1[j][3] + c1, 0.0f);
-    }
-    // layer 2: A fragments from layer 1's accumulators, 4 k-chunks of 16
-    uint32_t a2[4][4];
-#pragma unroll
-    for (int kc = 0; kc < 4; ++kc) {
-      a2[kc][0] = pack_bf16x2(h1[2 * kc][0], h1[2 * kc][1]);
-      a2[kc][1] = pack_bf16x2(h1[2 * kc][2], h1[2 * kc][3]);
-      a2[kc][2] = pack_bf16x2(h1[2 * kc + 1][0], h1[2 * kc + 1][1]);
-      a2[kc][3] = pack_bf16x2(h1[2 * kc + 1][2], h1[2 * kc + 1][3]);
-    }
-    if (h1out) {
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const uint32_t col = 8 * j + 2 * t;
-        if (r0 < M) {
-          h1out[(size_t)r0 * kHidden + col] = bf16_round(h1[j][0]);
-          h1out[(size_t)r0 * kHidden + col + 1] = bf16_round(h1[j][1]);
-        }
-        if (r1 < M) {
-          h1out[(size_t)r1 * kHidden + col] = bf16_round(h1[j][2]);
-          h1out[(size_t)r1 * kHidden + col + 1] = bf16_round(h1[j][3]);
-        }
-      }
-    }
-    float p0 = 0.0f, p1 = 0.0f;  // layer 3 partial dot products for rows r0, r1
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-      const uint32_t n = 8 * j + g;
-#pragma unroll
-      for (int kc = 0; kc < 4; ++kc)
-        mma_bf16_16816(acc, a2[kc], s_w2[(n * kHidden + 16 * kc + 2 * t) / 2],
-                       s_w2[(n * kHidden + 16 * kc + 8 + 2 * t) / 2]);
-      const uint32_t col = 8 * j + 2 * t;
-      const float v0 = fmaxf(acc[0] + s_b2[col], 0.0f), v1 = fmaxf(acc[1] + s_b2[col + 1], 0.0f);
-      const float v2 = fmaxf(acc[2] + s_b2[col], 0.0f), v3 = fmaxf(acc[3] + s_b2[col + 1], 0.0f);
-      p0 += v0 * s_w3[col] + v1 * s_w3[col + 1];
-      p1 += v2 * s_w3[col] + v3 * s_w3[col + 1];
-      if (h2out) {
-        if (r0 < M) {
-          h2out[(size_t)r0 * kHidden + col] = v0;
-          h2out[(size_t)r0 * kHidden + col + 1] = v1;
-        }
-        if (r1 < M) {
-          h2out[(size_t)r1 * kHidden + col] = v2;
-          h2out[(size_t)r1 * kHidden + col + 1] = v3;
-        }
-      }
-    }
-    p0 += __shfl_xor_sync(0xFFFFFFFFu, p0, 1);
-    p0 += __shfl_xor_sync(0xFFFFFFFFu, p0, 2);
-    p1 += __shfl_xor_sync(0xFFFFFFFFu, p1, 1);
-    p1 += __shfl_xor_sync(0xFFFFFFFFu, p1, 2);
-    if (t == 0) {
-      if (r0 < M) score[r0] = p0 + b3;
-      if (r1 < M) score[r1] = p1 + b3;
-    }
-  }
+  for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile * 16 < M; tile += warpsTotal)
+    mlp_tile(W, b3, tile, feat, M, score, h1out, h2out, xout);
 }
 
 // ---- per-view top-K --------------------------------------------------------------------------
@@ -330,12 +355,13 @@ __device__ __forceinline__ uint32_t block_exclusive_scan256(uint32_t v, uint32_t
   return prefix + x - v;
 }
 
-__global__ void __launch_bounds__(256) k_topk(FrameParams P)
+// The top-K of view v (a CTA of 256 threads).
+__device__ __forceinline__ void topk_view(const FrameParams& P, uint32_t v)
 {
   __shared__ uint32_t s_red[8];
   __shared__ uint32_t s_hist[256];
   __shared__ uint32_t s_pick[2];
-  const ViewDesc& V = P.views[blockIdx.x];
+  const ViewDesc& V = P.views[v];
   const uint32_t c0 = V.cmdStart, n = V.cmdCount;
   uint32_t ncand = 0;
   for (uint32_t i0 = 0; i0 < n; i0 += 256) {
@@ -402,6 +428,44 @@ __global__ void __launch_bounds__(256) k_topk(FrameParams P)
     __syncthreads();
     seenEq += tot;
     if (i < n) P.select[c0 + i] = (c && (key > T || (eq && before < needEq))) ? 1 : 0;
+  }
+}
+
+// One CTA per view: its top-K.
+__global__ void __launch_bounds__(256) k_topk(FrameParams P) { topk_view(P, blockIdx.x); }
+
+// Selection after k_features, one CTA per view: features 11 and 12, the
+// network's scores of the view's commands (a warp per 16 rows), the top-K,
+// and each command's draw flags as k_gate would set them (a gated command is
+// drawn if it is a candidate -- feature 0, the same visibility test -- and
+// among the top K, with the near-clip variant if its test said so -- feature
+// 1), so the frame needs no k_gate.
+__global__ void __launch_bounds__(256) k_select_view(FrameParams P)
+{
+  __shared__ MlpSmem W;
+  const uint32_t v = blockIdx.x;
+  mlp_load(W, P.mlp);
+  view_norm(P, v);
+  __syncthreads();  // the view's features and the weights
+  const ViewDesc& V = P.views[v];
+  const float b3 = P.mlp->b3;
+  for (uint32_t tile = threadIdx.x >> 5; tile * 16 < V.cmdCount; tile += blockDim.x >> 5)
+    mlp_tile(W, b3, tile, P.feat + (size_t)V.cmdStart * kFeatures, V.cmdCount, P.score + V.cmdStart, nullptr, nullptr,
+             nullptr);
+  __syncthreads();  // the view's scores
+  topk_view(P, v);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < V.cmdCount; i += blockDim.x) {
+    const uint32_t c = V.cmdStart + i;
+    const uint32_t flags = P.cmds[c].flags;
+    uint32_t draw = 1, nc = (flags & kCmdNearClip) ? 1u : 0u;
+    if (flags & kCmdGated) {
+      const float* f = P.feat + (size_t)c * kFeatures;
+      draw = f[0] != 0.0f ? 1u : 0u;
+      nc = f[1] != 0.0f ? 1u : 0u;
+    }
+    if (!P.select[c]) draw = 0;
+    P.cmdDraw[c] = draw | (nc << 1);
   }
 }
 
@@ -549,14 +613,18 @@ __global__ void k_adam(float* params, const float* grad, float* m, float* v, flo
 
 cudaError_t launch_selection(const FrameParams& P, uint32_t numCmds, bool useMlp, cudaStream_t stream)
 {
+  if (numCmds) k_features<<<(numCmds + 255) / 256, 256, 0, stream>>>(P, numCmds);
   if (numCmds) {
-    k_features<<<(numCmds + 255) / 256, 256, 0, stream>>>(P, numCmds);
-    k_view_norm<<<P.numViews, 256, 0, stream>>>(P);
-  }
-  if (useMlp && numCmds) {
-    const uint32_t tiles = (numCmds + 15) / 16;
-    k_mlp_forward<<<(tiles + 3) / 4, 128, 0, stream>>>(P.feat, numCmds, P.mlp, P.score, nullptr, nullptr, nullptr);
-    k_topk<<<P.numViews, 256, 0, stream>>>(P);
+    if (useMlp && P.fusedSelect) {
+      k_select_view<<<P.numViews, 256, 0, stream>>>(P);
+    } else {
+      k_view_norm<<<P.numViews, 256, 0, stream>>>(P);
+      if (useMlp) {
+        const uint32_t tiles = (numCmds + 15) / 16;
+        k_mlp_forward<<<(tiles + 3) / 4, 128, 0, stream>>>(P.feat, numCmds, P.mlp, P.score, nullptr, nullptr, nullptr);
+        k_topk<<<P.numViews, 256, 0, stream>>>(P);
+      }
+    }
   }
   return cudaGetLastError();
 }

@@ -208,6 +208,11 @@ struct FrameParams {
   const MlpDevice* mlp;
   float selectFrac;      // fraction of each view's candidates kept
   uint32_t* cullCount;   // per command: samples of occlusion-culled boxes it owns (labels; optional)
+  uint32_t fusedSelect;  // 1: one CTA per view scores, selects and gates (k_select_view; no k_gate)
 };
+
+// Views of at most this many commands are selected by one CTA each; larger
+// ones spread the network over many CTAs (k_mlp_forward, k_topk, k_gate).
+constexpr uint32_t kFusedSelectMaxCmds = 1024;
 
 }  // namespace occ
