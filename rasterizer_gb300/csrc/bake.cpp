@@ -14,7 +14,6 @@
 #include <limits>
 #include <queue>
 #include <string>
-#include <unordered_map>
 #include <utility>
 #include <vector>
 
@@ -81,9 +80,24 @@ struct Box {
 // a greedy maximal matching in vertex order, then one breadth-first augmenting
 // path search per still-unmatched vertex, blossoms kept in a union-find forest
 // that is invalidated by bumping a per-search stamp.
+// Triangle adjacency in compressed rows: the neighbours of v are
+// nbr[off[v] .. off[v+1]), in the order the graph construction found them.
+struct Adjacency {
+  std::vector<uint32_t> off;
+  std::vector<int> nbr;
+  struct Row {
+    const int* b;
+    const int* e;
+    const int* begin() const { return b; }
+    const int* end() const { return e; }
+  };
+  size_t size() const { return off.empty() ? 0 : off.size() - 1; }
+  Row operator[](int v) const { return Row{nbr.data() + off[v], nbr.data() + off[v + 1]}; }
+};
+
 class BlossomMatcher {
  public:
-  explicit BlossomMatcher(const std::vector<std::vector<int>>& adj)
+  explicit BlossomMatcher(const Adjacency& adj)
       : adj_(adj), mate_(adj.size(), -1), bridge_(adj.size()), node_(adj.size())
   {
     const int n = (int)adj.size();
@@ -243,19 +257,12 @@ class BlossomMatcher {
     }
   }
 
-  const std::vector<std::vector<int>>& adj_;
+  const Adjacency& adj_;
   std::vector<int> mate_;
   std::vector<std::pair<int, int>> bridge_;
   std::vector<Node> node_;
   std::queue<int> frontier_;
   int stamp_ = 0;
-};
-
-struct EdgeKeyHash {
-  size_t operator()(const std::pair<uint32_t, uint32_t>& k) const
-  {
-    return std::hash<uint64_t>{}(((uint64_t)k.first << 32) | k.second);
-  }
 };
 
 // Two triangles (v0,v1,v2) and (v2,v3,v0) may form a quad if v1 and v3 lie
@@ -271,28 +278,67 @@ bool mergeable(const V4& v0, const V4& v1, const V4& v2, const V4& v3)
   return !(gt_ss(a, maxDepthError) || gt_ss(b, maxDepthError));
 }
 
+// The directed edges of all triangles grouped by their first vertex; within a
+// group in (triangle, edge) order, i.e. the order in which the reference's
+// edge map receives them (QuadDecomposition.cpp:357-372).
+struct EdgeTable {
+  std::vector<uint32_t> start;  // per vertex: first entry of its group
+  std::vector<uint32_t> to;     // per entry: second vertex of the edge
+  std::vector<uint32_t> tri;    // per entry: triangle
+  std::vector<uint32_t> apex;   // per entry: the triangle's third vertex
+
+  EdgeTable(const uint32_t* idx, uint32_t triCount, uint32_t numVerts)
+      : start(numVerts + 1, 0), to(3 * (size_t)triCount), tri(3 * (size_t)triCount), apex(3 * (size_t)triCount)
+  {
+    for (size_t k = 0; k < 3 * (size_t)triCount; ++k) ++start[idx[k] + 1];
+    for (uint32_t v = 0; v < numVerts; ++v) start[v + 1] += start[v];
+    std::vector<uint32_t> cur(start.begin(), start.end() - 1);
+    for (uint32_t t = 0; t < triCount; ++t)
+      for (int e = 0; e < 3; ++e) {
+        const uint32_t a = idx[3 * t + e], b = idx[3 * t + (e + 1) % 3], c = idx[3 * t + (e + 2) % 3];
+        const uint32_t k = cur[a]++;
+        to[k] = b;
+        tri[k] = t;
+        apex[k] = c;
+      }
+  }
+};
+
 std::vector<uint32_t> decompose(const uint32_t* idx, uint32_t nIdx, const float* verts)
 {
   const uint32_t triCount = nIdx / 3;
-  std::vector<std::vector<int>> adj(triCount);
-  using Key = std::pair<uint32_t, uint32_t>;
-  std::unordered_map<Key, std::vector<std::pair<uint32_t, uint32_t>>, EdgeKeyHash> edges;
+  uint32_t numVerts = 0;
+  for (uint32_t k = 0; k < nIdx; ++k) numVerts = std::max(numVerts, idx[k] + 1);
+  const EdgeTable E(idx, triCount, numVerts);
   auto vtx = [&](uint32_t i) { return load4(verts + 4 * (size_t)i); };
+  // Mergeable neighbours, in the order the reference's loop finds them: for
+  // each triangle t (after its own edges entered the map), each edge e, the
+  // triangles t' <= t holding the reverse edge, in map order.
+  std::vector<std::pair<uint32_t, uint32_t>> found;
   for (uint32_t t = 0; t < triCount; ++t) {
     const uint32_t i[3] = {idx[3 * t], idx[3 * t + 1], idx[3 * t + 2]};
-    edges[Key(i[0], i[1])].push_back({t, i[2]});
-    edges[Key(i[1], i[2])].push_back({t, i[0]});
-    edges[Key(i[2], i[0])].push_back({t, i[1]});
     for (int e = 0; e < 3; ++e) {
-      auto it = edges.find(Key(i[(e + 1) % 3], i[e]));  // the shared edge runs the other way
-      if (it == edges.end()) continue;
-      for (const auto& pr : it->second) {
-        const uint32_t other = pr.first, apex = pr.second;
-        if (mergeable(vtx(i[e]), vtx(apex), vtx(i[(e + 1) % 3]), vtx(i[(e + 2) % 3]))) {
-          adj[t].push_back((int)other);
-          adj[other].push_back((int)t);
-        }
+      const uint32_t a = i[(e + 1) % 3], b = i[e];  // the shared edge runs the other way: a -> b
+      for (uint32_t k = E.start[a]; k < E.start[a + 1] && E.tri[k] <= t; ++k) {
+        if (E.to[k] != b) continue;
+        if (mergeable(vtx(i[e]), vtx(E.apex[k]), vtx(i[(e + 1) % 3]), vtx(i[(e + 2) % 3])))
+          found.emplace_back(t, E.tri[k]);
       }
+    }
+  }
+  Adjacency adj;
+  adj.off.assign((size_t)triCount + 1, 0);
+  for (const auto& pr : found) {
+    ++adj.off[pr.first + 1];
+    ++adj.off[pr.second + 1];
+  }
+  for (uint32_t t = 0; t < triCount; ++t) adj.off[t + 1] += adj.off[t];
+  adj.nbr.resize(adj.off[triCount]);
+  {
+    std::vector<uint32_t> cur(adj.off.begin(), adj.off.end() - 1);
+    for (const auto& pr : found) {
+      adj.nbr[cur[pr.first]++] = (int)pr.second;
+      adj.nbr[cur[pr.second]++] = (int)pr.first;
     }
   }
   BlossomMatcher matching(adj);
@@ -308,11 +354,10 @@ std::vector<uint32_t> decompose(const uint32_t* idx, uint32_t nIdx, const float*
     if (t >= (uint32_t)m) continue;  // emitted with the lower-numbered triangle
     bool done = false;
     for (int e = 0; e < 3 && !done; ++e) {
-      auto it = edges.find(Key(i[(e + 1) % 3], i[e]));
-      if (it == edges.end()) continue;
-      for (const auto& pr : it->second)
-        if (pr.first == (uint32_t)m) {
-          out.insert(out.end(), {i[e], i[(e + 2) % 3], i[(e + 1) % 3], pr.second});
+      const uint32_t a = i[(e + 1) % 3], b = i[e];
+      for (uint32_t k = E.start[a]; k < E.start[a + 1]; ++k)
+        if (E.to[k] == b && E.tri[k] == (uint32_t)m) {
+          out.insert(out.end(), {i[e], i[(e + 2) % 3], i[(e + 1) % 3], E.apex[k]});
           done = true;
           break;
         }
@@ -323,16 +368,52 @@ std::vector<uint32_t> decompose(const uint32_t* idx, uint32_t nIdx, const float*
 
 // ---- SAH batching -------------------------------------------------------------------
 
-int sah_split(const std::vector<Box>& boxes, uint32_t gran, uint32_t* begin, uint32_t* end)
+// Stable sort of the indices [begin, end) by c[index] under `<`, for keys
+// without NaN: an LSD radix sort (three passes of 11, 11, 10 bits) of the keys
+// mapped to unsigned integers in float order, both zeros mapped alike (`<`
+// ties them, so stability keeps their order).  The same permutation as
+// std::stable_sort with that comparison.
+void stable_sort_by_key(uint32_t* begin, uint32_t* end, const float* c, std::vector<uint64_t>& a,
+                        std::vector<uint64_t>& b)
+{
+  const size_t n = (size_t)(end - begin);
+  a.resize(n);
+  b.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    uint32_t u = c[begin[i]] == 0.0f ? 0u : fu(c[begin[i]]);
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    a[i] = ((uint64_t)u << 32) | begin[i];
+  }
+  const int shifts[3] = {32, 43, 54}, bits[3] = {11, 11, 10};
+  for (int pass = 0; pass < 3; ++pass) {
+    const uint32_t mask = (1u << bits[pass]) - 1u;
+    std::vector<size_t> cnt((size_t)mask + 2, 0);
+    for (size_t i = 0; i < n; ++i) ++cnt[((a[i] >> shifts[pass]) & mask) + 1];
+    for (size_t d = 0; d <= mask; ++d) cnt[d + 1] += cnt[d];
+    for (size_t i = 0; i < n; ++i) b[cnt[(a[i] >> shifts[pass]) & mask]++] = a[i];
+    a.swap(b);
+  }
+  for (size_t i = 0; i < n; ++i) begin[i] = (uint32_t)a[i];
+}
+
+void sort_by_axis(uint32_t* begin, uint32_t* end, const float* c, bool ctrNaN)
+{
+  static thread_local std::vector<uint64_t> ta, tb;
+  if (!ctrNaN && end - begin >= 2048) stable_sort_by_key(begin, end, c, ta, tb);
+  else std::stable_sort(begin, end, [c](uint32_t x, uint32_t y) { return c[x] < c[y]; });
+}
+
+// ctr[axis][i]: box i's centre along the axis (times two), computed once; the
+// sorts compare these floats exactly as the reference compares the centres.
+int sah_split(const std::vector<Box>& boxes, const std::vector<float> (&ctr)[3], bool ctrNaN, uint32_t gran,
+              uint32_t* begin, uint32_t* end)
 {
   const uint32_t n = (uint32_t)(end - begin);
   float bestCost = std::numeric_limits<float>::infinity();
   int bestAxis = -1, bestIndex = -1;
   std::vector<float> left(n), right(n);
   for (int axis = 0; axis < 3; ++axis) {
-    std::stable_sort(begin, end, [&](uint32_t a, uint32_t b) {
-      return boxes[a].center2(axis) < boxes[b].center2(axis);
-    });
+    sort_by_axis(begin, end, ctr[axis].data(), ctrNaN);
     Box acc;
     for (uint32_t i = 0; i < n; ++i) {
       acc.grow(boxes[begin[i]]);
@@ -353,18 +434,18 @@ int sah_split(const std::vector<Box>& boxes, uint32_t gran, uint32_t* begin, uin
     }
   }
   if (bestAxis < 0) return -1;
-  std::stable_sort(begin, end, [&](uint32_t a, uint32_t b) {
-    return boxes[a].center2(bestAxis) < boxes[b].center2(bestAxis);
-  });
+  // without NaN centres the range is still in the order of the last axis
+  // sorted, and sorting it again by that axis changes nothing
+  if (bestAxis != 2 || ctrNaN) sort_by_axis(begin, end, ctr[bestAxis].data(), ctrNaN);
   return bestIndex;
 }
 
-void sah_recurse(const std::vector<Box>& boxes, uint32_t target, uint32_t gran, uint32_t* begin, uint32_t* end,
-                 std::vector<std::vector<uint32_t>>& out)
+void sah_recurse(const std::vector<Box>& boxes, const std::vector<float> (&ctr)[3], bool ctrNaN, uint32_t target,
+                 uint32_t gran, uint32_t* begin, uint32_t* end, std::vector<std::vector<uint32_t>>& out)
 {
   // The reference's split search needs more than two split granules (its loop
   // bound is unsigned), and a split must exist; otherwise keep the range whole.
-  const int split = (size_t)(end - begin) > 2 * (size_t)gran ? sah_split(boxes, gran, begin, end) : -1;
+  const int split = (size_t)(end - begin) > 2 * (size_t)gran ? sah_split(boxes, ctr, ctrNaN, gran, begin, end) : -1;
   if (split < 0) {
     out.emplace_back(begin, end);
     return;
@@ -373,7 +454,7 @@ void sah_recurse(const std::vector<Box>& boxes, uint32_t target, uint32_t gran, 
   for (int i = 0; i < 2; ++i) {
     const size_t count = (size_t)(range[i + 1] - range[i]);
     if (count < target) out.emplace_back(range[i], range[i + 1]);
-    else sah_recurse(boxes, target, gran, range[i], range[i + 1], out);
+    else sah_recurse(boxes, ctr, ctrNaN, target, gran, range[i], range[i + 1], out);
   }
 }
 
@@ -414,7 +495,16 @@ int occ_sah_generate_batches(const float* aabbs, uint32_t n, uint32_t targetSize
   std::vector<uint32_t> order(n);
   for (uint32_t i = 0; i < n; ++i) order[i] = i;
   std::vector<std::vector<uint32_t>> batches;
-  sah_recurse(boxes, targetSize, splitGranularity, order.data(), order.data() + n, batches);
+  std::vector<float> ctr[3];
+  bool ctrNaN = false;
+  for (int axis = 0; axis < 3; ++axis) {
+    ctr[axis].resize(n);
+    for (uint32_t i = 0; i < n; ++i) {
+      ctr[axis][i] = boxes[i].center2(axis);
+      ctrNaN |= ctr[axis][i] != ctr[axis][i];
+    }
+  }
+  sah_recurse(boxes, ctr, ctrNaN, targetSize, splitGranularity, order.data(), order.data() + n, batches);
   uint32_t pos = 0;
   for (size_t b = 0; b < batches.size(); ++b) {
     offsets[b] = pos;
