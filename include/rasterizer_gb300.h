@@ -69,7 +69,9 @@ int occ_occluders_bake_device(occ_ctx ctx, uint32_t count, const float* vertices
                               const float* refBoxes, uint32_t* packed, float* bounds);
 /* occ_occluder_upload from device memory (e.g. occ_occluders_bake_device's
  * output): packed is a device pointer, bounds a host copy of the 20 floats
- * (refMin, refMax, boundsMin, boundsMax, center). */
+ * (refMin, refMax, boundsMin, boundsMax, center).  The copy into the
+ * context's occluder pool is queued on the context's stream: packed must stay
+ * valid (and unchanged) until the stream has run it (occ_ctx_synchronize). */
 int occ_occluder_upload_device(occ_ctx ctx, const uint32_t* packed, uint32_t packetCount, const float bounds[20],
                                occ_occluder* out);
 int occ_occluder_count(occ_ctx ctx, uint32_t* count);
