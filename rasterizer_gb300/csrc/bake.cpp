@@ -313,14 +313,20 @@ std::vector<uint32_t> decompose(const uint32_t* idx, uint32_t nIdx, const float*
   auto vtx = [&](uint32_t i) { return load4(verts + 4 * (size_t)i); };
   // Mergeable neighbours, in the order the reference's loop finds them: for
   // each triangle t (after its own edges entered the map), each edge e, the
-  // triangles t' <= t holding the reverse edge, in map order.
+  // triangles t' <= t holding the reverse edge, in map order.  A triangle with
+  // a repeated vertex holds an edge and its reverse; the reference then makes
+  // it its own neighbour, may match it with itself, and its augmenting search
+  // can then walk a parent chain that never ends (or the triangle is dropped
+  // from the output).  Here a triangle is never its own neighbour: the result
+  // is the reference's wherever the reference does not match a triangle with
+  // itself, and such a triangle is matched with another or emitted alone.
   std::vector<std::pair<uint32_t, uint32_t>> found;
   for (uint32_t t = 0; t < triCount; ++t) {
     const uint32_t i[3] = {idx[3 * t], idx[3 * t + 1], idx[3 * t + 2]};
     for (int e = 0; e < 3; ++e) {
       const uint32_t a = i[(e + 1) % 3], b = i[e];  // the shared edge runs the other way: a -> b
       for (uint32_t k = E.start[a]; k < E.start[a + 1] && E.tri[k] <= t; ++k) {
-        if (E.to[k] != b) continue;
+        if (E.to[k] != b || E.tri[k] == t) continue;
         if (mergeable(vtx(i[e]), vtx(E.apex[k]), vtx(i[(e + 1) % 3]), vtx(i[(e + 2) % 3])))
           found.emplace_back(t, E.tri[k]);
       }

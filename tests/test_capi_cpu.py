@@ -5,6 +5,7 @@ import ctypes as C
 import os
 import re
 import subprocess
+import sys
 import tempfile
 
 import numpy as np
@@ -129,3 +130,23 @@ def test_cpp_facade_links_against_the_library():
         subprocess.run(["g++", "-std=c++17", "-O0", "-I" + os.path.join(ROOT, "include"), p, "-o", exe, so,
                         "-Wl,-rpath," + os.path.dirname(so)], check=True)
         assert subprocess.run([exe]).returncode == 0
+
+
+def test_decomposition_of_triangles_with_a_repeated_vertex_terminates():
+    """A triangle with a repeated vertex holds an edge and its reverse; the
+    reference makes it its own neighbour and its matching can then loop
+    forever on such input.  The library never pairs a triangle with itself:
+    the call returns, and every triangle is emitted (in a pair or alone)."""
+    code = (
+        "import numpy as np\n"
+        "from rasterizer_gb300 import api\n"
+        "rng = np.random.default_rng(1)\n"
+        "v = (np.round(rng.uniform(-5, 5, (200, 4)) * 4) / 4).astype(np.float32); v[:, 3] = 1\n"
+        "v[5] = v[4]; v[6] = (v[4] + v[7]) / 2\n"
+        "t = rng.integers(0, 10, (200, 3)).astype(np.uint32)\n"
+        "for tris in (t, np.array([[8, 1, 8], [8, 5, 1]], np.uint32)):\n"
+        "    q = api.QuadDecomposition.decompose(tris.ravel(), v).reshape(-1, 4)\n"
+        "    assert (len(tris) + 1) // 2 <= len(q) <= len(tris), (len(tris), len(q))\n"
+        "print('ok')\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stderr

@@ -177,3 +177,59 @@ def test_query_special_values_against_reference():
     ovis, onc = orc.query(mins, maxs)
     assert np.array_equal(rvis, ovis) and np.array_equal(rnc, onc)
     assert rvis.sum() > 0 and (1 - rvis).sum() > 0
+
+
+def _adversarial_mesh(kind: str, seed: int):
+    rng = np.random.default_rng(seed)
+    if kind == "grid":  # quads split either way, shuffled, some triangles wound the other way
+        tris = []
+        for y in range(9):
+            for x in range(9):
+                a, b, c, d = y * 10 + x, y * 10 + x + 1, (y + 1) * 10 + x + 1, (y + 1) * 10 + x
+                tris += [(a, b, c), (a, c, d)] if rng.random() < 0.5 else [(a, b, d), (b, c, d)]
+        v = np.zeros((100, 4), np.float32)
+        v[:, 0], v[:, 2], v[:, 3] = np.arange(100) % 10, np.arange(100) // 10, 1
+        v[:, 1] = np.round(rng.uniform(0, 0.8, 100) * 4) / 4
+        tris = np.array(tris, np.uint32)
+        rng.shuffle(tris)
+        flip = rng.random(len(tris)) < 0.2
+        tris[flip] = tris[flip][:, ::-1]
+    else:  # non-manifold: edges shared by three or more triangles, duplicated triangles
+        v = (np.round(rng.uniform(-5, 5, (12, 4)) * 4) / 4).astype(np.float32)
+        v[:, 3] = 1
+        tris = rng.integers(0, 12, (300, 3)).astype(np.uint32)
+        tris = tris[(tris[:, 0] != tris[:, 1]) & (tris[:, 1] != tris[:, 2]) & (tris[:, 0] != tris[:, 2])]
+        tris = np.concatenate([tris, tris[:40]])
+    return v, np.ascontiguousarray(tris, np.uint32).ravel()
+
+
+@pytest.mark.parametrize("kind", ["grid", "nonmanifold"])
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_decomposition_adversarial_meshes(kind, seed):
+    """Shuffled triangle order, mixed windings, non-manifold edges and
+    duplicated triangles: the same quads as the reference's decomposition."""
+    v, i = _adversarial_mesh(kind, seed)
+    L = bindings.ref_lib()
+    out = np.zeros(4 * (i.size // 3), np.uint32)
+    n = L.ref_decompose(bindings._ptr(i), i.size, bindings._ptr(v), len(v), bindings._ptr(out))
+    assert np.array_equal(api.QuadDecomposition.decompose(i, v), out[:n])
+
+
+def test_sah_tied_and_signed_zero_centres():
+    """SAH on boxes whose centres tie (snapped) or are -0 and +0: the same
+    batches as the reference (its stable sorts keep tied boxes in order)."""
+    rng = np.random.default_rng(4)
+    n = 6000
+    lo = (np.round(rng.uniform(-50, 50, (n, 4)) / 8) * 8).astype(np.float32)
+    hi = (lo + np.round(rng.uniform(0, 3, (n, 4)))).astype(np.float32)
+    z = rng.integers(0, n, n // 10)
+    lo[z[::2], 0] = hi[z[::2], 0] = -0.0
+    lo[z[1::2], 0] = hi[z[1::2], 0] = 0.0
+    boxes = np.ascontiguousarray(np.concatenate([lo, hi], axis=1), np.float32)
+    L = bindings.ref_lib()
+    flat, offs = np.zeros(n, np.uint32), np.zeros(n + 1, np.uint32)
+    nb = L.ref_sah(bindings._ptr(boxes), n, 512, 8, bindings._ptr(flat), bindings._ptr(offs))
+    mine = api.SurfaceAreaHeuristic.generateBatches(boxes, 512, 8)
+    assert len(mine) == nb
+    for b in range(nb):
+        assert np.array_equal(mine[b], flat[offs[b]:offs[b + 1]])
