@@ -146,6 +146,24 @@ inline std::vector<std::unique_ptr<Occluder>> loadOccluders(const std::string& p
   return out;
 }
 
+// Occluder::bake on the GPU for many occluders at once (device pointers; see
+// occ_occluders_bake_device), asynchronous on the context's stream, and the
+// registration of a device-resident packed occluder (occ_occluder_upload_device).
+inline void bakeOnDevice(Context& ctx, const std::vector<uint32_t>& vertexStart, const float* dVertices,
+                         const std::vector<float>& refBoxes, uint32_t* dPacked, float* dBounds)
+{
+  check(occ_occluders_bake_device(ctx.handle(), (uint32_t)(vertexStart.size() - 1), dVertices, vertexStart.data(),
+                                  refBoxes.data(), dPacked, dBounds),
+        "occ_occluders_bake_device");
+}
+
+inline occ_occluder uploadFromDevice(Context& ctx, const uint32_t* dPacked, uint32_t packetCount, const float bounds[20])
+{
+  occ_occluder id = 0;
+  check(occ_occluder_upload_device(ctx.handle(), dPacked, packetCount, bounds, &id), "occ_occluder_upload_device");
+  return id;
+}
+
 class Rasterizer {
  public:
   Rasterizer(Context& ctx, uint32_t width, uint32_t height) : ctx_(ctx), w_(width), h_(height)
