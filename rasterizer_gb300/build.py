@@ -20,7 +20,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "--fmad=false", "-ftz=false", "-prec-div=true", "-prec-sqrt=true", "-lineinfo",
                      "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I" + CSRC, "-I" + INCLUDE]
-CXX_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c++17", "-I" + CSRC, "-I" + INCLUDE]
+CXX_FLAGS = ["-O2", "-fPIC", "-pthread", "-ffp-contract=off", "-fno-fast-math", "-std=c++17", "-I" + CSRC,
+             "-I" + INCLUDE]
 
 CU_SOURCES = ["kernels.cu", "learned.cu", "capi.cu", "bake_gpu.cu"]
 CXX_SOURCES = ["bake.cpp", "files.cpp"]
@@ -72,7 +73,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if failed:
         raise RuntimeError("build failed:\n" + "\n".join(failed))
     tmp = LIB + ".tmp"
-    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs
+    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))

@@ -11,9 +11,11 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <future>
 #include <limits>
 #include <queue>
 #include <string>
+#include <system_error>
 #include <utility>
 #include <vector>
 
@@ -457,11 +459,29 @@ void sah_recurse(const std::vector<Box>& boxes, const std::vector<float> (&ctr)[
     return;
   }
   uint32_t* range[3] = {begin, begin + split, end};
-  for (int i = 0; i < 2; ++i) {
-    const size_t count = (size_t)(range[i + 1] - range[i]);
-    if (count < target) out.emplace_back(range[i], range[i + 1]);
-    else sah_recurse(boxes, ctr, ctrNaN, target, gran, range[i], range[i + 1], out);
+  auto half = [&](int i, std::vector<std::vector<uint32_t>>& dst) {
+    if ((size_t)(range[i + 1] - range[i]) < target) dst.emplace_back(range[i], range[i + 1]);
+    else sah_recurse(boxes, ctr, ctrNaN, target, gran, range[i], range[i + 1], dst);
+  };
+  // Large halves are independent (disjoint index ranges, read-only boxes):
+  // the first runs on another thread, and its batches still come first.
+  constexpr size_t kParallelMin = 32768;
+  if (split >= (int)kParallelMin && (size_t)(end - begin) - (size_t)split >= kParallelMin) {
+    std::vector<std::vector<uint32_t>> first;
+    std::future<void> job;
+    try {
+      job = std::async(std::launch::async, [&] { half(0, first); });
+    } catch (const std::system_error&) {  // no thread to be had: in sequence
+      half(0, first);
+    }
+    std::vector<std::vector<uint32_t>> second;
+    half(1, second);
+    if (job.valid()) job.get();
+    for (auto* part : {&first, &second})
+      for (auto& b : *part) out.push_back(std::move(b));
+    return;
   }
+  for (int i = 0; i < 2; ++i) half(i, out);
 }
 
 }  // namespace
