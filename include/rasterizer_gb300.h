@@ -299,6 +299,21 @@ int occ_occluders_file_info(const char* path, uint32_t* count, uint64_t* words);
 int occ_occluders_load(const char* path, uint32_t capacityCount, uint64_t capacityWords, uint32_t* packetCounts,
                        uint32_t* packed, float* bounds);
 
+/* The demo's whole scene preparation in one call (Main.cpp:86-128):
+ * decompose, pad to whole packets with the first quad, per-quad boxes, SAH
+ * batches (targetSize, splitGranularity: the demo uses 512, 8), the reference
+ * box of all vertices, Occluder::bake per batch; the same bytes as those steps
+ * one by one.  *count and *words receive the occluder count and the packed
+ * words over all occluders; with packetCounts, packed and bounds all NULL
+ * only those sizes are computed.  Otherwise packetCounts[count], packed[words]
+ * (occluders back to back, in batch order) and bounds[20 * count] (refMin,
+ * refMax, boundsMin, boundsMax, center per occluder) receive the occluders;
+ * OCC_ERR_CAPACITY if capacityCount / capacityWords are too small (at most
+ * (nIndices/3 + 7)/8 + 1 occluders and 4 * (nIndices/3 + 7) words). */
+int occ_scene_bake(const float* vertices, uint32_t nVertices, const uint32_t* indices, uint32_t nIndices,
+                   uint32_t targetSize, uint32_t splitGranularity, uint32_t capacityCount, uint64_t capacityWords,
+                   uint32_t* count, uint64_t* words, uint32_t* packetCounts, uint32_t* packed, float* bounds);
+
 /* The coverage-mask table as the reference builds it on this host
  * (Rasterizer.cpp:547-604) and the table the GPU uses (generated on x86-64). */
 int occ_build_coverage_table(int64_t* out4096);

@@ -108,6 +108,38 @@ inline void loadMeshBin(const std::string& dir, std::vector<Vec4>& vertices, std
   indices.resize(ni);
 }
 
+// The demo's scene preparation in one call (Main.cpp:86-128): decomposition,
+// padding, SAH batches (targetSize, splitGranularity), one Occluder::bake per
+// batch in the box of all vertices.
+inline std::vector<std::unique_ptr<Occluder>> bakeScene(const std::vector<Vec4>& vertices,
+                                                        const std::vector<uint32_t>& indices, uint32_t targetSize = 512,
+                                                        uint32_t splitGranularity = 8)
+{
+  const uint32_t quads = (uint32_t)(indices.size() / 3) + 7;
+  const uint32_t capCount = quads / 8 + 1;
+  const uint64_t capWords = 4ull * quads;
+  std::vector<uint32_t> counts(capCount), packed(capWords ? capWords : 1);
+  std::vector<float> bounds(20 * (size_t)capCount);
+  uint32_t n = 0;
+  uint64_t words = 0;
+  check(occ_scene_bake(vertices.empty() ? nullptr : &vertices[0].v[0], (uint32_t)vertices.size(),
+                       indices.empty() ? nullptr : indices.data(), (uint32_t)indices.size(), targetSize,
+                       splitGranularity, capCount, capWords, &n, &words, counts.data(), packed.data(), bounds.data()),
+        "occ_scene_bake");
+  std::vector<std::unique_ptr<Occluder>> out;
+  size_t pos = 0;
+  for (uint32_t k = 0; k < n; ++k) {
+    auto o = std::make_unique<Occluder>();
+    o->m_packetCount = counts[k];
+    o->m_vertexData.assign(packed.begin() + pos, packed.begin() + pos + 8 * (size_t)counts[k]);
+    pos += 8 * (size_t)counts[k];
+    Vec4* dst[5] = {&o->m_refMin, &o->m_refMax, &o->m_boundsMin, &o->m_boundsMax, &o->m_center};
+    for (int j = 0; j < 5; ++j) std::memcpy(dst[j]->v, &bounds[20 * (size_t)k + 4 * j], 16);
+    out.push_back(std::move(o));
+  }
+  return out;
+}
+
 // Baked occluders of a scene in one file, and back.
 inline void saveOccluders(const std::string& path, const std::vector<std::unique_ptr<Occluder>>& occluders)
 {

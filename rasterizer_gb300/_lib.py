@@ -90,6 +90,7 @@ SIGNATURES = {
     "occ_sah_generate_batches": (I32, [P, U32, U32, U32, P, P, C.POINTER(U32)]),
     "occ_occluder_bake": (I32, [P, U32, P, P, P, C.POINTER(U32), P, P, P]),
     "occ_occluders_bake_device": (I32, [P, U32, P, P, P, P, P]),
+    "occ_scene_bake": (I32, [P, U32, P, U32, U32, U32, U32, C.c_uint64, C.POINTER(U32), C.POINTER(C.c_uint64), P, P, P]),
     "occ_occluder_upload_device": (I32, [P, P, U32, P, C.POINTER(U32)]),
     "occ_mesh_load_bin": (I32, [C.c_char_p, C.c_char_p, P, C.POINTER(U32), P, C.POINTER(U32)]),
     "occ_occluders_save": (I32, [C.c_char_p, U32, P, P, P]),

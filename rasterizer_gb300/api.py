@@ -168,10 +168,28 @@ def scene_batches(vertices, indices, targetSize: int = 512, splitGranularity: in
 
 
 def bake_scene(vertices, indices, targetSize: int = 512, splitGranularity: int = 8) -> list[Occluder]:
-    """The demo's scene preparation (Main.cpp:86-128): scene_batches, then one
-    occluder per batch quantised in the box of all vertices."""
-    sets, refMin, refMax = scene_batches(vertices, indices, targetSize, splitGranularity)
-    return [Occluder.bake(s, refMin, refMax) for s in sets]
+    """The demo's scene preparation (Main.cpp:86-128) in one native call
+    (occ_scene_bake): scene_batches, then one occluder per batch quantised in
+    the box of all vertices."""
+    v = _f32(vertices).reshape(-1, 4)
+    idx = np.ascontiguousarray(indices, np.uint32).ravel()
+    quads = idx.size // 3 + 7
+    cap_count, cap_words = quads // 8 + 1, 4 * quads
+    counts = np.zeros(max(cap_count, 1), np.uint32)
+    packed = np.zeros(max(cap_words, 1), np.uint32)
+    bounds = np.zeros((max(cap_count, 1), 20), np.float32)
+    n, w = C.c_uint32(), C.c_uint64()
+    check(lib().occ_scene_bake(_ptr(v), len(v), _ptr(idx), idx.size, targetSize, splitGranularity, cap_count,
+                               cap_words, C.byref(n), C.byref(w), _ptr(counts), _ptr(packed), _ptr(bounds)),
+          "occ_scene_bake")
+    out, pos = [], 0
+    for k in range(n.value):
+        c = int(counts[k])
+        b = bounds[k]
+        out.append(Occluder(packed[pos:pos + 8 * c].copy(), c, b[0:4].copy(), b[4:8].copy(), b[8:12].copy(),
+                            b[12:16].copy(), b[16:20].copy()))
+        pos += 8 * c
+    return out
 
 
 def bake_on_gpu(ctx: Context, vertex_sets, refMin, refMax) -> list[Occluder]:

@@ -16,6 +16,7 @@
 #include <queue>
 #include <string>
 #include <system_error>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -622,6 +623,82 @@ int occ_occluder_bake(const float* vertices, uint32_t nVertices, const float ref
     boundsMax[a] = mx.v[a];
     center[a] = xmul(xadd(mx.v[a], mn.v[a]), 0.5f);
   }
+  return OCC_OK;
+}
+
+// The demo's scene preparation in one call (Main.cpp:86-128): quads,
+// padding to whole packets with the first quad, per-quad boxes, SAH batches,
+// the reference box of all vertices, one Occluder::bake per batch (batches
+// baked on several threads, each into its own part of the output).
+int occ_scene_bake(const float* vertices, uint32_t nVertices, const uint32_t* indices, uint32_t nIndices,
+                   uint32_t targetSize, uint32_t splitGranularity, uint32_t capacityCount, uint64_t capacityWords,
+                   uint32_t* count, uint64_t* words, uint32_t* packetCounts, uint32_t* packed, float* bounds)
+{
+  if ((!vertices && nVertices) || (!indices && nIndices) || !count || !words || nIndices % 3 || !splitGranularity)
+    return OCC_ERR_INVALID_ARG;
+  std::vector<uint32_t> q(4 * (size_t)(nIndices / 3) + 4);
+  uint32_t nqIdx = 0;
+  if (nIndices) {
+    const int st = occ_quad_decompose(indices, nIndices, vertices, nVertices, q.data(), &nqIdx);
+    if (st != OCC_OK) return st;
+  }
+  q.resize(nqIdx);
+  while (!q.empty() && q.size() % 32) q.push_back(q[0]);  // Main.cpp:94-98
+  const uint32_t nq = (uint32_t)(q.size() / 4);
+  auto vtx = [&](uint32_t i) { return load4(vertices + 4 * (size_t)i); };
+  std::vector<float> boxes(8 * (size_t)nq);
+  for (uint32_t k = 0; k < nq; ++k) {
+    Box b;
+    for (int c = 0; c < 4; ++c) b.grow(vtx(q[4 * (size_t)k + c]));  // Main.cpp:100-107
+    std::memcpy(&boxes[8 * (size_t)k], b.lo.v, 16);
+    std::memcpy(&boxes[8 * (size_t)k + 4], b.hi.v, 16);
+  }
+  std::vector<uint32_t> flat(std::max<uint32_t>(nq, 1)), offs((size_t)nq + 2);
+  uint32_t nb = 0;
+  if (nq) {
+    const int st = occ_sah_generate_batches(boxes.data(), nq, targetSize, splitGranularity, flat.data(), offs.data(), &nb);
+    if (st != OCC_OK) return st;
+  }
+  Box ref;  // Main.cpp:109-113
+  for (uint32_t i = 0; i < nVertices; ++i) ref.grow(vtx(i));
+  std::vector<uint64_t> wordStart((size_t)nb + 1, 0);
+  for (uint32_t b = 0; b < nb; ++b) wordStart[b + 1] = wordStart[b] + 4ull * (offs[b + 1] - offs[b]);  // a word per vertex
+  *count = nb;
+  *words = wordStart[nb];
+  if (!packetCounts && !packed && !bounds) return OCC_OK;  // sizes only
+  if (!packetCounts || !packed || !bounds) return OCC_ERR_INVALID_ARG;
+  if (nb > capacityCount || wordStart[nb] > capacityWords) return OCC_ERR_CAPACITY;
+  // one Occluder::bake per batch; contiguous runs of batches per thread
+  std::vector<int> status(nb, OCC_OK);
+  auto bakeRange = [&](uint32_t b0, uint32_t b1) {
+    std::vector<float> v;
+    for (uint32_t b = b0; b < b1; ++b) {
+      v.resize(16 * (size_t)(offs[b + 1] - offs[b]));
+      size_t o = 0;
+      for (uint32_t k = offs[b]; k < offs[b + 1]; ++k)
+        for (int c = 0; c < 4; ++c, o += 4) std::memcpy(&v[o], vertices + 4 * (size_t)q[4 * (size_t)flat[k] + c], 16);
+      float* B = bounds + 20 * (size_t)b;
+      std::memcpy(B, ref.lo.v, 16);
+      std::memcpy(B + 4, ref.hi.v, 16);
+      status[b] = occ_occluder_bake(v.data(), (uint32_t)(v.size() / 4), B, B + 4, packed + wordStart[b],
+                                    &packetCounts[b], B + 8, B + 12, B + 16);
+    }
+  };
+  const uint32_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const uint32_t tasks = std::min<uint32_t>(hw, std::max<uint32_t>(1, nb / 64));
+  std::vector<std::future<void>> jobs;
+  for (uint32_t t = 1; t < tasks; ++t) {
+    const uint32_t b0 = (uint32_t)((uint64_t)nb * t / tasks), b1 = (uint32_t)((uint64_t)nb * (t + 1) / tasks);
+    try {
+      jobs.push_back(std::async(std::launch::async, bakeRange, b0, b1));
+    } catch (const std::system_error&) {  // no thread to be had: in sequence
+      bakeRange(b0, b1);
+    }
+  }
+  bakeRange(0, (uint32_t)((uint64_t)nb / tasks));
+  for (auto& j : jobs) j.get();
+  for (int st : status)
+    if (st != OCC_OK) return st;
   return OCC_OK;
 }
 

@@ -92,22 +92,12 @@ def test_mesh_bin_ragged_is_refused(tmp_path):
 FACADE_FILES = r"""
 #include "rasterizer_gb300/Rasterizer.hpp"
 #include <cstdio>
-// Host only: mesh files -> bake (decompose, pad, SAH, Occluder::bake) -> file -> load.
+// Host only: mesh files -> the demo's scene preparation -> file -> load.
 int main(int argc, char** argv) {
   std::vector<gb300::Vec4> v;
   std::vector<uint32_t> idx;
   gb300::loadMeshBin(argv[1], v, idx);
-  auto quads = gb300::QuadDecomposition::decompose(idx, v);
-  while (quads.size() % 32) quads.push_back(quads[0]);
-  gb300::Vec4 lo{{1e30f, 1e30f, 1e30f, 1e30f}}, hi{{-1e30f, -1e30f, -1e30f, -1e30f}};
-  for (auto& p : v) for (int k = 0; k < 4; ++k) { lo.v[k] = p.v[k] < lo.v[k] ? p.v[k] : lo.v[k]; hi.v[k] = p.v[k] > hi.v[k] ? p.v[k] : hi.v[k]; }
-  std::vector<std::unique_ptr<gb300::Occluder>> occ;
-  std::vector<gb300::Vec4> verts;
-  for (size_t q = 0; q < quads.size(); ++q) {
-    verts.push_back(v[quads[q]]);
-    if (verts.size() == 256) { occ.push_back(gb300::Occluder::bake(verts, lo, hi)); verts.clear(); }
-  }
-  if (!verts.empty()) occ.push_back(gb300::Occluder::bake(verts, lo, hi));
+  auto occ = gb300::bakeScene(v, idx);
   gb300::saveOccluders(argv[2], occ);
   auto back = gb300::loadOccluders(argv[2]);
   if (back.size() != occ.size()) return 2;
@@ -115,7 +105,9 @@ int main(int argc, char** argv) {
     if (back[k]->m_packetCount != occ[k]->m_packetCount || back[k]->m_vertexData != occ[k]->m_vertexData ||
         std::memcmp(back[k]->m_boundsMin.v, occ[k]->m_boundsMin.v, 16) || std::memcmp(back[k]->m_center.v, occ[k]->m_center.v, 16))
       return 3;
-  std::printf("%zu\n", occ.size());
+  // the same occluders as baking in steps: print the words for the caller to compare
+  for (auto& o : occ)
+    for (uint32_t w : o->m_vertexData) std::printf("%u\n", w);
   return 0;
 }
 """
@@ -134,4 +126,33 @@ def test_cpp_facade_files(tmp_path):
                     "-Wl,-rpath," + os.path.dirname(so)], check=True)
     r = subprocess.run([exe, str(tmp_path), str(tmp_path / "scene.occ")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    assert int(r.stdout) >= 1 and os.path.getsize(str(tmp_path / "scene.occ")) > 0
+    words = np.array([int(x) for x in r.stdout.split()], np.uint32)
+    want = np.concatenate([o.packed[:8 * o.packetCount] for o in api.bake_scene(mesh.vertices, mesh.indices)])
+    assert np.array_equal(words, want)
+
+
+def test_scene_bake_in_one_call_equals_the_steps():
+    """occ_scene_bake (the demo's preparation natively) gives the bytes of
+    decompose -> pad -> boxes -> SAH -> Occluder::bake per batch; empty
+    meshes give no occluders; bad indices and short buffers are refused."""
+    import ctypes as C
+    from rasterizer_gb300._lib import lib
+    for mesh in (scenes.boxes_scene(), scenes.city_scene(grid=16, target_tris=20_000)):
+        sets, lo, hi = api.scene_batches(mesh.vertices, mesh.indices)
+        want = [api.Occluder.bake(s, lo, hi) for s in sets]
+        got = api.bake_scene(mesh.vertices, mesh.indices)
+        assert len(got) == len(want) and all(_same(a, b) for a, b in zip(got, want))
+    assert api.bake_scene(np.zeros((0, 4), np.float32), np.zeros(0, np.uint32)) == []
+    v = np.zeros((4, 4), np.float32)
+    n, w = C.c_uint32(), C.c_uint64()
+    bad = np.array([0, 1, 9], np.uint32)
+    assert lib().occ_scene_bake(v.ctypes.data, 4, bad.ctypes.data, 3, 512, 8, 0, 0, C.byref(n), C.byref(w),
+                                None, None, None) == -1
+    mesh = scenes.boxes_scene()
+    vv = np.ascontiguousarray(mesh.vertices, np.float32).reshape(-1, 4)
+    ii = np.ascontiguousarray(mesh.indices, np.uint32)
+    assert lib().occ_scene_bake(vv.ctypes.data, len(vv), ii.ctypes.data, ii.size, 512, 8, 0, 0, C.byref(n),
+                                C.byref(w), None, None, None) == 0 and n.value >= 1
+    counts, packed, bounds = np.zeros(1, np.uint32), np.zeros(8, np.uint32), np.zeros(20, np.float32)
+    assert lib().occ_scene_bake(vv.ctypes.data, len(vv), ii.ctypes.data, ii.size, 512, 8, 1, 8, C.byref(n),
+                                C.byref(w), counts.ctypes.data, packed.ctypes.data, bounds.ctypes.data) == -4
