@@ -523,6 +523,12 @@ def run_large(ctx, net, dev):
     prep_s = t.lap()
     occ = [api.Occluder.bake(s, ref_lo, ref_hi) for s in sets]              # Occluder::bake per batch (host)
     host_bake_s = t.lap()
+    native = api.bake_scene(mesh.vertices, mesh.indices)                    # the same in one native call
+    native_s = t.lap()
+    native_same = len(native) == len(occ) and all(
+        a.packetCount == b.packetCount and np.array_equal(a.packed[:8 * a.packetCount], b.packed[:8 * b.packetCount])
+        for a, b in zip(native, occ))
+    del native
     bake_s = prep_s + host_bake_s
     gpu_bake = _gpu_bake_timing(ctx, sets, ref_lo, ref_hi, occ)
     t.lap()
@@ -584,6 +590,7 @@ def run_large(ctx, net, dev):
                         f"per launch ({LARGE_NQ} pool)",
             "bake_seconds": bake_s,
             "bake_steps_seconds": {"decompose_and_sah": prep_s, "occluder_bake_host": host_bake_s},
+            "scene_bake_one_call": {"seconds": native_s, "identical": bool(native_same)},
             "gpu_bake": gpu_bake,
             "baked_file": {"load_seconds": load_s, "bytes": file_bytes, "identical": bool(same),
                            "speedup_vs_bake": bake_s / max(load_s, 1e-9)},
