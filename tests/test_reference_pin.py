@@ -233,3 +233,58 @@ def test_sah_tied_and_signed_zero_centres():
     assert len(mine) == nb
     for b in range(nb):
         assert np.array_equal(mine[b], flat[offs[b]:offs[b + 1]])
+
+
+def test_decomposition_random_meshes():
+    """60 random small meshes (shared vertices, planar and non-planar, no
+    repeated index within a triangle): the same quads as the reference."""
+    L = bindings.ref_lib()
+    for seed in range(60):
+        rng = np.random.default_rng(1000 + seed)
+        nv = int(rng.integers(4, 60))
+        v = (np.round(rng.uniform(-3, 3, (nv, 4)) * 2) / 2).astype(np.float32)
+        v[:, 3] = 1
+        if seed % 2:
+            v[:, 1] = 0  # planar: many mergeable pairs
+        t = rng.integers(0, nv, (int(rng.integers(1, 200)), 3)).astype(np.uint32)
+        t = t[(t[:, 0] != t[:, 1]) & (t[:, 1] != t[:, 2]) & (t[:, 0] != t[:, 2])]
+        if not len(t):
+            continue
+        i = np.ascontiguousarray(t).ravel()
+        out = np.zeros(4 * len(t), np.uint32)
+        n = L.ref_decompose(bindings._ptr(i), i.size, bindings._ptr(v), nv, bindings._ptr(out))
+        assert np.array_equal(api.QuadDecomposition.decompose(i, v), out[:n]), seed
+
+
+def test_bake_random_and_special_vertex_sets():
+    """100 random Occluder::bake inputs: degenerate quads, NaN / infinite /
+    huge / subnormal / signed-zero coordinates, integral coordinates (ties in
+    the bounds), a reference box of zero height: packed words, bounds and
+    centre bit for bit as the reference's."""
+    L = bindings.ref_lib()
+    specials = np.array([np.nan, np.inf, -np.inf, -0.0, 0.0, 1e38, -1e38, 1e-40], np.float32)
+    for seed in range(100):
+        rng = np.random.default_rng(2000 + seed)
+        nq = 8 * int(rng.integers(1, 40))
+        v = rng.normal(0, 10, (4 * nq, 4)).astype(np.float32)
+        v[:, 3] = 1
+        mode = seed % 5
+        if mode == 1:
+            v[: 4 * (nq // 3)] = v[0]
+        if mode == 2:
+            k = rng.integers(0, len(v), 6)
+            v[k, rng.integers(0, 3, 6)] = rng.choice(specials, 6)
+        if mode == 3:
+            v = np.round(v)
+        lo = np.array([-20, -20, -20, 1], np.float32)
+        hi = np.array([20, 20, 20, 1], np.float32)
+        if mode == 4:
+            hi[1] = lo[1]
+        packed = np.zeros(len(v), np.uint32)
+        bmin, bmax, ctr = (np.zeros(4, np.float32) for _ in range(3))
+        pc = L.ref_bake(bindings._ptr(v), len(v), bindings._ptr(lo), bindings._ptr(hi), bindings._ptr(packed),
+                        bindings._ptr(bmin), bindings._ptr(bmax), bindings._ptr(ctr))
+        o = api.Occluder.bake(v, lo, hi)
+        assert o.packetCount == pc and np.array_equal(o.packed[:8 * pc], packed[:8 * pc]), seed
+        for mine, ref in ((o.boundsMin, bmin), (o.boundsMax, bmax), (o.center, ctr)):
+            assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32)), seed
