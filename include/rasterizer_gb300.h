@@ -228,12 +228,13 @@ int occ_batch_set_zero_depth(occ_batch b, int enable);
  * captured again with them.  tuned[6] = {setup, fill, walk, raster CTAs per
  * SM, tiles per fetch, query form: 255 = one box per thread in place, 1..8 =
  * frustum survivors listed per warp over that many rounds of 32 boxes};
- * msBefore/msAfter[7] as occ_batch_profile (either may be NULL). */
+ * msBefore/msAfter[7] as occ_batch_profile (either may be NULL).  No reference
+ * counterpart (the reference has no launch shapes). */
 int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[6], float msBefore[7], float msAfter[7]);
 /* Sets the launch shapes directly, in occ_batch_autotune's tuned[6] layout
  * (0 in any entry: the default), e.g. to reuse a tuned choice for a batch of
  * the same shape without timing it again.  CTAs per SM and tiles per fetch
- * up to 64; query form 0, 1..8 or 255. */
+ * up to 64; query form 0, 1..8 or 255.  No reference counterpart. */
 int occ_batch_set_tuning(occ_batch b, const uint32_t tune[6]);
 /* Work counts of the last launch (syncs): block rows walked, row-walk
  * checkpoints, super-tile list entries, chunks with a drawn occluder, warp-tiles
