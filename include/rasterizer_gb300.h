@@ -104,17 +104,22 @@ int occ_raster_query_batch_device(occ_raster r, uint32_t n, const void* dMins, c
                                   void* dVisibleBits, void* dNeedsClippingBits);
 /* No counterpart in the reference (its queries never allocate).  The same
  * queries as occ_raster_query_batch for callers that must not allocate device
- * memory: code in a cudaLaunchHostFunc callback, where CUDA calls may not
- * synchronise; frame loops with a fixed memory budget reserved at start-up;
- * engines that forbid cudaMalloc/cudaFree on their hot thread because both can
- * stall the whole device.  Boxes and result bits are staged in one fixed
- * device array of OCC_NOALLOC_MAX_QUERIES boxes (about 2 MiB, held on every
- * GPU that loads the library until exit); larger n is rejected.  The first
- * call on a device looks up the array's device address, so make that first
- * call before any stream capture.  All calls on a device share the array:
- * calls whose work overlaps on the GPU race and must be serialised.  Pending
- * rasterisation is not run here (running it may allocate): flush first.
- * Synchronous: returns when the bits are in the host buffers. */
+ * memory: frame loops with a fixed memory budget reserved at start-up, and
+ * engines that forbid cudaMalloc/cudaFree on their frame thread because both
+ * can synchronise and stall the whole device.  Boxes and result bits are
+ * staged in one fixed device array of OCC_NOALLOC_MAX_QUERIES boxes (about
+ * 2 MiB, held on every GPU that loads the library until exit); larger n is
+ * rejected.  Call it from an ordinary host thread, never from a host function
+ * enqueued with cudaLaunchHostFunc: it makes CUDA calls and blocks until the
+ * bits are in the host buffers.  The first call on a device looks up the
+ * array's device address (a one-time set-up), so make that first call before
+ * any stream capture.  "Allocates nothing" holds once the library's device
+ * code is loaded on the device: with lazy module loading the first kernel
+ * launch or symbol lookup loads it, and loading allocates, so flush a
+ * rasterizer or make one no-allocation call during set-up.  All calls on a
+ * device share the array and it keeps the last call's contents: calls whose
+ * work overlaps on the GPU race and must be serialised.  Pending
+ * rasterisation is not run here (running it may allocate): flush first. */
 #define OCC_NOALLOC_MAX_QUERIES 65536u
 int occ_raster_query_batch_noalloc(occ_raster r, uint32_t n, const float* mins, const float* maxs,
                                    uint32_t* visibleBits, uint32_t* needsClippingBits);

@@ -16,7 +16,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref.so")
-REF_SOURCES = "/root/reference/SoftwareRasterizer"
+# where the reference's sources lie; OCC_REF_DIR overrides the default
+REF_SOURCES = os.environ.get("OCC_REF_DIR", "/root/reference/SoftwareRasterizer")
 
 P = C.c_void_p
 U32 = C.c_uint32

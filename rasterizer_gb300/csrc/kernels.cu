@@ -1873,14 +1873,14 @@ cudaError_t launch_cull_labels(const FrameParams& P, cudaStream_t stream)
 
 // ---- queries without device allocation -------------------------------------------------
 //
-// Callers that must not allocate device memory -- code running in a
-// cudaLaunchHostFunc callback (where CUDA API calls are not allowed to
-// synchronise), frame loops with a fixed memory budget that reserve
-// everything at start-up, or engines that forbid cudaMalloc/cudaFree on their
-// hot thread because both can stall the whole device -- still need to test
-// boxes against a rasterizer.  For them occ_raster_query_batch_noalloc stages
-// the boxes and the result bits in the fixed array below instead of in
-// per-context buffers that grow on demand.
+// Callers that must not allocate device memory -- frame loops with a fixed
+// memory budget that reserve everything at start-up, or engines that forbid
+// cudaMalloc/cudaFree on their frame thread because both can synchronise and
+// stall the whole device -- still need to test boxes against a rasterizer.
+// For them occ_raster_query_batch_noalloc stages the boxes and the result bits
+// in the fixed array below instead of in per-context buffers that grow on
+// demand.  It is called from an ordinary host thread (it makes CUDA calls and
+// waits for the bits), not from a host function on a stream.
 //
 // The array holds at most kNoAllocMaxQueries boxes (about 2 MiB in all) and
 // lives on every GPU that loads this library until the process exits.  All
