@@ -46,6 +46,8 @@ int occ_version(void);
 
 /* ---- context ---------------------------------------------------------------- */
 int occ_ctx_create(int device, occ_ctx* out);
+/* Destroy a context after every rasterizer, batch and selector made on it:
+ * they refer to its stream and occluder pool. */
 int occ_ctx_destroy(occ_ctx ctx);
 int occ_ctx_synchronize(occ_ctx ctx);
 void* occ_ctx_stream(occ_ctx ctx); /* the context's cudaStream_t */
@@ -219,8 +221,10 @@ int occ_mlp_train_step(occ_mlp m, uint32_t n, const float* features, const float
  * per view (top scores); trackWins counts per occluder the pixels whose final
  * depth it produced (labels, and the next launch's previous-frame feature). */
 int occ_batch_set_selection(occ_batch b, occ_mlp mlp, float fraction, int trackWins);
-/* With enable != 0, each launch first zeroes the depth of every view it
- * clears.  The reference's clear only marks blocks (hiZ := 1) and its
+/* With enable != 0, every view the batch clears also starts each launch with
+ * zero depth, the state of a freshly created rasterizer: the kernels write
+ * zeros to the blocks no fragment reaches (no separate pass over the buffer).
+ * The reference's clear only marks blocks (hiZ := 1) and its
  * queryVisibility still reads the old depth of a cleared block that a query
  * box covers partially (Rasterizer.cpp:305-344), so a frame's results depend
  * on the frames before it; zeroed depth makes each frame stand alone (used to
@@ -230,17 +234,21 @@ int occ_batch_set_zero_depth(occ_batch b, int enable);
  * launch shapes -- resident CTAs per SM of the persistent setup, list-fill and
  * raster kernels, row-walk CTAs per SM, tiles per raster queue fetch, the
  * query kernel's form -- and keeps, per stage, the fastest; the graph is
- * captured again with them.  tuned[6] = {setup, fill, walk, raster CTAs per
- * SM, tiles per fetch, query form: 255 = one box per thread in place, 1..8 =
- * frustum survivors listed per warp over that many rounds of 32 boxes};
- * msBefore/msAfter[7] as occ_batch_profile (either may be NULL).  No reference
- * counterpart (the reference has no launch shapes). */
-int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[6], float msBefore[7], float msAfter[7]);
-/* Sets the launch shapes directly, in occ_batch_autotune's tuned[6] layout
- * (0 in any entry: the default), e.g. to reuse a tuned choice for a batch of
- * the same shape without timing it again.  CTAs per SM and tiles per fetch
- * up to 64; query form 0, 1..8 or 255.  No reference counterpart. */
-int occ_batch_set_tuning(occ_batch b, const uint32_t tune[6]);
+ * captured again with them.  tuned[OCC_TUNING_FIELDS] = {setup, fill, walk,
+ * raster CTAs per SM, raster units per queue fetch, query form: 255 = one box
+ * per thread in place, 1..8 = frustum survivors listed per warp over that many
+ * rounds of 32 boxes, raster unit rows: 1, 2 or 4 block rows of 8 blocks per
+ * warp, reserved (0)}; msBefore/msAfter[7] as occ_batch_profile (either may be
+ * NULL).  No reference counterpart (the reference has no launch shapes). */
+#define OCC_TUNING_FIELDS 8
+int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[OCC_TUNING_FIELDS], float msBefore[7],
+                       float msAfter[7]);
+/* Sets the launch shapes directly, in occ_batch_autotune's layout (0 in any
+ * entry: the default), e.g. to reuse a tuned choice for a batch of the same
+ * shape without timing it again.  CTAs per SM and units per fetch up to 64;
+ * query form 0, 1..8 or 255; unit rows 0, 1, 2 or 4.  No reference
+ * counterpart. */
+int occ_batch_set_tuning(occ_batch b, const uint32_t tune[OCC_TUNING_FIELDS]);
 /* Work counts of the last launch (syncs): block rows walked, row-walk
  * checkpoints, super-tile list entries, chunks with a drawn occluder, warp-tiles
  * rasterised (the others only cleared), the batch's chunk count, and the

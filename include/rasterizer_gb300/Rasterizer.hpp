@@ -340,7 +340,7 @@ class Batch {
   void setSecondPass(bool enable) { check(occ_batch_set_second_pass(b_, enable ? 1 : 0), "occ_batch_set_second_pass"); }
   void autotune(uint32_t iterations = 5) { check(occ_batch_autotune(b_, iterations, nullptr, nullptr, nullptr), "occ_batch_autotune"); }
   // launch shapes in occ_batch_autotune's layout (0 = default)
-  void setTuning(const uint32_t tune[6]) { check(occ_batch_set_tuning(b_, tune), "occ_batch_set_tuning"); }
+  void setTuning(const uint32_t tune[OCC_TUNING_FIELDS]) { check(occ_batch_set_tuning(b_, tune), "occ_batch_set_tuning"); }
   void launch() { check(occ_batch_launch(b_), "occ_batch_launch"); }
   // false if a launch since the last check outgrew the scratch (grown now: run the frame again)
   bool check_capacity()

@@ -40,6 +40,16 @@ def unpack_bits(words: np.ndarray, n: int) -> np.ndarray:
 _context_serial = itertools.count(1)
 
 
+def _context_open(child) -> bool:
+    """True while the context that made `child` is open.  A context's close()
+    closes its children first; only when the garbage collector finalises a
+    context before a child whose weak entry it had already dropped (objects
+    in one reference cycle, e.g. at interpreter exit) is the child's native
+    object gone with the context, and the child must not touch it."""
+    ctx = getattr(child, "ctx", None)
+    return ctx is None or getattr(ctx, "handle", None) is not None
+
+
 class Context:
     """One GPU and one CUDA stream; owns the uploaded occluders.  Closing it
     first closes the rasterizers, batches and selectors made on it."""
@@ -329,7 +339,8 @@ class Rasterizer:
 
     def close(self):
         if getattr(self, "handle", None):
-            lib().occ_raster_destroy(self.handle)
+            if _context_open(self):
+                lib().occ_raster_destroy(self.handle)
             self.handle = None
 
     def __del__(self):
@@ -504,7 +515,8 @@ class PreparedBatch:
 
     def close(self):
         if getattr(self, "handle", None):
-            lib().occ_batch_destroy(self.handle)
+            if _context_open(self):
+                lib().occ_batch_destroy(self.handle)
             self.handle = None
 
     def __del__(self):
@@ -575,28 +587,28 @@ class PreparedBatch:
                                             int(bool(trackWins))), "occ_batch_set_selection")
         self._selector = mlp  # the captured launch reads the network's weights
 
+    # occ_batch_autotune / occ_batch_set_tuning layout (OCC_TUNING_FIELDS entries, the last reserved)
+    TUNING_KEYS = ("setup_ctas_per_sm", "fill_ctas_per_sm", "walk_ctas_per_sm", "raster_ctas_per_sm",
+                   "raster_units_per_fetch", "query_rounds", "raster_unit_rows", "reserved")
+
     def autotune(self, iterations: int = 5) -> dict:
         """Picks the launch shapes of the persistent kernels by timing the
         batch's own frame stage by stage; returns the choice and the stage
         times before and after."""
-        tuned = np.zeros(6, np.uint32)
+        tuned = np.zeros(len(self.TUNING_KEYS), np.uint32)
         before = np.zeros(7, np.float32)
         after = np.zeros(7, np.float32)
         check(lib().occ_batch_autotune(self.handle, iterations, _ptr(tuned), _ptr(before), _ptr(after)),
               "occ_batch_autotune")
-        keys = ("setup_ctas_per_sm", "fill_ctas_per_sm", "walk_ctas_per_sm", "raster_ctas_per_sm",
-                "raster_tiles_per_fetch", "query_rounds")
         names = ("setup", "scan", "fill", "walk", "raster", "query", "selection")
-        return {"tuned": {k: int(v) for k, v in zip(keys, tuned)},
+        return {"tuned": {k: int(v) for k, v in zip(self.TUNING_KEYS[:-1], tuned)},
                 "ms_before": {k: float(v) for k, v in zip(names, before)},
                 "ms_after": {k: float(v) for k, v in zip(names, after)}}
 
     def setTuning(self, tuned: dict) -> None:
         """Sets launch shapes directly (keys as `autotune()["tuned"]`; missing
         keys or 0: the default)."""
-        keys = ("setup_ctas_per_sm", "fill_ctas_per_sm", "walk_ctas_per_sm", "raster_ctas_per_sm",
-                "raster_tiles_per_fetch", "query_rounds")
-        t = np.array([int(tuned.get(k, 0)) for k in keys], np.uint32)
+        t = np.array([int(tuned.get(k, 0)) for k in self.TUNING_KEYS], np.uint32)
         check(lib().occ_batch_set_tuning(self.handle, _ptr(t)), "occ_batch_set_tuning")
 
     def stats(self) -> dict:
@@ -672,7 +684,8 @@ class OccluderSelector:
 
     def close(self):
         if getattr(self, "handle", None):
-            lib().occ_mlp_destroy(self.handle)
+            if _context_open(self):
+                lib().occ_mlp_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

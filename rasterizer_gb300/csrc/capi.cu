@@ -35,7 +35,7 @@ cudaError_t launch_mlp_backward(const float* score, const float* target, uint32_
 uint32_t mlp_grad_blocks(uint32_t B);
 cudaError_t launch_mlp_publish(const float* params, MlpDevice* mlp, cudaStream_t stream);
 cudaError_t launch_cull_labels(const FrameParams& P, cudaStream_t stream);
-void tuning_limits(uint32_t out[4]);
+void tuning_limits(uint32_t out[6]);
 cudaError_t launch_adam(float* params, const float* grad, float* m, float* v, float lr, uint32_t step,
                         cudaStream_t stream);
 int mlp_param_count();
@@ -390,7 +390,7 @@ int run_batch(occ_ctx_s* ctx, FrameScratch& S, std::vector<ViewJob>& jobs, bool 
   OCC_CHECK(S.activeChunks.reserve(L.chunks.size()));
   OCC_CHECK(S.viewActive.reserve(L.chunks.size()));
   OCC_CHECK(S.viewActiveCount.reserve(nv));
-  OCC_CHECK(S.activeTiles.reserve((size_t)L.numTiles * kUnitsPerTile));
+  OCC_CHECK(S.activeTiles.reserve((size_t)L.numTiles * kMaxUnitsPerTile));
   if (S.header.n == 0) {
     OCC_CHECK(S.header.reserve(1));
     OCC_CUDA(cudaMemsetAsync(S.header.p, 0, sizeof(FrameHeader), ctx->stream));
@@ -1005,7 +1005,7 @@ struct occ_batch_s {
   const struct occ_mlp_s* mlp = nullptr;
   float selectFrac = 1.0f;
   bool trackWins = false, features = false;
-  bool zeroDepth = false;  // zero every view's depth at the start of each launch
+  bool zeroDepth = false;  // cleared views start each launch with zero depth (kViewZeroDepth)
   bool secondPass = false; // after the top-K pass, draw the other candidates still visible
   bool cullLabels = false; // per-pixel owners and per-command cull counts (training labels)
   LaunchTuning tune{};     // launch shapes (occ_batch_autotune)
@@ -1124,10 +1124,6 @@ int capture(occ_batch_s* b)
   OCC_CUDA(cudaEventRecord(b->ringEv[b->cur], ctx->stream));
   OCC_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t e1 = cudaMemcpyAsync(S.tables.p, b->ring[b->cur].p, b->offCmds, cudaMemcpyHostToDevice, ctx->stream);
-  if (b->zeroDepth)
-    for (auto& J : b->jobs)
-      if (e1 == cudaSuccess && J.clear)
-        e1 = cudaMemsetAsync(J.r->depth.p, 0, (size_t)J.r->width * J.r->height * sizeof(uint16_t), ctx->stream);
   if (labels) {
     for (auto& J : b->jobs)
       if (e1 == cudaSuccess)
@@ -1396,6 +1392,9 @@ int occ_batch_set_selection(occ_batch b, occ_mlp mlp, float fraction, int trackW
   if (mlp && !(fraction > 0.0f && fraction <= 1.0f)) return fail(OCC_ERR_INVALID_ARG, "fraction must be in (0, 1]");
   if (mlp && mlp->ctx != b->ctx) return fail(OCC_ERR_INVALID_ARG, "network from another context");
   const size_t n = std::max<size_t>(b->L.cmds.size(), 1);
+  if (trackWins)
+    for (const auto& V : b->L.views)
+      if (V.cmdCount > 65534u) return fail(OCC_ERR_INVALID_ARG, "win counting takes at most 65,534 occluders per view");
   b->features = mlp != nullptr || trackWins != 0;
   b->mlp = mlp;
   b->selectFrac = fraction;
@@ -1440,10 +1439,10 @@ static int profile_with(occ_batch b, const LaunchTuning& t, uint32_t iterations,
   return st;
 }
 
-int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[6], float msBefore[7], float msAfter[7])
+int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[8], float msBefore[7], float msAfter[7])
 {
   if (!b || !iterations) return fail(OCC_ERR_INVALID_ARG, "bad argument");
-  uint32_t lim[4];
+  uint32_t lim[6];
   tuning_limits(lim);
   LaunchTuning best = b->tune;
   float ms[7], base[7];
@@ -1473,7 +1472,9 @@ int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[6], floa
   OCC_CHECK(search(&LaunchTuning::setupPerSm, 0, upTo(lim[0])));
   OCC_CHECK(search(&LaunchTuning::fillPerSm, 2, upTo(lim[1])));
   OCC_CHECK(search(&LaunchTuning::walkPerSm, 3, {2, 4, 8, 16}));
-  OCC_CHECK(search(&LaunchTuning::rasterPerSm, 4, upTo(lim[2])));
+  OCC_CHECK(search(&LaunchTuning::rasterRows, 4, {1, 2, 4}));
+  const uint32_t rows = best.rasterRows ? best.rasterRows : kDefaultRasterRows;
+  OCC_CHECK(search(&LaunchTuning::rasterPerSm, 4, upTo(lim[rows == 1 ? 2 : (rows == 2 ? 3 : 4)])));
   OCC_CHECK(search(&LaunchTuning::rasterChunk, 4, {1, 2, 4, 8, 16}));
   OCC_CHECK(search(&LaunchTuning::queryRounds, 5, {kQueryPerThread, 1, 2, 4, 8}));
   b->tune = best;
@@ -1486,6 +1487,8 @@ int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[6], floa
     tuned[3] = best.rasterPerSm;
     tuned[4] = best.rasterChunk;
     tuned[5] = best.queryRounds;
+    tuned[6] = best.rasterRows ? best.rasterRows : kDefaultRasterRows;
+    tuned[7] = 0;
   }
   return OCC_OK;
 }
@@ -1529,12 +1532,15 @@ int occ_batch_set_second_pass(occ_batch b, int enable)
   return capture(b);
 }
 
-int occ_batch_set_tuning(occ_batch b, const uint32_t tune[6])
+int occ_batch_set_tuning(occ_batch b, const uint32_t tune[8])
 {
   if (!b || !tune) return fail(OCC_ERR_INVALID_ARG, "null argument");
   for (int i = 0; i < 5; ++i)
     if (tune[i] > 64) return fail(OCC_ERR_INVALID_ARG, "launch shape out of range (at most 64)");
   if (tune[5] > kQueryRounds && tune[5] != kQueryPerThread) return fail(OCC_ERR_INVALID_ARG, "unknown query form");
+  if (tune[6] != 0 && tune[6] != 1 && tune[6] != 2 && tune[6] != 4)
+    return fail(OCC_ERR_INVALID_ARG, "raster unit rows must be 1, 2 or 4 (0: the default)");
+  if (tune[7] != 0) return fail(OCC_ERR_INVALID_ARG, "tuning entry 7 is reserved (0)");
   LaunchTuning t{};
   t.setupPerSm = tune[0];
   t.fillPerSm = tune[1];
@@ -1542,6 +1548,7 @@ int occ_batch_set_tuning(occ_batch b, const uint32_t tune[6])
   t.rasterPerSm = tune[3];
   t.rasterChunk = tune[4];
   t.queryRounds = tune[5];
+  t.rasterRows = tune[6];
   b->tune = t;
   return capture(b);
 }
@@ -1550,7 +1557,14 @@ int occ_batch_set_zero_depth(occ_batch b, int enable)
 {
   if (!b) return fail(OCC_ERR_INVALID_ARG, "null batch");
   b->zeroDepth = enable != 0;
-  return capture(b);
+  // the kernels zero the depth of every block of a cleared view that no
+  // fragment reaches; the flag travels in the view table of the next launch
+  for (size_t v = 0; v < b->L.views.size(); ++v) {
+    uint32_t& f = b->L.views[v].flags;
+    f = (b->zeroDepth && b->jobs[v].clear) ? (f | kViewZeroDepth) : (f & ~kViewZeroDepth);
+  }
+  b->dirty = true;
+  return OCC_OK;
 }
 
 int occ_batch_read_selection(occ_batch b, uint32_t view, float* features, uint32_t* wins, uint8_t* candidate,

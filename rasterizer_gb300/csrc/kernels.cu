@@ -51,7 +51,8 @@ static uint32_t g_walkBlocks = 152 * 8;
 // Persistent grids of the setup / list-fill / raster kernels (resident CTAs x SMs),
 // looping over the launch's active chunks and tiles.
 static uint32_t g_sms = 152;
-static uint32_t g_setupPerSm = 4, g_fillPerSm = 4, g_rasterPerSm = 4;  // occupancy limits
+static uint32_t g_setupPerSm = 4, g_fillPerSm = 4;  // occupancy limits
+static uint32_t g_rasterPerSm[3] = {6, 6, 4};        // per raster unit shape R = 1, 2, 4
 
 static uint32_t grid_of(uint32_t tuned, uint32_t limit, uint32_t work)
 {
@@ -903,37 +904,44 @@ __global__ void __launch_bounds__(256) k_walk(FrameParams P)
 
 // ---- k_raster ------------------------------------------------------------------------
 //
-// One CTA of 128 threads per raster unit of 8 x kRasterRows blocks (half a
-// warp-tile).  Thread t owns pixel row t%8 of block t/8 (4 packed words in
-// registers); the eight threads of a block keep its hiZ in step.  The CTA
-// walks its super-tile's quad list in order, keeps the quads that overlap the
-// unit and are not already hidden in an ordered local list, and turns them
-// into (quad, block) fragments, 128 at a time: every thread computes one
-// fragment (coverage mask, packed depth rows), then each block's eight threads
-// merge the fragments aimed at it in list order with the reference's hiZ
-// test, fast-clear overwrite and max-merge (Rasterizer.cpp:1148-1290).  A unit
-// is mostly latency (record loads, fragment arithmetic, the ordered merge):
-// small units let eight CTAs per SM overlap eight of them.
+// Persistent warps, each on its own: a warp takes a queued raster unit of
+// 8 x R blocks (R = 1, 2 or 4 block rows of an 8x4-block warp-tile) from the
+// global queue, walks the unit's super-tile quad list in order, keeps the
+// quads that overlap the unit and are not already hidden in an ordered local
+// list, and turns them into (quad, block) fragments, 32 at a time: every lane
+// computes one fragment (coverage mask, packed depth rows) into its slot in the
+// warp's shared memory, then each block's lanes merge the fragments aimed at
+// the block in list order with the reference's hiZ test, fast-clear overwrite
+// and max-merge (Rasterizer.cpp:1148-1290).  A block is held by 32 / (8 R)
+// lanes, each with 2 R of its pixel rows in registers.  Only warp-level
+// synchronisation is used: units are latency chains (record loads, fragment
+// arithmetic, the ordered merge), and up to 32 warps per SM overlap as many.
 
-constexpr int kUnitBlocks = kTileW * kRasterRows;       // 16 blocks
-constexpr int kRasterThreads = 8 * kUnitBlocks;          // one thread per block row: 128
-constexpr int kRasterMinBlocks = 8;  // resident CTAs per SM the register budget is sized for
-constexpr int kLocalCap = 512;   // overlapping quads buffered per unit
-constexpr int kFragStride = 33;  // words per fragment slot (padding: conflict-free banks)
-constexpr int kScanPerRound = 2 * kRasterThreads;
-constexpr int kMaskWords = kRasterThreads / 32;
+template <int R>
+struct UnitShape {
+  static constexpr int kBlocks = 8 * R;                  // blocks per unit
+  static constexpr int kLanesPerBlock = 32 / kBlocks;    // 4, 2, 1
+  static constexpr int kRowsPerLane = 8 / kLanesPerBlock;  // 2, 4, 8
+};
 
-struct RasterSmem {
-  uint32_t lq[kLocalCap];        // quad index
-  uint32_t lrect[kLocalCap];     // quad rect within the unit: x0 | y0 << 3 | w << 5 | h << 9
-  uint32_t loff[kLocalCap];      // first fragment of each local quad
-  uint32_t frag[kRasterThreads * kFragStride];
-  uint32_t meta[kRasterThreads]; // per fragment slot: maxZ << 16 | valid << 5 | target block
-  uint32_t fcmd[kRasterThreads]; // per fragment slot: command (win counting only)
-  uint32_t bmask[kUnitBlocks][kMaskWords];  // per block: fragment slots aimed at it
-  uint32_t hiz[kUnitBlocks];     // per block: current hiZ
-  uint32_t scan[kRasterThreads / 32];
-  uint32_t n;
+constexpr int kRasterWarps = 4;                    // warps per CTA (they share nothing)
+// resident CTAs per SM the register budget is sized for: 80 registers a
+// thread at 1 or 2 block rows (no spills of the merge state), 128 at 4
+template <int R>
+constexpr int kRasterMinBlocks = R == 4 ? 4 : 6;
+constexpr int kRasterThreads = 32 * kRasterWarps;
+constexpr int kWarpListCap = 64;                   // listed quads buffered per warp
+constexpr int kFragStride = 33;                    // words per fragment slot (odd: conflict-free banks)
+
+struct WarpRasterSmem {
+  uint32_t frag[32 * kFragStride];  // one fragment slot per lane: 8 rows x 4 packed words
+  uint32_t meta[32];                // per slot: maxZ << 16 | target block
+  uint32_t fcmd[32];                // per slot: command within the view + 1 (win counting)
+  uint32_t bmask[32];               // per block: slots aimed at it
+  uint32_t hiz[32];                 // per block: current hiZ
+  uint32_t lq[kWarpListCap];        // listed quad
+  uint32_t lrect[kWarpListCap];     // its rectangle in the unit: x0 | y0 << 3 | w << 5 | h << 9
+  uint32_t loff[kWarpListCap];      // its first fragment
 };
 
 // Row y of a fragment, masked by the coverage mask, into its slot.
@@ -1055,85 +1063,97 @@ __device__ __forceinline__ bool fragment_to(const FrameParams& P, const QuadRast
 }
 
 // Quads whose depth may overflow are rare: their copy stays out of line so
-// that the common path keeps its registers.
-static __device__ __noinline__ bool fragment_to_unsafe(const FrameParams& P, const QuadRaster& Q, uint32_t ckq,
-                                                       uint32_t bx, uint32_t by, uint32_t tx0, uint32_t* dst)
+// that the common path keeps its registers.  It reloads quad q's record
+// itself: a record passed by reference would have to live in local memory
+// on every path.
+static __device__ __noinline__ bool fragment_to_unsafe(const FrameParams& P, uint32_t q, uint32_t ckq, uint32_t bx,
+                                                       uint32_t by, uint32_t tx0, uint32_t* dst)
 {
+  const QuadRaster Q = P.rec[q];
   return fragment_to<false>(P, Q, ckq, bx, by, tx0, dst);
 }
 
-__device__ __forceinline__ bool make_fragment(const FrameParams& P, const QuadRaster& Q, uint32_t ckq, uint32_t bx,
-                                              uint32_t by, uint32_t tx0, uint32_t* dst)
+__device__ __forceinline__ bool make_fragment(const FrameParams& P, const QuadRaster& Q, uint32_t q, uint32_t ckq,
+                                              uint32_t bx, uint32_t by, uint32_t tx0, uint32_t* dst)
 {
   if (Q.flags & kQuadSafe) return fragment_to<true>(P, Q, ckq, bx, by, tx0, dst);
-  return fragment_to_unsafe(P, Q, ckq, bx, by, tx0, dst);
+  return fragment_to_unsafe(P, q, ckq, bx, by, tx0, dst);
 }
 
-// Merges fragment slot `slot` into this thread's pixel row of its block: the
-// reference's hiZ test, fast-clear overwrite or max-merge with memory, and the
-// block's new hiZ (minimum over its eight threads, `groupMask`).  With kWins,
-// own[x] tracks the command (+1) that produced pixel x's value.
-template <bool kWins>
-__device__ __forceinline__ void merge_slot(const ViewDesc& V, const RasterSmem& S, uint32_t slot, uint32_t py,
-                                           uint32_t blk, uint32_t groupMask, uint32_t (&row)[4], uint32_t& hiz,
-                                           bool& have, uint32_t (&own)[8])
+// Merges fragment slot `slot` into this lane's RPL pixel rows (from row0) of
+// its block: the reference's hiZ test, fast-clear overwrite or max-merge with
+// memory, and the block's new hiZ (minimum over the block's lanes,
+// `groupMask`).  With kWins, own[r][i] holds the owners (command within the
+// view + 1, or 0) of pixels 2i and 2i+1 of row r as two 16-bit halves.
+template <int RPL, int LPB, bool kWins>
+__device__ __forceinline__ void merge_slot(const ViewDesc& V, const WarpRasterSmem& S, uint32_t slot, uint32_t row0,
+                                           uint32_t blk, uint32_t groupMask, uint32_t (&row)[RPL][4], uint32_t& hiz,
+                                           bool& have, uint32_t (&own)[RPL][4])
 {
   const uint32_t mz = S.meta[slot] >> 16;
   if (hiz >= mz) return;  // the reference's hiZ test (Rasterizer.cpp:1148-1152)
-  const uint32_t* src = S.frag + slot * kFragStride + 4 * py;
+  const uint32_t* src = S.frag + slot * kFragStride + 4 * row0;
+  const uint32_t c1 = kWins ? S.fcmd[slot] : 0u;
   if (hiz == 1) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      if (kWins) {
-        const uint32_t c1 = S.fcmd[slot] + 1;
-        own[2 * i] = (src[i] & 0xFFFFu) ? c1 : 0u;
-        own[2 * i + 1] = (src[i] >> 16) ? c1 : 0u;
+    for (int r = 0; r < RPL; ++r)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t w = src[4 * r + i];
+        if (kWins) own[r][i] = ((w & 0xFFFFu) ? c1 : 0u) | ((w >> 16) ? (c1 << 16) : 0u);
+        row[r][i] = w;
       }
-      row[i] = src[i];
-    }
   } else {
     if (!have) {
-      const uint4 a = *reinterpret_cast<const uint4*>(V.depth + (size_t)blk * 64 + 8 * py);
-      row[0] = a.x; row[1] = a.y; row[2] = a.z; row[3] = a.w;
+      const uint4* d = reinterpret_cast<const uint4*>(V.depth + (size_t)blk * 64 + 8 * row0);
+#pragma unroll
+      for (int r = 0; r < RPL; ++r) {
+        const uint4 a = d[r];
+        row[r][0] = a.x; row[r][1] = a.y; row[r][2] = a.z; row[r][3] = a.w;
+      }
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      if (kWins) {
-        const uint32_t c1 = S.fcmd[slot] + 1;
-        if ((src[i] & 0xFFFFu) > (row[i] & 0xFFFFu)) own[2 * i] = c1;
-        if ((src[i] >> 16) > (row[i] >> 16)) own[2 * i + 1] = c1;
+    for (int r = 0; r < RPL; ++r)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t w = src[4 * r + i];
+        if (kWins) {
+          if ((w & 0xFFFFu) > (row[r][i] & 0xFFFFu)) own[r][i] = (own[r][i] & 0xFFFF0000u) | c1;
+          if ((w >> 16) > (row[r][i] >> 16)) own[r][i] = (own[r][i] & 0xFFFFu) | (c1 << 16);
+        }
+        row[r][i] = vmax_u16x2(row[r][i], w);
       }
-      row[i] = vmax_u16x2(row[i], src[i]);
-    }
   }
   have = true;
-  uint32_t mn = vmin_u16x2(vmin_u16x2(row[0], row[1]), vmin_u16x2(row[2], row[3]));
-  mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 1));
-  mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 2));
-  mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 4));
+  uint32_t mn = 0xFFFFFFFFu;
+#pragma unroll
+  for (int r = 0; r < RPL; ++r) mn = vmin_u16x2(mn, vmin_u16x2(vmin_u16x2(row[r][0], row[r][1]), vmin_u16x2(row[r][2], row[r][3])));
+#pragma unroll
+  for (int o = 1; o < LPB; o <<= 1) mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, o));
   hiz = ::min(mn & 0xFFFFu, mn >> 16);
 }
 
-// Runs the buffered local list (n quads, F fragments): fragments in order,
-// kRasterThreads at a time.  With kWins, own[x] tracks the command (+1) that
-// produced pixel x's value.
-template <bool kWins>
-__device__ __forceinline__ void raster_local_list(const FrameParams& P, const ViewDesc& V, RasterSmem& S, uint32_t n,
-                                                  uint32_t F, uint32_t tx0, uint32_t ty0, uint32_t tid, uint32_t blk,
-                                                  bool inView, uint32_t (&row)[4], uint32_t& hiz, bool& have,
-                                                  uint32_t (&own)[8])
+// Per-lane state of one raster unit.
+template <int R>
+struct UnitState {
+  static constexpr int RPL = UnitShape<R>::kRowsPerLane;
+  uint32_t tx0, ty0, myBlock, row0, blk, groupMask, hiz;
+  bool inView, have;
+  uint32_t row[RPL][4];
+  uint32_t own[RPL][4];
+};
+
+// Runs the buffered local list (n quads, F fragments) 32 fragments at a time.
+template <int R, bool kWins>
+__device__ __forceinline__ void raster_list(const FrameParams& P, const ViewDesc& V, WarpRasterSmem& S, uint32_t n,
+                                            uint32_t F, uint32_t lane, UnitState<R>& U)
 {
-  const uint32_t lane = tid & 31;
-  const uint32_t py = tid & 7;  // pixel row owned by this thread
-  const uint32_t myBlock = tid >> 3;
-  const uint32_t groupMask = 0xFFu << (lane & ~7u);
-  // S.loff holds each local quad's first fragment, F the fragment count
-  for (uint32_t f0 = 0; f0 < F; f0 += kRasterThreads) {
-    if (tid < kUnitBlocks * kMaskWords) (&S.bmask[0][0])[tid] = 0;
-    const uint32_t f = f0 + tid;
-    uint32_t target = 0, q = 0, bx = 0, by = 0;
-    const bool haveF = f < F;
-    if (haveF) {
+  using Sh = UnitShape<R>;
+  for (uint32_t f0 = 0; f0 < F; f0 += 32) {
+    const uint32_t f = f0 + lane;
+    uint32_t meta = 0, target = 0;
+    bool valid = false;
+    if (f < F) {
       uint32_t lo = 0, hi = n - 1;  // last local quad whose first fragment is <= f
       while (lo < hi) {
         const uint32_t mid = (lo + hi + 1) >> 1;
@@ -1145,13 +1165,7 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
       const uint32_t rr = k / rw, cc = k - rr * rw;
       const uint32_t lx = (rc & 7u) + cc, ly = ((rc >> 3) & 3u) + rr;
       target = ly * kTileW + lx;
-      bx = tx0 + lx;
-      by = ty0 + ly;
-      q = S.lq[lo];
-    }
-    __syncthreads();  // bmask cleared
-    uint32_t meta = 0;
-    if (haveF) {
+      const uint32_t q = S.lq[lo];
       const QuadRaster Q = P.rec[q];
       const uint32_t ckq = __ldg(P.ckBase + q);
       const uint32_t ownerHiz = S.hiz[target];
@@ -1159,37 +1173,196 @@ __device__ __forceinline__ void raster_local_list(const FrameParams& P, const Vi
       // so a block with hiZ >= maxZ now still has it when this fragment's
       // turn comes, unless hiZ == 1 and maxZ == 1.
       const bool skip = ownerHiz >= Q.maxZ && !(ownerHiz == 1 && Q.maxZ == 1);
-      if (!skip && make_fragment(P, Q, ckq, bx, by, tx0, S.frag + tid * kFragStride)) {
-        meta = ((uint32_t)Q.maxZ << 16) | 32u | target;
-        if (kWins) S.fcmd[tid] = P.walk[q].pad[0];
-        atomicOr(&S.bmask[target][tid >> 5], 1u << lane);
+      if (!skip && make_fragment(P, Q, q, ckq, U.tx0 + lx, U.ty0 + ly, U.tx0, S.frag + lane * kFragStride)) {
+        valid = true;
+        meta = ((uint32_t)Q.maxZ << 16) | target;
+        if (kWins) S.fcmd[lane] = P.walk[q].pad[0] - V.cmdStart + 1u;
       }
     }
-    S.meta[tid] = meta;
-    __syncthreads();
-    // merge, in slot order, the fragments aimed at this thread's block
-    if (inView) {
-#pragma unroll 1
-      for (int wd = 0; wd < kMaskWords; ++wd) {
-        uint32_t mine = S.bmask[myBlock][wd];
-        while (mine) {
-          const uint32_t slot = 32u * wd + __ffs(mine) - 1;
-          mine &= mine - 1;
-          merge_slot<kWins>(V, S, slot, py, blk, groupMask, row, hiz, have, own);
-        }
-      }
-      if (py == 0) S.hiz[myBlock] = hiz;
+    S.meta[lane] = meta;
+    // slots aimed at each block: lanes with the same target form one group
+    const uint32_t grp = __match_any_sync(0xFFFFFFFFu, valid ? target : 64u + lane);
+    if (lane < (uint32_t)Sh::kBlocks) S.bmask[lane] = 0;
+    __syncwarp();
+    if (valid) S.bmask[target] = grp;
+    __syncwarp();
+    // merge, in slot order, the fragments aimed at this lane's block
+    uint32_t mine = U.inView ? S.bmask[U.myBlock] : 0u;
+    while (mine) {
+      const uint32_t slot = __ffs(mine) - 1;
+      mine &= mine - 1;
+      merge_slot<Sh::kRowsPerLane, Sh::kLanesPerBlock, kWins>(V, S, slot, U.row0, U.blk, U.groupMask, U.row, U.hiz,
+                                                              U.have, U.own);
     }
-    __syncthreads();
+    if (U.row0 == 0) S.hiz[U.myBlock] = U.hiz;
+    __syncwarp();
   }
+}
+
+// Pixels of one lane whose owners differ: runs of equal owners along the
+// lane's n pixel pairs (own: 16-bit owner halves), one atomic per run.  Out
+// of line: rare, and kept out of the kernel's hot instruction stream.
+static __device__ __noinline__ void add_win_runs(uint32_t* wins, uint32_t cmdStart, const uint32_t* own, int n)
+{
+  uint32_t cur = 0, cnt = 0;
+  for (int i = 0; i < 2 * n; ++i) {
+    const uint32_t k = (own[i >> 1] >> (16 * (i & 1))) & 0xFFFFu;
+    if (k != cur) {
+      if (cur) atomicAdd(&wins[cmdStart + cur - 1], cnt);
+      cur = k;
+      cnt = 0;
+    }
+    ++cnt;
+  }
+  if (cur) atomicAdd(&wins[cmdStart + cur - 1], cnt);
+}
+
+// Per-pixel owners (global command + 1, or 0) of one lane's rows: all of them
+// (the first pass) or the pixels this pass changed (the second pass).
+static __device__ __noinline__ void write_owners(uint32_t* o, uint32_t cmdStart, const uint32_t* own, int rows,
+                                                 bool all)
+{
+  for (int i = 0; i < 8 * rows; ++i) {
+    const uint32_t k = (own[i >> 1] >> (16 * (i & 1))) & 0xFFFFu;
+    if (all || k) o[i] = k ? cmdStart + k : 0u;
+  }
+}
+
+// Adds the pixels this lane's rows won to their commands (wins) and writes
+// the per-pixel owners.  A pixel is won by the command whose fragment set its
+// final value (the fast-clear overwrite or a strictly larger max-merge).
+template <int R>
+__device__ __forceinline__ void count_wins(const FrameParams& P, const ViewDesc& V, const UnitState<R>& U,
+                                           uint32_t lane)
+{
+  constexpr int RPL = UnitShape<R>::kRowsPerLane;
+  const uint32_t k0 = U.own[0][0] & 0xFFFFu;
+  bool same = true;
+#pragma unroll
+  for (int r = 0; r < RPL; ++r)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) same &= U.own[r][i] == (k0 | (k0 << 16));
+  if (__all_sync(0xFFFFFFFFu, same)) {
+    // every lane's rows won by one command (the common case): one atomic per command
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, k0);
+    if (k0 && lane == (uint32_t)(__ffs(peers) - 1))
+      atomicAdd(&P.wins[V.cmdStart + k0 - 1], 8u * RPL * (uint32_t)__popc(peers));
+  } else if (!same || (V.owner && U.inView)) {
+    // a copy in local memory for the out-of-line paths (U.own stays in registers)
+    uint32_t own[4 * RPL];
+#pragma unroll
+    for (int r = 0; r < RPL; ++r)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) own[4 * r + i] = U.own[r][i];
+    if (!same) add_win_runs(P.wins, V.cmdStart, own, 4 * RPL);
+    else if (k0) atomicAdd(&P.wins[V.cmdStart + k0 - 1], 8u * RPL);
+    if (V.owner && U.inView)
+      write_owners(V.owner + (size_t)U.blk * 64 + 8 * U.row0, V.cmdStart, own, RPL, P.phase == 0);
+  } else if (k0) {
+    atomicAdd(&P.wins[V.cmdStart + k0 - 1], 8u * RPL);
+  }
+}
+
+// One raster unit: queue record {warp-tile * 4 + first block row, view,
+// first entry and length of the unit's super-tile list}.
+template <int R, bool kWins>
+__device__ __forceinline__ void raster_unit(const FrameParams& P, WarpRasterSmem& S, const uint4 rec, uint32_t lane)
+{
+  using Sh = UnitShape<R>;
+  constexpr int RPL = Sh::kRowsPerLane, LPB = Sh::kLanesPerBlock;
+  const ViewDesc& V = P.views[rec.y];
+  UnitState<R> U;
+  const uint32_t lt = (rec.x >> 2) - V.tileStart;
+  U.tx0 = (lt % V.tilesX) * kTileW;
+  U.ty0 = (lt / V.tilesX) * kTileH + (rec.x & 3u);
+  U.myBlock = lane / LPB;
+  U.row0 = (lane % LPB) * RPL;
+  const uint32_t bx = U.tx0 + (U.myBlock & 7u), by = U.ty0 + (U.myBlock >> 3);
+  U.inView = bx < V.blocksX && by < V.blocksY;
+  U.blk = U.inView ? by * V.blocksX + bx : 0u;
+  U.groupMask = LPB == 1 ? (1u << lane) : (((1u << LPB) - 1u) << (lane & ~(uint32_t)(LPB - 1)));
+  const bool clearing = (V.flags & kViewClear) != 0 && P.phase == 0;
+  U.hiz = clearing ? 1u : (U.inView ? (uint32_t)V.hiz[U.blk] : 0xFFFFu);
+  U.have = false;
+#pragma unroll
+  for (int r = 0; r < RPL; ++r)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      U.row[r][i] = 0;
+      U.own[r][i] = 0;
+    }
+  if (U.row0 == 0) S.hiz[U.myBlock] = U.hiz;
+  __syncwarp();
+  const uint32_t listLen = rec.w;
+  const uint4* list = P.stList + rec.z;
+  const uint32_t below = (1u << lane) - 1u;
+  uint32_t n = 0, F = 0;
+  // 32 list entries per round, one per lane, appended to the local list in
+  // list order unless they miss the unit or are already hidden in every
+  // block they touch here
+#pragma unroll 1
+  for (uint32_t base = 0; base < listLen; base += 32) {
+    const uint4 e = base + lane < listLen ? __ldg(list + base + lane) : make_uint4(0, 0, 0, 0);
+    const uint32_t qx0 = e.y & 0xFFFFu, qy0 = e.y >> 16, qx1 = e.z & 0xFFFFu, qy1 = e.z >> 16;
+    const uint32_t x0 = ::max(qx0, U.tx0), x1 = ::min(qx1, U.tx0 + kTileW);
+    const uint32_t y0 = ::max(qy0, U.ty0), y1 = ::min(qy1, U.ty0 + R);
+    bool o = x0 < x1 && y0 < y1;  // padding entries have an empty box
+    if (o) {
+      // hidden if every block it touches here already has hiZ >= its maxZ
+      // (exact for the rest of the list: see raster_list)
+      const uint32_t mz = e.w;
+      bool hidden = true;
+      for (uint32_t yy = y0 - U.ty0; yy < y1 - U.ty0 && hidden; ++yy)
+        for (uint32_t xx = x0 - U.tx0; xx < x1 - U.tx0; ++xx) {
+          const uint32_t h = S.hiz[yy * kTileW + xx];
+          if (!(h >= mz && !(h == 1 && mz == 1))) {
+            hidden = false;
+            break;
+          }
+        }
+      o = !hidden;
+    }
+    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, o);
+    if (!bal) continue;
+    const uint32_t nf = o ? (x1 - x0) * (y1 - y0) : 0u;
+    const uint32_t incl = warp_inclusive_scan(nf, lane);
+    if (o) {
+      const uint32_t pos = n + __popc(bal & below);
+      S.lq[pos] = e.x;
+      S.lrect[pos] = (x0 - U.tx0) | ((y0 - U.ty0) << 3) | ((x1 - x0) << 5) | ((y1 - y0) << 9);
+      S.loff[pos] = F + incl - nf;
+    }
+    n += __popc(bal);
+    F += __shfl_sync(0xFFFFFFFFu, incl, 31);
+    __syncwarp();
+    if (n > (uint32_t)(kWarpListCap - 32)) {  // the next round may append 32
+      raster_list<R, kWins>(P, V, S, n, F, lane, U);
+      n = 0;
+      F = 0;
+    }
+  }
+  if (n > 0) raster_list<R, kWins>(P, V, S, n, F, lane, U);
+  if (U.inView) {
+    if ((clearing || U.have) && U.row0 == 0) V.hiz[U.blk] = (uint16_t)U.hiz;
+    uint4* d = reinterpret_cast<uint4*>(V.depth + (size_t)U.blk * 64 + 8 * U.row0);
+    if (U.have) {
+#pragma unroll
+      for (int r = 0; r < RPL; ++r) d[r] = make_uint4(U.row[r][0], U.row[r][1], U.row[r][2], U.row[r][3]);
+    } else if (clearing && (V.flags & kViewZeroDepth)) {
+#pragma unroll
+      for (int r = 0; r < RPL; ++r) d[r] = make_uint4(0, 0, 0, 0);
+    }
+  }
+  if (kWins) count_wins<R>(P, V, U, lane);
 }
 
 // ---- k_tile_prep ----------------------------------------------------------------------
 // One warp per warp-tile (8x4 blocks, one lane per block): applies the view's
 // clear (hiZ := 1, Rasterizer.cpp:107-121) to every block, then either queues
-// the tile for k_raster (a quad of its super-tile list reaches it; long lists
-// are not checked) or finishes it here: no quad touches it, so its per-tile
-// hiZ minimum is final.
+// the tile's raster units of R block rows for k_raster (a quad of its
+// super-tile list reaches the unit; long lists are not checked) or finishes
+// them here: no quad touches them, so their hiZ is final (and with
+// kViewZeroDepth their depth is zeroed).
 
 __device__ __forceinline__ uint32_t view_of_tile(const FrameParams& P, uint32_t wt)
 {
@@ -1203,12 +1376,18 @@ __device__ __forceinline__ uint32_t view_of_tile(const FrameParams& P, uint32_t 
 
 constexpr uint32_t kPrepScanMax = 256;  // lists up to this length are checked against the tile
 
+__device__ __forceinline__ uint32_t raster_rows(const FrameParams& P)
+{
+  return P.tune.rasterRows ? P.tune.rasterRows : kDefaultRasterRows;
+}
+
 __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
 {
   __shared__ uint32_t s_n, s_base;
   if (P.header->overflow) return;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t wt = blockIdx.x * 8 + warp;
+  const uint32_t R = raster_rows(P), units = kTileH / R, all = (1u << units) - 1u;
   if (threadIdx.x == 0) s_n = 0;
   __syncthreads();
   uint32_t queue = 0, slot = 0, v = 0;  // queue: bit u = raster unit u of the tile
@@ -1231,22 +1410,32 @@ __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
     listLen = len;
     listStart = len ? P.stStart[s] : 0u;
     if (len > kPrepScanMax) {
-      queue = (1u << kUnitsPerTile) - 1u;
+      queue = all;
     } else if (len) {
       // queue a unit only if a quad of the super-tile list reaches it
       const uint4* list = P.stList + P.stStart[s];
-      for (uint32_t i0 = 0; i0 < len && queue != (1u << kUnitsPerTile) - 1u; i0 += 32) {
+      for (uint32_t i0 = 0; i0 < len && queue != all; i0 += 32) {
         uint32_t hit = 0;
         if (i0 + lane < len) {
           const uint4 e = __ldg(list + i0 + lane);
           if ((e.y & 0xFFFFu) < tx0 + kTileW && (e.z & 0xFFFFu) > tx0)
-            for (uint32_t u = 0; u < (uint32_t)kUnitsPerTile; ++u) {
-              const uint32_t uy0 = ty0 + u * kRasterRows;
-              if ((e.y >> 16) < uy0 + kRasterRows && (e.z >> 16) > uy0) hit |= 1u << u;
+            for (uint32_t u = 0; u < units; ++u) {
+              const uint32_t uy0 = ty0 + u * R;
+              if ((e.y >> 16) < uy0 + R && (e.z >> 16) > uy0) hit |= 1u << u;
             }
         }
         queue |= __reduce_or_sync(0xFFFFFFFFu, hit);
       }
+    }
+    if (clearing && (V.flags & kViewZeroDepth) && queue != all) {
+      // block rows of the units left unqueued: 8 blocks (1 KB) per row, 32 B per lane
+      const uint32_t nbx = ::min((uint32_t)kTileW, V.blocksX - tx0);
+      for (uint32_t r = 0; r < (uint32_t)kTileH; ++r)
+        if (!((queue >> (r / R)) & 1u) && ty0 + r < V.blocksY && lane / 4 < nbx) {
+          uint4* d = reinterpret_cast<uint4*>(V.depth + ((size_t)(ty0 + r) * V.blocksX + tx0) * 64) + 2 * lane;
+          d[0] = make_uint4(0, 0, 0, 0);
+          d[1] = make_uint4(0, 0, 0, 0);
+        }
     }
     if (lane == 0 && queue) slot = atomicAdd(&s_n, (uint32_t)__popc(queue));
   }
@@ -1255,8 +1444,8 @@ __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
   __syncthreads();
   if (lane == 0 && queue) {
     uint32_t k = s_base + slot;
-    for (uint32_t u = 0; u < (uint32_t)kUnitsPerTile; ++u)
-      if (queue & (1u << u)) P.activeTileList[k++] = make_uint4(wt * kUnitsPerTile + u, v, listStart, listLen);
+    for (uint32_t u = 0; u < units; ++u)
+      if (queue & (1u << u)) P.activeTileList[k++] = make_uint4(wt * 4 + u * R, v, listStart, listLen);
   }
 }
 
@@ -1278,173 +1467,28 @@ __global__ void __launch_bounds__(256) k_tile_min(FrameParams P)
 }
 
 // ---- k_raster -------------------------------------------------------------------------
-// Persistent CTAs of kRasterThreads threads take queued raster units a few at
-// a time (dynamic, heavy units vary a lot): per unit, the super-tile list is
-// filtered to the quads that reach the unit and are not already hidden, then
-// rasterised in list order (raster_local_list) and the unit's blocks written back.
+// Persistent CTAs of kRasterWarps independent warps; each warp takes queued
+// raster units a few at a time from the global queue (dynamic: heavy units
+// vary a lot) and rasterises them one after the other (raster_unit).
 
-template <bool kWins>
-__device__ __forceinline__ void raster_tile(const FrameParams& P, RasterSmem& S, const uint4 rec)
+template <int R, bool kWins>
+__global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks<R>) k_raster(FrameParams P)
 {
-  const uint32_t unit = rec.x, v = rec.y;
-  const uint32_t tid = threadIdx.x, lane = tid & 31;
-  const ViewDesc& V = P.views[v];
-  const uint32_t lt = unit / kUnitsPerTile - V.tileStart;  // the warp-tile holding the unit
-  const uint32_t tx = lt % V.tilesX, ty = lt / V.tilesX;
-  const uint32_t tx0 = tx * kTileW, ty0 = ty * kTileH + (unit % kUnitsPerTile) * kRasterRows;
-  const uint32_t myBlock = tid >> 3, py = tid & 7;
-  const uint32_t bx = tx0 + (myBlock & 7), by = ty0 + (myBlock >> 3);
-  const bool inView = bx < V.blocksX && by < V.blocksY;
-  const uint32_t blk = inView ? by * V.blocksX + bx : 0;
-  const bool clearing = (V.flags & kViewClear) != 0 && P.phase == 0;
-  uint32_t hiz = clearing ? 1u : (inView ? (uint32_t)V.hiz[blk] : 0xFFFFu);
-  bool have = false;
-  uint32_t row[4] = {0, 0, 0, 0};
-  uint32_t own[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  const uint32_t listLen = rec.w;  // the unit's super-tile list, from k_tile_prep
-  const uint4* list = P.stList + rec.z;
-  if (py == 0) S.hiz[myBlock] = hiz;
-  __syncthreads();
-  uint32_t n = 0, F = 0;
-  // kScanPerRound list entries per round (two consecutive ones per thread),
-  // appended to the local list in list order unless already hidden in every
-  // block they touch; one scan of (fragments << 16 | quads) places both
-  for (uint32_t base = 0; base < listLen; base += kScanPerRound) {
-    uint4 e[2];
-    bool ov[2];
-    uint32_t rect[2];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const uint32_t idx = base + 2 * tid + k;
-      e[k] = idx < listLen ? __ldg(list + idx) : make_uint4(0, 0, 0, 0);
-    }
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const uint32_t qx0 = e[k].y & 0xFFFFu, qy0 = e[k].y >> 16, qx1 = e[k].z & 0xFFFFu, qy1 = e[k].z >> 16;
-      const uint32_t x0 = ::max(qx0, tx0), x1 = ::min(qx1, tx0 + kTileW);
-      const uint32_t y0 = ::max(qy0, ty0), y1 = ::min(qy1, ty0 + kRasterRows);
-      bool o = x0 < x1 && y0 < y1;  // padding entries have an empty box
-      if (o) {
-        // hidden if every block it touches here already has hiZ >= its maxZ
-        // (exact for the rest of the list: see raster_local_list)
-        const uint32_t mz = e[k].w;
-        bool hidden = true;
-        for (uint32_t yy = y0 - ty0; yy < y1 - ty0 && hidden; ++yy)
-          for (uint32_t xx = x0 - tx0; xx < x1 - tx0; ++xx) {
-            const uint32_t h = S.hiz[yy * kTileW + xx];
-            if (!(h >= mz && !(h == 1 && mz == 1))) {
-              hidden = false;
-              break;
-            }
-          }
-        o = !hidden;
-      }
-      ov[k] = o;
-      rect[k] = (x0 - tx0) | ((y0 - ty0) << 3) | ((x1 - x0) << 5) | ((y1 - y0) << 9);
-    }
-    uint32_t fr[2];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) fr[k] = ov[k] ? ((rect[k] >> 5) & 15u) * ((rect[k] >> 9) & 7u) : 0u;
-    const uint32_t cnt = (ov[0] ? 1u : 0u) + (ov[1] ? 1u : 0u);
-    uint32_t tot;  // per round at most 256 quads and 4,096 fragments: the halves do not carry
-    const uint32_t ex = block_exclusive_scan<kRasterThreads>(cnt | ((fr[0] + fr[1]) << 16), tot, S.scan);
-    uint32_t pos = n + (ex & 0xFFFFu), fpos = F + (ex >> 16);
-#pragma unroll
-    for (int k = 0; k < 2; ++k)
-      if (ov[k]) {
-        S.lq[pos] = e[k].x;
-        S.lrect[pos] = rect[k];
-        S.loff[pos] = fpos;
-        ++pos;
-        fpos += fr[k];
-      }
-    n += tot & 0xFFFFu;
-    F += tot >> 16;
-    __syncthreads();
-    if (n > (uint32_t)(kLocalCap - kScanPerRound) || (base + kScanPerRound >= listLen && n > 0)) {
-      raster_local_list<kWins>(P, V, S, n, F, tx0, ty0, tid, blk, inView, row, hiz, have, own);
-      n = 0;
-      F = 0;
-    }
-  }
-  if (inView) {
-    if ((clearing || have) && py == 0) V.hiz[blk] = (uint16_t)hiz;
-    if (have) *reinterpret_cast<uint4*>(V.depth + (size_t)blk * 64 + 8 * py) = make_uint4(row[0], row[1], row[2], row[3]);
-  }
-  if (kWins) {
-    // a pixel is won by the command whose fragment set its final value (the
-    // fast-clear overwrite or a strictly larger max-merge); one atomic per
-    // distinct command per warp (rows won by one command: the common case)
-    // or per warp and pixel column
-    bool same = true;
-#pragma unroll
-    for (int x = 1; x < 8; ++x) same &= own[x] == own[0];
-    if (__all_sync(0xFFFFFFFFu, same)) {
-      const uint32_t key = inView ? own[0] : 0u;
-      const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
-      if (key && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&P.wins[key - 1], 8u * (uint32_t)__popc(peers));
-    } else {
-#pragma unroll
-      for (int x = 0; x < 8; ++x) {
-        const uint32_t key = inView ? own[x] : 0u;
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
-        if (key && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&P.wins[key - 1], (uint32_t)__popc(peers));
-      }
-    }
-    if (V.owner && inView) {
-      uint32_t* o = V.owner + (size_t)blk * 64 + 8 * py;
-      if (P.phase == 0) {
-        reinterpret_cast<uint4*>(o)[0] = make_uint4(own[0], own[1], own[2], own[3]);
-        reinterpret_cast<uint4*>(o)[1] = make_uint4(own[4], own[5], own[6], own[7]);
-      } else {
-#pragma unroll
-        for (int x = 0; x < 8; ++x)
-          if (own[x]) o[x] = own[x];  // pixels the second pass changed
-      }
-    }
-  }
-}
-
-template <bool kWins>
-__global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) k_raster(FrameParams P)
-{
-  __shared__ RasterSmem S;
-  __shared__ uint32_t s_next;
-  __shared__ __align__(16) uint4 s_rec[2];  // this unit's queue record and the next one's
+  __shared__ WarpRasterSmem S[kRasterWarps];
   if (P.header->overflow) return;
+  const uint32_t lane = threadIdx.x & 31;
+  WarpRasterSmem& W = S[threadIdx.x >> 5];
   const uint32_t nActive = P.header->activeTiles;
   const uint32_t chunk = P.tune.rasterChunk ? P.tune.rasterChunk : 1u;  // units per fetch
-  if (threadIdx.x == 0) {
-    const uint32_t i0 = atomicAdd(&P.header->tileCursor, chunk);
-    s_next = i0;
-    if (i0 < nActive) s_rec[0] = P.activeTileList[i0];
-  }
-  __syncthreads();
-  uint32_t i = s_next, buf = 0;
+  uint32_t i = 0;
+  if (lane == 0) i = atomicAdd(&P.header->tileCursor, chunk);
+  i = __shfl_sync(0xFFFFFFFFu, i, 0);
   while (i < nActive) {
     uint32_t nxt = 0;
-    if (threadIdx.x == 0) nxt = atomicAdd(&P.header->tileCursor, chunk);  // next fetch, ahead of time
+    if (lane == 0) nxt = atomicAdd(&P.header->tileCursor, chunk);  // next fetch, ahead of time
     const uint32_t end = ::min(i + chunk, nActive);
-    for (uint32_t j = i; j < end; ++j) {
-      const uint4 rec = s_rec[buf];
-      if (threadIdx.x == 0) {
-        // the next unit's record, copied while this one is rasterised (the
-        // buffer it lands in was last read before the previous unit's barrier)
-        const uint32_t k = j + 1 < end ? j + 1 : nxt;
-        if (k < nActive) {
-          const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&s_rec[buf ^ 1u]);
-          asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(P.activeTileList + k) : "memory");
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
-      }
-      raster_tile<kWins>(P, S, rec);
-      if (threadIdx.x == 0) asm volatile("cp.async.wait_all;" ::: "memory");
-      __syncthreads();  // shared state is reused by the next unit; the next record has landed
-      buf ^= 1u;
-    }
-    if (threadIdx.x == 0) s_next = nxt;
-    __syncthreads();
-    i = s_next;
+    for (uint32_t j = i; j < end; ++j) raster_unit<R, kWins>(P, W, __ldg(P.activeTileList + j), lane);
+    i = __shfl_sync(0xFFFFFFFFu, nxt, 0);
   }
 }
 
@@ -1743,9 +1787,17 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
   mark(4);
   if (doRaster && P.numTiles) {
     k_tile_prep<<<(P.numTiles + 7) / 8, 256, 0, stream>>>(P);
-    const uint32_t grid = grid_of(P.tune.rasterPerSm, g_rasterPerSm, P.numTiles * kUnitsPerTile);
-    if (P.wins) k_raster<true><<<grid, kRasterThreads, 0, stream>>>(P);
-    else k_raster<false><<<grid, kRasterThreads, 0, stream>>>(P);
+    const uint32_t R = P.tune.rasterRows ? P.tune.rasterRows : kDefaultRasterRows;
+    const uint32_t shape = R == 1 ? 0u : (R == 2 ? 1u : 2u);
+    const uint32_t units = P.numTiles * (kTileH / R);
+    const uint32_t grid = grid_of(P.tune.rasterPerSm, g_rasterPerSm[shape], (units + kRasterWarps - 1) / kRasterWarps);
+    const bool w = P.wins != nullptr;
+    if (R == 1) w ? k_raster<1, true><<<grid, kRasterThreads, 0, stream>>>(P)
+                  : k_raster<1, false><<<grid, kRasterThreads, 0, stream>>>(P);
+    else if (R == 4) w ? k_raster<4, true><<<grid, kRasterThreads, 0, stream>>>(P)
+                       : k_raster<4, false><<<grid, kRasterThreads, 0, stream>>>(P);
+    else w ? k_raster<2, true><<<grid, kRasterThreads, 0, stream>>>(P)
+           : k_raster<2, false><<<grid, kRasterThreads, 0, stream>>>(P);
     k_tile_min<<<(P.numTiles + 7) / 8, 256, 0, stream>>>(P);
   }
   mark(5);
@@ -1819,18 +1871,25 @@ cudaError_t set_kernel_attributes()
     g_setupPerSm = (uint32_t)nb;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fill, kChunk, kMaxStPerView * 16) == cudaSuccess && nb > 0)
     g_fillPerSm = (uint32_t)nb;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster<true>, kRasterThreads, 0) == cudaSuccess && nb > 0)
-    g_rasterPerSm = (uint32_t)nb;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster<1, true>, kRasterThreads, 0) == cudaSuccess && nb > 0)
+    g_rasterPerSm[0] = (uint32_t)nb;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster<2, true>, kRasterThreads, 0) == cudaSuccess && nb > 0)
+    g_rasterPerSm[1] = (uint32_t)nb;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster<4, true>, kRasterThreads, 0) == cudaSuccess && nb > 0)
+    g_rasterPerSm[2] = (uint32_t)nb;
   return cudaSuccess;
 }
 
-// Occupancy limits (resident CTAs per SM) of the persistent kernels, and the SM count.
-void tuning_limits(uint32_t out[4])
+// Occupancy limits (resident CTAs per SM) of the persistent kernels -- setup,
+// list fill, raster at unit rows 1, 2 and 4 -- and the SM count.
+void tuning_limits(uint32_t out[6])
 {
   out[0] = g_setupPerSm;
   out[1] = g_fillPerSm;
-  out[2] = g_rasterPerSm;
-  out[3] = g_sms;
+  out[2] = g_rasterPerSm[0];
+  out[3] = g_rasterPerSm[1];
+  out[4] = g_rasterPerSm[2];
+  out[5] = g_sms;
 }
 
 // ---- cull labels ---------------------------------------------------------------------------

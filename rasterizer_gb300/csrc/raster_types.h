@@ -19,15 +19,16 @@ constexpr int kSuperTile = 16;            // binning super-tile edge, in 8x8 blo
 constexpr int kTileW = 8;                 // warp-tile: 8 x 4 blocks, one lane per block
 constexpr int kTileH = 4;
 constexpr int kCkSpan = 8;                // row-walk checkpoint every 8 block columns (== kTileW)
-constexpr int kRasterRows = 2;            // raster unit: 8 x kRasterRows blocks (a part of a warp-tile)
-constexpr int kUnitsPerTile = kTileH / kRasterRows;
+constexpr uint32_t kDefaultRasterRows = 2;  // raster unit: 8 x R blocks of a warp-tile, R = 1, 2 or 4
+constexpr int kMaxUnitsPerTile = kTileH;    // raster units per warp-tile at R = 1
 constexpr int kMaxCmdPerChunk = 40;       // commands are >= 8 quads, so <= 33 per chunk
 constexpr int kCkFloats = 12;             // 4 edge offsets + 8 depth lanes
 constexpr int kMaxStPerView = 3072;       // super-tiles per view (e.g. 12288 x 6144 pixels)
 constexpr uint32_t kNoAllocMaxQueries = 65536;  // boxes per occ_raster_query_batch_noalloc call
 
 enum : uint32_t {
-  kViewClear = 1u << 0,   // hiZ := 1 before rasterising (Rasterizer::clear)
+  kViewClear = 1u << 0,      // hiZ := 1 before rasterising (Rasterizer::clear)
+  kViewZeroDepth = 1u << 1,  // with kViewClear: depth := 0 as well (a freshly created rasterizer's state)
 };
 
 enum : uint32_t {
@@ -155,7 +156,8 @@ constexpr uint32_t kQueryPerThread = 255;
 struct LaunchTuning {
   uint32_t setupPerSm, fillPerSm, walkPerSm, rasterPerSm, rasterChunk;
   uint32_t queryRounds;  // 0: chosen by slot count; else a k_query form (above)
-  uint32_t pad[2];
+  uint32_t rasterRows;   // block rows per raster unit: 1, 2 or 4 (0: kDefaultRasterRows)
+  uint32_t pad;
 };
 
 struct FrameParams {
@@ -196,8 +198,8 @@ struct FrameParams {
   uint32_t* activeChunkList;  // chunks with a drawn command (header->activeChunks of them)
   uint32_t* viewActiveChunks; // per view, from its chunkStart: local indices of its active chunks, in order
   uint32_t* viewActiveCount;  // per view: how many
-  uint4* activeTileList;      // queued raster units (header->activeTiles): {unit, view, first entry and
-                              // length of the unit's super-tile list}
+  uint4* activeTileList;      // queued raster units (header->activeTiles): {warp-tile * 4 + first block
+                              // row, view, first entry and length of the unit's super-tile list}
   // learned occluder selection and win counts (all optional)
   float* feat;           // per command: kFeatures features
   float* score;          // per command: MLP score

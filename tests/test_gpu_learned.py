@@ -132,14 +132,17 @@ def _boxes_view(ctx, w=640, h=360, queries=3000):
                      mins=mins, maxs=maxs)
 
 
-def test_pixel_wins_match_oracle(ctx):
+@pytest.mark.parametrize("rows", [1, 2, 4])
+def test_pixel_wins_match_oracle(ctx, rows):
     """Wins (pixels whose final depth an occluder produced) == the oracle drawn
     occluder by occluder, each pixel owned by the last occluder that changed it.
     The oracle starts from zeroed depth, so a nonzero value written into a
-    cleared block counts as a change, which is the GPU's rule for cleared blocks."""
+    cleared block counts as a change, which is the GPU's rule for cleared
+    blocks.  Every raster unit shape (1, 2, 4 block rows per warp)."""
     occ, view = _boxes_view(ctx)
     scene = to_baked(occ)
     b = api.PreparedBatch(ctx, [view])
+    b.setTuning({"raster_unit_rows": rows})
     b.setSelection(None, trackWins=True)
     b.launch()
     assert b.check()

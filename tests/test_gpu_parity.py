@@ -272,6 +272,46 @@ def test_autotuned_launch_shapes_keep_results(ctx):
     b.close()
 
 
+@pytest.mark.parametrize("rows", [1, 2, 4])
+def test_raster_unit_shapes(ctx, rows):
+    """Raster units of 1, 2 and 4 block rows per warp (a choice of the
+    autotuner) give the oracle's frames: two views on persistent rasterizers,
+    frames in the reference's clear (stale depth merged and queried), then in
+    the zero-depth clear, with win counting on (the other kernel variant)."""
+    occ = city_occluders()
+    scene = to_baked(occ)
+    w, h = 960, 544
+    mvps, _ = scenes.camera_path(40, seed=31, width=w, height_px=h)
+    mins, maxs = scenes.query_boxes(20000, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    rs = [api.Rasterizer(ctx, w, h) for _ in range(2)]
+    starts = (0, 11)
+    views = [dict(raster=r, mvp=mvps[s], clear=True, occluders=occ, flags=np.full(len(occ), 2, np.uint8),
+                  mins=mins, maxs=maxs) for r, s in zip(rs, starts)]
+    b = api.PreparedBatch(ctx, views)
+    b.setTuning({"raster_unit_rows": rows})
+    orcs = [Oracle(w, h) for _ in rs]
+    for o, s in zip(orcs, starts):
+        o.frame_plain(scene, mvps[s])  # the preparing frame
+    for step, (f, zero, wins) in enumerate(((3, False, False), (7, False, True), (19, True, True), (23, True, False))):
+        if step == 1 or step == 3:
+            b.setSelection(None, 1.0, trackWins=wins)
+        b.setZeroDepth(zero)
+        for v, o in enumerate(orcs):
+            b.setModelViewProjection(v, mvps[f + starts[v]])
+            if zero:
+                o.write_depth(np.zeros(w * h, np.uint16))
+        b.launch()
+        assert b.check()
+        for v, (r, o) in enumerate(zip(rs, orcs)):
+            o.frame_plain(scene, mvps[f + starts[v]])
+            vis, nc = b.results(v)
+            ovis, onc = o.query(mins, maxs)
+            assert np.array_equal(vis.astype(np.uint8), ovis), (rows, f, v)
+            assert np.array_equal(nc.astype(np.uint8), onc), (rows, f, v)
+            _compare(r, o, ("depth", "hiz"))
+    b.close()
+
+
 def test_large_city_4k_main_view(ctx):
     """The 2M-triangle city's 3840x2160 main view (129,600 blocks, full 32-bit
     block index) with every occluder gated, and 200k boxes, against the oracle."""

@@ -1,8 +1,10 @@
 """occ_raster_query_batch_noalloc: queries for callers that must not allocate
-device memory (host callbacks, fixed-budget frame loops), staged in one fixed
-device array instead of per-context buffers.  Checked through the C ABI
-against occ_raster_query_batch on two calls in a row (the second call reuses
-the array the first one left behind).  This file is named to run last."""
+device memory (fixed-budget frame loops, engines that forbid cudaMalloc on
+their frame thread), staged in one fixed device array instead of per-context
+buffers.  Checked through the C ABI against occ_raster_query_batch on calls in
+a row (each call reuses the array the previous one left behind), including a
+batch that fills the array and an empty batch.  This file is named to run
+last."""
 import ctypes as C
 
 import numpy as np
@@ -37,8 +39,9 @@ def test_noalloc_queries_match_the_allocating_entry_point():
     ctx = api.Context(0)
     r = api.Rasterizer(ctx, 1920, 1080)
     gpu_plain_frame(r, boxes_occluders(), scenes.boxes_camera())
-    # two calls in a row, different sizes: the second must not see the first's leftovers
-    for n, seed in ((4096, 43), (1000, 7)):
+    # calls in a row, different sizes: none may see the previous call's leftovers;
+    # 65,536 boxes use every word of the fixed array
+    for n, seed in ((4096, 43), (65536, 11), (1000, 7)):
         mins, maxs = scenes.query_boxes(n, seed=seed)
         mins, maxs = np.ascontiguousarray(mins), np.ascontiguousarray(maxs)
         (rv, rn), (gv, gn) = _query_both(lib, r, mins, maxs)
@@ -47,6 +50,11 @@ def test_noalloc_queries_match_the_allocating_entry_point():
         assert np.array_equal(gn, rn)
         vis = api.unpack_bits(gv, n)
         assert 0 < vis.sum() < n
+    # an empty batch succeeds and writes nothing
+    mins = np.zeros((1, 4), np.float32)
+    bits = np.full(1, 0xDEADBEEF, np.uint32)
+    assert lib.occ_raster_query_batch_noalloc(r.handle, 0, _ptr(mins), _ptr(mins), _ptr(bits), _ptr(bits)) == 0
+    assert bits[0] == 0xDEADBEEF
     r.close()
     ctx.close()
 
