@@ -177,6 +177,18 @@ int occ_batch_set_mvps(occ_batch b, uint32_t first, uint32_t count, const float*
  * words per array; view v's bits start at word firstWord[v] (numViews entries). */
 int occ_batch_result_words(occ_batch b, uint32_t* words);
 int occ_batch_results_all(occ_batch b, uint32_t* visibleBits, uint32_t* needsClippingBits, uint32_t* firstWord);
+/* occ_batch_results_all without waiting: the copies are queued on the
+ * context's stream behind the launches queued so far, and the buffers hold
+ * the bits once the stream has run them (occ_ctx_synchronize).  Page-locked
+ * host buffers keep the copies asynchronous.  No reference counterpart. */
+int occ_batch_results_all_async(occ_batch b, uint32_t* visibleBits, uint32_t* needsClippingBits);
+/* Replaces the query boxes of views first .. first+count-1: each view's
+ * numQueries boxes, the views back to back in mins / maxs (float4 per box),
+ * e.g. the boxes of moving objects every frame, as the reference takes every
+ * query's box from the caller (Rasterizer.cpp:123-281).  The copies are
+ * queued on the context's stream ahead of the next launch; page-locked host
+ * arrays must stay unchanged until the stream has run them. */
+int occ_batch_set_queries(occ_batch b, uint32_t first, uint32_t count, const float* mins, const float* maxs);
 int occ_batch_results(occ_batch b, uint32_t view, uint32_t* visibleBits, uint32_t* needsClippingBits);
 int occ_batch_check(occ_batch b); /* syncs; OCC_ERR_CAPACITY if a launch overflowed */
 /* Runs the frame `iterations` times kernel by kernel with CUDA events between

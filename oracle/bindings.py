@@ -73,6 +73,7 @@ def oracle_lib():
         lib.orc_write_hiz.argtypes = [P, P]
         lib.orc_read_counters.argtypes = [P, P]
         lib.orc_frame_plain.argtypes = [P, U32, P, P, P, P, P, P]
+        lib.orc_frame_gated.argtypes = [P, U32, P, P, P, P, P, P, P, P, P]
         lib.orc_setup_dump.restype = U32
         lib.orc_setup_dump.argtypes = [P, P, U32, P, P, C.c_int, P]
         _oracle_lib = lib
@@ -150,6 +151,25 @@ def aligned_u32(n: int) -> np.ndarray:
     buf = np.zeros(n + 16, dtype=np.uint32)
     off = (-buf.ctypes.data % 32) // 4
     return buf[off:off + n]
+
+
+def save_baked_scene(path, sc: "BakedScene") -> None:
+    """A baked scene as one npz: the packed words back to back, per occluder
+    packet counts, quantisation boxes, bounds and centres."""
+    np.savez_compressed(path, packed=np.concatenate([p[:8 * int(k)] for p, k in zip(sc.packed, sc.packets)]),
+                        packets=sc.packets, ref=sc.ref, bounds=sc.bounds, centers=sc.centers)
+
+
+def load_baked_scene(path) -> "BakedScene":
+    """The inverse of save_baked_scene (32-byte aligned packed arrays)."""
+    z = np.load(path)
+    packed, at = [], 0
+    for k in z["packets"]:
+        buf = aligned_u32(8 * int(k))
+        buf[:] = z["packed"][at:at + 8 * int(k)]
+        packed.append(buf)
+        at += 8 * int(k)
+    return BakedScene(packed, z["ref"], z["bounds"], z["centers"])
 
 
 class Oracle:
@@ -239,6 +259,23 @@ class Oracle:
                                     _ptr(np.ascontiguousarray(ref_max, np.float32)), int(near_clip), _ptr(out))
         return out[:n]
 
+    def frame_gated(self, scene: BakedScene, mvp, eye):
+        """Main.cpp:181-206: occluders front to back by squared centre distance
+        to `eye`, each queried against the live buffer before it is drawn.
+        Returns (drawing order, per-occluder flags visible | nearClip << 1)."""
+        n = len(scene)
+        ptrs = (P * n)(*[scene.packed[i].ctypes.data for i in range(n)])
+        packets = np.ascontiguousarray(scene.packets, np.uint32)
+        order = np.zeros(n, np.uint32)
+        flags = np.zeros(n, np.uint8)
+        e = np.zeros(4, np.float32)
+        e[:3] = np.asarray(eye, np.float32)[:3]
+        self.lib.orc_frame_gated(self.h, n, C.cast(ptrs, P), _ptr(packets), _ptr(np.ascontiguousarray(scene.ref)),
+                                 _ptr(np.ascontiguousarray(scene.bounds)),
+                                 _ptr(np.ascontiguousarray(scene.centers, np.float32)), _ptr(e),
+                                 _ptr(np.ascontiguousarray(mvp, np.float32)), _ptr(order), _ptr(flags))
+        return order, flags
+
     def frame_plain(self, scene: BakedScene, mvp, order=None):
         idx = np.arange(len(scene)) if order is None else np.asarray(order)
         ptrs = (P * len(idx))(*[scene.packed[i].ctypes.data for i in idx])
@@ -319,6 +356,36 @@ class Reference:
             if v[0]:
                 self.rasterize(scene.packed[i], scene.packets[i], scene.ref[i, :4], scene.ref[i, 4:], bool(c[0]))
         return flags
+
+
+class ReferenceScene:
+    """A scene baked and held by the reference's own code (Main.cpp:86-128),
+    drawn by its frame loops (x86-64)."""
+
+    def __init__(self, vertices: np.ndarray, indices: np.ndarray):
+        self.lib = ref_lib()
+        v = np.ascontiguousarray(vertices, np.float32)
+        i = np.ascontiguousarray(indices, np.uint32)
+        self.h = self.lib.ref_scene_build(_ptr(i), i.size, _ptr(v), len(v))
+
+    def close(self):
+        if self.h:
+            self.lib.ref_scene_free(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def __len__(self):
+        return self.lib.ref_scene_count(self.h)
+
+    def frame_plain(self, r: "Reference", scratch: "Reference", mvp):
+        self.lib.ref_frame_plain(r.h, scratch.h, self.h, None, len(self), _ptr(np.ascontiguousarray(mvp, np.float32)),
+                                 None)
+
+    def frame_gated(self, r: "Reference", mvp, eye):
+        e = np.zeros(4, np.float32)
+        e[:3] = np.asarray(eye, np.float32)[:3]
+        self.lib.ref_frame_gated(r.h, self.h, _ptr(np.ascontiguousarray(mvp, np.float32)), _ptr(e))
 
 
 def reference_bake_scene(vertices: np.ndarray, indices: np.ndarray) -> BakedScene:

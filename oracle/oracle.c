@@ -815,3 +815,45 @@ void orc_frame_plain(orc_raster* r, uint32_t n, const uint32_t* const* occ_packe
     orc_rasterize(r, occ_packed[k], occ_packets[k], occ_ref + 8 * k, occ_ref + 8 * k + 4, nc);
   }
 }
+
+/* Main.cpp:181-206: front-to-back order by squared centre distance, each
+ * occluder queried against the live buffer before it is drawn. */
+typedef struct {
+  float d;
+  uint32_t k;
+} dist_key;
+
+static int cmp_dist(const void* a, const void* b)
+{
+  const dist_key* x = (const dist_key*)a;
+  const dist_key* y = (const dist_key*)b;
+  if (x->d < y->d) return -1;
+  if (y->d < x->d) return 1;
+  return x->k < y->k ? -1 : (x->k > y->k ? 1 : 0);
+}
+
+void orc_frame_gated(orc_raster* r, uint32_t n, const uint32_t* const* occ_packed, const uint32_t* occ_packets,
+                     const float* occ_ref, const float* occ_bounds, const float* occ_centers, const float* eye,
+                     const float* mvp, uint32_t* order_out, uint8_t* flags)
+{
+  dist_key* keys = (dist_key*)malloc(sizeof(dist_key) * (n ? n : 1));
+  for (uint32_t k = 0; k < n; ++k) {
+    /* _mm_dp_ps(d, d, 0x7f): x, y, z products, w masked to +0 */
+    const float d[4] = {xsub(occ_centers[4 * k], eye[0]), xsub(occ_centers[4 * k + 1], eye[1]),
+                        xsub(occ_centers[4 * k + 2], eye[2]), 0.0f};
+    keys[k].d = xdp4(d, d);
+    keys[k].k = k;
+  }
+  qsort(keys, n, sizeof(dist_key), cmp_dist);
+  orc_clear(r);
+  orc_set_mvp(r, mvp);
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint32_t k = keys[i].k;
+    if (order_out) order_out[i] = k;
+    int nc = 0;
+    const int vis = orc_query(r, occ_bounds + 8 * k, occ_bounds + 8 * k + 4, &nc);
+    if (flags) flags[k] = (uint8_t)((vis ? 1 : 0) | (nc ? 2 : 0));
+    if (vis) orc_rasterize(r, occ_packed[k], occ_packets[k], occ_ref + 8 * k, occ_ref + 8 * k + 4, nc);
+  }
+  free(keys);
+}

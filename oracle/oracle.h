@@ -70,6 +70,17 @@ void orc_frame_plain(orc_raster* r, uint32_t n, const uint32_t* const* occ_packe
                      const uint32_t* occ_packets, const float* occ_ref /* n x 8: min4,max4 */,
                      const float* occ_bounds /* n x 8 */, const float* mvp, uint8_t* flags);
 
+/* Main.cpp's own frame loop (Main.cpp:181-206): clear, set MVP, occluders
+ * sorted front to back by the squared distance of their centre (occ_centers,
+ * n x 4) to `eye` (DPPS sum of the x, y, z products), each queried against
+ * the live buffer and rasterised with the near-clip variant the query gives.
+ * Equal distances keep submission order (the reference's std::sort leaves
+ * their order unspecified).  order_out (may be NULL) receives the drawing
+ * order, flags (may be NULL) per occluder visible | needsClipping << 1. */
+void orc_frame_gated(orc_raster* r, uint32_t n, const uint32_t* const* occ_packed, const uint32_t* occ_packets,
+                     const float* occ_ref, const float* occ_bounds, const float* occ_centers, const float* eye,
+                     const float* mvp, uint32_t* order_out, uint8_t* flags);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,6 +72,8 @@ SIGNATURES = {
     "occ_batch_set_mvps": (I32, [P, U32, U32, P]),
     "occ_batch_result_words": (I32, [P, C.POINTER(U32)]),
     "occ_batch_results_all": (I32, [P, P, P, P]),
+    "occ_batch_results_all_async": (I32, [P, P, P]),
+    "occ_batch_set_queries": (I32, [P, U32, U32, P, P]),
     "occ_batch_autotune": (I32, [P, U32, P, P, P]),
     "occ_batch_set_tuning": (I32, [P, P]),
     "occ_mlp_param_count": (I32, []),

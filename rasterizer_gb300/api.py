@@ -559,6 +559,37 @@ class PreparedBatch:
             out.append((unpack_bits(self._vis[a:a + nw], n), unpack_bits(self._nc[a:a + nw], n)))
         return out
 
+    def resultsAllAsync(self, visible: np.ndarray, needsClipping: np.ndarray | None = None) -> None:
+        """Queues the copy of every view's result bits into `visible` /
+        `needsClipping` (uint32, resultWords() words; page-locked memory keeps
+        it asynchronous) behind the launches queued so far; read them after
+        ctx.synchronize()."""
+        n = self.resultWords()
+        for a in (visible, needsClipping):
+            if a is not None and (a.dtype != np.uint32 or a.size < n or not a.flags.c_contiguous):
+                raise ValueError(f"result buffers must be contiguous uint32 arrays of {n} words")
+        check(lib().occ_batch_results_all_async(self.handle, _ptr(visible),
+                                                None if needsClipping is None else _ptr(needsClipping)),
+              "occ_batch_results_all_async")
+
+    def resultWords(self) -> int:
+        w = C.c_uint32()
+        check(lib().occ_batch_result_words(self.handle, C.byref(w)), "occ_batch_result_words")
+        return w.value
+
+    def setQueries(self, mins, maxs, first: int = 0, count: int | None = None) -> None:
+        """New query boxes for views first .. first+count-1 (each view's
+        number of boxes, the views back to back: (n, 4) float32).  Queued on
+        the context's stream ahead of the next launch: keep the arrays alive
+        and unchanged until the stream has run the copies."""
+        count = len(self.ws.nq) - first if count is None else count
+        need = int(sum(self.ws.nq[first:first + count]))
+        mins, maxs = _f32(mins).reshape(-1, 4), _f32(maxs).reshape(-1, 4)
+        if len(mins) != need or len(maxs) != need:
+            raise ValueError(f"expected {need} boxes for views {first}..{first + count - 1}")
+        self._query_hold = (mins, maxs)  # kept alive until the next call
+        check(lib().occ_batch_set_queries(self.handle, first, count, _ptr(mins), _ptr(maxs)), "occ_batch_set_queries")
+
     def check(self) -> bool:
         """True if every launch since the last check fitted the scratch; on
         False the batch has been re-sized and the frames must be re-run."""

@@ -1275,6 +1275,37 @@ int occ_batch_results_all(occ_batch b, uint32_t* visibleBits, uint32_t* needsCli
   return OCC_OK;
 }
 
+int occ_batch_results_all_async(occ_batch b, uint32_t* visibleBits, uint32_t* needsClippingBits)
+{
+  if (!b) return fail(OCC_ERR_INVALID_ARG, "null batch");
+  const size_t nw = b->L.querySlots / 32;
+  if (nw) {
+    if (visibleBits)
+      OCC_CUDA(cudaMemcpyAsync(visibleBits, b->vis.p, nw * 4, cudaMemcpyDeviceToHost, b->ctx->stream));
+    if (needsClippingBits)
+      OCC_CUDA(cudaMemcpyAsync(needsClippingBits, b->nc.p, nw * 4, cudaMemcpyDeviceToHost, b->ctx->stream));
+  }
+  return OCC_OK;
+}
+
+int occ_batch_set_queries(occ_batch b, uint32_t first, uint32_t count, const float* mins, const float* maxs)
+{
+  if (!b || first > b->L.views.size() || count > b->L.views.size() - first)
+    return fail(OCC_ERR_INVALID_ARG, "bad argument");
+  size_t at = 0;  // boxes consumed from the host arrays
+  for (uint32_t v = first; v < first + count; ++v) {
+    const ViewDesc& V = b->L.views[v];
+    if (!V.queryCount) continue;
+    if (!mins || !maxs) return fail(OCC_ERR_INVALID_ARG, "null query boxes");
+    OCC_CUDA(cudaMemcpyAsync(b->qmin.p + V.queryStart, mins + 4 * at, (size_t)V.queryCount * 16,
+                             cudaMemcpyHostToDevice, b->ctx->stream));
+    OCC_CUDA(cudaMemcpyAsync(b->qmax.p + V.queryStart, maxs + 4 * at, (size_t)V.queryCount * 16,
+                             cudaMemcpyHostToDevice, b->ctx->stream));
+    at += V.queryCount;
+  }
+  return OCC_OK;
+}
+
 int occ_batch_result_words(occ_batch b, uint32_t* words)
 {
   if (!b || !words) return fail(OCC_ERR_INVALID_ARG, "null argument");

@@ -22,7 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from oracle.bindings import Reference, reference_bake_scene  # noqa: E402
+from oracle.bindings import Reference, reference_bake_scene, save_baked_scene  # noqa: E402
 from rasterizer_gb300 import scenes  # noqa: E402
 
 # fixture cases: (name, scene builder, resolution, camera list, query spec)
@@ -73,6 +73,9 @@ def main():
     g["city"] = {"mesh": c.digest(), "triangles": c.triangles, "occluders": len(sc), "quads": sc.quads,
                  "bake": scene_digest(sc), "frame_indices": list(CITY_FRAMES),
                  "frames": run_frames(sc, 1920, 1080, [mvps[f] for f in CITY_FRAMES], mins, maxs)}
+    # the city's occluders as the reference bakes them, for the benchmark's CPU
+    # arms (any host, no native library of this project involved)
+    save_baked_scene(os.path.join(HERE, "city_occluders.npz"), sc)
 
     # one small frame kept raw: the boxes scene at 320x200 seen from above the footprint
     sc = reference_bake_scene(m.vertices, m.indices)

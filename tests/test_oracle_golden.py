@@ -100,3 +100,39 @@ def test_city_frames():
         vis, nc = orc.query(mins, maxs)
         _check_frame(orc, flags, vis, nc, g)
         assert g["near_clipped"] == int(((flags & 3) == 3).sum())
+
+
+def test_city_bake_fixture():
+    """tests/golden/city_occluders.npz holds the reference's own bake of the
+    city (the occluders the benchmark's CPU arms draw, with no native library
+    of this project involved): same digest as the reference's bake, and the
+    library's host bake gives the same bytes."""
+    from oracle.bindings import load_baked_scene
+    sc = load_baked_scene(os.path.join(HERE, "golden", "city_occluders.npz"))
+    assert scene_digest(sc) == GOLDEN["city"]["bake"]
+    lib = to_baked(city_occluders())
+    assert len(lib) == len(sc)
+    assert all(np.array_equal(a, b) for a, b in zip(lib.packed, sc.packed))
+
+
+def test_gated_frame_loop_draws_front_to_back():
+    """The gated, distance-sorted frame loop of Main.cpp:181-206 in the oracle:
+    the drawing order ascends in squared distance, and every occluder it
+    rasterises was visible against the buffer drawn so far, so the result
+    never culls a box that the plain all-occluder frame shows."""
+    sc = to_baked(city_occluders())
+    mvps, eyes = scenes.camera_path(300, seed=7)
+    mins, maxs = scenes.query_boxes(20000, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    orc, full = Oracle(1920, 1080), Oracle(1920, 1080)
+    for f in (0, 150):
+        orc.write_depth(np.zeros(1920 * 1080, np.uint16))
+        order, flags = orc.frame_gated(sc, mvps[f], eyes[f])
+        d = ((sc.centers[order, :3].astype(np.float64) - eyes[f][:3]) ** 2).sum(axis=1)
+        assert np.all(np.diff(d) >= -1e-3 * np.maximum(d[1:], 1.0))
+        assert sorted(order.tolist()) == list(range(len(sc)))
+        full.write_depth(np.zeros(1920 * 1080, np.uint16))
+        fflags = full.frame_plain(sc, mvps[f])
+        assert (flags & 1).sum() <= (fflags & 1).sum()  # gating skips occluders already hidden
+        vis, _ = orc.query(mins, maxs)
+        fvis, _ = full.query(mins, maxs)
+        assert not (fvis.astype(bool) & ~vis.astype(bool)).any()
