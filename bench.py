@@ -116,51 +116,80 @@ class ClockSampler:
 # ---- CPU legs -------------------------------------------------------------------------
 
 _CPU_STATE = None
+CITY_FIXTURE = os.path.join(ROOT, "tests", "golden", "city_occluders.npz")
 
 
 def headline_views():
-    """(views, frames, 16) matrices of the headline's street-level views."""
+    """(views, frames, 16) matrices and (views, frames, 4) eyes of the headline's street-level views."""
     from rasterizer_gb300 import scenes
-    return np.stack([scenes.camera_path(64, seed=7000 + k)[0] for k in range(LEARNED_VIEWS)])
+    paths = [scenes.camera_path(64, seed=7000 + k) for k in range(LEARNED_VIEWS)]
+    return np.stack([m for m, _ in paths]), np.stack([e for _, e in paths])
+
+
+def headline_config(world: int) -> dict:
+    """The workload both arms run (the same dict in both bench lines)."""
+    return {"workload": f"{LEARNED_VIEWS} street-level 1920x1080 views of the dense city per step (seeded paths, "
+                        f"259,534 tris baked into 386 occluders / 129,768 quads), {NQ} lognormal query boxes per view",
+            "resolution": f"{W}x{H}", "views_per_step": LEARNED_VIEWS, "queries_per_view": NQ,
+            "l2": f"inputs larger than L2 ({LEARNED_VIEWS} depth buffers of 4 MB per step)",
+            "parallelism": f"replicas x{world}"}
 
 
 def _cpu_state():
-    """Per-process CPU oracle state: the baked city, the headline's views, the
-    queries and one persistent Oracle rasterizer per view slot (built once per
-    process)."""
+    """Per-process CPU state: the city's occluders as the reference bakes them
+    (tests/golden/city_occluders.npz: no native library of this project is
+    loaded), the headline's views, the queries and one Oracle rasterizer."""
     global _CPU_STATE
     if _CPU_STATE is None:
-        sys.path.insert(0, ROOT)
-        sys.path.insert(0, os.path.join(ROOT, "tests"))
-        from oracle.bindings import Oracle
-        from helpers import city_occluders, to_baked
+        from oracle.bindings import Oracle, load_baked_scene
         from rasterizer_gb300 import scenes
-        scene = to_baked(city_occluders())
+        scene = load_baked_scene(CITY_FIXTURE)
         mins, maxs = scenes.query_boxes(NQ, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
-        _CPU_STATE = (scene, headline_views(), mins, maxs, Oracle(W, H))
+        mvps, eyes = headline_views()
+        _CPU_STATE = (scene, mvps, eyes, mins, maxs, Oracle(W, H))
     return _CPU_STATE
 
 
 def _cpu_frame(f: int) -> int:
-    """One view (plain loop + all queries) on the CPU oracle: view f % 64 at frame f // 64."""
-    scene, mvps, mins, maxs, orc = _cpu_state()
-    orc.frame_plain(scene, mvps[f % LEARNED_VIEWS, (f // LEARNED_VIEWS) % mvps.shape[1]])
+    """One view on the CPU oracle with the reference's own frame loop
+    (Main.cpp:181-206: occluders front to back, each queried against the live
+    buffer before it is drawn) and all its queries: view f % 64 at frame f // 64."""
+    scene, mvps, eyes, mins, maxs, orc = _cpu_state()
+    v, t = f % LEARNED_VIEWS, (f // LEARNED_VIEWS) % mvps.shape[1]
+    orc.frame_gated(scene, mvps[v, t], eyes[v, t])
     orc.query(mins, maxs)
     return 1
 
 
-def cpu_baseline(budget_s: float = 12.0, max_frames: int = 60):
-    _cpu_state()
-    _cpu_frame(0)  # warm-up
+def _cpu_frame_plain(f: int) -> int:
+    """The same view with the plain all-occluder loop (the parity loop)."""
+    scene, mvps, eyes, mins, maxs, orc = _cpu_state()
+    v, t = f % LEARNED_VIEWS, (f // LEARNED_VIEWS) % mvps.shape[1]
+    orc.frame_plain(scene, mvps[v, t])
+    orc.query(mins, maxs)
+    return 1
+
+
+def _timed_frames(fn, budget_s: float, max_frames: int):
     done, t0 = 0, time.perf_counter()
     while done < max_frames and time.perf_counter() - t0 < budget_s:
-        _cpu_frame(done)
+        fn(done)
         done += 1
-    secs = time.perf_counter() - t0
+    return done, time.perf_counter() - t0
+
+
+def cpu_baseline(budget_s: float = 12.0, max_frames: int = 128):
+    _cpu_state()
+    _cpu_frame(0)  # warm-up
+    done, secs = _timed_frames(_cpu_frame, budget_s, max_frames)
+    pdone, psecs = _timed_frames(_cpu_frame_plain, budget_s / 3, max_frames)
     return {"value": done / secs, "unit": "views/s", "cores": 1, "kind": "port",
-            "sample": f"{done} views of the headline workload (the first {done} of its 64 street views, "
-                      f"plain all-occluder loop, all {NQ} queries each), 1 host thread, CPU oracle (portable "
-                      f"restatement; the reference's AVX2 build does not run on the Arm host)"}
+            "sample": f"{done} views of the headline workload (its 64 street views in order, then their next "
+                      f"frames), the reference's own frame loop (Main.cpp:181-206, occluders front to back, "
+                      f"each queried against the live buffer) on its own bake, all {NQ} queries each, 1 host "
+                      f"thread, CPU oracle (portable restatement; the reference's AVX2 build does not run on "
+                      f"the Arm host)",
+            "plain_loop_views_per_s": pdone / psecs, "plain_loop_sample": f"{pdone} views, all-occluder loop"}
 
 
 def _warm(_):
@@ -169,8 +198,9 @@ def _warm(_):
 
 
 def run_reference(args):
-    """--impl reference: the reference algorithm on all host cores (oracle port),
-    one frame per step, steps spread over one process per core."""
+    """--impl reference: the reference's own frame loop on all host cores
+    (oracle port), each step one round of the headline's 64 views spread
+    over one process per core (16 cores: 4 views each)."""
     import multiprocessing as mp
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -181,25 +211,64 @@ def run_reference(args):
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
         pool.map(_warm, range(cores), chunksize=1)
-        pool.map(_cpu_frame, range(args.warmup * cores), chunksize=1)
+        for w in range(args.warmup):
+            pool.map(_cpu_frame, range(w * LEARNED_VIEWS, (w + 1) * LEARNED_VIEWS), chunksize=1)
         t0 = time.perf_counter()
-        total = sum(pool.map(_cpu_frame, range(args.steps), chunksize=1))
+        total = 0
+        for st in range(args.steps):
+            total += sum(pool.map(_cpu_frame, range(st * LEARNED_VIEWS, (st + 1) * LEARNED_VIEWS), chunksize=1))
         dt = time.perf_counter() - t0
     value = total / dt
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "views/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/u16",
-            "data": "synthetic",
-            "config": {"workload": f"{LEARNED_VIEWS} street-level 1920x1080 views of the dense city (259,534 "
-                                   f"tris, 386 occluders, seeded paths), {NQ} lognormal query boxes per view; "
-                                   f"the reference's plain all-occluder loop (it has no learned selection)",
-                       "views_per_step": 1},
+            "data": "synthetic", "config": headline_config(1),
             "cpu_baseline": {"value": value, "unit": "views/s", "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} views (one per step, {cores} worker processes, each with "
-                                       f"its own persistent rasterizer); CPU oracle, because the reference's "
-                                       f"AVX2 build cannot run on aarch64"},
+                             "sample": f"{args.steps} steps of {LEARNED_VIEWS} views (the headline's 64 street "
+                                       f"views, each step their next frame), the reference's own frame loop "
+                                       f"(Main.cpp:181-206) on its own bake (tests/golden/city_occluders.npz), "
+                                       f"all {NQ} queries per view, {cores} worker processes; CPU oracle, because "
+                                       f"the reference's AVX2 build cannot run on aarch64 (one x86 core: the "
+                                       f"AVX2 build draws these views 5.3x as fast as the oracle)"},
             "e2e": {"value": value, "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def cpu_compare(frames: int = 16):
+    """x86-64 with oracle/_ref only: one core, the headline's views, the
+    reference's AVX2 build against the portable oracle, both frame loops
+    (each frame followed by its 100k queries).  Prints one JSON line."""
+    from oracle import bindings
+    from oracle.bindings import Reference, ReferenceScene
+    from rasterizer_gb300 import scenes
+    if not bindings.reference_available():
+        raise SystemExit("cpu-compare needs x86-64 and the reference sources")
+    bindings.build_oracle()
+    bindings.build_reference()
+    scene, mvps, eyes, mins, maxs, orc = _cpu_state()
+    mesh = scenes.city_scene()
+    rs = ReferenceScene(mesh.vertices, mesh.indices)
+    ref, scratch = Reference(W, H), Reference(W, H)
+    out = {"host": os.uname().machine, "frames": frames, "queries_per_frame": NQ}
+    legs = {
+        "oracle_gated": lambda v, t: orc.frame_gated(scene, mvps[v, t], eyes[v, t]),
+        "reference_gated": lambda v, t: rs.frame_gated(ref, mvps[v, t], eyes[v, t]),
+        "oracle_plain": lambda v, t: orc.frame_plain(scene, mvps[v, t]),
+        "reference_plain": lambda v, t: rs.frame_plain(ref, scratch, mvps[v, t]),
+    }
+    for name, frame in legs.items():
+        q = (lambda: orc.query(mins, maxs)) if name.startswith("oracle") else (lambda: ref.query(mins, maxs))
+        frame(0, 0)
+        q()
+        t0 = time.perf_counter()
+        for f in range(frames):
+            frame(f % LEARNED_VIEWS, f // LEARNED_VIEWS)
+            q()
+        out[name + "_views_per_s"] = frames / (time.perf_counter() - t0)
+    out["oracle_over_reference_gated"] = out["oracle_gated_views_per_s"] / out["reference_gated_views_per_s"]
+    out["oracle_over_reference_plain"] = out["oracle_plain_views_per_s"] / out["reference_plain_views_per_s"]
+    rs.close()
+    print(json.dumps(out), flush=True)
 
 
 # ---- GPU leg --------------------------------------------------------------------------
@@ -369,15 +438,26 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
     ok = plain.check()
     plain.close()
 
-    # headline: batched + learned launches, barrier + synchronize around the timed region
+    # headline: batched + learned launches in the zero-depth clear (each frame
+    # stands alone, so its culls compare with the full frame at the same
+    # poses), barrier + synchronize around the timed region; each launch's
+    # result bits are copied out behind its end event (outside the timing)
     sel = api.PreparedBatch(ctx, views)
     sel.setSelection(net, k_st, trackWins=True)
+    sel.setZeroDepth(True)
     move = mover(sel, paths, 64)
     for i in range(args.warmup):
         move(i)
         sel.launch()
     ok = sel.check() and ok
     tuning = sel.autotune(5)  # launch shapes for this batch, picked before the timed region
+    for i in range(args.warmup):
+        move(i)
+        sel.launch()
+    ok = sel.check() and ok
+    kept = min(args.steps, 64)  # launches whose bits are kept for the cull count
+    words = sel.resultWords()
+    bits = torch.empty((kept, words), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     sampler = ClockSampler(dev.index) if rank == 0 else None
@@ -390,6 +470,8 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
         starts[i].record(stream)
         sel.launch()
         ends[i].record(stream)
+        if i < kept:
+            sel.resultsAllAsync(bits[i])
     ctx.synchronize()
     torch.cuda.synchronize()
     _barrier(world)
@@ -399,8 +481,21 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
     stats = sel.stats()
     prof = sel.profile(20)
     kern = dict(zip(["setup", "scan", "fill", "walk", "raster", "query", "selection"], [float(x) for x in prof]))
-    # end to end through the public API: the step's 64 matrices from the host,
-    # launch, every view's result bits back to the host
+    # culls kept and false culls of those timed launches, against the full
+    # frames (every candidate, zero-depth clear) at the same poses
+    timed_tracks = [L.Track(t.width, t.height, t.occluders, t.mvps[[i % 64 for i in range(kept)]], t.query_start,
+                            t.query_count, t.kind) for t in paths]
+    full_timed = L.run_full(ctx, occ, timed_tracks, pmin, pmax)
+    res_first = sel.resultsAll()[2]
+    timed_culls = L.CullStats()
+    for i in range(kept):
+        for v in range(LEARNED_VIEWS):
+            a0 = int(res_first[v])
+            vis = api.unpack_bits(bits[i, a0:a0 + (NQ + 31) // 32], NQ)
+            timed_culls.add_culls(~vis, full_timed[i][v])
+    del full_timed
+    # end to end through the public API: the step's 64 matrices from the
+    # host, launch, every view's result bits back to the host
     e2e_steps = 50
     sel.resultsAll()
     t1 = time.perf_counter()
@@ -409,6 +504,30 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
         sel.launch()
         vis_words, nc_words, _ = sel.resultsAll()
     e2e_s = time.perf_counter() - t1
+    # the same with every view's query boxes uploaded from the host each step
+    # (moving objects: the reference takes every query's box from the caller),
+    # two box sets alternating, page-locked
+    nbox = LEARNED_VIEWS * NQ
+    box_sets = []
+    for j in range(2):
+        lo = torch.empty((nbox, 4), dtype=torch.float32, pin_memory=True).numpy()
+        hi = torch.empty((nbox, 4), dtype=torch.float32, pin_memory=True).numpy()
+        shift = np.float32(0.25 * j)
+        lo[:] = np.tile(pmin, (LEARNED_VIEWS, 1)) + shift
+        hi[:] = np.tile(pmax, (LEARNED_VIEWS, 1)) + shift
+        lo[:, 3] = hi[:, 3] = 1.0
+        box_sets.append((lo, hi))
+    for i in range(3):
+        sel.setQueries(*box_sets[i % 2])
+        sel.launch()
+        sel.resultsAll()
+    t1 = time.perf_counter()
+    for i in range(e2e_steps):
+        move(i)
+        sel.setQueries(*box_sets[i % 2])
+        sel.launch()
+        vis_words, nc_words, _ = sel.resultsAll()
+    e2e_dyn_s = time.perf_counter() - t1
     sel.close()
     for v in views:
         v["raster"].close()
@@ -423,12 +542,20 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
     headline = {
         "value": world * LEARNED_VIEWS * args.steps / (dev_ms * 1e-3), "ms_per_step": dev_ms / args.steps,
         "clocks": clocks, "kernels": kern,
+        "culls_timed": dict(timed_culls.as_culls_dict(), launches=kept, views=kept * LEARNED_VIEWS,
+                            against="full frames (every candidate, zero-depth clear) at the same poses"),
         "roofline": {"bound": "hbm", "kernel": "k_raster (with k_tile_prep)", "unit": "GB/s",
                      "achieved": raster_bytes / (kern["raster"] * 1e-3) / 1e9, "algorithmic_bytes": raster_bytes},
         "e2e": {"value": world * LEARNED_VIEWS * e2e_steps / e2e_s, "unit": "views/s",
                 "h2d_bytes_per_step": stats["table_bytes"], "d2h_bytes_per_step": int(vis_words.nbytes + nc_words.nbytes),
                 "path": "PreparedBatch.setModelViewProjections (64 matrices) / launch / resultsAll (every view's "
                         "bits, one copy) through the Python mirror of the C ABI, wall clock"},
+        "e2e_dynamic_boxes": {
+            "value": world * LEARNED_VIEWS * e2e_steps / e2e_dyn_s, "unit": "views/s",
+            "h2d_bytes_per_step": stats["table_bytes"] + 2 * 16 * nbox,
+            "d2h_bytes_per_step": int(vis_words.nbytes + nc_words.nbytes),
+            "path": "as e2e, plus PreparedBatch.setQueries: every view's 100k boxes (min and max float4) from "
+                    "page-locked host memory each step, two box sets alternating"},
         "launches_per_step": 4 + 9}
     # ---- the 256-view workload (mixed resolutions) ----
     k_mv = pick(L.multiview_tracks(centers, quads, NQ, frames=4, seed=9))
@@ -740,16 +867,13 @@ def run_gpu(args):
                     frac=head["roofline"]["achieved"] / peak, traffic=traffic.get("k_raster_batched"))
         line.update({
             "value": head["value"], "unit": "views/s", "steps": args.steps, "ms_per_step": head["ms_per_step"],
-            "config": {"workload": f"batched + learned: {LEARNED_VIEWS} street-level 1920x1080 views of the dense "
-                                   f"city per launch (seeded paths, {len(occ)} occluders, {NQ} lognormal query "
-                                   f"boxes per view), the selector's top {k:.0%} of each view's candidates",
-                       "culls_kept_vs_full": at_k.get("learned", {}).get("culls_retained"),
-                       "false_culls": at_k.get("learned", {}).get("false_culls"),
-                       "resolution": f"{W}x{H}", "views_per_step": LEARNED_VIEWS,
-                       "l2": f"inputs larger than L2 ({LEARNED_VIEWS} depth buffers of 4 MB per launch)",
-                       "timing": "CUDA events on the library stream around each batched graph launch; max over "
-                                 "ranks", "parallelism": f"replicas x{world}"},
-            "roofline": roof, "e2e": head["e2e"], "clocks": head["clocks"],
+            "config": headline_config(world),
+            "method": f"batched + learned: each view draws the selector's top {k:.0%} of its candidate occluders "
+                      f"in the zero-depth clear (every frame stands alone), one CUDA graph launch per step",
+            "culls": dict(head["culls_timed"], held_out_paths=at_k.get("learned")),
+            "timing": "CUDA events on the library stream around each batched graph launch; max over ranks",
+            "roofline": roof, "e2e": head["e2e"], "e2e_dynamic_boxes": head["e2e_dynamic_boxes"],
+            "clocks": head["clocks"],
             "gpu_launches": head["launches_per_step"] * args.steps, "kernels_ms": head["kernels"]})
     else:
         line.update({"value": plain["value"], "unit": "views/s", "steps": plain["steps"],
@@ -890,12 +1014,17 @@ def main():
     ap.add_argument("--profile-train", type=int, default=0, help="training steps after --profile-learned")
     ap.add_argument("--profile-misc", action="store_true",
                     help="only launch the kernels outside the batched frame once each (for ncu)")
+    ap.add_argument("--cpu-compare", action="store_true",
+                    help="x86-64 with the reference's sources: one core, the reference's AVX2 build against the "
+                         "portable oracle on the headline's views (both frame loops)")
     ap.add_argument("--profile-extras", action="store_true",
                     help="--profile-learned: first launch with the second pass and the cull labels")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.profile_misc:
+    if args.cpu_compare:
+        cpu_compare()
+    elif args.profile_misc:
         run_profile_misc()
     elif args.profile_learned:
         run_profile_learned(args.profile_learned, args.profile_views, args.profile_train, args.profile_extras)

@@ -298,6 +298,21 @@ class CullStats:
         self.quads_candidates += int(quads[cand].sum())
         self.quads_drawn += int(quads[drawn].sum())
 
+    def add_culls(self, culled: np.ndarray, full_frame: dict) -> None:
+        """Culls only (no selection statistics): `culled` against the full frame."""
+        fu = full_frame["culled"]
+        occ = fu & full_frame["visible_empty"]
+        self.full += int(occ.sum())
+        self.kept += int((culled & occ).sum())
+        self.false += int((culled & ~fu).sum())
+        self.full_all += int(fu.sum())
+        self.kept_all += int((culled & fu).sum())
+
+    def as_culls_dict(self) -> dict:
+        return dict(occlusion_culls_full=self.full, occlusion_culls_kept=self.kept,
+                    culls_retained=round(self.retained, 5), false_culls=self.false,
+                    all_culls_full=self.full_all, all_culls_retained=round(self.kept_all / max(self.full_all, 1), 5))
+
     def as_dict(self) -> dict:
         return dict(occlusion_culls_full=self.full, occlusion_culls_kept=self.kept,
                     culls_retained=round(self.retained, 5), false_culls=self.false,

@@ -345,3 +345,59 @@ def test_cull_labels_consistent(ctx):
         assert counts.sum() <= 16 * int((~vis).sum())
         assert not ((counts > 0) & (wins == 0)).any()
     b.close()
+
+
+@pytest.mark.parametrize("zero", [True, False], ids=["zero-depth", "stale-depth"])
+def test_headline_batch_matches_oracle(ctx, zero):
+    """The benchmark's headline batch itself: 64 street-level 1920x1080 views
+    of the city (the benchmark's seeded paths), the selector's top 5 % of each
+    view's candidates, 100k query boxes per view, three consecutive launches
+    (each launch's features hold the previous launch's wins and draw flags).
+    Every view's depth, hiZ and query bits equal the oracle drawing the
+    selected occluders in order on its own persistent rasterizer: in the
+    zero-depth clear the headline times (a zeroed buffer each launch), and in
+    the reference's clear (stale depth kept and queried)."""
+    from rasterizer_gb300 import learned as L
+    occ = city_occluders()
+    scene = to_baked(occ)
+    nq = 100_000
+    pmin, pmax = scenes.query_boxes(nq, seed=44, footprint=300.0, lognormal=(0.0, 1.0), y_range=(0.0, 20.0))
+    paths = L.street_tracks(64, 64, seed0=7000, n_occluders=len(occ), queries=nq)
+    views = L._views(ctx, occ, paths, pmin, pmax)
+    net = api.OccluderSelector(ctx, seed=0)
+    b = api.PreparedBatch(ctx, views)
+    w, h = 1920, 1080
+    orcs = [Oracle(w, h) for _ in paths]
+    for o, t in zip(orcs, paths):
+        o.frame_plain(scene, t.mvps[0])  # the preparing frame (every candidate, the reference's clear)
+    b.setSelection(net, 0.05, trackWins=True)
+    b.setZeroDepth(zero)
+    zeros = np.zeros(w * h, np.uint16)
+    drawn = 0
+    for f in (1, 2, 3):
+        for v, t in enumerate(paths):
+            b.setModelViewProjection(v, t.mvps[f])
+        b.launch()
+        assert b.check()
+        res = b.resultsAll(unpack=True)
+        for v, (t, o) in enumerate(zip(paths, orcs)):
+            s = b.selection(v)
+            if zero:
+                o.write_depth(zeros)
+            o.clear()
+            o.set_mvp(t.mvps[f])
+            for i in np.nonzero(s["selected"])[0]:
+                o.rasterize(scene.packed[i], scene.packets[i], scene.ref[i, :4], scene.ref[i, 4:],
+                            bool(s["features"][i, 1]))
+            drawn += int(s["selected"].sum())
+            r = views[v]["raster"]
+            assert not mismatch_report(f"launch {f} view {v} depth", r.readDepthRaw(), o.depth())
+            assert not mismatch_report(f"launch {f} view {v} hiz", r.readHiZ(), o.hiz())
+            ovis, onc = o.query(pmin, pmax)
+            assert np.array_equal(res[v][0].astype(np.uint8), ovis), (f, v)
+            assert np.array_equal(res[v][1].astype(np.uint8), onc), (f, v)
+    assert drawn > 3 * 64
+    b.close()
+    net.close()
+    for v in views:
+        v["raster"].close()
