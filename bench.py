@@ -213,10 +213,10 @@ def run_reference(args):
         pool.map(_warm, range(cores), chunksize=1)
         for w in range(args.warmup):
             pool.map(_cpu_frame, range(w * LEARNED_VIEWS, (w + 1) * LEARNED_VIEWS), chunksize=1)
+        # the steps' views as one stream of tasks: a worker takes the next view
+        # as soon as it is free, so no step waits for its slowest view
         t0 = time.perf_counter()
-        total = 0
-        for st in range(args.steps):
-            total += sum(pool.map(_cpu_frame, range(st * LEARNED_VIEWS, (st + 1) * LEARNED_VIEWS), chunksize=1))
+        total = sum(pool.imap_unordered(_cpu_frame, range(args.steps * LEARNED_VIEWS), chunksize=1))
         dt = time.perf_counter() - t0
     value = total / dt
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "views/s", "n_gpus": args.gpus,
@@ -225,11 +225,13 @@ def run_reference(args):
             "data": "synthetic", "config": headline_config(1),
             "cpu_baseline": {"value": value, "unit": "views/s", "cores": cores, "kind": "port",
                              "sample": f"{args.steps} steps of {LEARNED_VIEWS} views (the headline's 64 street "
-                                       f"views, each step their next frame), the reference's own frame loop "
+                                       f"views, each step their next frame, one stream of tasks over the "
+                                       f"workers), the reference's own frame loop "
                                        f"(Main.cpp:181-206) on its own bake (tests/golden/city_occluders.npz), "
                                        f"all {NQ} queries per view, {cores} worker processes; CPU oracle, because "
                                        f"the reference's AVX2 build cannot run on aarch64 (one x86 core: the "
-                                       f"AVX2 build draws these views 5.3x as fast as the oracle)"},
+                                       f"AVX2 build draws these views about 5x as fast as the oracle, "
+                                       f"bench.py --cpu-compare)"},
             "e2e": {"value": value, "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

@@ -618,9 +618,9 @@ class PreparedBatch:
                                             int(bool(trackWins))), "occ_batch_set_selection")
         self._selector = mlp  # the captured launch reads the network's weights
 
-    # occ_batch_autotune / occ_batch_set_tuning layout (OCC_TUNING_FIELDS entries, the last reserved)
+    # occ_batch_autotune / occ_batch_set_tuning layout (OCC_TUNING_FIELDS entries)
     TUNING_KEYS = ("setup_ctas_per_sm", "fill_ctas_per_sm", "walk_ctas_per_sm", "raster_ctas_per_sm",
-                   "raster_units_per_fetch", "query_rounds", "raster_unit_rows", "reserved")
+                   "raster_units_per_fetch", "query_rounds", "raster_unit_rows", "raster_threads_per_unit")
 
     def autotune(self, iterations: int = 5) -> dict:
         """Picks the launch shapes of the persistent kernels by timing the
@@ -632,7 +632,7 @@ class PreparedBatch:
         check(lib().occ_batch_autotune(self.handle, iterations, _ptr(tuned), _ptr(before), _ptr(after)),
               "occ_batch_autotune")
         names = ("setup", "scan", "fill", "walk", "raster", "query", "selection")
-        return {"tuned": {k: int(v) for k, v in zip(self.TUNING_KEYS[:-1], tuned)},
+        return {"tuned": {k: int(v) for k, v in zip(self.TUNING_KEYS, tuned)},
                 "ms_before": {k: float(v) for k, v in zip(names, before)},
                 "ms_after": {k: float(v) for k, v in zip(names, after)}}
 

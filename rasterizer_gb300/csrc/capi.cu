@@ -35,7 +35,7 @@ cudaError_t launch_mlp_backward(const float* score, const float* target, uint32_
 uint32_t mlp_grad_blocks(uint32_t B);
 cudaError_t launch_mlp_publish(const float* params, MlpDevice* mlp, cudaStream_t stream);
 cudaError_t launch_cull_labels(const FrameParams& P, cudaStream_t stream);
-void tuning_limits(uint32_t out[6]);
+void tuning_limits(uint32_t out[7]);
 cudaError_t launch_adam(float* params, const float* grad, float* m, float* v, float lr, uint32_t step,
                         cudaStream_t stream);
 int mlp_param_count();
@@ -1473,7 +1473,7 @@ static int profile_with(occ_batch b, const LaunchTuning& t, uint32_t iterations,
 int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[8], float msBefore[7], float msAfter[7])
 {
   if (!b || !iterations) return fail(OCC_ERR_INVALID_ARG, "bad argument");
-  uint32_t lim[6];
+  uint32_t lim[7];
   tuning_limits(lim);
   LaunchTuning best = b->tune;
   float ms[7], base[7];
@@ -1503,9 +1503,24 @@ int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[8], floa
   OCC_CHECK(search(&LaunchTuning::setupPerSm, 0, upTo(lim[0])));
   OCC_CHECK(search(&LaunchTuning::fillPerSm, 2, upTo(lim[1])));
   OCC_CHECK(search(&LaunchTuning::walkPerSm, 3, {2, 4, 8, 16}));
-  OCC_CHECK(search(&LaunchTuning::rasterRows, 4, {1, 2, 4}));
-  const uint32_t rows = best.rasterRows ? best.rasterRows : kDefaultRasterRows;
-  OCC_CHECK(search(&LaunchTuning::rasterPerSm, 4, upTo(lim[rows == 1 ? 2 : (rows == 2 ? 3 : 4)])));
+  // raster form: one warp per unit of 1, 2 or 4 block rows, or a CTA per 8x2 unit
+  {
+    float bestMs = 3.0e38f;
+    LaunchTuning pick = best;
+    for (uint32_t form : {1u, 2u, 4u, 128u}) {
+      LaunchTuning t = best;
+      t.rasterThreads = form == 128u ? 128u : 32u;
+      t.rasterRows = form == 128u ? 2u : form;
+      OCC_CHECK(profile_with(b, t, iterations, ms));
+      if (ms[4] < bestMs) {
+        bestMs = ms[4];
+        pick = t;
+      }
+    }
+    best = pick;
+  }
+  const uint32_t limIdx = best.rasterThreads == 128u ? 5 : (best.rasterRows == 1 ? 2 : (best.rasterRows == 2 ? 3 : 4));
+  OCC_CHECK(search(&LaunchTuning::rasterPerSm, 4, upTo(lim[limIdx])));
   OCC_CHECK(search(&LaunchTuning::rasterChunk, 4, {1, 2, 4, 8, 16}));
   OCC_CHECK(search(&LaunchTuning::queryRounds, 5, {kQueryPerThread, 1, 2, 4, 8}));
   b->tune = best;
@@ -1519,7 +1534,7 @@ int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[8], floa
     tuned[4] = best.rasterChunk;
     tuned[5] = best.queryRounds;
     tuned[6] = best.rasterRows ? best.rasterRows : kDefaultRasterRows;
-    tuned[7] = 0;
+    tuned[7] = best.rasterThreads;
   }
   return OCC_OK;
 }
@@ -1571,7 +1586,10 @@ int occ_batch_set_tuning(occ_batch b, const uint32_t tune[8])
   if (tune[5] > kQueryRounds && tune[5] != kQueryPerThread) return fail(OCC_ERR_INVALID_ARG, "unknown query form");
   if (tune[6] != 0 && tune[6] != 1 && tune[6] != 2 && tune[6] != 4)
     return fail(OCC_ERR_INVALID_ARG, "raster unit rows must be 1, 2 or 4 (0: the default)");
-  if (tune[7] != 0) return fail(OCC_ERR_INVALID_ARG, "tuning entry 7 is reserved (0)");
+  if (tune[7] != 0 && tune[7] != 32 && tune[7] != 128)
+    return fail(OCC_ERR_INVALID_ARG, "raster threads per unit must be 32 or 128 (0: chosen per launch)");
+  if (tune[7] == 128 && tune[6] != 0 && tune[6] != 2)
+    return fail(OCC_ERR_INVALID_ARG, "the 128-thread raster form takes units of 2 block rows");
   LaunchTuning t{};
   t.setupPerSm = tune[0];
   t.fillPerSm = tune[1];
@@ -1580,6 +1598,7 @@ int occ_batch_set_tuning(occ_batch b, const uint32_t tune[8])
   t.rasterChunk = tune[4];
   t.queryRounds = tune[5];
   t.rasterRows = tune[6];
+  t.rasterThreads = tune[7];
   b->tune = t;
   return capture(b);
 }

@@ -53,6 +53,7 @@ static uint32_t g_walkBlocks = 152 * 8;
 static uint32_t g_sms = 152;
 static uint32_t g_setupPerSm = 4, g_fillPerSm = 4;  // occupancy limits
 static uint32_t g_rasterPerSm[3] = {6, 6, 4};        // per raster unit shape R = 1, 2, 4
+static uint32_t g_rasterCtaPerSm = 8;                 // the 128-thread form
 
 static uint32_t grid_of(uint32_t tuned, uint32_t limit, uint32_t work)
 {
@@ -1492,6 +1493,308 @@ __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks<R>) k_raster(
   }
 }
 
+// ---- k_raster_cta: four warps per raster unit ------------------------------------------
+//
+// The other raster form: one CTA of 128 threads per 8x2-block unit, thread t
+// owning pixel row t%8 of block t/8.  The CTA filters the unit's super-tile
+// list 256 entries a round and computes 128 fragments a round, so a unit with
+// a long list or many fragments finishes four times sooner than on one warp;
+// the price is CTA barriers between the phases.  Views with few units and
+// long lists (one large view) favour it; batches of many views favour the
+// warp form.
+
+constexpr int kCtaUnitBlocks = kTileW * 2;               // 16 blocks (8 x 2)
+constexpr int kCtaThreads = 8 * kCtaUnitBlocks;          // one thread per block row: 128
+constexpr int kCtaMinBlocks = 8;
+constexpr int kCtaListCap = 512;                         // listed quads buffered per unit
+constexpr int kCtaScanPerRound = 2 * kCtaThreads;
+constexpr int kCtaMaskWords = kCtaThreads / 32;
+
+struct CtaRasterSmem {
+  uint32_t lq[kCtaListCap];      // quad index
+  uint32_t lrect[kCtaListCap];   // quad rect within the unit: x0 | y0 << 3 | w << 5 | h << 9
+  uint32_t loff[kCtaListCap];    // first fragment of each listed quad
+  uint32_t frag[kCtaThreads * kFragStride];
+  uint32_t meta[kCtaThreads];    // per fragment slot: maxZ << 16 | target block
+  uint32_t fcmd[kCtaThreads];    // per fragment slot: command (win counting only)
+  uint32_t bmask[kCtaUnitBlocks][kCtaMaskWords];  // per block: fragment slots aimed at it
+  uint32_t hiz[kCtaUnitBlocks];  // per block: current hiZ
+  uint32_t scan[kCtaThreads / 32];
+};
+
+// Merges fragment slot `slot` into this thread's pixel row of its block (the
+// reference's hiZ test, fast-clear overwrite or max-merge) and the block's new
+// hiZ over its eight threads (`groupMask`).  With kWins, own[x] tracks the
+// command (+1) that produced pixel x's value.
+template <bool kWins>
+__device__ __forceinline__ void merge_slot_row(const ViewDesc& V, const CtaRasterSmem& S, uint32_t slot, uint32_t py,
+                                               uint32_t blk, uint32_t groupMask, uint32_t (&row)[4], uint32_t& hiz,
+                                               bool& have, uint32_t (&own)[8])
+{
+  const uint32_t mz = S.meta[slot] >> 16;
+  if (hiz >= mz) return;  // the reference's hiZ test (Rasterizer.cpp:1148-1152)
+  const uint32_t* src = S.frag + slot * kFragStride + 4 * py;
+  const uint32_t c1 = kWins ? S.fcmd[slot] + 1 : 0u;
+  if (hiz == 1) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (kWins) {
+        own[2 * i] = (src[i] & 0xFFFFu) ? c1 : 0u;
+        own[2 * i + 1] = (src[i] >> 16) ? c1 : 0u;
+      }
+      row[i] = src[i];
+    }
+  } else {
+    if (!have) {
+      const uint4 a = *reinterpret_cast<const uint4*>(V.depth + (size_t)blk * 64 + 8 * py);
+      row[0] = a.x; row[1] = a.y; row[2] = a.z; row[3] = a.w;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (kWins) {
+        if ((src[i] & 0xFFFFu) > (row[i] & 0xFFFFu)) own[2 * i] = c1;
+        if ((src[i] >> 16) > (row[i] >> 16)) own[2 * i + 1] = c1;
+      }
+      row[i] = vmax_u16x2(row[i], src[i]);
+    }
+  }
+  have = true;
+  uint32_t mn = vmin_u16x2(vmin_u16x2(row[0], row[1]), vmin_u16x2(row[2], row[3]));
+  mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 1));
+  mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 2));
+  mn = vmin_u16x2(mn, __shfl_xor_sync(groupMask, mn, 4));
+  hiz = ::min(mn & 0xFFFFu, mn >> 16);
+}
+
+// Runs the listed quads (n of them, F fragments) kCtaThreads fragments a round.
+template <bool kWins>
+__device__ __forceinline__ void raster_list_cta(const FrameParams& P, const ViewDesc& V, CtaRasterSmem& S, uint32_t n,
+                                                uint32_t F, uint32_t tx0, uint32_t ty0, uint32_t tid, uint32_t blk,
+                                                bool inView, uint32_t (&row)[4], uint32_t& hiz, bool& have,
+                                                uint32_t (&own)[8])
+{
+  const uint32_t lane = tid & 31;
+  const uint32_t py = tid & 7;  // pixel row owned by this thread
+  const uint32_t myBlock = tid >> 3;
+  const uint32_t groupMask = 0xFFu << (lane & ~7u);
+  for (uint32_t f0 = 0; f0 < F; f0 += kCtaThreads) {
+    if (tid < kCtaUnitBlocks * kCtaMaskWords) (&S.bmask[0][0])[tid] = 0;
+    const uint32_t f = f0 + tid;
+    uint32_t target = 0, q = 0, bx = 0, by = 0;
+    const bool haveF = f < F;
+    if (haveF) {
+      uint32_t lo = 0, hi = n - 1;  // last listed quad whose first fragment is <= f
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (S.loff[mid] <= f) lo = mid; else hi = mid - 1;
+      }
+      const uint32_t k = f - S.loff[lo];
+      const uint32_t rc = S.lrect[lo];
+      const uint32_t rw = (rc >> 5) & 15u;
+      const uint32_t rr = k / rw, cc = k - rr * rw;
+      const uint32_t lx = (rc & 7u) + cc, ly = ((rc >> 3) & 3u) + rr;
+      target = ly * kTileW + lx;
+      bx = tx0 + lx;
+      by = ty0 + ly;
+      q = S.lq[lo];
+    }
+    __syncthreads();  // bmask cleared
+    uint32_t meta = 0;
+    if (haveF) {
+      const QuadRaster Q = P.rec[q];
+      const uint32_t ckq = __ldg(P.ckBase + q);
+      const uint32_t ownerHiz = S.hiz[target];
+      // early skip (see raster_list): exact, hiZ only falls through the fast-clear overwrite
+      const bool skip = ownerHiz >= Q.maxZ && !(ownerHiz == 1 && Q.maxZ == 1);
+      if (!skip && make_fragment(P, Q, q, ckq, bx, by, tx0, S.frag + tid * kFragStride)) {
+        meta = ((uint32_t)Q.maxZ << 16) | target;
+        if (kWins) S.fcmd[tid] = P.walk[q].pad[0];
+        atomicOr(&S.bmask[target][tid >> 5], 1u << lane);
+      }
+    }
+    S.meta[tid] = meta;
+    __syncthreads();
+    // merge, in slot order, the fragments aimed at this thread's block
+    if (inView) {
+#pragma unroll 1
+      for (int wd = 0; wd < kCtaMaskWords; ++wd) {
+        uint32_t mine = S.bmask[myBlock][wd];
+        while (mine) {
+          const uint32_t slot = 32u * wd + __ffs(mine) - 1;
+          mine &= mine - 1;
+          merge_slot_row<kWins>(V, S, slot, py, blk, groupMask, row, hiz, have, own);
+        }
+      }
+      if (py == 0) S.hiz[myBlock] = hiz;
+    }
+    __syncthreads();
+  }
+}
+
+// One 8x2-block unit (queue record as raster_unit's, first block row even).
+template <bool kWins>
+__device__ __forceinline__ void raster_unit_cta(const FrameParams& P, CtaRasterSmem& S, const uint4 rec)
+{
+  const uint32_t tid = threadIdx.x, lane = tid & 31;
+  const ViewDesc& V = P.views[rec.y];
+  const uint32_t lt = (rec.x >> 2) - V.tileStart;
+  const uint32_t tx0 = (lt % V.tilesX) * kTileW, ty0 = (lt / V.tilesX) * kTileH + (rec.x & 3u);
+  const uint32_t myBlock = tid >> 3, py = tid & 7;
+  const uint32_t bx = tx0 + (myBlock & 7), by = ty0 + (myBlock >> 3);
+  const bool inView = bx < V.blocksX && by < V.blocksY;
+  const uint32_t blk = inView ? by * V.blocksX + bx : 0;
+  const bool clearing = (V.flags & kViewClear) != 0 && P.phase == 0;
+  uint32_t hiz = clearing ? 1u : (inView ? (uint32_t)V.hiz[blk] : 0xFFFFu);
+  bool have = false;
+  uint32_t row[4] = {0, 0, 0, 0};
+  uint32_t own[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const uint32_t listLen = rec.w;
+  const uint4* list = P.stList + rec.z;
+  if (py == 0) S.hiz[myBlock] = hiz;
+  __syncthreads();
+  uint32_t n = 0, F = 0;
+  // kCtaScanPerRound list entries per round (two consecutive ones per thread),
+  // listed in list order unless already hidden in every block they touch;
+  // one scan of (fragments << 16 | quads) places both
+  for (uint32_t base = 0; base < listLen; base += kCtaScanPerRound) {
+    uint4 e[2];
+    bool ov[2];
+    uint32_t rect[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const uint32_t idx = base + 2 * tid + k;
+      e[k] = idx < listLen ? __ldg(list + idx) : make_uint4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const uint32_t qx0 = e[k].y & 0xFFFFu, qy0 = e[k].y >> 16, qx1 = e[k].z & 0xFFFFu, qy1 = e[k].z >> 16;
+      const uint32_t x0 = ::max(qx0, tx0), x1 = ::min(qx1, tx0 + kTileW);
+      const uint32_t y0 = ::max(qy0, ty0), y1 = ::min(qy1, ty0 + 2);
+      bool o = x0 < x1 && y0 < y1;  // padding entries have an empty box
+      if (o) {
+        const uint32_t mz = e[k].w;
+        bool hidden = true;
+        for (uint32_t yy = y0 - ty0; yy < y1 - ty0 && hidden; ++yy)
+          for (uint32_t xx = x0 - tx0; xx < x1 - tx0; ++xx) {
+            const uint32_t h = S.hiz[yy * kTileW + xx];
+            if (!(h >= mz && !(h == 1 && mz == 1))) {
+              hidden = false;
+              break;
+            }
+          }
+        o = !hidden;
+      }
+      ov[k] = o;
+      rect[k] = (x0 - tx0) | ((y0 - ty0) << 3) | ((x1 - x0) << 5) | ((y1 - y0) << 9);
+    }
+    uint32_t fr[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) fr[k] = ov[k] ? ((rect[k] >> 5) & 15u) * ((rect[k] >> 9) & 7u) : 0u;
+    const uint32_t cnt = (ov[0] ? 1u : 0u) + (ov[1] ? 1u : 0u);
+    uint32_t tot;  // per round at most 256 quads and 4,096 fragments: the halves do not carry
+    const uint32_t ex = block_exclusive_scan<kCtaThreads>(cnt | ((fr[0] + fr[1]) << 16), tot, S.scan);
+    uint32_t pos = n + (ex & 0xFFFFu), fpos = F + (ex >> 16);
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+      if (ov[k]) {
+        S.lq[pos] = e[k].x;
+        S.lrect[pos] = rect[k];
+        S.loff[pos] = fpos;
+        ++pos;
+        fpos += fr[k];
+      }
+    n += tot & 0xFFFFu;
+    F += tot >> 16;
+    __syncthreads();
+    if (n > (uint32_t)(kCtaListCap - kCtaScanPerRound) || (base + kCtaScanPerRound >= listLen && n > 0)) {
+      raster_list_cta<kWins>(P, V, S, n, F, tx0, ty0, tid, blk, inView, row, hiz, have, own);
+      n = 0;
+      F = 0;
+    }
+  }
+  if (inView) {
+    if ((clearing || have) && py == 0) V.hiz[blk] = (uint16_t)hiz;
+    uint4* d = reinterpret_cast<uint4*>(V.depth + (size_t)blk * 64 + 8 * py);
+    if (have) *d = make_uint4(row[0], row[1], row[2], row[3]);
+    else if (clearing && (V.flags & kViewZeroDepth)) *d = make_uint4(0, 0, 0, 0);
+  }
+  if (kWins) {
+    // pixels won per command: one atomic per distinct command per warp when
+    // every row has one owner (the common case), else per warp and pixel column
+    bool same = true;
+#pragma unroll
+    for (int x = 1; x < 8; ++x) same &= own[x] == own[0];
+    if (__all_sync(0xFFFFFFFFu, same)) {
+      const uint32_t key = inView ? own[0] : 0u;
+      const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+      if (key && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&P.wins[key - 1], 8u * (uint32_t)__popc(peers));
+    } else {
+#pragma unroll
+      for (int x = 0; x < 8; ++x) {
+        const uint32_t key = inView ? own[x] : 0u;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+        if (key && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&P.wins[key - 1], (uint32_t)__popc(peers));
+      }
+    }
+    if (V.owner && inView) {
+      uint32_t* o = V.owner + (size_t)blk * 64 + 8 * py;
+      if (P.phase == 0) {
+        reinterpret_cast<uint4*>(o)[0] = make_uint4(own[0], own[1], own[2], own[3]);
+        reinterpret_cast<uint4*>(o)[1] = make_uint4(own[4], own[5], own[6], own[7]);
+      } else {
+#pragma unroll
+        for (int x = 0; x < 8; ++x)
+          if (own[x]) o[x] = own[x];  // pixels the second pass changed
+      }
+    }
+  }
+}
+
+// Persistent CTAs taking queued 8x2 units one at a time; the next record is
+// copied with cp.async while the current unit is rasterised.
+template <bool kWins>
+__global__ void __launch_bounds__(kCtaThreads, kCtaMinBlocks) k_raster_cta(FrameParams P)
+{
+  __shared__ CtaRasterSmem S;
+  __shared__ uint32_t s_next;
+  __shared__ __align__(16) uint4 s_rec[2];  // this unit's queue record and the next one's
+  if (P.header->overflow) return;
+  const uint32_t nActive = P.header->activeTiles;
+  const uint32_t chunk = P.tune.rasterChunk ? P.tune.rasterChunk : 1u;  // units per fetch
+  if (threadIdx.x == 0) {
+    const uint32_t i0 = atomicAdd(&P.header->tileCursor, chunk);
+    s_next = i0;
+    if (i0 < nActive) s_rec[0] = P.activeTileList[i0];
+  }
+  __syncthreads();
+  uint32_t i = s_next, buf = 0;
+  while (i < nActive) {
+    uint32_t nxt = 0;
+    if (threadIdx.x == 0) nxt = atomicAdd(&P.header->tileCursor, chunk);  // next fetch, ahead of time
+    const uint32_t end = ::min(i + chunk, nActive);
+    for (uint32_t j = i; j < end; ++j) {
+      const uint4 rec = s_rec[buf];
+      if (threadIdx.x == 0) {
+        // the next unit's record, copied while this one is rasterised (the
+        // buffer it lands in was last read before the previous unit's barrier)
+        const uint32_t k = j + 1 < end ? j + 1 : nxt;
+        if (k < nActive) {
+          const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&s_rec[buf ^ 1u]);
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(P.activeTileList + k) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+      }
+      raster_unit_cta<kWins>(P, S, rec);
+      if (threadIdx.x == 0) asm volatile("cp.async.wait_all;" ::: "memory");
+      __syncthreads();  // shared state is reused by the next unit; the next record has landed
+      buf ^= 1u;
+    }
+    if (threadIdx.x == 0) s_next = nxt;
+    __syncthreads();
+    i = s_next;
+  }
+}
+
 // Recomputes the per-warp-tile hiZ minimum of one view (after hiZ was written
 // from the host).  One warp per tile.
 __global__ void __launch_bounds__(128) k_tile_hiz(const uint16_t* hiz, uint16_t* tileHiz, uint32_t blocksX,
@@ -1786,18 +2089,31 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
     k_walk<<<P.tune.walkPerSm ? P.tune.walkPerSm * g_sms : g_walkBlocks, 256, 0, stream>>>(P);
   mark(4);
   if (doRaster && P.numTiles) {
-    k_tile_prep<<<(P.numTiles + 7) / 8, 256, 0, stream>>>(P);
-    const uint32_t R = P.tune.rasterRows ? P.tune.rasterRows : kDefaultRasterRows;
-    const uint32_t shape = R == 1 ? 0u : (R == 2 ? 1u : 2u);
-    const uint32_t units = P.numTiles * (kTileH / R);
-    const uint32_t grid = grid_of(P.tune.rasterPerSm, g_rasterPerSm[shape], (units + kRasterWarps - 1) / kRasterWarps);
-    const bool w = P.wins != nullptr;
-    if (R == 1) w ? k_raster<1, true><<<grid, kRasterThreads, 0, stream>>>(P)
-                  : k_raster<1, false><<<grid, kRasterThreads, 0, stream>>>(P);
-    else if (R == 4) w ? k_raster<4, true><<<grid, kRasterThreads, 0, stream>>>(P)
-                       : k_raster<4, false><<<grid, kRasterThreads, 0, stream>>>(P);
-    else w ? k_raster<2, true><<<grid, kRasterThreads, 0, stream>>>(P)
-           : k_raster<2, false><<<grid, kRasterThreads, 0, stream>>>(P);
+    // raster form: a warp per unit of R block rows, or a CTA per 8x2 unit when
+    // the launch has few units (a warp would leave most of the GPU idle and
+    // long lists in sequence)
+    FrameParams Q = P;
+    uint32_t threads = P.tune.rasterThreads;
+    if (!threads) threads = P.numTiles * 2u < 4u * g_sms * g_rasterPerSm[1] * kRasterWarps ? 128u : 32u;
+    Q.tune.rasterThreads = threads;
+    Q.tune.rasterRows = threads == 128u ? 2u : (P.tune.rasterRows ? P.tune.rasterRows : kDefaultRasterRows);
+    k_tile_prep<<<(Q.numTiles + 7) / 8, 256, 0, stream>>>(Q);
+    const uint32_t R = Q.tune.rasterRows;
+    const uint32_t units = Q.numTiles * (kTileH / R);
+    const bool w = Q.wins != nullptr;
+    if (threads == 128u) {
+      const uint32_t grid = grid_of(Q.tune.rasterPerSm, g_rasterCtaPerSm, units);
+      w ? k_raster_cta<true><<<grid, kCtaThreads, 0, stream>>>(Q) : k_raster_cta<false><<<grid, kCtaThreads, 0, stream>>>(Q);
+    } else {
+      const uint32_t shape = R == 1 ? 0u : (R == 2 ? 1u : 2u);
+      const uint32_t grid = grid_of(Q.tune.rasterPerSm, g_rasterPerSm[shape], (units + kRasterWarps - 1) / kRasterWarps);
+      if (R == 1) w ? k_raster<1, true><<<grid, kRasterThreads, 0, stream>>>(Q)
+                    : k_raster<1, false><<<grid, kRasterThreads, 0, stream>>>(Q);
+      else if (R == 4) w ? k_raster<4, true><<<grid, kRasterThreads, 0, stream>>>(Q)
+                         : k_raster<4, false><<<grid, kRasterThreads, 0, stream>>>(Q);
+      else w ? k_raster<2, true><<<grid, kRasterThreads, 0, stream>>>(Q)
+             : k_raster<2, false><<<grid, kRasterThreads, 0, stream>>>(Q);
+    }
     k_tile_min<<<(P.numTiles + 7) / 8, 256, 0, stream>>>(P);
   }
   mark(5);
@@ -1877,19 +2193,23 @@ cudaError_t set_kernel_attributes()
     g_rasterPerSm[1] = (uint32_t)nb;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster<4, true>, kRasterThreads, 0) == cudaSuccess && nb > 0)
     g_rasterPerSm[2] = (uint32_t)nb;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster_cta<true>, kCtaThreads, 0) == cudaSuccess && nb > 0)
+    g_rasterCtaPerSm = (uint32_t)nb;
   return cudaSuccess;
 }
 
 // Occupancy limits (resident CTAs per SM) of the persistent kernels -- setup,
-// list fill, raster at unit rows 1, 2 and 4 -- and the SM count.
-void tuning_limits(uint32_t out[6])
+// list fill, raster at unit rows 1, 2 and 4, the 128-thread raster form --
+// and the SM count.
+void tuning_limits(uint32_t out[7])
 {
   out[0] = g_setupPerSm;
   out[1] = g_fillPerSm;
   out[2] = g_rasterPerSm[0];
   out[3] = g_rasterPerSm[1];
   out[4] = g_rasterPerSm[2];
-  out[5] = g_sms;
+  out[5] = g_rasterCtaPerSm;
+  out[6] = g_sms;
 }
 
 // ---- cull labels ---------------------------------------------------------------------------

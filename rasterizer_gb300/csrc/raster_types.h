@@ -157,7 +157,8 @@ struct LaunchTuning {
   uint32_t setupPerSm, fillPerSm, walkPerSm, rasterPerSm, rasterChunk;
   uint32_t queryRounds;  // 0: chosen by slot count; else a k_query form (above)
   uint32_t rasterRows;   // block rows per raster unit: 1, 2 or 4 (0: kDefaultRasterRows)
-  uint32_t pad;
+  uint32_t rasterThreads;  // threads per raster unit: 32 (one warp) or 128 (a CTA, units of 2 rows);
+                           // 0: chosen by the launch's unit count
 };
 
 struct FrameParams {

@@ -132,17 +132,17 @@ def _boxes_view(ctx, w=640, h=360, queries=3000):
                      mins=mins, maxs=maxs)
 
 
-@pytest.mark.parametrize("rows", [1, 2, 4])
-def test_pixel_wins_match_oracle(ctx, rows):
+@pytest.mark.parametrize("rows,threads", [(1, 32), (2, 32), (4, 32), (2, 128)])
+def test_pixel_wins_match_oracle(ctx, rows, threads):
     """Wins (pixels whose final depth an occluder produced) == the oracle drawn
     occluder by occluder, each pixel owned by the last occluder that changed it.
     The oracle starts from zeroed depth, so a nonzero value written into a
     cleared block counts as a change, which is the GPU's rule for cleared
-    blocks.  Every raster unit shape (1, 2, 4 block rows per warp)."""
+    blocks.  Every raster form (1, 2, 4 block rows per warp; 2 rows per CTA)."""
     occ, view = _boxes_view(ctx)
     scene = to_baked(occ)
     b = api.PreparedBatch(ctx, [view])
-    b.setTuning({"raster_unit_rows": rows})
+    b.setTuning({"raster_unit_rows": rows, "raster_threads_per_unit": threads})
     b.setSelection(None, trackWins=True)
     b.launch()
     assert b.check()
