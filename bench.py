@@ -924,9 +924,10 @@ def run_profile_frames(frames: int, start: int = 0):
 
 def run_profile_learned(frames: int, views: int, train_steps: int, extras: bool = False):
     """A short GPU-only run for profilers: the headline's batched + learned
-    launch (first `views` street views, untrained selector at K = 10 %, the
-    same kernels and the same number of drawn occluders per view), `frames`
-    graph launches, then `train_steps` listwise training steps on random rows.
+    launch (first `views` street views, untrained selector at K = 5 % in the
+    zero-depth clear: the same kernels and the same number of drawn occluders
+    per view), `frames` graph launches, then `train_steps` listwise training
+    steps on random rows.
     With `extras`, the first launch also runs the second pass and the cull
     labels (every kernel of the library then runs at least once)."""
     from rasterizer_gb300 import api, learned as L, scenes
@@ -938,7 +939,8 @@ def run_profile_learned(frames: int, views: int, train_steps: int, extras: bool 
     paths = L.street_tracks(views, 64, seed0=7000, n_occluders=len(occ), queries=NQ)
     vs = L._views(ctx, occ, paths, pmin, pmax)
     b = api.PreparedBatch(ctx, vs)
-    b.setSelection(net, 0.1, trackWins=True)
+    b.setSelection(net, 0.05, trackWins=True)
+    b.setZeroDepth(True)
     if extras:
         b.setSecondPass(True)
         b.setCullLabels(True)
