@@ -299,6 +299,17 @@ int occ_quad_decompose(const uint32_t* indices, uint32_t nIndices, const float* 
  * batched quad indices (n entries), offsets numBatches+1 entries (room for n+1). */
 int occ_sah_generate_batches(const float* aabbs, uint32_t n, uint32_t targetSize, uint32_t splitGranularity,
                              uint32_t* flat, uint32_t* offsets, uint32_t* numBatches);
+/* SurfaceAreaHeuristic::generateBatches (SurfaceAreaHeuristic.cpp:96-104) on
+ * the GPU, the same batches as occ_sah_generate_batches: aabbs and flat are
+ * device pointers (n x (min4, max4) floats; n indices), offsets and
+ * numBatches host memory (room for n+1 offsets).  Runs on the context's
+ * stream and returns when the batches are known.  Boxes with a NaN centre
+ * coordinate (min + max) give OCC_ERR_UNSUPPORTED: the reference's order for
+ * them comes from its library's merge sort under a comparison that is no
+ * strict order; the host form handles them. */
+int occ_sah_generate_batches_device(occ_ctx ctx, const float* aabbs, uint32_t n, uint32_t targetSize,
+                                    uint32_t splitGranularity, uint32_t* flat, uint32_t* offsets,
+                                    uint32_t* numBatches);
 /* Occluder::bake: vertices nVertices float4 (quads of 4, a multiple of 32: whole
  * packets of 8 quads; the reference asserts 16 but reads 32 at a time);
  * packedOut nVertices words; returns the packet count (32-byte vectors). */

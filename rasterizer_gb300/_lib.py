@@ -90,6 +90,7 @@ SIGNATURES = {
     "occ_mlp_train_step_listwise": (I32, [P, U32, P, P, U32, P, C.c_float, C.POINTER(C.c_float)]),
     "occ_quad_decompose": (I32, [P, U32, P, U32, P, C.POINTER(U32)]),
     "occ_sah_generate_batches": (I32, [P, U32, U32, U32, P, P, C.POINTER(U32)]),
+    "occ_sah_generate_batches_device": (I32, [P, P, U32, U32, U32, P, P, C.POINTER(U32)]),
     "occ_occluder_bake": (I32, [P, U32, P, P, P, C.POINTER(U32), P, P, P]),
     "occ_occluders_bake_device": (I32, [P, U32, P, P, P, P, P]),
     "occ_scene_bake": (I32, [P, U32, P, U32, U32, U32, U32, C.c_uint64, C.POINTER(U32), C.POINTER(C.c_uint64), P, P, P]),

@@ -159,6 +159,34 @@ class SurfaceAreaHeuristic:
                                              C.byref(nb)), "occ_sah_generate_batches")
         return [flat[offs[i]:offs[i + 1]].copy() for i in range(nb.value)]
 
+    @staticmethod
+    def generateBatchesDevice(ctx: "Context", aabbs, targetSize: int, splitGranularity: int,
+                              timed: list | None = None) -> list[np.ndarray]:
+        """The same batches computed on the GPU (occ_sah_generate_batches_device).
+        aabbs: (n, 8) float32 on the host (copied to the device first) or a
+        device tensor.  With `timed` (a list), appends the call's seconds
+        (inputs already on the device)."""
+        import time
+        import torch
+        dev = torch.device("cuda", ctx.device)
+        if isinstance(aabbs, torch.Tensor):
+            d = aabbs.to(dev, torch.float32).contiguous()
+        else:
+            d = torch.from_numpy(_f32(aabbs).reshape(-1, 8)).to(dev)
+        n = d.shape[0]
+        flat = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+        offs = np.zeros(n + 2, np.uint32)
+        nb = C.c_uint32()
+        torch.cuda.synchronize(dev)  # the upload ran on torch's stream
+        t0 = time.perf_counter()
+        check(lib().occ_sah_generate_batches_device(ctx.handle, d.data_ptr(), n, targetSize, splitGranularity,
+                                                    flat.data_ptr(), _ptr(offs), C.byref(nb)),
+              "occ_sah_generate_batches_device")
+        if timed is not None:
+            timed.append(time.perf_counter() - t0)
+        f = flat.cpu().numpy().view(np.uint32)
+        return [f[offs[i]:offs[i + 1]].copy() for i in range(nb.value)]
+
 
 def scene_batches(vertices, indices, targetSize: int = 512, splitGranularity: int = 8):
     """The demo's scene preparation up to the bake (Main.cpp:86-128): quads,

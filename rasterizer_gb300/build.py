@@ -23,7 +23,7 @@ NVCC_FLAGS = ARCH + ["-O3", "--fmad=false", "-ftz=false", "-prec-div=true", "-pr
 CXX_FLAGS = ["-O2", "-fPIC", "-pthread", "-ffp-contract=off", "-fno-fast-math", "-std=c++17", "-I" + CSRC,
              "-I" + INCLUDE]
 
-CU_SOURCES = ["kernels.cu", "learned.cu", "capi.cu", "bake_gpu.cu"]
+CU_SOURCES = ["kernels.cu", "learned.cu", "capi.cu", "bake_gpu.cu", "sah_gpu.cu"]
 CXX_SOURCES = ["bake.cpp", "files.cpp"]
 
 

@@ -15,6 +15,7 @@
 #include "coverage_table.h"
 #include "coverage_table_build.h"
 #include "raster_types.h"
+#include "sah_scratch.h"
 #include "x86_emu.cuh"
 
 namespace occ {
@@ -48,6 +49,8 @@ cudaError_t launch_query2d(const ViewDesc* view, uint32_t minX, uint32_t maxX, u
 int set_error(int code, const char* msg);
 cudaError_t launch_bake(const BakeJob* jobs, uint32_t count, const float4* vertices, float4* normals,
                         uint32_t* cluster, uint32_t* order, uint32_t* packed, float* bounds, cudaStream_t stream);
+int sah_generate_device(SahScratch& S, uint32_t n, const float* aabbs, uint32_t target, uint32_t gran,
+                        uint32_t* flat, std::vector<uint32_t>& offsets, cudaStream_t st, std::string& err);
 }  // namespace occ
 
 using namespace occ;
@@ -190,6 +193,7 @@ struct occ_ctx_s {
   DevBuf<BakeJob> bakeJobs;
   DevBuf<float4> bakeNormals;
   DevBuf<uint32_t> bakeCluster, bakeOrder;
+  DevBuf<uint8_t> sah;  // GPU SAH batching scratch (sah_gpu.cu), grown on demand
 };
 
 struct occ_raster_s {
@@ -635,6 +639,70 @@ int occ_occluders_bake_device(occ_ctx ctx, uint32_t count, const float* vertices
   OCC_CUDA(cudaMemcpyAsync(ctx->bakeJobs.p, jobs.data(), count * sizeof(BakeJob), cudaMemcpyHostToDevice, ctx->stream));
   OCC_CUDA(launch_bake(ctx->bakeJobs.p, count, reinterpret_cast<const float4*>(vertices), ctx->bakeNormals.p,
                        ctx->bakeCluster.p, ctx->bakeOrder.p, packed, bounds, ctx->stream));
+  return OCC_OK;
+}
+
+int occ_sah_generate_batches_device(occ_ctx ctx, const float* aabbs, uint32_t n, uint32_t targetSize,
+                                    uint32_t splitGranularity, uint32_t* flat, uint32_t* offsets,
+                                    uint32_t* numBatches)
+{
+  if (!ctx || !offsets || !numBatches || !splitGranularity || (n && (!aabbs || !flat)))
+    return fail(OCC_ERR_INVALID_ARG, "null argument");
+  if (n >= (1u << 30)) return fail(OCC_ERR_INVALID_ARG, "at most 2^30 - 1 boxes");
+  if (reinterpret_cast<uintptr_t>(aabbs) % 16 != 0)
+    return fail(OCC_ERR_INVALID_ARG, "aabbs must be 16-byte aligned (rows of two float4)");
+  if (n <= 2 * splitGranularity) {  // as occ_sah_generate_batches: one batch
+    std::vector<uint32_t> iota(n);
+    for (uint32_t i = 0; i < n; ++i) iota[i] = i;
+    if (n) OCC_CUDA(cudaMemcpyAsync(flat, iota.data(), (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    OCC_CUDA(cudaStreamSynchronize(ctx->stream));
+    offsets[0] = 0;
+    offsets[1] = n;
+    *numBatches = n ? 1 : 0;
+    return OCC_OK;
+  }
+  // carve the scratch (256-byte aligned pieces)
+  const size_t tiles = (n + 2047) / 2048;
+  const size_t sizes[] = {16 * (size_t)n, 16 * (size_t)n, 12 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n,
+                          8 * (size_t)n, 8 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n,
+                          4 * 256 * tiles, 4 * ((size_t)n + 1), (size_t)n, 8 * (size_t)n, 16 * tiles,
+                          16 * tiles, 4};
+  size_t total = 0;
+  for (size_t z : sizes) total += align_up(z, 256);
+  OCC_CHECK(ctx->sah.reserve(total));
+  uint8_t* p = ctx->sah.p;
+  void* piece[17];
+  for (int k = 0; k < 17; ++k) {
+    piece[k] = p;
+    p += align_up(sizes[k], 256);
+  }
+  SahScratch S;
+  S.lo = static_cast<float4*>(piece[0]);
+  S.hi = static_cast<float4*>(piece[1]);
+  S.mk = static_cast<uint32_t*>(piece[2]);
+  S.idx[0] = static_cast<uint32_t*>(piece[3]);
+  S.idx[1] = static_cast<uint32_t*>(piece[4]);
+  S.key[0] = static_cast<unsigned long long*>(piece[5]);
+  S.key[1] = static_cast<unsigned long long*>(piece[6]);
+  S.rng = static_cast<uint32_t*>(piece[7]);
+  S.left = static_cast<float*>(piece[8]);
+  S.right = static_cast<float*>(piece[9]);
+  S.hist = static_cast<uint32_t*>(piece[10]);
+  S.starts = static_cast<uint32_t*>(piece[11]);
+  S.rangeAxis = static_cast<int8_t*>(piece[12]);
+  S.best = static_cast<unsigned long long*>(piece[13]);
+  S.aggLo = static_cast<float4*>(piece[14]);
+  S.aggHi = static_cast<float4*>(piece[15]);
+  S.flag = static_cast<uint32_t*>(piece[16]);
+  std::vector<uint32_t> offs;
+  std::string err;
+  const int st = sah_generate_device(S, n, aabbs, targetSize, splitGranularity, flat, offs, ctx->stream, err);
+  if (st < 0) return fail(OCC_ERR_CUDA, "occ_sah_generate_batches_device: " + err);
+  if (st > 0)
+    return fail(OCC_ERR_UNSUPPORTED, "a box centre is NaN: the reference's order for it comes from its library's "
+                                     "merge sort; use occ_sah_generate_batches");
+  std::copy(offs.begin(), offs.end(), offsets);
+  *numBatches = (uint32_t)offs.size() - 1;
   return OCC_OK;
 }
 

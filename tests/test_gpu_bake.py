@@ -137,3 +137,74 @@ def test_query_batch_device(ctx):
     vb = dvb.cpu().numpy().view(np.uint32)
     nb = dnb.cpu().numpy().view(np.uint32)
     assert np.array_equal(api.unpack_bits(vb, len(mins)), hv) and np.array_equal(api.unpack_bits(nb, len(mins)), hn)
+
+
+# ---- SAH batching on the GPU ---------------------------------------------------------
+
+def _scene_quad_boxes(mesh):
+    """The per-quad boxes the scene preparation hands to SAH (Main.cpp:86-128)."""
+    v = np.ascontiguousarray(mesh.vertices, np.float32).reshape(-1, 4)
+    q = api.QuadDecomposition.decompose(mesh.indices, v)
+    pad = (-q.size) % 32
+    if pad:
+        q = np.concatenate([q, np.full(pad, q[0], np.uint32)])
+    return api._quad_boxes(v[q.reshape(-1, 4)])
+
+
+def _tied_boxes(n, seed, snap):
+    """Boxes with many equal centres and centres of -0 and +0 (equal under `<`)."""
+    rng = np.random.default_rng(seed)
+    lo = rng.uniform(-50, 50, (n, 4)).astype(np.float32)
+    if snap:
+        lo = np.round(lo / snap) * snap
+    lo[:, 3] = 1.0
+    hi = (lo + np.round(rng.uniform(0, 3, (n, 4)))).astype(np.float32)
+    hi[:, 3] = 1.0
+    z = rng.integers(0, n, n // 10)
+    lo[z[::2], 0], hi[z[::2], 0] = np.float32(-0.0), np.float32(-0.0)
+    lo[z[1::2], 0], hi[z[1::2], 0] = np.float32(0.0), np.float32(0.0)
+    return np.ascontiguousarray(np.concatenate([lo, hi], axis=1), np.float32)
+
+
+def _same_batches(a, b):
+    return len(a) == len(b) and all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+@pytest.mark.parametrize("case", ["boxes", "city", "tied8", "tied0", "tied25", "small-target"])
+def test_gpu_sah_equals_host(ctx, case):
+    """SurfaceAreaHeuristic::generateBatches on the GPU (level by level: stable
+    radix sorts, segmented area scans, first cheapest split by atomicMin)
+    gives the host's batches byte for byte, the host being pinned to the
+    reference (Castle and Sponza on x86, tied and signed-zero centres)."""
+    target, gran = 512, 8
+    if case == "boxes":
+        boxes = _scene_quad_boxes(scenes.boxes_scene())
+    elif case == "city":
+        boxes = _scene_quad_boxes(scenes.city_scene())
+    elif case == "small-target":
+        boxes, target, gran = _tied_boxes(4000, 7, 4.0), 40, 4
+    else:
+        snap = {"tied8": 8.0, "tied0": 0.0, "tied25": 25.0}[case]
+        boxes = _tied_boxes(6000, 1 + len(case), snap)
+    host = api.SurfaceAreaHeuristic.generateBatches(boxes, target, gran)
+    dev = api.SurfaceAreaHeuristic.generateBatchesDevice(ctx, boxes, target, gran)
+    assert len(host) > 1
+    assert _same_batches(dev, host)
+
+
+def test_gpu_sah_large_city_and_edges(ctx):
+    """The 2M-triangle city's million quads; inputs of at most two granules
+    (one batch); a NaN centre is refused (the host form handles it)."""
+    boxes = _scene_quad_boxes(scenes.city_scene(grid=128, target_tris=2_000_000))
+    t = []
+    dev = api.SurfaceAreaHeuristic.generateBatchesDevice(ctx, boxes, 512, 8, timed=t)
+    host = api.SurfaceAreaHeuristic.generateBatches(boxes, 512, 8)
+    assert len(host) > 1000 and _same_batches(dev, host)
+    small = _tied_boxes(16, 3, 0.0)
+    assert _same_batches(api.SurfaceAreaHeuristic.generateBatchesDevice(ctx, small, 512, 8),
+                         api.SurfaceAreaHeuristic.generateBatches(small, 512, 8))
+    bad = _tied_boxes(100, 4, 0.0)
+    bad[5, 1] = np.nan
+    with pytest.raises(api.OccError) as e:
+        api.SurfaceAreaHeuristic.generateBatchesDevice(ctx, bad, 8, 2)
+    assert e.value.status == -5
