@@ -1,33 +1,39 @@
 """Benchmark: views/s of the batched + learned path on one GB300, next to the
 plain path and the reference's CPU algorithm.
 
-Scene: a seeded 64x64 grid of extruded buildings, 259,534 triangles baked by
-the library into 386 occluders (129,768 quads); 100,000 query boxes
-(lognormal extents) per view.
+Scene: a seeded 64x64 grid of extruded buildings, 259,534 triangles baked
+into 386 occluders (129,768 quads); 100,000 query boxes (lognormal extents)
+per view.
 
   value    (headline) batched + learned: 64 street-level 1920x1080 views
            (seeded camera paths, each view moving every step) per graph
            launch; each view draws the selector's top K of its candidate
            occluders (K = the smallest fraction keeping >= 99% of the
-           occlusion culls on held-out validation views) and answers its
-           queries.  Device time per launch (CUDA events on the library's
-           stream); the selector is trained first, on the GPU, outside the
-           timed region.  Culls kept vs the full frames and false culls are
-           measured on held-out test paths and reported in `config`;
+           occlusion culls on held-out validation views) in the zero-depth
+           clear and answers its queries.  Device time per launch (CUDA
+           events on the library's stream); the selector is trained first,
+           on the GPU, outside the timed region.  `culls`: culls kept and
+           false culls of the timed launches themselves against full frames
+           at the same poses (and on held-out paths);
   e2e      the same launches through the public API with host data: 64
            matrices from the host, launch, every view's result bits back;
+           e2e_dynamic_boxes: plus every view's boxes from the host each step;
   plain_single_view  the plain all-occluder loop, one 1080p view per launch
            along a 300-frame path (L2 flushed between frames), with its
            per-kernel times, roofline and end-to-end figure;
   batched  the 256-view mixed-resolution workload, one launch vs one launch per view;
-  learned  training report, K sweep against the nearest-first ordering, and
-           the 256-view workload with learned selection;
+  learned  training report, K sweep against the nearest-first ordering, the
+           256-view workload with learned selection, and the large workload
+           (2M-triangle city, 4K + 63 views) with its bake timings (host and
+           GPU SAH, GPU Occluder::bake, baked-file load);
   cpu_baseline  the CPU oracle (portable restatement of the reference) on
-           one host core, plain loop, on a bounded sample of the headline's views.
+           one host core, the reference's own frame loop (Main.cpp:181-206)
+           on its own bake, on a bounded sample of the headline's views.
 
---impl reference times the reference's CPU algorithm (the oracle port: the
-reference's AVX2 build cannot run on the Arm host) with all host cores on the
-headline's views, plain all-occluder loop (the reference has no learned selection).
+--impl reference times the same loop with all host cores on the headline's
+views (the oracle port: the reference's AVX2 build cannot run on the Arm
+host; the reference has no learned selection).  --cpu-compare (x86 with the
+reference's sources) times the AVX2 build against the oracle on one core.
 """
 from __future__ import annotations
 
@@ -648,8 +654,29 @@ def run_large(ctx, net, dev):
     from rasterizer_gb300 import api, learned as L, scenes
     t = L.Timer()
     mesh = scenes.city_scene(grid=128, target_tris=2_000_000)
-    sets, ref_lo, ref_hi = api.scene_batches(mesh.vertices, mesh.indices)  # quads and SAH batches (host)
-    prep_s = t.lap()
+    t.lap()
+    # the scene preparation of api.scene_batches step by step: quads, per-quad
+    # boxes, SAH batches (host), and the same batches on the GPU
+    v = np.ascontiguousarray(mesh.vertices, np.float32).reshape(-1, 4)
+    q = api.QuadDecomposition.decompose(mesh.indices, v)
+    decompose_s = t.lap()
+    pad = (-q.size) % 32
+    if pad:
+        q = np.concatenate([q, np.full(pad, q[0], np.uint32)])
+    corners = v[q.reshape(-1, 4)]
+    qboxes = api._quad_boxes(corners)
+    t.lap()
+    batches = api.SurfaceAreaHeuristic.generateBatches(qboxes, 512, 8)
+    sah_host_s = t.lap()
+    sah_gpu_times = []
+    for _ in range(3):
+        gb = api.SurfaceAreaHeuristic.generateBatchesDevice(ctx, qboxes, 512, 8, timed=sah_gpu_times)
+    sah_same = len(gb) == len(batches) and all(np.array_equal(a, b) for a, b in zip(gb, batches))
+    del gb
+    ref_lo, ref_hi = api._box_of(v)
+    sets = [np.ascontiguousarray(corners[b].reshape(-1, 4)) for b in batches]
+    prep_s = decompose_s + sah_host_s
+    t.lap()
     occ = [api.Occluder.bake(s, ref_lo, ref_hi) for s in sets]              # Occluder::bake per batch (host)
     host_bake_s = t.lap()
     native = api.bake_scene(mesh.vertices, mesh.indices)                    # the same in one native call
@@ -718,7 +745,11 @@ def run_large(ctx, net, dev):
                         f"occluders), one 3840x2160 main view + 63 mixed views per launch, {nq} query boxes "
                         f"per launch ({LARGE_NQ} pool)",
             "bake_seconds": bake_s,
-            "bake_steps_seconds": {"decompose_and_sah": prep_s, "occluder_bake_host": host_bake_s},
+            "bake_steps_seconds": {"decompose": decompose_s, "sah_host": sah_host_s,
+                                   "occluder_bake_host": host_bake_s},
+            "gpu_sah": {"quads": int(len(qboxes)), "batches": len(batches), "seconds": min(sah_gpu_times),
+                        "identical_to_host": bool(sah_same), "host_seconds": sah_host_s,
+                        "note": "occ_sah_generate_batches_device, boxes already on the device, best of 3"},
             "scene_bake_one_call": {"seconds": native_s, "identical": bool(native_same)},
             "gpu_bake": gpu_bake,
             "baked_file": {"load_seconds": load_s, "bytes": file_bytes, "identical": bool(same),
