@@ -36,7 +36,9 @@ constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kHidden * kFeatures, kOffW2 = kOffB1
 // 11 feature 8 rescaled to [0, 1] over the view's candidates (0 = nearest)   (k_view_norm)
 // 12 rect pixels / the largest rect of the view's candidates                 (k_view_norm)
 // 13 log2(1 + previous-launch wins) / log2(1 + W*H)
-// 14 drawn in the previous launch   15 bias 1
+// 14 drawn in the previous launch
+// 15 rank in the view's nearest-first order over its candidates, 0 = nearest,
+//    1 = farthest (non-candidates 1)                                        (k_view_norm)
 // Features 13-14 need win counting; without it they are 0.
 
 // Eye position of a view: clip x = clip y = clip w = 0 (rows hold the
@@ -109,14 +111,22 @@ __global__ void __launch_bounds__(256) k_features(FrameParams P, uint32_t numCmd
   f[12] = 0.0f;
   f[13] = log2f(1.0f + (float)prev) / lwh;
   f[14] = (P.cmdDraw[c] & 5u) ? 1.0f : 0.0f;  // drawn by either pass of the previous launch (k_gate)
-  f[15] = 1.0f;
+  f[15] = 1.0f;  // k_view_norm: rank in the view's nearest-first order
   P.cand[c] = cand ? 1 : 0;
 }
 
-// Features 11 and 12 of view v from its candidates (a CTA of 256 threads).
+constexpr uint32_t kRankMaxCmds = 2048;  // views ranked exactly (larger: the normalised distance)
+
+// Features 11, 12 and 15 of view v from its candidates (a CTA of 256
+// threads): distance rescaled over the candidates, area relative to the
+// largest, and the rank in the reference's nearest-first order (Main.cpp:
+// 184-190: centre distance to the eye, equal distances in command order)
+// over the candidates, 0 = nearest, 1 = farthest.
 __device__ __forceinline__ void view_norm(const FrameParams& P, uint32_t v)
 {
   __shared__ float s_red[3][8];
+  __shared__ float s_dist[kRankMaxCmds];  // the view's candidates' distances (non-candidates: +inf)
+  __shared__ uint32_t s_ncand;
   const ViewDesc& V = P.views[v];
   const uint32_t c0 = V.cmdStart, n = V.cmdCount;
   float dmin = 3.0e38f, dmax = -3.0e38f, amax = 0.0f;
@@ -145,19 +155,40 @@ __device__ __forceinline__ void view_norm(const FrameParams& P, uint32_t v)
     amax = fmaxf(amax, s_red[2][k]);
   }
   const float span = dmax - dmin;
+  const bool exact = n <= kRankMaxCmds;
+  if (threadIdx.x == 0) s_ncand = 0;
+  __syncthreads();
+  uint32_t nc = 0;
+  for (uint32_t i = threadIdx.x; i < n; i += 256) {
+    const bool cand = P.cand[c0 + i] != 0;
+    nc += cand ? 1u : 0u;
+    if (exact) s_dist[i] = cand ? P.feat[(size_t)(c0 + i) * kFeatures + 8] : __int_as_float(0x7F800000);
+  }
+  atomicAdd(&s_ncand, nc);
+  __syncthreads();
+  const float rankScale = s_ncand > 1 ? 1.0f / (float)(s_ncand - 1) : 0.0f;
   for (uint32_t i = threadIdx.x; i < n; i += 256) {
     float* f = P.feat + (size_t)(c0 + i) * kFeatures;
     if (P.cand[c0 + i]) {
       f[11] = span > 0.0f ? (f[8] - dmin) / span : 0.0f;
       f[12] = amax > 0.0f ? f[3] / amax : 0.0f;
+      if (exact) {
+        const float d = s_dist[i];
+        uint32_t rank = 0;
+        for (uint32_t j = 0; j < n; ++j) rank += (s_dist[j] < d || (s_dist[j] == d && j < i)) ? 1u : 0u;
+        f[15] = (float)rank * rankScale;
+      } else {
+        f[15] = f[11];
+      }
     } else {
       f[11] = 1.0f;
       f[12] = 0.0f;
+      f[15] = 1.0f;
     }
   }
 }
 
-// One CTA per view: features 11 and 12 (win counting without a selector).
+// One CTA per view: features 11, 12 and 15 (win counting without a selector).
 __global__ void __launch_bounds__(256) k_view_norm(FrameParams P) { view_norm(P, blockIdx.x); }
 
 // ---- MLP forward: mma.sync m16n8k16, bf16 x bf16 -> fp32 ------------------------------------

@@ -248,7 +248,8 @@ def test_top_k_subset_matches_oracle(ctx, fraction):
 def test_trained_selector_gains_over_nearest_first(ctx, tmp_path):
     """A selector trained on the GPU (small recipe) against the reference's
     nearest-first ordering truncated at the same K, on held-out views of the
-    256-view workload: more occlusion culls kept, none false, and the
+    256-view workload (K = 35 %) and on held-out street-level 1080p paths at
+    the headline's K = 5 %: more occlusion culls kept, none false, and the
     checkpoint round trip reproduces its scores."""
     from rasterizer_gb300 import learned as L
     occ = city_occluders()
@@ -268,6 +269,13 @@ def test_trained_selector_gains_over_nearest_first(ctx, tmp_path):
     assert a.full > 100_000
     assert a.retained > b.retained
     assert a.quads_drawn < 0.6 * a.quads_candidates
+    street = L.street_tracks(4, 20, seed0=5000, n_occluders=len(occ), queries=len(mins))
+    sfull = L.run_full(ctx, occ, street, mins, maxs)
+    a = L.evaluate_learned(ctx, occ, street, mins, maxs, net, 0.05, sfull)
+    b = L.evaluate_heuristic(ctx, occ, street, mins, maxs, "nearest", 0.05, sfull)
+    print("street K=5%: learned", a.as_dict(), "nearest", b.as_dict())
+    assert a.false == 0 and a.full > 100_000
+    assert a.retained > b.retained
     # checkpoint: weights and Adam state survive a save/load into a fresh network
     x = _random_features(300, 31)
     path = tmp_path / "selector.npz"
