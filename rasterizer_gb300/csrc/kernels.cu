@@ -129,10 +129,17 @@ __device__ __forceinline__ uint32_t avg_u16x2(uint32_t a, uint32_t b)
   return (a | b) - (((a ^ b) >> 1) & 0x7FFF7FFFu);
 }
 
-// packDepthPremultiplied of two lanes: lo -> bits 0..15, hi -> bits 16..31.
+// packDepthPremultiplied of two lanes (Rasterizer.cpp:508-525): each float's
+// bits shifted right by 12 (arithmetic), saturated to [0, 65535] as
+// _mm256_packus_epi32 does; lo -> bits 0..15, hi -> bits 16..31.  One
+// saturating pack instruction: its first source fills the upper half.
 __device__ __forceinline__ uint32_t pack2(float lo, float hi)
 {
-  return x86::pack_depth(lo) | (x86::pack_depth(hi) << 16);
+  uint32_t d;
+  asm("cvt.pack.sat.u16.s32 %0, %1, %2;"
+      : "=r"(d)
+      : "r"((int32_t)__float_as_uint(hi) >> 12), "r"((int32_t)__float_as_uint(lo) >> 12));
+  return d;
 }
 
 template <int NT>
@@ -932,10 +939,10 @@ template <int R>
 constexpr int kRasterMinBlocks = R == 4 ? 4 : 6;
 constexpr int kRasterThreads = 32 * kRasterWarps;
 constexpr int kWarpListCap = 64;                   // listed quads buffered per warp
-constexpr int kFragStride = 33;                    // words per fragment slot (odd: conflict-free banks)
+constexpr int kFragStride = 36;                    // words per fragment slot: rows move as 16-byte words
 
 struct WarpRasterSmem {
-  uint32_t frag[32 * kFragStride];  // one fragment slot per lane: 8 rows x 4 packed words
+  __align__(16) uint32_t frag[32 * kFragStride];  // one fragment slot per lane: 8 rows x 4 packed words
   uint32_t meta[32];                // per slot: maxZ << 16 | target block
   uint32_t fcmd[32];                // per slot: command within the view + 1 (win counting)
   uint32_t bmask[32];               // per block: slots aimed at it
@@ -958,10 +965,7 @@ __device__ __forceinline__ void put_row(uint32_t* dst, int y, uint64_t mask, uin
     w2 &= __byte_perm(hi, 0, 0x1100);
     w3 &= __byte_perm(hi, 0, 0x3322);
   }
-  dst[4 * y + 0] = w0;
-  dst[4 * y + 1] = w1;
-  dst[4 * y + 2] = w2;
-  dst[4 * y + 3] = w3;
+  *reinterpret_cast<uint4*>(dst + 4 * y) = make_uint4(w0, w1, w2, w3);
 }
 
 // Fragment of quad Q at block (bx, by): packed depth rows with the coverage
@@ -1093,17 +1097,20 @@ __device__ __forceinline__ void merge_slot(const ViewDesc& V, const WarpRasterSm
 {
   const uint32_t mz = S.meta[slot] >> 16;
   if (hiz >= mz) return;  // the reference's hiZ test (Rasterizer.cpp:1148-1152)
-  const uint32_t* src = S.frag + slot * kFragStride + 4 * row0;
+  const uint4* src = reinterpret_cast<const uint4*>(S.frag + slot * kFragStride + 4 * row0);
   const uint32_t c1 = kWins ? S.fcmd[slot] : 0u;
   if (hiz == 1) {
 #pragma unroll
-    for (int r = 0; r < RPL; ++r)
+    for (int r = 0; r < RPL; ++r) {
+      const uint4 q = src[r];
+      const uint32_t wr[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const uint32_t w = src[4 * r + i];
+        const uint32_t w = wr[i];
         if (kWins) own[r][i] = ((w & 0xFFFFu) ? c1 : 0u) | ((w >> 16) ? (c1 << 16) : 0u);
         row[r][i] = w;
       }
+    }
   } else {
     if (!have) {
       const uint4* d = reinterpret_cast<const uint4*>(V.depth + (size_t)blk * 64 + 8 * row0);
@@ -1114,16 +1121,19 @@ __device__ __forceinline__ void merge_slot(const ViewDesc& V, const WarpRasterSm
       }
     }
 #pragma unroll
-    for (int r = 0; r < RPL; ++r)
+    for (int r = 0; r < RPL; ++r) {
+      const uint4 q = src[r];
+      const uint32_t wr[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const uint32_t w = src[4 * r + i];
+        const uint32_t w = wr[i];
         if (kWins) {
           if ((w & 0xFFFFu) > (row[r][i] & 0xFFFFu)) own[r][i] = (own[r][i] & 0xFFFF0000u) | c1;
           if ((w >> 16) > (row[r][i] >> 16)) own[r][i] = (own[r][i] & 0xFFFFu) | (c1 << 16);
         }
         row[r][i] = vmax_u16x2(row[r][i], w);
       }
+    }
   }
   have = true;
   uint32_t mn = 0xFFFFFFFFu;
@@ -1514,7 +1524,7 @@ struct CtaRasterSmem {
   uint32_t lq[kCtaListCap];      // quad index
   uint32_t lrect[kCtaListCap];   // quad rect within the unit: x0 | y0 << 3 | w << 5 | h << 9
   uint32_t loff[kCtaListCap];    // first fragment of each listed quad
-  uint32_t frag[kCtaThreads * kFragStride];
+  __align__(16) uint32_t frag[kCtaThreads * kFragStride];
   uint32_t meta[kCtaThreads];    // per fragment slot: maxZ << 16 | target block
   uint32_t fcmd[kCtaThreads];    // per fragment slot: command (win counting only)
   uint32_t bmask[kCtaUnitBlocks][kCtaMaskWords];  // per block: fragment slots aimed at it
@@ -1533,7 +1543,8 @@ __device__ __forceinline__ void merge_slot_row(const ViewDesc& V, const CtaRaste
 {
   const uint32_t mz = S.meta[slot] >> 16;
   if (hiz >= mz) return;  // the reference's hiZ test (Rasterizer.cpp:1148-1152)
-  const uint32_t* src = S.frag + slot * kFragStride + 4 * py;
+  const uint4 q = *reinterpret_cast<const uint4*>(S.frag + slot * kFragStride + 4 * py);
+  const uint32_t src[4] = {q.x, q.y, q.z, q.w};
   const uint32_t c1 = kWins ? S.fcmd[slot] + 1 : 0u;
   if (hiz == 1) {
 #pragma unroll
