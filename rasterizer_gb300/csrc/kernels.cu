@@ -587,8 +587,9 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
   __shared__ CmdConst s_cc[kMaxCmdPerChunk];
   __shared__ uint32_t s_cmdStart[kMaxCmdPerChunk];
   __shared__ uint32_t s_scan[kChunk / 32];
+  __shared__ __align__(16) uint32_t s_words[kChunk * 4];  // the chunk's packed words (Occluder.cpp:153-156 layout)
 
-  const uint32_t tid = threadIdx.x;
+  const uint32_t tid = threadIdx.x, lane = tid & 31;
   const uint32_t nActive = P.header->activeChunks;
   for (uint32_t ai = blockIdx.x; ai < nActive; ai += gridDim.x) {
     const uint32_t c = P.activeChunkList[ai];
@@ -606,6 +607,23 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
     }
     __syncthreads();
 
+    // the chunk's packed words into shared memory, one coalesced 16-byte load
+    // per thread: thread t loads vector t % 8 of the chunk's 8-quad group t / 8
+    // (a group's 32 words are corner-major: word 8j + i is corner j of quad i)
+    {
+      const uint32_t g0 = (c << kChunkShift) + 8 * (tid >> 3);  // first quad of the group
+      if (8 * (tid >> 3) < ch.quadCount) {
+        uint32_t k = 0;
+        for (uint32_t i = 1; i < ch.cmdCount; ++i)
+          if (s_cmdStart[i] <= g0) k = i;
+        if (s_cc[k].draw) {
+          const Cmd& cmd = P.cmds[ch.cmdFirst + k];
+          const uint4* src = reinterpret_cast<const uint4*>(P.pool + cmd.wordOffset + (g0 - cmd.quadStart) * 4);
+          reinterpret_cast<uint4*>(s_words)[tid] = __ldg(src + (tid & 7));
+        }
+      }
+    }
+    __syncthreads();
     const uint32_t q = (c << kChunkShift) + tid;
     QuadRaster R;
     QuadWalk Wk;
@@ -615,13 +633,9 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
       for (uint32_t i = 1; i < ch.cmdCount; ++i)
         if (s_cmdStart[i] <= q) k = i;
       if (s_cc[k].draw) {
-        const Cmd& cmd = P.cmds[ch.cmdFirst + k];
-        const uint32_t local = q - cmd.quadStart;     // quad within the occluder
-        const uint32_t group = local >> 3, lane = local & 7;
-        const uint32_t* base = P.pool + cmd.wordOffset + group * 32;
         uint32_t w4[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) w4[j] = __ldg(base + 8 * j + lane);
+        for (int j = 0; j < 4; ++j) w4[j] = s_words[(tid >> 3) * 32 + 8 * j + (tid & 7)];
         valid = quad_setup(V, w4, s_cc[k], R, Wk);
         Wk.pad[0] = ch.cmdFirst + k;  // command of this quad (win counts)
       }
@@ -641,11 +655,22 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
     Wk.rowLocal = rowLocal;
     P.rec[q] = R;
     P.walk[q] = Wk;
-    if (valid) {
-      const uint32_t sx0 = R.minX / kSuperTile, sx1 = (R.maxX - 1u) / kSuperTile;
-      const uint32_t sy0 = R.minY / kSuperTile, sy1 = (R.maxY - 1u) / kSuperTile;
-      for (uint32_t sy = sy0; sy <= sy1; ++sy)
-        for (uint32_t sx = sx0; sx <= sx1; ++sx) atomicAdd(&s_stCount[sy * V.stX + sx], 1u);
+    // super-tile counts, warp-aggregated: each round every lane offers its
+    // next super-tile, lanes offering the same one add together (one atomic)
+    {
+      const uint32_t sx0 = valid ? R.minX / kSuperTile : 0u, sx1 = valid ? (R.maxX - 1u) / kSuperTile : 0u;
+      const uint32_t sy1 = valid ? (R.maxY - 1u) / kSuperTile : 0u;
+      uint32_t sx = sx0, sy = valid ? R.minY / kSuperTile : 0u;
+      bool pending = valid;
+      while (__any_sync(0xFFFFFFFFu, pending)) {
+        const uint32_t key = pending ? sy * V.stX + sx : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+        if (pending && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&s_stCount[key], (uint32_t)__popc(peers));
+        if (pending && ++sx > sx1) {
+          sx = sx0;
+          pending = ++sy <= sy1;
+        }
+      }
     }
     __syncthreads();
     for (uint32_t st = tid; st < nst; st += kChunk) P.mat[V.matBase + st * V.chunkCount + ch.localIndex] = s_stCount[st];
