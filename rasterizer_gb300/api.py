@@ -648,7 +648,8 @@ class PreparedBatch:
 
     # occ_batch_autotune / occ_batch_set_tuning layout (OCC_TUNING_FIELDS entries)
     TUNING_KEYS = ("setup_ctas_per_sm", "fill_ctas_per_sm", "walk_ctas_per_sm", "raster_ctas_per_sm",
-                   "raster_units_per_fetch", "query_rounds", "raster_unit_rows", "raster_threads_per_unit")
+                   "raster_units_per_fetch", "query_rounds", "raster_unit_rows", "raster_threads_per_unit",
+                   "super_tile_blocks")
 
     def autotune(self, iterations: int = 5) -> dict:
         """Picks the launch shapes of the persistent kernels by timing the

@@ -257,7 +257,9 @@ struct BatchLayout {
   uint32_t totalQuads = 0;
 };
 
-int build_layout(occ_ctx_s* ctx, const std::vector<ViewJob>& jobs, BatchLayout& L)
+// stShift: super-tile edge 1 << stShift blocks (3 or 4); a view whose grid
+// of such super-tiles would exceed kMaxStPerView takes 16-block super-tiles.
+int build_layout(occ_ctx_s* ctx, const std::vector<ViewJob>& jobs, BatchLayout& L, uint32_t stShift = 4)
 {
   uint32_t quadBase = 0, chunkBase = 0, tileBase = 0, stBase = 0, matBase = 0, queryBase = 0;
   for (size_t v = 0; v < jobs.size(); ++v) {
@@ -318,8 +320,11 @@ int build_layout(occ_ctx_s* ctx, const std::vector<ViewJob>& jobs, BatchLayout& 
     V.tilesY = div_up(r->blocksY, kTileH);
     V.tileStart = tileBase;
     tileBase += V.tilesX * V.tilesY;
-    V.stX = div_up(r->blocksX, kSuperTile);
-    V.stY = div_up(r->blocksY, kSuperTile);
+    uint32_t sh = stShift;
+    if ((size_t)div_up(r->blocksX, 1u << sh) * div_up(r->blocksY, 1u << sh) > (size_t)kMaxStPerView) sh = 4;
+    V.stShift = sh;
+    V.stX = div_up(r->blocksX, 1u << sh);
+    V.stY = div_up(r->blocksY, 1u << sh);
     V.stBase = stBase;
     stBase += V.stX * V.stY;
     L.maxStPerView = std::max(L.maxStPerView, V.stX * V.stY);
@@ -1232,6 +1237,49 @@ int capture(occ_batch_s* b)
 
 }  // namespace
 
+namespace {
+
+// Lays a prepared batch out again with super-tiles of 1 << shift blocks: the
+// view table (super-tile grids and count-matrix ranges) changes, the count
+// matrix and list heads are reserved for it, every ring slot is rewritten and
+// the graph captured again.  Matrices, view flags and owner buffers carry over.
+int relayout(occ_batch_s* b, uint32_t shift)
+{
+  BatchLayout L;
+  OCC_CHECK(build_layout(b->ctx, b->jobs, L, shift));
+  for (size_t v = 0; v < L.views.size(); ++v) {
+    L.views[v].flags = b->L.views[v].flags;
+    L.views[v].owner = b->L.views[v].owner;
+  }
+  b->L = std::move(L);
+  FrameScratch& S = b->S;
+  OCC_CHECK(S.mat.reserve(b->L.matSize));
+  OCC_CHECK(S.stStart.reserve(b->L.numSt));
+  OCC_CHECK(S.stLen.reserve(b->L.numSt));
+  for (int k = 0; k < kRing; ++k) {
+    OCC_CUDA(cudaEventSynchronize(b->ringEv[k]));
+    write_tables(b, b->ring[k].p);
+  }
+  b->tune.superTile = 1u << shift;
+  b->dirty = false;
+  return capture(b);
+}
+
+// Launches until a launch fits the scratch (each overflow grows it), at most
+// a few times; the frames are re-run by the caller's own timing afterwards.
+int settle(occ_batch_s* b)
+{
+  for (int i = 0; i < 4; ++i) {
+    OCC_CHECK(occ_batch_launch(b));
+    const int st = occ_batch_check(b);
+    if (st == OCC_OK) return OCC_OK;
+    if (st != OCC_ERR_CAPACITY) return st;
+  }
+  return fail(OCC_ERR_CAPACITY, "the batch's scratch did not settle");
+}
+
+}  // namespace
+
 extern "C" {
 
 int occ_batch_prepare(occ_ctx ctx, uint32_t numViews, const occ_view_work* views, occ_batch* out)
@@ -1268,7 +1316,7 @@ int occ_batch_prepare(occ_ctx ctx, uint32_t numViews, const occ_view_work* views
   FrameScratch& S = b->S;
   S.capCks = std::max(S.capCks, 2 * S.capCks + 65536);
   S.capSt = std::max(S.capSt, 2 * S.capSt + 65536);
-  OCC_CHECK(build_layout(ctx, b->jobs, b->L));
+  OCC_CHECK(build_layout(ctx, b->jobs, b->L, 4));
   const uint32_t nv = (uint32_t)b->L.views.size();
   b->offCmds = align_up(nv * sizeof(ViewDesc), 256);
   b->offChunks = align_up(b->offCmds + b->L.cmds.size() * sizeof(Cmd), 256);
@@ -1538,7 +1586,7 @@ static int profile_with(occ_batch b, const LaunchTuning& t, uint32_t iterations,
   return st;
 }
 
-int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[8], float msBefore[7], float msAfter[7])
+int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[9], float msBefore[7], float msAfter[7])
 {
   if (!b || !iterations) return fail(OCC_ERR_INVALID_ARG, "bad argument");
   uint32_t lim[7];
@@ -1568,6 +1616,25 @@ int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[8], floa
     for (uint32_t i = 1; i <= n; ++i) v.push_back(i);
     return v;
   };
+  // super-tile edge (binning granularity): changes the layout and every stage
+  // from setup to raster, so whole frames decide
+  {
+    float bestMs = 3.0e38f;
+    uint32_t bestShift = b->tune.superTile == 8 ? 3u : 4u;
+    for (uint32_t shift : {4u, 3u}) {
+      OCC_CHECK(relayout(b, shift));
+      OCC_CHECK(settle(b));
+      OCC_CHECK(profile_with(b, best, iterations, ms));
+      const float frame = ms[0] + ms[1] + ms[2] + ms[3] + ms[4];
+      if (frame < bestMs) {
+        bestMs = frame;
+        bestShift = shift;
+      }
+    }
+    OCC_CHECK(relayout(b, bestShift));
+    OCC_CHECK(settle(b));
+    best.superTile = 1u << bestShift;
+  }
   OCC_CHECK(search(&LaunchTuning::setupPerSm, 0, upTo(lim[0])));
   OCC_CHECK(search(&LaunchTuning::fillPerSm, 2, upTo(lim[1])));
   OCC_CHECK(search(&LaunchTuning::walkPerSm, 3, {2, 4, 8, 16}));
@@ -1603,6 +1670,7 @@ int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[8], floa
     tuned[5] = best.queryRounds;
     tuned[6] = best.rasterRows ? best.rasterRows : kDefaultRasterRows;
     tuned[7] = best.rasterThreads;
+    tuned[8] = best.superTile;
   }
   return OCC_OK;
 }
@@ -1646,7 +1714,7 @@ int occ_batch_set_second_pass(occ_batch b, int enable)
   return capture(b);
 }
 
-int occ_batch_set_tuning(occ_batch b, const uint32_t tune[8])
+int occ_batch_set_tuning(occ_batch b, const uint32_t tune[9])
 {
   if (!b || !tune) return fail(OCC_ERR_INVALID_ARG, "null argument");
   for (int i = 0; i < 5; ++i)
@@ -1658,6 +1726,8 @@ int occ_batch_set_tuning(occ_batch b, const uint32_t tune[8])
     return fail(OCC_ERR_INVALID_ARG, "raster threads per unit must be 32 or 128 (0: chosen per launch)");
   if (tune[7] == 128 && tune[6] != 0 && tune[6] != 2)
     return fail(OCC_ERR_INVALID_ARG, "the 128-thread raster form takes units of 2 block rows");
+  if (tune[8] != 0 && tune[8] != 8 && tune[8] != 16)
+    return fail(OCC_ERR_INVALID_ARG, "super-tile edge must be 8 or 16 blocks (0: 16)");
   LaunchTuning t{};
   t.setupPerSm = tune[0];
   t.fillPerSm = tune[1];
@@ -1667,7 +1737,11 @@ int occ_batch_set_tuning(occ_batch b, const uint32_t tune[8])
   t.queryRounds = tune[5];
   t.rasterRows = tune[6];
   t.rasterThreads = tune[7];
+  const uint32_t shift = tune[8] == 8 ? 3u : 4u;
+  const bool newLayout = (b->tune.superTile == 8 ? 3u : 4u) != shift;
+  t.superTile = 1u << shift;
   b->tune = t;
+  if (newLayout) return relayout(b, shift);
   return capture(b);
 }
 

@@ -658,9 +658,10 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
     // super-tile counts, warp-aggregated: each round every lane offers its
     // next super-tile, lanes offering the same one add together (one atomic)
     {
-      const uint32_t sx0 = valid ? R.minX / kSuperTile : 0u, sx1 = valid ? (R.maxX - 1u) / kSuperTile : 0u;
-      const uint32_t sy1 = valid ? (R.maxY - 1u) / kSuperTile : 0u;
-      uint32_t sx = sx0, sy = valid ? R.minY / kSuperTile : 0u;
+      const uint32_t sh = V.stShift;
+      const uint32_t sx0 = valid ? (uint32_t)R.minX >> sh : 0u, sx1 = valid ? (R.maxX - 1u) >> sh : 0u;
+      const uint32_t sy1 = valid ? (R.maxY - 1u) >> sh : 0u;
+      uint32_t sx = sx0, sy = valid ? (uint32_t)R.minY >> sh : 0u;
       bool pending = valid;
       while (__any_sync(0xFFFFFFFFu, pending)) {
         const uint32_t key = pending ? sy * V.stX + sx : 0xFFFFFFFFu;
@@ -815,8 +816,8 @@ __global__ void __launch_bounds__(kChunk) k_fill(FrameParams P)
     __syncthreads();
     int sx0 = 0, sx1 = -1, sy0 = 0, sy1 = -1;
     if (valid) {
-      sx0 = R.minX / kSuperTile; sx1 = (R.maxX - 1) / kSuperTile;
-      sy0 = R.minY / kSuperTile; sy1 = (R.maxY - 1) / kSuperTile;
+      sx0 = (int)((uint32_t)R.minX >> V.stShift); sx1 = (int)((uint32_t)(R.maxX - 1) >> V.stShift);
+      sy0 = (int)((uint32_t)R.minY >> V.stShift); sy1 = (int)((uint32_t)(R.maxY - 1) >> V.stShift);
       atomicMin(&s_rect[0], sx0); atomicMax(&s_rect[1], sx1);
       atomicMin(&s_rect[2], sy0); atomicMax(&s_rect[3], sy1);
     }
@@ -1441,7 +1442,7 @@ __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
       if (inView) V.hiz[blk] = 1;
       if (lt == 0 && lane < 8) V.hiz[V.blocksX * V.blocksY + lane] = 1;  // padding entries
     }
-    const uint32_t s = V.stBase + (ty0 / kSuperTile) * V.stX + (tx0 / kSuperTile);
+    const uint32_t s = V.stBase + (ty0 >> V.stShift) * V.stX + (tx0 >> V.stShift);
     const uint32_t len = V.cmdCount ? P.stLen[s] : 0u;
     listLen = len;
     listStart = len ? P.stStart[s] : 0u;

@@ -15,7 +15,7 @@ namespace occ {
 
 constexpr int kChunkShift = 8;
 constexpr int kChunk = 1 << kChunkShift;  // quads per setup CTA
-constexpr int kSuperTile = 16;            // binning super-tile edge, in 8x8 blocks (multiple of kTileW, kTileH)
+constexpr int kSuperTile = 16;            // default binning super-tile edge, in 8x8 blocks (8 or 16: whole warp-tiles)
 constexpr int kTileW = 8;                 // warp-tile: 8 x 4 blocks, one lane per block
 constexpr int kTileH = 4;
 constexpr int kCkSpan = 8;                // row-walk checkpoint every 8 block columns (== kTileW)
@@ -60,6 +60,7 @@ struct ViewDesc {
   uint32_t matBase;                     // count matrix base: stX*stY*chunkCount entries
   uint32_t queryStart, queryCount;      // query slots; queryStart is a multiple of 32
   uint32_t flags;
+  uint32_t stShift;                     // super-tile edge = 1 << stShift blocks (3 or 4)
   uint32_t* owner;   // optional, width*height (depth layout): command + 1 that produced each
                      // pixel's final value this launch, 0 if none (cull labels of the selector)
 };
@@ -159,6 +160,7 @@ struct LaunchTuning {
   uint32_t rasterRows;   // block rows per raster unit: 1, 2 or 4 (0: kDefaultRasterRows)
   uint32_t rasterThreads;  // threads per raster unit: 32 (one warp) or 128 (a CTA, units of 2 rows);
                            // 0: chosen by the launch's unit count
+  uint32_t superTile;      // binning super-tile edge in blocks: 8 or 16 (0: kSuperTile); set by the host layout
 };
 
 struct FrameParams {

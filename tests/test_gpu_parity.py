@@ -272,11 +272,12 @@ def test_autotuned_launch_shapes_keep_results(ctx):
     b.close()
 
 
-@pytest.mark.parametrize("rows,threads", [(1, 32), (2, 32), (4, 32), (2, 128)])
-def test_raster_unit_shapes(ctx, rows, threads):
+@pytest.mark.parametrize("rows,threads,st", [(1, 32, 16), (2, 32, 16), (4, 32, 16), (2, 128, 16), (2, 32, 8),
+                                             (2, 128, 8)])
+def test_raster_unit_shapes(ctx, rows, threads, st):
     """Raster units of 1, 2 and 4 block rows per warp, and 2-row units per
-    128-thread CTA (choices of the autotuner), give the oracle's frames: two
-    views on persistent rasterizers,
+    128-thread CTA, with super-tiles of 16 and 8 blocks (choices of the
+    autotuner), give the oracle's frames: two views on persistent rasterizers,
     frames in the reference's clear (stale depth merged and queried), then in
     the zero-depth clear, with win counting on (the other kernel variant)."""
     occ = city_occluders()
@@ -289,7 +290,7 @@ def test_raster_unit_shapes(ctx, rows, threads):
     views = [dict(raster=r, mvp=mvps[s], clear=True, occluders=occ, flags=np.full(len(occ), 2, np.uint8),
                   mins=mins, maxs=maxs) for r, s in zip(rs, starts)]
     b = api.PreparedBatch(ctx, views)
-    b.setTuning({"raster_unit_rows": rows, "raster_threads_per_unit": threads})
+    b.setTuning({"raster_unit_rows": rows, "raster_threads_per_unit": threads, "super_tile_blocks": st})
     orcs = [Oracle(w, h) for _ in rs]
     for o, s in zip(orcs, starts):
         o.frame_plain(scene, mvps[s])  # the preparing frame
