@@ -609,18 +609,20 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
 
     // the chunk's packed words into shared memory, one coalesced 16-byte load
     // per thread: thread t loads vector t % 8 of the chunk's 8-quad group t / 8
-    // (a group's 32 words are corner-major: word 8j + i is corner j of quad i)
+    // (a group's 32 words are corner-major: word 8j + i is corner j of quad i).
+    // A group lies in one command, the command of thread t's own quad too.
+    const uint32_t g0 = (c << kChunkShift) + 8 * (tid >> 3);  // first quad of the group
+    uint32_t k = 0;
     {
-      const uint32_t g0 = (c << kChunkShift) + 8 * (tid >> 3);  // first quad of the group
-      if (8 * (tid >> 3) < ch.quadCount) {
-        uint32_t k = 0;
-        for (uint32_t i = 1; i < ch.cmdCount; ++i)
-          if (s_cmdStart[i] <= g0) k = i;
-        if (s_cc[k].draw) {
-          const Cmd& cmd = P.cmds[ch.cmdFirst + k];
-          const uint4* src = reinterpret_cast<const uint4*>(P.pool + cmd.wordOffset + (g0 - cmd.quadStart) * 4);
-          reinterpret_cast<uint4*>(s_words)[tid] = __ldg(src + (tid & 7));
-        }
+      uint32_t hi = ch.cmdCount - 1;  // last command starting at or before the group
+      while (k < hi) {
+        const uint32_t mid = (k + hi + 1) >> 1;
+        if (s_cmdStart[mid] <= g0) k = mid; else hi = mid - 1;
+      }
+      if (8 * (tid >> 3) < ch.quadCount && s_cc[k].draw) {
+        const Cmd& cmd = P.cmds[ch.cmdFirst + k];
+        const uint4* src = reinterpret_cast<const uint4*>(P.pool + cmd.wordOffset + (g0 - cmd.quadStart) * 4);
+        reinterpret_cast<uint4*>(s_words)[tid] = __ldg(src + (tid & 7));
       }
     }
     __syncthreads();
@@ -629,9 +631,6 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
     QuadWalk Wk;
     bool valid = false;
     if (tid < ch.quadCount) {
-      uint32_t k = 0;
-      for (uint32_t i = 1; i < ch.cmdCount; ++i)
-        if (s_cmdStart[i] <= q) k = i;
       if (s_cc[k].draw) {
         uint32_t w4[4];
 #pragma unroll
