@@ -33,6 +33,7 @@
 // the in-range blocks of a row form one interval.  Skipping them or testing
 // them gives the same result.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <mutex>
@@ -2096,11 +2097,31 @@ __global__ void __launch_bounds__(256) k_read_back(const uint16_t* depth, const 
 // The frame's kernels in order; with `ev`, an event is recorded before the
 // first stage and after each of the six stages (setup, scan, list fill, row
 // walk, raster, query), also for stages that do not run.
+// NVTX ranges naming the frame's stages on the host timeline of a profiler
+// (the launches a stage issues sit inside its range).
+struct StageRanges {
+  int open = -1;
+  void next(int i)
+  {
+    static const char* const kNames[6] = {"occ setup", "occ scan", "occ list fill", "occ row walk", "occ raster",
+                                          "occ query"};
+    if (open >= 0) nvtxRangePop();
+    open = i < 6 ? i : -1;
+    if (open >= 0) nvtxRangePushA(kNames[i]);
+  }
+  ~StageRanges()
+  {
+    if (open >= 0) nvtxRangePop();
+  }
+};
+
 static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
                                 bool doQuery, cudaStream_t stream, cudaEvent_t* ev)
 {
+  StageRanges ranges;
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], stream);
+    ranges.next(i);
   };
   mark(0);
   if (doRaster) {
