@@ -65,7 +65,7 @@ struct ViewDesc {
                      // pixel's final value this launch, 0 if none (cull labels of the selector)
 };
 
-struct Cmd {
+struct alignas(16) Cmd {
   uint32_t view;
   uint32_t wordOffset;   // first packed word of the occluder in the occluder pool
   uint32_t quadStart;    // first global quad index
@@ -76,7 +76,7 @@ struct Cmd {
   float boundsMin[4], boundsMax[4];
 };
 
-struct Chunk {
+struct alignas(16) Chunk {
   uint32_t view;
   uint32_t localIndex;   // chunk index within its view
   uint32_t quadCount;    // real quads in this chunk (the rest is padding)
@@ -85,8 +85,9 @@ struct Chunk {
   uint32_t pad[3];
 };
 
-// Per-quad setup output read by the rasteriser (48 bytes).
-struct QuadRaster {
+// Per-quad setup output read by the rasteriser (48 bytes, moved as three
+// 16-byte words).
+struct alignas(16) QuadRaster {
   uint16_t minX, minY, maxX, maxY;  // block bbox [min, max); minX == maxX marks an invalid quad
   uint16_t maxZ;                    // packed 16-bit nearest depth bound
   uint8_t mode, flags;
@@ -96,8 +97,9 @@ struct QuadRaster {
   float nx[4];                      // normalised edge x coefficients
 };
 
-// Per-quad setup output read by the row walk (48 bytes).
-struct QuadWalk {
+// Per-quad setup output read by the row walk (48 bytes, moved as three
+// 16-byte words).
+struct alignas(16) QuadWalk {
   float plane0;     // depth at the bbox origin
   float off[4];     // edge offsets at the bbox origin (quantisation units)
   float ny[4];      // normalised edge y coefficients
@@ -220,4 +222,9 @@ struct FrameParams {
 // ones spread the network over many CTAs (k_mlp_forward, k_topk, k_gate).
 constexpr uint32_t kFusedSelectMaxCmds = 1024;
 
+}  // namespace occ
+
+namespace occ {
+static_assert(sizeof(QuadRaster) == 48 && sizeof(QuadWalk) == 48 && sizeof(Cmd) % 16 == 0 && sizeof(Chunk) == 32,
+              "record sizes");
 }  // namespace occ
