@@ -1408,18 +1408,36 @@ int occ_batch_set_queries(occ_batch b, uint32_t first, uint32_t count, const flo
 {
   if (!b || first > b->L.views.size() || count > b->L.views.size() - first)
     return fail(OCC_ERR_INVALID_ARG, "bad argument");
-  size_t at = 0;  // boxes consumed from the host arrays
+  // views whose slot ranges follow one another without padding (box counts
+  // that are multiples of 32) take one copy per array together
+  size_t at = 0;                     // boxes consumed from the host arrays
+  uint32_t runStart = 0, runLen = 0;  // device slots of the pending copy
+  size_t runAt = 0;
+  auto flush = [&]() -> int {
+    if (!runLen) return OCC_OK;
+    OCC_CUDA(cudaMemcpyAsync(b->qmin.p + runStart, mins + 4 * runAt, (size_t)runLen * 16, cudaMemcpyHostToDevice,
+                             b->ctx->stream));
+    OCC_CUDA(cudaMemcpyAsync(b->qmax.p + runStart, maxs + 4 * runAt, (size_t)runLen * 16, cudaMemcpyHostToDevice,
+                             b->ctx->stream));
+    runLen = 0;
+    return OCC_OK;
+  };
   for (uint32_t v = first; v < first + count; ++v) {
     const ViewDesc& V = b->L.views[v];
     if (!V.queryCount) continue;
     if (!mins || !maxs) return fail(OCC_ERR_INVALID_ARG, "null query boxes");
-    OCC_CUDA(cudaMemcpyAsync(b->qmin.p + V.queryStart, mins + 4 * at, (size_t)V.queryCount * 16,
-                             cudaMemcpyHostToDevice, b->ctx->stream));
-    OCC_CUDA(cudaMemcpyAsync(b->qmax.p + V.queryStart, maxs + 4 * at, (size_t)V.queryCount * 16,
-                             cudaMemcpyHostToDevice, b->ctx->stream));
+    if (runLen && runStart + runLen == V.queryStart) {
+      runLen += V.queryCount;
+    } else {
+      OCC_CHECK(flush());
+      runStart = V.queryStart;
+      runLen = V.queryCount;
+      runAt = at;
+    }
     at += V.queryCount;
+    if (V.queryCount % 32) OCC_CHECK(flush());  // the next view starts after padding
   }
-  return OCC_OK;
+  return flush();
 }
 
 int occ_batch_result_words(occ_batch b, uint32_t* words)

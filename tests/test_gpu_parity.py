@@ -446,3 +446,39 @@ def test_bulk_matrices_and_results(ctx):
         vv, nn = b.results(v)
         assert np.array_equal(vv, sv) and np.array_equal(nn, sn)
     b.close()
+
+
+def test_batch_query_boxes_replaced_per_launch(ctx):
+    """occ_batch_set_queries: new boxes for every view before a launch (views
+    of 64, 50 and 96 boxes: contiguous slot ranges copied together, a padded
+    one alone) answer as the oracle does, and occ_batch_results_all_async
+    returns the same bits as the synchronous copy."""
+    occ = boxes_occluders()
+    scene = to_baked(occ)
+    w, h = 640, 360
+    mvp = scenes.boxes_camera(w, h)
+    counts = (64, 50, 96)
+    first = [scenes.query_boxes(n, seed=60 + k) for k, n in enumerate(counts)]
+    views = [dict(raster=api.Rasterizer(ctx, w, h), mvp=mvp, clear=True, occluders=occ,
+                  flags=np.full(len(occ), 2, np.uint8), mins=m, maxs=M) for m, M in first]
+    b = api.PreparedBatch(ctx, views)
+    orc = Oracle(w, h)
+    orc.frame_plain(scene, mvp)
+    for rnd in range(2):
+        new = [scenes.query_boxes(n, seed=70 + 5 * rnd + k) for k, n in enumerate(counts)]
+        b.setQueries(np.concatenate([m for m, _ in new]), np.concatenate([M for _, M in new]))
+        b.launch()
+        assert b.check()
+        res = b.resultsAll(unpack=True)
+        words = b.resultWords()
+        vis_a, nc_a = np.zeros(words, np.uint32), np.zeros(words, np.uint32)
+        b.resultsAllAsync(vis_a, nc_a)
+        ctx.synchronize()
+        vis_s, nc_s, _ = b.resultsAll()
+        assert np.array_equal(vis_a, vis_s) and np.array_equal(nc_a, nc_s)
+        for (m, M), (vis, nc) in zip(new, res):
+            ovis, onc = orc.query(m, M)
+            assert np.array_equal(vis.astype(np.uint8), ovis) and np.array_equal(nc.astype(np.uint8), onc)
+    b.close()
+    for v in views:
+        v["raster"].close()
