@@ -770,11 +770,11 @@ int occ_raster_create(occ_ctx ctx, uint32_t width, uint32_t height, occ_raster* 
   OCC_CHECK(r->depth.reserve((size_t)width * height));
   OCC_CHECK(r->hiz.reserve(blocks + 8));
   const size_t tiles = (size_t)div_up(r->blocksX, kTileW) * div_up(r->blocksY, kTileH);
-  OCC_CHECK(r->tileHiz.reserve(tiles));
+  OCC_CHECK(r->tileHiz.reserve((size_t)tiles * 4));  // the minimum hiZ of each tile's 4 block rows
   // the reference value-initialises both (Rasterizer.cpp:70-71)
   OCC_CUDA(cudaMemsetAsync(r->depth.p, 0, (size_t)width * height * 2, ctx->stream));
   OCC_CUDA(cudaMemsetAsync(r->hiz.p, 0, (blocks + 8) * 2, ctx->stream));
-  OCC_CUDA(cudaMemsetAsync(r->tileHiz.p, 0, tiles * 2, ctx->stream));
+  OCC_CUDA(cudaMemsetAsync(r->tileHiz.p, 0, (size_t)tiles * 8, ctx->stream));
   OCC_CUDA(cudaStreamSynchronize(ctx->stream));
   *out = r.release();
   return OCC_OK;

@@ -35,6 +35,7 @@
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include <mutex>
 
@@ -61,6 +62,19 @@ static uint32_t grid_of(uint32_t tuned, uint32_t limit, uint32_t work)
   const uint32_t perSm = tuned ? ::min(tuned, limit) : limit;
   return ::max(1u, ::min(work, perSm * g_sms));
 }
+
+// Programmatic dependent launch.  Every kernel of a flush after the first is
+// launched with programmatic stream serialisation: it is scheduled once all
+// CTAs of its predecessor have started (pdl_trigger at the top of every
+// kernel), so its launch and whatever it does before pdl_wait overlap the
+// predecessor's tail.  pdl_wait returns when the predecessor grid has
+// completed and its memory operations are visible; nothing a predecessor
+// writes is read before it.  Launched without the attribute, both return at
+// once.  The environment variable OCC_PDL=0 launches every kernel plainly.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+static bool g_pdl = true;
 
 // Primitive mode for the 8-bit configuration (area signs | W signs << 4),
 // the classification of Rasterizer.cpp:30-64.
@@ -176,14 +190,37 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t& t
 // skipped as a whole, which skips exactly the same blocks.  The result is the
 // OR over blocks, so tiles and blocks may be visited in any order.
 
-// One block (bx, by) of the rectangle: skipped if maxZ <= its hiZ, visible if
-// the rectangle covers it whole, else any covered pixel with depth < maxZ
-// (Rasterizer.cpp:303-344).
-__device__ __forceinline__ bool query2d_block(const ViewDesc& V, uint32_t bx, uint32_t by, uint32_t minX,
-                                              uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ)
+// Per warp-tile, the minimum hiZ of each of its four block rows (tileHiz[4 t
+// + r], 0xFFFF for rows outside the view); written by the raster unit that
+// owns the row, or by the tile preparation for rows no unit is queued for.
+__device__ __forceinline__ uint2 tile_rows(const ViewDesc& V, uint32_t t)
 {
-  const uint32_t blk = by * V.blocksX + bx;
-  if (maxZ <= (uint32_t)V.hiz[blk]) return false;
+  return *reinterpret_cast<const uint2*>(V.tileHiz + 4 * (size_t)t);
+}
+__device__ __forceinline__ uint32_t row_min(const uint2 rm, uint32_t r)
+{
+  const uint32_t w = r & 2u ? rm.y : rm.x;
+  return r & 1u ? w >> 16 : w & 0xFFFFu;
+}
+__device__ __forceinline__ uint32_t tile_min(const uint2 rm)
+{
+  const uint32_t m = vmin_u16x2(rm.x, rm.y);
+  return ::min(m & 0xFFFFu, m >> 16);
+}
+
+// Two forms of each helper: kBatch loads what a step needs together (a block
+// row's hiZ values, four pixel rows of a block) for the shortest chain of
+// dependent loads, where few boxes are in flight (one view's boxes, a thread
+// each); the other form loads one value at a time and stops at the first
+// visible one, for the fewest instructions where many boxes keep the GPU busy.
+
+// One block (bx, by) of the rectangle whose hiZ is below maxZ: visible if the
+// rectangle covers it whole, else if any covered pixel has depth < maxZ
+// (Rasterizer.cpp:303-344).
+template <bool kBatch>
+__device__ __forceinline__ bool query2d_open_block(const ViewDesc& V, uint32_t bx, uint32_t by, uint32_t minX,
+                                                   uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ)
+{
   int32_t sy = (int32_t)(minY - 8 * by);
   sy = sy < 0 ? 0 : sy;
   int32_t ey = (int32_t)(maxY - 8 * by);
@@ -199,30 +236,72 @@ __device__ __forceinline__ bool query2d_block(const ViewDesc& V, uint32_t bx, ui
 #pragma unroll
   for (int w = 0; w < 4; ++w)
     cm[w] = ((2 * w >= sx && 2 * w <= ex) ? 0x0000FFFFu : 0u) | ((2 * w + 1 >= sx && 2 * w + 1 <= ex) ? 0xFFFF0000u : 0u);
-  const uint16_t* d = V.depth + (size_t)blk * 64;
-  for (int32_t y = sy; y <= ey; ++y) {
-    const uint4 row = *reinterpret_cast<const uint4*>(d + 8 * y);
-    // a pixel is visible where its depth < maxZ (Rasterizer.cpp:333-336)
-    if ((__vcmpltu2(row.x, mz2) & cm[0]) | (__vcmpltu2(row.y, mz2) & cm[1]) | (__vcmpltu2(row.z, mz2) & cm[2]) |
-        (__vcmpltu2(row.w, mz2) & cm[3]))
-      return true;
+  const uint4* d = reinterpret_cast<const uint4*>(V.depth + (size_t)(by * V.blocksX + bx) * 64);
+  // a pixel is visible where its depth < maxZ (Rasterizer.cpp:333-336)
+  auto hit = [&](const uint4& row) {
+    return ((__vcmpltu2(row.x, mz2) & cm[0]) | (__vcmpltu2(row.y, mz2) & cm[1]) | (__vcmpltu2(row.z, mz2) & cm[2]) |
+            (__vcmpltu2(row.w, mz2) & cm[3])) != 0u;
+  };
+  if (!kBatch) {
+    for (int32_t y = sy; y <= ey; ++y)
+      if (hit(d[y])) return true;
+    return false;
+  }
+#pragma unroll
+  for (int y0 = 0; y0 < 8; y0 += 4) {  // the block is one 128-byte line
+    if (y0 > ey || y0 + 3 < sy) continue;
+    uint4 row[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) row[k] = (y0 + k >= sy && y0 + k <= ey) ? d[y0 + k] : make_uint4(0, 0, 0, 0);
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) any |= y0 + k >= sy && y0 + k <= ey && hit(row[k]);
+    if (any) return true;
   }
   return false;
 }
 
-// Blocks of tile (tx, ty) inside the rectangle.
-__device__ bool query2d_tile(const ViewDesc& V, uint32_t tx, uint32_t ty, uint32_t minX, uint32_t maxX,
+// One block of the rectangle: skipped if maxZ <= its hiZ, else as above.
+template <bool kBatch>
+__device__ __forceinline__ bool query2d_block(const ViewDesc& V, uint32_t bx, uint32_t by, uint32_t minX,
+                                              uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ)
+{
+  if (maxZ <= (uint32_t)V.hiz[by * V.blocksX + bx]) return false;
+  return query2d_open_block<kBatch>(V, bx, by, minX, maxX, minY, maxY, maxZ);
+}
+
+// Blocks of tile (tx, ty) inside the rectangle, rows whose minimum hiZ is
+// >= maxZ skipped (all their blocks are); kBatch: a block row at a time, the
+// row's hiZ values (at most 8) loaded together.  rm: the tile's row minima.
+template <bool kBatch>
+__device__ bool query2d_tile(const ViewDesc& V, uint32_t tx, uint32_t ty, uint2 rm, uint32_t minX, uint32_t maxX,
                              uint32_t minY, uint32_t maxY, uint32_t maxZ)
 {
   const uint32_t bx0 = minX >> 3, bx1 = maxX >> 3, by0 = minY >> 3, by1 = maxY >> 3;
   const uint32_t ya = ::max(by0, ty * kTileH), yb = ::min(by1, ty * kTileH + kTileH - 1);
   const uint32_t xa = ::max(bx0, tx * kTileW), xb = ::min(bx1, tx * kTileW + kTileW - 1);
-  for (uint32_t by = ya; by <= yb; ++by)
-    for (uint32_t bx = xa; bx <= xb; ++bx)
-      if (query2d_block(V, bx, by, minX, maxX, minY, maxY, maxZ)) return true;
+  for (uint32_t by = ya; by <= yb; ++by) {
+    if (maxZ <= row_min(rm, by - ty * kTileH)) continue;
+    if (!kBatch) {
+      for (uint32_t bx = xa; bx <= xb; ++bx)
+        if (query2d_block<false>(V, bx, by, minX, maxX, minY, maxY, maxZ)) return true;
+      continue;
+    }
+    const uint16_t* h = V.hiz + by * V.blocksX + xa;
+    uint32_t open = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < (uint32_t)kTileW; ++k)
+      if (xa + k <= xb && maxZ > (uint32_t)h[k]) open |= 1u << k;
+    while (open) {
+      const uint32_t k = (uint32_t)(__ffs(open) - 1);
+      open &= open - 1;
+      if (query2d_open_block<true>(V, xa + k, by, minX, maxX, minY, maxY, maxZ)) return true;
+    }
+  }
   return false;
 }
 
+template <bool kBatch>
 __device__ bool query2d(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY, uint32_t maxZ)
 {
   const uint32_t tilesX = (V.blocksX + kTileW - 1) / kTileW;
@@ -230,8 +309,9 @@ __device__ bool query2d(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_
   const uint32_t ty0 = (minY >> 3) / kTileH, ty1 = (maxY >> 3) / kTileH;
   for (uint32_t ty = ty0; ty <= ty1; ++ty)
     for (uint32_t tx = tx0; tx <= tx1; ++tx) {
-      if (maxZ <= (uint32_t)V.tileHiz[ty * tilesX + tx]) continue;
-      if (query2d_tile(V, tx, ty, minX, maxX, minY, maxY, maxZ)) return true;
+      const uint2 rm = tile_rows(V, ty * tilesX + tx);
+      if (maxZ <= tile_min(rm)) continue;
+      if (query2d_tile<kBatch>(V, tx, ty, rm, minX, maxX, minY, maxY, maxZ)) return true;
     }
   return false;
 }
@@ -493,6 +573,8 @@ __device__ __forceinline__ uint32_t nck_of(const QuadRaster& R)
 
 __global__ void __launch_bounds__(256) k_gate(FrameParams P)
 {
+  pdl_trigger();
+  pdl_wait();
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= P.numCmds) return;
   const Cmd& cmd = P.cmds[c];
@@ -514,6 +596,8 @@ __global__ void __launch_bounds__(256) k_gate(FrameParams P)
 // rasterize, Main.cpp:192-206).  The lanes share the query2D over warp-tiles.
 __global__ void __launch_bounds__(256) k_gate_second(FrameParams P)
 {
+  pdl_trigger();
+  pdl_wait();
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t c = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (c >= P.numCmds) return;  // whole warp
@@ -537,8 +621,8 @@ __global__ void __launch_bounds__(256) k_gate_second(FrameParams P)
         bool hit = false;
         if (t < nt) {
           const uint32_t tx = tx0 + t % ntx, ty = ty0 + t / ntx;
-          if (maxZ > (uint32_t)V.tileHiz[ty * tilesX + tx])
-            hit = query2d_tile(V, tx, ty, rect[0], rect[1], rect[2], rect[3], maxZ);
+          const uint2 rm = tile_rows(V, ty * tilesX + tx);
+          if (maxZ > tile_min(rm)) hit = query2d_tile<false>(V, tx, ty, rm, rect[0], rect[1], rect[2], rect[3], maxZ);
         }
         found = __ballot_sync(0xFFFFFFFFu, hit) != 0;
       }
@@ -555,6 +639,8 @@ __global__ void __launch_bounds__(256) k_chunk_gate(FrameParams P)
 {
   __shared__ uint32_t s_scan[8];
   __shared__ uint32_t s_base;
+  pdl_trigger();
+  pdl_wait();
   const uint32_t v = blockIdx.x, tid = threadIdx.x;
   const ViewDesc& V = P.views[v];
   uint32_t n = 0;
@@ -590,6 +676,8 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
   __shared__ uint32_t s_scan[kChunk / 32];
   __shared__ __align__(16) uint32_t s_words[kChunk * 4];  // the chunk's packed words (Occluder.cpp:153-156 layout)
 
+  pdl_trigger();
+  pdl_wait();
   const uint32_t tid = threadIdx.x, lane = tid & 31;
   const uint32_t nActive = P.header->activeChunks;
   for (uint32_t ai = blockIdx.x; ai < nActive; ai += gridDim.x) {
@@ -701,6 +789,8 @@ __global__ void __launch_bounds__(256) k_scan(FrameParams P, uint32_t numSt)
 {
   __shared__ uint32_t s_scan[8];
   __shared__ uint32_t s_last;
+  pdl_trigger();
+  pdl_wait();
   const uint32_t tid = threadIdx.x, lane = tid & 31;
   // the first numViews CTAs: one view each (its chunk totals, block scans);
   // the others: one warp per super-tile (its row of the count matrix).  Few
@@ -797,6 +887,8 @@ __global__ void __launch_bounds__(kChunk) k_fill(FrameParams P)
   extern __shared__ uint32_t s_dyn[];  // per union super-tile: 8 warp ballots + 8 warp prefixes
   __shared__ uint32_t s_rowLocal[kChunk];
   __shared__ int s_rect[4];
+  pdl_trigger();
+  pdl_wait();
   if (P.header->overflow) return;
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t nActive = P.header->activeChunks;
@@ -923,11 +1015,12 @@ __device__ __forceinline__ void walk_row(const FrameParams& P, const QuadRaster&
   }
 }
 
-__global__ void __launch_bounds__(256) k_walk(FrameParams P)
+// The row walk's part of k_walk_prep: CTA `cta` of `ctas`, 256 threads,
+// grid-striding over the batch's rows.
+__device__ __forceinline__ void walk_rows(const FrameParams& P, uint32_t cta, uint32_t ctas)
 {
-  if (P.header->overflow) return;
   const uint32_t total = P.header->totalRows;
-  for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < total; row += gridDim.x * blockDim.x) {
+  for (uint32_t row = cta * 256 + threadIdx.x; row < total; row += ctas * 256) {
     const uint2 own = P.rowOwner[row];
     const QuadRaster Q = P.rec[own.x];
     const QuadWalk Wk = P.walk[own.x];
@@ -1390,16 +1483,24 @@ __device__ __forceinline__ void raster_unit(const FrameParams& P, WarpRasterSmem
       for (int r = 0; r < RPL; ++r) d[r] = make_uint4(0, 0, 0, 0);
     }
   }
+  // the unit's block rows' minimum hiZ (its lanes are block-major, 8 R blocks)
+  {
+    uint32_t h = U.inView ? U.hiz : 0xFFFFu;
+#pragma unroll
+    for (int o = 1; o < 32 / R; o <<= 1) h = ::min(h, __shfl_xor_sync(0xFFFFFFFFu, h, o));
+    if (lane % (32 / R) == 0) V.tileHiz[4 * (size_t)lt + (rec.x & 3u) + lane / (32 / R)] = (uint16_t)h;
+  }
   if (kWins) count_wins<R>(P, V, U, lane);
 }
 
-// ---- k_tile_prep ----------------------------------------------------------------------
+// ---- tile preparation (k_walk_prep) --------------------------------------------------
 // One warp per warp-tile (8x4 blocks, one lane per block): applies the view's
 // clear (hiZ := 1, Rasterizer.cpp:107-121) to every block, then either queues
-// the tile's raster units of R block rows for k_raster (a quad of its
-// super-tile list reaches the unit; long lists are not checked) or finishes
-// them here: no quad touches them, so their hiZ is final (and with
-// kViewZeroDepth their depth is zeroed).
+// the tile's raster units of R block rows for the raster kernel (a quad of
+// its super-tile list reaches the unit; long lists are not checked) or
+// finishes them here: no quad touches them, so their hiZ is final (and with
+// kViewZeroDepth their depth is zeroed).  The block rows of the unqueued
+// units get their minimum hiZ here, the others from their raster unit.
 
 __device__ __forceinline__ uint32_t view_of_tile(const FrameParams& P, uint32_t wt)
 {
@@ -1418,12 +1519,24 @@ __device__ __forceinline__ uint32_t raster_rows(const FrameParams& P)
   return P.tune.rasterRows ? P.tune.rasterRows : kDefaultRasterRows;
 }
 
-__global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
+// Per-row minima of a warp-tile from one warp: `h` is this lane's block hiZ
+// (lane = row * 8 + column; 0xFFFF outside the view), rows `rows` (bit r =
+// row r) are stored.
+__device__ __forceinline__ void store_tile_rows(const ViewDesc& V, uint32_t lt, uint32_t h, uint32_t rows,
+                                                uint32_t lane)
+{
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) h = ::min(h, __shfl_xor_sync(0xFFFFFFFFu, h, o));
+  const uint32_t r = lane >> 3;
+  if ((lane & 7u) == 0 && ((rows >> r) & 1u)) V.tileHiz[4 * (size_t)lt + r] = (uint16_t)h;
+}
+
+// CTA `cta` of the tile preparation: warps over warp-tiles cta * 8 ...
+__device__ __forceinline__ void tile_prep(const FrameParams& P, uint32_t cta)
 {
   __shared__ uint32_t s_n, s_base;
-  if (P.header->overflow) return;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t wt = blockIdx.x * 8 + warp;
+  const uint32_t wt = cta * 8 + warp;
   const uint32_t R = raster_rows(P), units = kTileH / R, all = (1u << units) - 1u;
   if (threadIdx.x == 0) s_n = 0;
   __syncthreads();
@@ -1474,6 +1587,11 @@ __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
           d[1] = make_uint4(0, 0, 0, 0);
         }
     }
+    // rows of the units left unqueued are final: their minima now
+    uint32_t rows = 0;
+    for (uint32_t r = 0; r < (uint32_t)kTileH; ++r)
+      if (!((queue >> (r / R)) & 1u)) rows |= 1u << r;
+    if (rows) store_tile_rows(V, lt, inView ? (clearing ? 1u : (uint32_t)V.hiz[blk]) : 0xFFFFu, rows, lane);
     if (lane == 0 && queue) slot = atomicAdd(&s_n, (uint32_t)__popc(queue));
   }
   __syncthreads();
@@ -1486,21 +1604,16 @@ __global__ void __launch_bounds__(256) k_tile_prep(FrameParams P)
   }
 }
 
-// Per warp-tile minimum hiZ of every view (after rasterisation; the queries
-// skip a tile whose minimum is >= their depth).  One warp per tile.
-__global__ void __launch_bounds__(256) k_tile_min(FrameParams P)
+// The two stages between the list fill and the raster, in one launch: CTAs
+// [0, walkCtas) walk the batch's rows (grid-striding), the others prepare 8
+// warp-tiles each as the walk's CTAs retire.
+__global__ void __launch_bounds__(256) k_walk_prep(FrameParams P, uint32_t walkCtas)
 {
+  pdl_trigger();
+  pdl_wait();
   if (P.header->overflow) return;
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t wt = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (wt >= P.numTiles) return;
-  const ViewDesc& V = P.views[view_of_tile(P, wt)];
-  const uint32_t lt = wt - V.tileStart;
-  const uint32_t bx = (lt % V.tilesX) * kTileW + (lane & 7), by = (lt / V.tilesX) * kTileH + (lane >> 3);
-  uint32_t m = (bx < V.blocksX && by < V.blocksY) ? (uint32_t)V.hiz[by * V.blocksX + bx] : 0xFFFFu;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = ::min(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
-  if (lane == 0) V.tileHiz[lt] = (uint16_t)m;
+  if (blockIdx.x < walkCtas) walk_rows(P, blockIdx.x, walkCtas);
+  else tile_prep(P, blockIdx.x - walkCtas);
 }
 
 // ---- k_raster -------------------------------------------------------------------------
@@ -1512,6 +1625,8 @@ template <int R, bool kWins>
 __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks<R>) k_raster(FrameParams P)
 {
   __shared__ WarpRasterSmem S[kRasterWarps];
+  pdl_trigger();
+  pdl_wait();
   if (P.header->overflow) return;
   const uint32_t lane = threadIdx.x & 31;
   WarpRasterSmem& W = S[threadIdx.x >> 5];
@@ -1524,7 +1639,10 @@ __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks<R>) k_raster(
     uint32_t nxt = 0;
     if (lane == 0) nxt = atomicAdd(&P.header->tileCursor, chunk);  // next fetch, ahead of time
     const uint32_t end = ::min(i + chunk, nActive);
-    for (uint32_t j = i; j < end; ++j) raster_unit<R, kWins>(P, W, __ldg(P.activeTileList + j), lane);
+    for (uint32_t j = i; j < end; ++j) {
+      const uint4 rec = __ldg(P.activeTileList + j);
+      raster_unit<R, kWins>(P, W, rec, lane);
+    }
     i = __shfl_sync(0xFFFFFFFFu, nxt, 0);
   }
 }
@@ -1556,6 +1674,7 @@ struct CtaRasterSmem {
   uint32_t bmask[kCtaUnitBlocks][kCtaMaskWords];  // per block: fragment slots aimed at it
   uint32_t hiz[kCtaUnitBlocks];  // per block: current hiZ
   uint32_t scan[kCtaThreads / 32];
+  uint32_t rowMin[kCtaThreads / 32];  // per warp: minimum final hiZ of its 4 blocks
 };
 
 // Merges fragment slot `slot` into this thread's pixel row of its block (the
@@ -1755,6 +1874,12 @@ __device__ __forceinline__ void raster_unit_cta(const FrameParams& P, CtaRasterS
     if (have) *d = make_uint4(row[0], row[1], row[2], row[3]);
     else if (clearing && (V.flags & kViewZeroDepth)) *d = make_uint4(0, 0, 0, 0);
   }
+  {
+    uint32_t h = inView ? hiz : 0xFFFFu;
+#pragma unroll
+    for (int o = 8; o < 32; o <<= 1) h = ::min(h, __shfl_xor_sync(0xFFFFFFFFu, h, o));  // 4 blocks
+    if (lane == 0) S.rowMin[tid >> 5] = h;
+  }
   if (kWins) {
     // pixels won per command: one atomic per distinct command per warp when
     // every row has one owner (the common case), else per warp and pixel column
@@ -1795,6 +1920,8 @@ __global__ void __launch_bounds__(kCtaThreads, kCtaMinBlocks) k_raster_cta(Frame
   __shared__ CtaRasterSmem S;
   __shared__ uint32_t s_next;
   __shared__ __align__(16) uint4 s_rec[2];  // this unit's queue record and the next one's
+  pdl_trigger();
+  pdl_wait();
   if (P.header->overflow) return;
   const uint32_t nActive = P.header->activeTiles;
   const uint32_t chunk = P.tune.rasterChunk ? P.tune.rasterChunk : 1u;  // units per fetch
@@ -1824,6 +1951,12 @@ __global__ void __launch_bounds__(kCtaThreads, kCtaMinBlocks) k_raster_cta(Frame
       raster_unit_cta<kWins>(P, S, rec);
       if (threadIdx.x == 0) asm volatile("cp.async.wait_all;" ::: "memory");
       __syncthreads();  // shared state is reused by the next unit; the next record has landed
+      if (threadIdx.x < 2) {  // the unit's two block rows' minimum hiZ (warps 2r, 2r + 1)
+        const ViewDesc& V = P.views[rec.y];
+        const uint32_t r = threadIdx.x;
+        V.tileHiz[4 * (size_t)((rec.x >> 2) - V.tileStart) + (rec.x & 3u) + r] =
+            (uint16_t)::min(S.rowMin[2 * r], S.rowMin[2 * r + 1]);
+      }
       buf ^= 1u;
     }
     if (threadIdx.x == 0) s_next = nxt;
@@ -1832,8 +1965,8 @@ __global__ void __launch_bounds__(kCtaThreads, kCtaMinBlocks) k_raster_cta(Frame
   }
 }
 
-// Recomputes the per-warp-tile hiZ minimum of one view (after hiZ was written
-// from the host).  One warp per tile.
+// Recomputes the per-warp-tile row minima of one view's hiZ (after hiZ was
+// written from the host).  One warp per tile.
 __global__ void __launch_bounds__(128) k_tile_hiz(const uint16_t* hiz, uint16_t* tileHiz, uint32_t blocksX,
                                                   uint32_t blocksY, uint32_t tilesX, uint32_t tiles)
 {
@@ -1843,14 +1976,14 @@ __global__ void __launch_bounds__(128) k_tile_hiz(const uint16_t* hiz, uint16_t*
   const uint32_t bx = (t % tilesX) * kTileW + (lane & 7), by = (t / tilesX) * kTileH + (lane >> 3);
   uint32_t m = (bx < blocksX && by < blocksY) ? hiz[by * blocksX + bx] : 0xFFFFu;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = ::min(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
-  if (lane == 0) tileHiz[t] = (uint16_t)m;
+  for (int o = 1; o < 8; o <<= 1) m = ::min(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+  if ((lane & 7u) == 0) tileHiz[4 * (size_t)t + (lane >> 3)] = (uint16_t)m;  // per block row
 }
 
 // ---- k_query -------------------------------------------------------------------------
 
 // Front-end status -> visibility for boxes with small rectangles (query2D per
-// thread); `big` marks the ones left to query_big_boxes.  Small means at most
+// thread); `big` marks the ones left to the CTA's warps (collect_big).  Small means at most
 // a warp-tile's worth of blocks where the warp's lanes are full (kFull, the
 // survivor lists of k_query), at most two warp-tiles where many lanes idle.
 template <bool kFull>
@@ -1869,11 +2002,116 @@ __device__ __forceinline__ void query_resolve(const ViewDesc& V, int st, const u
       const uint32_t nty = (rect[3] >> 3) / kTileH - (rect[2] >> 3) / kTileH + 1;
       big = ntx * nty > 2;
     }
-    if (!big) vis = query2d(V, rect[0], rect[1], rect[2], rect[3], maxZ);
+    if (!big) vis = query2d<!kFull>(V, rect[0], rect[1], rect[2], rect[3], maxZ);
   }
 }
 
-// Boxes with large rectangles: the whole warp tests one box at a time, its
+// Boxes with large rectangles are collected per CTA and tested after the
+// CTA's other boxes by all of its warps, one box per warp at a time (a warp
+// testing its own large boxes one after the other would leave the few warps
+// holding several of them to set the stage's time).  All 32 lanes; a box that
+// does not fit the CTA's list is tested by its own warp at once (returns its
+// visibility in `vis`).
+constexpr uint32_t kBigPerCta = 256;
+
+struct BigBoxes {
+  uint4 box[kBigPerCta];  // {slot, minX | maxX << 16, minY | maxY << 16, maxZ}
+  uint32_t count, next;
+};
+
+__device__ __forceinline__ bool query_big_box(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_t minY,
+                                              uint32_t maxY, uint32_t mz, uint32_t lane);
+__device__ __forceinline__ uint32_t query_view(const FrameParams& P, uint32_t slot, uint32_t lo, uint32_t hi);
+
+__device__ __forceinline__ void collect_big(const FrameParams& P, BigBoxes& B, bool big, uint32_t slot,
+                                            uint32_t view, const uint32_t* rect, uint32_t maxZ, uint32_t lane,
+                                            bool& vis)
+{
+  const uint32_t m = __ballot_sync(0xFFFFFFFFu, big);
+  if (!m) return;
+  uint32_t base = 0;
+  if (lane == 0) base = atomicAdd(&B.count, (uint32_t)__popc(m));
+  base = __shfl_sync(0xFFFFFFFFu, base, 0);
+  const uint32_t at = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+  if (big && at < kBigPerCta)
+    B.box[at] = make_uint4(slot, rect[0] | (rect[1] << 16), rect[2] | (rect[3] << 16), maxZ);
+  uint32_t over = __ballot_sync(0xFFFFFFFFu, big && at >= kBigPerCta);
+  while (over) {
+    const int j = __ffs(over) - 1;
+    over &= over - 1;
+    const uint32_t r0 = __shfl_sync(0xFFFFFFFFu, rect[0], j), r1 = __shfl_sync(0xFFFFFFFFu, rect[1], j);
+    const uint32_t r2 = __shfl_sync(0xFFFFFFFFu, rect[2], j), r3 = __shfl_sync(0xFFFFFFFFu, rect[3], j);
+    const uint32_t mz = __shfl_sync(0xFFFFFFFFu, maxZ, j), vj = __shfl_sync(0xFFFFFFFFu, view, j);
+    const bool found = query_big_box(P.views[vj], r0, r1, r2, r3, mz, lane);
+    if ((int)lane == j) vis = found;
+  }
+}
+
+// After the CTA barrier that follows every collect_big: the warps take the
+// CTA's large boxes one at a time; a visible one sets bit (slot - slot0) of
+// the CTA's bit array `bits`.  All 32 lanes.
+__device__ __forceinline__ void test_big(const FrameParams& P, BigBoxes& B, uint32_t slot0, uint32_t* bits,
+                                         uint32_t lane)
+{
+  const uint32_t n = ::min(B.count, kBigPerCta);
+  for (;;) {
+    uint32_t i = 0;
+    if (lane == 0) i = atomicAdd(&B.next, 1u);
+    i = __shfl_sync(0xFFFFFFFFu, i, 0);
+    if (i >= n) break;
+    const uint4 e = B.box[i];
+    const ViewDesc& V = P.views[query_view(P, e.x, 0, P.numViews - 1)];
+    if (query_big_box(V, e.y & 0xFFFFu, e.y >> 16, e.z & 0xFFFFu, e.z >> 16, e.w, lane) && lane == 0)
+      atomicOr(bits + ((e.x - slot0) >> 5), 1u << (e.x & 31u));
+  }
+}
+
+// query2D of one box with a large rectangle by the whole warp: its
+// warp-tiles 32 at a time, one per lane, after their minimum hiZ (a tile whose
+// minimum is >= maxZ holds no block the reference would read).  When few of
+// the 32 tiles pass, each is then tested one block per lane (a tile has 8 x 4
+// = 32 blocks); when many pass, each lane tests its own tile's blocks in
+// sequence.  Returns the same on every lane.
+constexpr uint32_t kBigSplitMax = 4;  // tiles passing a round, at most, tested a block per lane
+
+__device__ __forceinline__ bool query_big_box(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_t minY,
+                                              uint32_t maxY, uint32_t mz, uint32_t lane)
+{
+  const uint32_t tilesX = (V.blocksX + kTileW - 1) / kTileW;
+  const uint32_t bx0 = minX >> 3, bx1 = maxX >> 3, by0 = minY >> 3, by1 = maxY >> 3;
+  const uint32_t tx0 = bx0 / kTileW, ty0 = by0 / kTileH;
+  const uint32_t ntx = bx1 / kTileW - tx0 + 1, nt = ntx * (by1 / kTileH - ty0 + 1);
+  for (uint32_t t0 = 0; t0 < nt; t0 += 32) {
+    const uint32_t t = t0 + lane;
+    uint32_t tx = 0, ty = 0;
+    uint2 rm = make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu);
+    bool open = false;
+    if (t < nt) {
+      tx = tx0 + t % ntx;
+      ty = ty0 + t / ntx;
+      rm = tile_rows(V, ty * tilesX + tx);
+      open = mz > tile_min(rm);
+    }
+    uint32_t openMask = __ballot_sync(0xFFFFFFFFu, open);
+    if ((uint32_t)__popc(openMask) > kBigSplitMax) {
+      const bool hit = open && query2d_tile<true>(V, tx, ty, rm, minX, maxX, minY, maxY, mz);
+      if (__ballot_sync(0xFFFFFFFFu, hit)) return true;
+      continue;
+    }
+    while (openMask) {
+      const uint32_t tt = t0 + (uint32_t)(__ffs(openMask) - 1);
+      openMask &= openMask - 1;
+      const uint32_t bx = (tx0 + tt % ntx) * kTileW + (lane & (kTileW - 1));
+      const uint32_t by = (ty0 + tt / ntx) * kTileH + lane / kTileW;
+      const bool hit = bx >= bx0 && bx <= bx1 && by >= by0 && by <= by1 &&
+                       query2d_block<true>(V, bx, by, minX, maxX, minY, maxY, mz);
+      if (__ballot_sync(0xFFFFFFFFu, hit)) return true;
+    }
+  }
+  return false;
+}
+
+// Boxes with large rectangles in k_query: the whole warp tests one box at a time, its
 // warp-tiles 32 at a time, one per lane, after their minimum hiZ (a tile whose
 // minimum is >= maxZ holds no block the reference would read).  kSplit: each
 // tile that passes is then tested one block per lane (a tile has 8 x 4 = 32
@@ -1902,8 +2140,9 @@ __device__ __forceinline__ void query_big_boxes(const FrameParams& P, bool big, 
       bool open = false;
       if (t < nt) {
         const uint32_t tx = tx0 + t % ntx, ty = ty0 + t / ntx;
-        open = mz > (uint32_t)V.tileHiz[ty * tilesX + tx];
-        if (!kSplit && open) open = query2d_tile(V, tx, ty, minX, maxX, minY, maxY, mz);
+        const uint2 rm = tile_rows(V, ty * tilesX + tx);
+        open = mz > tile_min(rm);
+        if (!kSplit && open) open = query2d_tile<false>(V, tx, ty, rm, minX, maxX, minY, maxY, mz);
       }
       if (!kSplit) {
         found = __ballot_sync(0xFFFFFFFFu, open) != 0;
@@ -1916,7 +2155,7 @@ __device__ __forceinline__ void query_big_boxes(const FrameParams& P, bool big, 
         const uint32_t bx = (tx0 + tt % ntx) * kTileW + (lane & (kTileW - 1));
         const uint32_t by = (ty0 + tt / ntx) * kTileH + lane / kTileW;
         const bool hit = bx >= bx0 && bx <= bx1 && by >= by0 && by <= by1 &&
-                         query2d_block(V, bx, by, minX, maxX, minY, maxY, mz);
+                         query2d_block<false>(V, bx, by, minX, maxX, minY, maxY, mz);
         found = __ballot_sync(0xFFFFFFFFu, hit) != 0;
       }
     }
@@ -1937,27 +2176,42 @@ __device__ __forceinline__ uint32_t query_view(const FrameParams& P, uint32_t sl
 // One thread per query slot, the whole front end and query2D in place: the
 // fastest form when there are too few slots to keep the GPU busy after
 // compaction (a single view's 100k boxes).
-__global__ void __launch_bounds__(256, 6) k_query_thread(FrameParams P)
+__global__ void __launch_bounds__(256, 4) k_query_thread(FrameParams P)
 {
-  if (P.header->overflow) return;
+  __shared__ BigBoxes s_big;
+  __shared__ uint32_t s_vis[8];
+  pdl_trigger();
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_big.count = s_big.next = 0;
+  if (threadIdx.x < 8) s_vis[threadIdx.x] = 0;
   bool vis = false, nc = false, big = false;
   uint32_t rect[4] = {0, 0, 0, 0}, maxZ = 0, view = 0;
+  // the box's projection reads only the view table and the boxes, written
+  // before the launch: it runs while the raster finishes
+  int st = 0;
+  bool have = false;
   if (slot < P.numQuerySlots) {
     view = query_view(P, slot, 0, P.numViews - 1);
     const ViewDesc& V = P.views[view];
     if (slot - V.queryStart < V.queryCount) {
       const float4 a = P.qmin[slot], b = P.qmax[slot];
       const float bmin[4] = {a.x, a.y, a.z, a.w}, bmax[4] = {b.x, b.y, b.z, b.w};
-      const int st = query_front(V, bmin, bmax, rect, &maxZ);
-      query_resolve<false>(V, st, rect, maxZ, vis, nc, big);
+      st = query_front(V, bmin, bmax, rect, &maxZ);
+      have = true;
     }
   }
-  query_big_boxes<false>(P, big, rect, maxZ, view, lane, vis);
+  pdl_wait();
+  if (P.header->overflow) return;  // the same for every thread
+  __syncthreads();                 // s_big and s_vis set
+  if (have) query_resolve<false>(P.views[view], st, rect, maxZ, vis, nc, big);
+  collect_big(P, s_big, big, slot, view, rect, maxZ, lane, vis);
   const uint32_t vb = __ballot_sync(0xFFFFFFFFu, vis), nb = __ballot_sync(0xFFFFFFFFu, nc);
+  __syncthreads();
+  test_big(P, s_big, blockIdx.x * blockDim.x, s_vis, lane);
+  __syncthreads();
   if (lane == 0 && slot < P.numQuerySlots) {
-    P.visBits[slot >> 5] = vb;
+    P.visBits[slot >> 5] = vb | s_vis[warp];
     P.ncBits[slot >> 5] = nb;
   }
 }
@@ -1973,7 +2227,7 @@ __global__ void __launch_bounds__(256, 6) k_query(FrameParams P, uint32_t rounds
 {
   __shared__ uint32_t s_slot[8][32 * kQueryRounds], s_view[8][32 * kQueryRounds];
   __shared__ uint32_t s_vis[8][kQueryRounds], s_nc[8][kQueryRounds];
-  if (P.header->overflow) return;
+  pdl_trigger();
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t first = ((gridDim.x - 1 - blockIdx.x) * 8 + warp) * 32 * rounds;
   if (first >= P.numQuerySlots) return;
@@ -2010,6 +2264,10 @@ __global__ void __launch_bounds__(256, 6) k_query(FrameParams P, uint32_t rounds
     }
     n += (uint32_t)__popc(m);
   }
+  // the frustum tests above read only the view table and the boxes, written
+  // before the launch; the rest reads the rasterised hiZ
+  pdl_wait();
+  if (P.header->overflow) return;
   __syncwarp();
   for (uint32_t base = 0; base < n; base += 32) {
     const uint32_t k = base + lane;
@@ -2050,7 +2308,7 @@ __global__ void __launch_bounds__(256, 6) k_query(FrameParams P, uint32_t rounds
 __global__ void k_query2d(const ViewDesc* V, uint32_t minX, uint32_t maxX, uint32_t minY, uint32_t maxY,
                           uint32_t maxZ, uint32_t* out)
 {
-  *out = query2d(*V, minX, maxX, minY, maxY, maxZ) ? 1u : 0u;
+  *out = query2d<true>(*V, minX, maxX, minY, maxY, maxZ) ? 1u : 0u;
 }
 
 // ---- readBackDepth (Rasterizer.cpp:351-399) ---------------------------------------------
@@ -2115,6 +2373,25 @@ struct StageRanges {
   }
 };
 
+// Launches `kernel` on `stream`; with `pdl`, as a programmatic dependent of
+// the kernel before it (pdl_trigger / pdl_wait).
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_k(bool pdl, void (*kernel)(KArgs...), uint32_t grid, uint32_t block, size_t smem,
+                            cudaStream_t stream, Args... args)
+{
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1u : 0u;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t maxStPerView, bool doRaster,
                                 bool doQuery, cudaStream_t stream, cudaEvent_t* ev)
 {
@@ -2123,55 +2400,70 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
     if (ev) cudaEventRecord(ev[i], stream);
     ranges.next(i);
   };
+  // the first kernel follows the counter reset (a memset) in plain stream
+  // order; each later one is a programmatic dependent of the kernel before it
+  // (none when events are recorded between the stages)
+  bool chained = false;
+  cudaError_t e = cudaSuccess;
+  auto go = [&](cudaError_t r) {
+    if (e == cudaSuccess) e = r;
+    chained = g_pdl && ev == nullptr;
+  };
   mark(0);
-  if (doRaster) {
+  if (doRaster || doQuery) {
     // activeChunks, activeTiles, tileCursor
-    cudaError_t e = cudaMemsetAsync(&P.header->activeChunks, 0, 3 * sizeof(uint32_t), stream);
+    e = cudaMemsetAsync(&P.header->activeChunks, 0, kHeaderResetWords * sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
+  }
+  if (doRaster) {
     if (P.numChunks) {
-      if (P.phase) k_gate_second<<<(P.numCmds + 7) / 8, 256, 0, stream>>>(P);
-      else if (!P.fusedSelect) k_gate<<<(P.numCmds + 255) / 256, 256, 0, stream>>>(P);  // else k_select_view did
-      k_chunk_gate<<<P.numViews, 256, 0, stream>>>(P);
-      k_setup<<<grid_of(P.tune.setupPerSm, g_setupPerSm, P.numChunks), kChunk,
-                (size_t)maxStPerView * sizeof(uint32_t), stream>>>(P);
+      if (P.phase) go(launch_k(chained, k_gate_second, (P.numCmds + 7) / 8, 256, 0, stream, P));
+      else if (!P.fusedSelect) go(launch_k(chained, k_gate, (P.numCmds + 255) / 256, 256, 0, stream, P));
+      // (with fusedSelect, k_select_view did the gating)
+      go(launch_k(chained, k_chunk_gate, P.numViews, 256, 0, stream, P));
+      go(launch_k(chained, k_setup, grid_of(P.tune.setupPerSm, g_setupPerSm, P.numChunks), kChunk,
+                  (size_t)maxStPerView * sizeof(uint32_t), stream, P));
     }
   }
   mark(1);
-  if (doRaster) k_scan<<<P.numViews + ::max(1u, ::min((numSt + 7) / 8, 4 * g_sms)), 256, 0, stream>>>(P, numSt);
+  if (doRaster)
+    go(launch_k(chained, k_scan, P.numViews + ::max(1u, ::min((numSt + 7) / 8, 4 * g_sms)), 256, 0, stream, P,
+                numSt));
   mark(2);
   if (doRaster && P.numChunks)
-    k_fill<<<grid_of(P.tune.fillPerSm, g_fillPerSm, P.numChunks), kChunk, (size_t)maxStPerView * 64, stream>>>(P);
+    go(launch_k(chained, k_fill, grid_of(P.tune.fillPerSm, g_fillPerSm, P.numChunks), kChunk,
+                (size_t)maxStPerView * 64, stream, P));
   mark(3);
-  if (doRaster && P.numChunks)
-    k_walk<<<P.tune.walkPerSm ? P.tune.walkPerSm * g_sms : g_walkBlocks, 256, 0, stream>>>(P);
+  // raster form: a warp per unit of R block rows, or a CTA per 8x2 unit when
+  // the launch has few units (a warp would leave most of the GPU idle and
+  // long lists in sequence)
+  FrameParams Q = P;
+  uint32_t threads = P.tune.rasterThreads;
+  if (!threads) threads = P.numTiles * 2u < 4u * g_sms * g_rasterPerSm[1] * kRasterWarps ? 128u : 32u;
+  Q.tune.rasterThreads = threads;
+  Q.tune.rasterRows = threads == 128u ? 2u : (P.tune.rasterRows ? P.tune.rasterRows : kDefaultRasterRows);
+  if (doRaster && (P.numChunks || P.numTiles)) {
+    // tile preparation and the row walk, one launch
+    const uint32_t prep = (Q.numTiles + 7) / 8;
+    const uint32_t walk = P.numChunks ? (P.tune.walkPerSm ? P.tune.walkPerSm * g_sms : g_walkBlocks) : 0u;
+    go(launch_k(chained, k_walk_prep, walk + prep, 256, 0, stream, Q, walk));
+  }
   mark(4);
   if (doRaster && P.numTiles) {
-    // raster form: a warp per unit of R block rows, or a CTA per 8x2 unit when
-    // the launch has few units (a warp would leave most of the GPU idle and
-    // long lists in sequence)
-    FrameParams Q = P;
-    uint32_t threads = P.tune.rasterThreads;
-    if (!threads) threads = P.numTiles * 2u < 4u * g_sms * g_rasterPerSm[1] * kRasterWarps ? 128u : 32u;
-    Q.tune.rasterThreads = threads;
-    Q.tune.rasterRows = threads == 128u ? 2u : (P.tune.rasterRows ? P.tune.rasterRows : kDefaultRasterRows);
-    k_tile_prep<<<(Q.numTiles + 7) / 8, 256, 0, stream>>>(Q);
     const uint32_t R = Q.tune.rasterRows;
     const uint32_t units = Q.numTiles * (kTileH / R);
     const bool w = Q.wins != nullptr;
     if (threads == 128u) {
       const uint32_t grid = grid_of(Q.tune.rasterPerSm, g_rasterCtaPerSm, units);
-      w ? k_raster_cta<true><<<grid, kCtaThreads, 0, stream>>>(Q) : k_raster_cta<false><<<grid, kCtaThreads, 0, stream>>>(Q);
+      go(launch_k(chained, w ? k_raster_cta<true> : k_raster_cta<false>, grid, kCtaThreads, 0, stream, Q));
     } else {
       const uint32_t shape = R == 1 ? 0u : (R == 2 ? 1u : 2u);
       const uint32_t grid = grid_of(Q.tune.rasterPerSm, g_rasterPerSm[shape], (units + kRasterWarps - 1) / kRasterWarps);
-      if (R == 1) w ? k_raster<1, true><<<grid, kRasterThreads, 0, stream>>>(Q)
-                    : k_raster<1, false><<<grid, kRasterThreads, 0, stream>>>(Q);
-      else if (R == 4) w ? k_raster<4, true><<<grid, kRasterThreads, 0, stream>>>(Q)
-                         : k_raster<4, false><<<grid, kRasterThreads, 0, stream>>>(Q);
-      else w ? k_raster<2, true><<<grid, kRasterThreads, 0, stream>>>(Q)
-             : k_raster<2, false><<<grid, kRasterThreads, 0, stream>>>(Q);
+      void (*k)(FrameParams) = R == 1 ? (w ? k_raster<1, true> : k_raster<1, false>)
+                               : R == 4 ? (w ? k_raster<4, true> : k_raster<4, false>)
+                                        : (w ? k_raster<2, true> : k_raster<2, false>);
+      go(launch_k(chained, k, grid, kRasterThreads, 0, stream, Q));
     }
-    k_tile_min<<<(P.numTiles + 7) / 8, 256, 0, stream>>>(P);
   }
   mark(5);
   if (doQuery && P.numQuerySlots) {
@@ -2180,12 +2472,13 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
     if (rounds == 0)  // by slot count: the warp lists pay once the slots fill the GPU a few times over
       rounds = ctas < 4 * wave ? kQueryPerThread : ::min(kQueryRounds, ::max(1u, ctas / (6 * wave)));
     if (rounds == kQueryPerThread || rounds > kQueryRounds)
-      k_query_thread<<<ctas, 256, 0, stream>>>(P);
+      go(launch_k(chained, k_query_thread, ctas, 256, 0, stream, P));
     else
-      k_query<<<(ctas + rounds - 1) / rounds, 256, 0, stream>>>(P, rounds);
+      go(launch_k(chained, k_query, (ctas + rounds - 1) / rounds, 256, 0, stream, P, rounds));
   }
 
   mark(6);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
@@ -2234,6 +2527,8 @@ cudaError_t set_kernel_attributes()
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
   g_sms = (uint32_t)sms;
   g_walkBlocks = (uint32_t)sms * 8;
+  const char* pdl = getenv("OCC_PDL");
+  g_pdl = !(pdl && pdl[0] == '0');
   cudaError_t e = cudaFuncSetAttribute(k_setup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 4));
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kMaxStPerView * 64));
@@ -2351,7 +2646,7 @@ __global__ void __launch_bounds__(256) k_query_noalloc(NoAllocScratch* S, uint32
       vis = true;
       nc = true;
     } else if (st == 2) {
-      vis = query2d(V, rect[0], rect[1], rect[2], rect[3], maxZ);
+      vis = query2d<true>(V, rect[0], rect[1], rect[2], rect[3], maxZ);
     }
   }
   const uint32_t vb = __ballot_sync(0xFFFFFFFFu, vis), nb = __ballot_sync(0xFFFFFFFFu, nc);

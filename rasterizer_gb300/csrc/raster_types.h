@@ -49,7 +49,8 @@ enum : int {
 struct ViewDesc {
   uint16_t* depth;   // width*height u16, 8x8 blocks of 8 rows x 8 pixels, block-major
   uint16_t* hiz;     // blocks + 8
-  uint16_t* tileHiz; // per warp-tile (8x4 blocks, row-major): min of the tile's hiZ values
+  uint16_t* tileHiz; // per warp-tile (8x4 blocks, row-major), 4 entries: the minimum hiZ of
+                     // each of its block rows (0xFFFF for rows outside the view)
   uint32_t width, height, blocksX, blocksY;
   float cols[16];    // prebaked matrix columns (Rasterizer.cpp:91-104)
   float rows[16];    // rows of the transposed input matrix (frustum planes)
@@ -137,6 +138,7 @@ struct FrameHeader {
   uint32_t tileCursor;    // next entry of the active tile list (k_raster)
   uint32_t pad2;
 };
+constexpr uint32_t kHeaderResetWords = 3;  // activeChunks, activeTiles, tileCursor
 
 // One occluder of a GPU bake: vertexCount float4 (a multiple of 32) from
 // vertexStart in the launch's vertex array, quantised in [refMin, refMax].
