@@ -442,9 +442,10 @@ int run_batch(occ_ctx_s* ctx, FrameScratch& S, std::vector<ViewJob>& jobs, bool 
     P.views = reinterpret_cast<const ViewDesc*>(S.tables.p + offViews);
     P.numViews = nv;
     P.numCmds = (uint32_t)L.cmds.size();
+    for (const auto& Vd : L.views) P.maxViewCmds = std::max(P.maxViewCmds, Vd.cmdCount);
     P.matSize = L.matSize;
     P.activeChunkList = S.activeChunks.p;
-    P.viewActiveChunks = S.viewActive.p;
+    P.chunkRank = S.viewActive.p;
     P.viewActiveCount = S.viewActiveCount.p;
     P.activeTileList = S.activeTiles.p;
     P.cmds = reinterpret_cast<const Cmd*>(S.tables.p + offCmds);
@@ -1138,9 +1139,10 @@ int capture(occ_batch_s* b)
   P.views = reinterpret_cast<const ViewDesc*>(S.tables.p);
   P.numViews = (uint32_t)b->L.views.size();
   P.numCmds = (uint32_t)b->L.cmds.size();
+  for (const auto& Vd : b->L.views) P.maxViewCmds = std::max(P.maxViewCmds, Vd.cmdCount);
   P.matSize = b->L.matSize;
   P.activeChunkList = S.activeChunks.p;
-    P.viewActiveChunks = S.viewActive.p;
+    P.chunkRank = S.viewActive.p;
     P.viewActiveCount = S.viewActiveCount.p;
   P.activeTileList = S.activeTiles.p;
   P.cmds = reinterpret_cast<const Cmd*>(S.tables.p + b->offCmds);

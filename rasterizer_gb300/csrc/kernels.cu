@@ -64,14 +64,15 @@ static uint32_t grid_of(uint32_t tuned, uint32_t limit, uint32_t work)
 }
 
 // Programmatic dependent launch.  Every kernel of a flush after the first is
-// launched with programmatic stream serialisation: it is scheduled once all
-// CTAs of its predecessor have started (pdl_trigger at the top of every
-// kernel), so its launch and whatever it does before pdl_wait overlap the
-// predecessor's tail.  pdl_wait returns when the predecessor grid has
-// completed and its memory operations are visible; nothing a predecessor
-// writes is read before it.  Launched without the attribute, both return at
-// once.  The environment variable OCC_PDL=0 launches every kernel plainly.
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+// launched with programmatic stream serialisation: it is scheduled as the
+// CTAs of its predecessor exit, before that grid has completed, so its launch
+// and whatever it does before pdl_wait overlap the predecessor's last CTAs.
+// pdl_wait returns when the predecessor grid has completed and its memory
+// operations are visible; nothing a predecessor writes is read before it.
+// (No kernel signals its dependents earlier: CTAs waiting in pdl_wait slow
+// the ones still working on their SM.)  Launched without the attribute,
+// pdl_wait returns at once.  The environment variable OCC_PDL=0 launches
+// every kernel plainly.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 static bool g_pdl = true;
@@ -571,12 +572,8 @@ __device__ __forceinline__ uint32_t nck_of(const QuadRaster& R)
 // camera plane.  With a selection, commands outside the view's top-K are not
 // drawn.
 
-__global__ void __launch_bounds__(256) k_gate(FrameParams P)
+__device__ __forceinline__ void gate_cmd(const FrameParams& P, uint32_t c)
 {
-  pdl_trigger();
-  pdl_wait();
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= P.numCmds) return;
   const Cmd& cmd = P.cmds[c];
   const ViewDesc& V = P.views[cmd.view];
   uint32_t draw = 1, nc = (cmd.flags & kCmdNearClip) ? 1u : 0u;
@@ -590,13 +587,19 @@ __global__ void __launch_bounds__(256) k_gate(FrameParams P)
   P.cmdDraw[c] = draw | (nc << 1);
 }
 
+__global__ void __launch_bounds__(256) k_gate(FrameParams P)
+{
+  pdl_wait();
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < P.numCmds) gate_cmd(P, c);
+}
+
 // Second pass of a selection, one warp per command: a candidate left out of
 // the top-K is drawn if its bounds are still visible against the first pass's
 // buffer (queryVisibility, as the reference's loop runs it before each
 // rasterize, Main.cpp:192-206).  The lanes share the query2D over warp-tiles.
 __global__ void __launch_bounds__(256) k_gate_second(FrameParams P)
 {
-  pdl_trigger();
   pdl_wait();
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t c = blockIdx.x * 8 + (threadIdx.x >> 5);
@@ -632,32 +635,41 @@ __global__ void __launch_bounds__(256) k_gate_second(FrameParams P)
   if (lane == 0) P.cmdDraw[c] = draw | (nc << 1) | (first << 2);
 }
 
-// One thread per chunk: chunks with a drawn command go to the active list (in
-// any order: a chunk's outputs do not depend on where it is processed); the
-// others contribute no rows, checkpoints or list entries.
-__global__ void __launch_bounds__(256) k_chunk_gate(FrameParams P)
+// One CTA per view, one thread per chunk: chunks with a drawn command go to
+// the active list (in any order: a chunk's outputs do not depend on where it
+// is processed) and get their rank among the view's active chunks (chunk
+// order), which indexes their totals and count-matrix columns; the others
+// contribute no rows, checkpoints or list entries.
+// With `gate` (views of at most kChunkGateThreads commands, no selection
+// pass), the CTA first gates the view's commands itself, one per thread, in
+// place of k_gate.
+constexpr uint32_t kChunkGateThreads = 1024;
+
+__global__ void __launch_bounds__(kChunkGateThreads) k_chunk_gate(FrameParams P, uint32_t gate)
 {
-  __shared__ uint32_t s_scan[8];
+  __shared__ uint32_t s_scan[kChunkGateThreads / 32];
   __shared__ uint32_t s_base;
-  pdl_trigger();
   pdl_wait();
   const uint32_t v = blockIdx.x, tid = threadIdx.x;
   const ViewDesc& V = P.views[v];
+  if (gate) {
+    if (tid < V.cmdCount) gate_cmd(P, V.cmdStart + tid);
+    __syncthreads();  // the CTA's cmdDraw stores, visible to its threads
+  }
   uint32_t n = 0;
-  for (uint32_t i0 = 0; i0 < V.chunkCount; i0 += 256) {
+  for (uint32_t i0 = 0; i0 < V.chunkCount; i0 += kChunkGateThreads) {
     const uint32_t i = i0 + tid, c = V.chunkStart + i;
     bool active = false;
     if (i < V.chunkCount) {
       const Chunk ch = P.chunks[c];
       for (uint32_t k = 0; k < ch.cmdCount && !active; ++k) active = (P.cmdDraw[ch.cmdFirst + k] & 1u) != 0;
-      if (!active) P.chunkTot[c] = Totals{0, 0, 0, 0};
     }
     uint32_t tot;
-    const uint32_t ex = block_exclusive_scan<256>(active ? 1u : 0u, tot, s_scan);
+    const uint32_t ex = block_exclusive_scan<kChunkGateThreads>(active ? 1u : 0u, tot, s_scan);
     if (tid == 0 && tot) s_base = atomicAdd(&P.header->activeChunks, tot);
     __syncthreads();
     if (active) {
-      P.viewActiveChunks[V.chunkStart + n + ex] = i;
+      P.chunkRank[c] = n + ex;
       P.activeChunkList[s_base + ex] = c;
     }
     n += tot;
@@ -676,7 +688,6 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
   __shared__ uint32_t s_scan[kChunk / 32];
   __shared__ __align__(16) uint32_t s_words[kChunk * 4];  // the chunk's packed words (Occluder.cpp:153-156 layout)
 
-  pdl_trigger();
   pdl_wait();
   const uint32_t tid = threadIdx.x, lane = tid & 31;
   const uint32_t nActive = P.header->activeChunks;
@@ -684,6 +695,7 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
     const uint32_t c = P.activeChunkList[ai];
     const Chunk ch = P.chunks[c];
     const ViewDesc& V = P.views[ch.view];
+    const uint32_t rank = P.chunkRank[c];
     const uint32_t nst = V.stX * V.stY;
     for (uint32_t i = tid; i < nst; i += kChunk) s_stCount[i] = 0;
     if (tid < ch.cmdCount) {
@@ -762,8 +774,8 @@ __global__ void __launch_bounds__(kChunk) k_setup(FrameParams P)
       }
     }
     __syncthreads();
-    for (uint32_t st = tid; st < nst; st += kChunk) P.mat[V.matBase + st * V.chunkCount + ch.localIndex] = s_stCount[st];
-    if (tid == 0) P.chunkTot[c] = Totals{totRows, totCks, 0, 0};
+    for (uint32_t st = tid; st < nst; st += kChunk) P.mat[V.matBase + st * V.chunkCount + rank] = s_stCount[st];
+    if (tid == 0) P.chunkTot[V.chunkStart + rank] = Totals{totRows, totCks, 0, 0};
     __syncthreads();  // shared arrays are reused by the next chunk
   }
 }
@@ -789,7 +801,6 @@ __global__ void __launch_bounds__(256) k_scan(FrameParams P, uint32_t numSt)
 {
   __shared__ uint32_t s_scan[8];
   __shared__ uint32_t s_last;
-  pdl_trigger();
   pdl_wait();
   const uint32_t tid = threadIdx.x, lane = tid & 31;
   // the first numViews CTAs: one view each (its chunk totals, block scans);
@@ -798,14 +809,15 @@ __global__ void __launch_bounds__(256) k_scan(FrameParams P, uint32_t numSt)
   if (blockIdx.x < P.numViews) {
     const uint32_t v = blockIdx.x;
     const ViewDesc& V = P.views[v];
+    const uint32_t na = V.chunkCount ? P.viewActiveCount[v] : 0u;  // active chunks, by rank
     uint32_t carryR = 0, carryC = 0;
-    for (uint32_t i0 = 0; i0 < V.chunkCount; i0 += 256) {
+    for (uint32_t i0 = 0; i0 < na; i0 += 256) {
       const uint32_t i = i0 + tid;
-      const Totals t = i < V.chunkCount ? P.chunkTot[V.chunkStart + i] : Totals{0, 0, 0, 0};
+      const Totals t = i < na ? P.chunkTot[V.chunkStart + i] : Totals{0, 0, 0, 0};
       uint32_t totR, totC;
       const uint32_t exR = block_exclusive_scan<256>(t.rows, totR, s_scan);
       const uint32_t exC = block_exclusive_scan<256>(t.cks, totC, s_scan);
-      if (i < V.chunkCount) P.chunkBase[V.chunkStart + i] = Totals{carryR + exR, carryC + exC, 0, 0};
+      if (i < na) P.chunkBase[V.chunkStart + i] = Totals{carryR + exR, carryC + exC, 0, 0};
       carryR += totR;
       carryC += totC;
     }
@@ -819,19 +831,26 @@ __global__ void __launch_bounds__(256) k_scan(FrameParams P, uint32_t numSt)
       if (P.views[mid].stBase <= b) lo = mid; else hi = mid - 1;
     }
     const ViewDesc& V = P.views[lo];
-    // the row over the view's active chunks only, in chunk order (the other
-    // entries are neither written nor read)
+    // the row over the view's active chunks, by rank (chunk order); the other
+    // entries are neither written nor read.  128 entries a step: four
+    // coalesced loads in flight, then four warp scans.
     uint32_t* m = P.mat + V.matBase + (b - V.stBase) * V.chunkCount;
-    const uint32_t* act = P.viewActiveChunks + V.chunkStart;
     const uint32_t na = V.chunkCount ? P.viewActiveCount[lo] : 0u;
     uint32_t carry = 0;
-    for (uint32_t i0 = 0; i0 < na; i0 += 32) {
-      const uint32_t i = i0 + lane;
-      const uint32_t idx = i < na ? act[i] : 0u;
-      const uint32_t v = i < na ? m[idx] : 0u;
-      const uint32_t inc = warp_inclusive_scan(v, lane);
-      if (i < na) m[idx] = carry + inc - v;
-      carry += __shfl_sync(0xFFFFFFFFu, inc, 31);
+    for (uint32_t i0 = 0; i0 < na; i0 += 128) {
+      uint32_t x[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t i = i0 + 32 * k + lane;
+        x[k] = i < na ? m[i] : 0u;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t i = i0 + 32 * k + lane;
+        const uint32_t inc = warp_inclusive_scan(x[k], lane);
+        if (i < na) m[i] = carry + inc - x[k];
+        carry += __shfl_sync(0xFFFFFFFFu, inc, 31);
+      }
     }
     if (lane == 0) P.stLen[b] = carry;
   }
@@ -887,7 +906,6 @@ __global__ void __launch_bounds__(kChunk) k_fill(FrameParams P)
   extern __shared__ uint32_t s_dyn[];  // per union super-tile: 8 warp ballots + 8 warp prefixes
   __shared__ uint32_t s_rowLocal[kChunk];
   __shared__ int s_rect[4];
-  pdl_trigger();
   pdl_wait();
   if (P.header->overflow) return;
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -896,10 +914,12 @@ __global__ void __launch_bounds__(kChunk) k_fill(FrameParams P)
     const uint32_t c = P.activeChunkList[ai];
     const Chunk ch = P.chunks[c];
     const ViewDesc& V = P.views[ch.view];
+    const uint32_t rank = P.chunkRank[c];
     const uint32_t q = (c << kChunkShift) + tid;
     const QuadRaster R = P.rec[q];
     const bool valid = tid < ch.quadCount && R.minX < R.maxX;
-    const uint32_t ckChunk = P.viewBase[ch.view].cks + P.chunkBase[c].cks;
+    const Totals cb = P.chunkBase[V.chunkStart + rank];
+    const uint32_t ckChunk = P.viewBase[ch.view].cks + cb.cks;
     if (valid) P.ckBase[q] = ckChunk + R.ckLocal;
     s_rowLocal[tid] = P.walk[q].rowLocal;  // this thread's quad only
     if (tid == 0) {
@@ -929,7 +949,10 @@ __global__ void __launch_bounds__(kChunk) k_fill(FrameParams P)
     }
     __syncthreads();
     for (int u = tid; u < nu; u += kChunk) {
-      uint32_t acc = 0;
+      // the chunk's first entry in super-tile u's list (one load latency for
+      // all of them), plus the warps before
+      const uint32_t st = (uint32_t)(uy0 + u / uw) * V.stX + (uint32_t)(ux0 + u % uw);
+      uint32_t acc = P.stStart[V.stBase + st] + P.mat[V.matBase + st * V.chunkCount + rank];
 #pragma unroll
       for (int w = 0; w < 8; ++w) {
         s_pre[u * 8 + w] = acc;
@@ -944,14 +967,12 @@ __global__ void __launch_bounds__(kChunk) k_fill(FrameParams P)
       for (int sy = sy0; sy <= sy1; ++sy)
         for (int sx = sx0; sx <= sx1; ++sx) {
           const int u = (sy - uy0) * uw + (sx - ux0);
-          const uint32_t rank = s_pre[u * 8 + warp] + __popc(s_bal[u * 8 + warp] & lt);
-          const uint32_t st = (uint32_t)sy * V.stX + (uint32_t)sx;
-          P.stList[P.stStart[V.stBase + st] + P.mat[V.matBase + st * V.chunkCount + ch.localIndex] + rank] = entry;
+          P.stList[s_pre[u * 8 + warp] + __popc(s_bal[u * 8 + warp] & lt)] = entry;
         }
     }
     // rows of this chunk's quads -> (quad, row) entries for the row walk
     if (valid) {
-      const uint32_t rowG = P.viewBase[ch.view].rows + P.chunkBase[c].rows + s_rowLocal[tid];
+      const uint32_t rowG = P.viewBase[ch.view].rows + cb.rows + s_rowLocal[tid];
       const uint32_t rows = (uint32_t)(R.maxY - R.minY);
       for (uint32_t i = 0; i < rows; ++i) P.rowOwner[rowG + i] = make_uint2(q, i);
     }
@@ -1609,7 +1630,6 @@ __device__ __forceinline__ void tile_prep(const FrameParams& P, uint32_t cta)
 // warp-tiles each as the walk's CTAs retire.
 __global__ void __launch_bounds__(256) k_walk_prep(FrameParams P, uint32_t walkCtas)
 {
-  pdl_trigger();
   pdl_wait();
   if (P.header->overflow) return;
   if (blockIdx.x < walkCtas) walk_rows(P, blockIdx.x, walkCtas);
@@ -1625,7 +1645,6 @@ template <int R, bool kWins>
 __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks<R>) k_raster(FrameParams P)
 {
   __shared__ WarpRasterSmem S[kRasterWarps];
-  pdl_trigger();
   pdl_wait();
   if (P.header->overflow) return;
   const uint32_t lane = threadIdx.x & 31;
@@ -1920,7 +1939,6 @@ __global__ void __launch_bounds__(kCtaThreads, kCtaMinBlocks) k_raster_cta(Frame
   __shared__ CtaRasterSmem S;
   __shared__ uint32_t s_next;
   __shared__ __align__(16) uint4 s_rec[2];  // this unit's queue record and the next one's
-  pdl_trigger();
   pdl_wait();
   if (P.header->overflow) return;
   const uint32_t nActive = P.header->activeTiles;
@@ -2180,7 +2198,6 @@ __global__ void __launch_bounds__(256, 4) k_query_thread(FrameParams P)
 {
   __shared__ BigBoxes s_big;
   __shared__ uint32_t s_vis[8];
-  pdl_trigger();
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x == 0) s_big.count = s_big.next = 0;
@@ -2188,7 +2205,7 @@ __global__ void __launch_bounds__(256, 4) k_query_thread(FrameParams P)
   bool vis = false, nc = false, big = false;
   uint32_t rect[4] = {0, 0, 0, 0}, maxZ = 0, view = 0;
   // the box's projection reads only the view table and the boxes, written
-  // before the launch: it runs while the raster finishes
+  // before the launch: it may run while the raster's last CTAs finish
   int st = 0;
   bool have = false;
   if (slot < P.numQuerySlots) {
@@ -2227,7 +2244,6 @@ __global__ void __launch_bounds__(256, 6) k_query(FrameParams P, uint32_t rounds
 {
   __shared__ uint32_t s_slot[8][32 * kQueryRounds], s_view[8][32 * kQueryRounds];
   __shared__ uint32_t s_vis[8][kQueryRounds], s_nc[8][kQueryRounds];
-  pdl_trigger();
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t first = ((gridDim.x - 1 - blockIdx.x) * 8 + warp) * 32 * rounds;
   if (first >= P.numQuerySlots) return;
@@ -2374,7 +2390,7 @@ struct StageRanges {
 };
 
 // Launches `kernel` on `stream`; with `pdl`, as a programmatic dependent of
-// the kernel before it (pdl_trigger / pdl_wait).
+// the kernel before it (pdl_wait).
 template <typename... KArgs, typename... Args>
 static cudaError_t launch_k(bool pdl, void (*kernel)(KArgs...), uint32_t grid, uint32_t block, size_t smem,
                             cudaStream_t stream, Args... args)
@@ -2417,10 +2433,14 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
   }
   if (doRaster) {
     if (P.numChunks) {
+      // the gating: k_gate_second for a selection's second pass; k_select_view
+      // did it with fusedSelect; else k_chunk_gate itself (views of at most
+      // kChunkGateThreads commands) or k_gate
+      const bool inChunkGate = !P.phase && !P.fusedSelect && P.maxViewCmds <= kChunkGateThreads;
       if (P.phase) go(launch_k(chained, k_gate_second, (P.numCmds + 7) / 8, 256, 0, stream, P));
-      else if (!P.fusedSelect) go(launch_k(chained, k_gate, (P.numCmds + 255) / 256, 256, 0, stream, P));
-      // (with fusedSelect, k_select_view did the gating)
-      go(launch_k(chained, k_chunk_gate, P.numViews, 256, 0, stream, P));
+      else if (!P.fusedSelect && !inChunkGate)
+        go(launch_k(chained, k_gate, (P.numCmds + 255) / 256, 256, 0, stream, P));
+      go(launch_k(chained, k_chunk_gate, P.numViews, kChunkGateThreads, 0, stream, P, inChunkGate ? 1u : 0u));
       go(launch_k(chained, k_setup, grid_of(P.tune.setupPerSm, g_setupPerSm, P.numChunks), kChunk,
                   (size_t)maxStPerView * sizeof(uint32_t), stream, P));
     }

@@ -171,6 +171,7 @@ struct FrameParams {
   const ViewDesc* views;
   uint32_t numViews;
   uint32_t numCmds;
+  uint32_t maxViewCmds;  // commands of the view with the most
   uint32_t matSize;      // entries of `mat` over all views
   LaunchTuning tune;
   uint32_t phase;        // 0: the frame (or the top-K pass); 1: the second pass of a
@@ -183,9 +184,10 @@ struct FrameParams {
   const uint32_t* pool;  // packed occluder words
   QuadRaster* rec;
   QuadWalk* walk;
-  Totals* chunkTot;      // per chunk totals (rows, cks)
-  Totals* chunkBase;     // per chunk exclusive prefix within the view
-  uint32_t* mat;         // super-tile x chunk counts -> exclusive prefixes (per view, st-major)
+  Totals* chunkTot;      // per active chunk, at chunkStart + rank: totals (rows, cks)
+  Totals* chunkBase;     // per active chunk, at chunkStart + rank: exclusive prefix within the view
+  uint32_t* mat;         // super-tile x active chunk (by rank) counts -> exclusive prefixes (per view,
+                         // st-major, chunkCount columns)
   uint32_t* stStart;     // per global super-tile: list start (global)
   uint32_t* stLen;
   Totals* viewTot;
@@ -203,7 +205,7 @@ struct FrameParams {
   uint32_t* cmdDraw;     // per command: bit0 drawn (this pass), bit1 near-clipped, bit2 drawn by
                          // the first pass of this launch (second pass only)
   uint32_t* activeChunkList;  // chunks with a drawn command (header->activeChunks of them)
-  uint32_t* viewActiveChunks; // per view, from its chunkStart: local indices of its active chunks, in order
+  uint32_t* chunkRank;        // per active chunk: its rank among its view's active chunks (chunk order)
   uint32_t* viewActiveCount;  // per view: how many
   uint4* activeTileList;      // queued raster units (header->activeTiles): {warp-tile * 4 + first block
                               // row, view, first entry and length of the unit's super-tile list}
