@@ -552,7 +552,7 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
         "clocks": clocks, "kernels": kern,
         "culls_timed": dict(timed_culls.as_culls_dict(), launches=kept, views=kept * LEARNED_VIEWS,
                             against="full frames (every candidate, zero-depth clear) at the same poses"),
-        "roofline": {"bound": "hbm", "kernel": "k_raster (with k_tile_prep)", "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": "k_raster", "unit": "GB/s",
                      "achieved": raster_bytes / (kern["raster"] * 1e-3) / 1e9, "algorithmic_bytes": raster_bytes},
         "e2e": {"value": world * LEARNED_VIEWS * e2e_steps / e2e_s, "unit": "views/s",
                 "h2d_bytes_per_step": stats["table_bytes"], "d2h_bytes_per_step": int(vis_words.nbytes + nc_words.nbytes),
@@ -813,7 +813,7 @@ def run_plain(ctx, r, occ, mvps, mins, maxs, world, dev, args):
     ok = batch.check()
     dev_ms = max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(starts, ends)), world, dev)
     prof = batch.profile(min(steps, 300))
-    names = ["k_setup", "k_scan", "k_fill", "k_walk", "k_raster", "k_query"]
+    names = ["k_setup", "k_scan", "k_fill", "k_walk_prep", "k_raster", "k_query"]
     kern = {n: float(v) for n, v in zip(names, prof)}
     top = max(kern, key=kern.get)
     q_setup = sum(o.quads for o in occ)
