@@ -1,27 +1,40 @@
 // GPU occluder rasteriser and visibility queries (sm_103a).
 //
-// One flush runs six kernels over a batch of views (raster_types.h):
+// One flush runs these kernels over a batch of views (raster_types.h), each
+// after the first a programmatic dependent of the one before:
 //
-//   k_setup     one CTA per 256-quad chunk: per-occluder prologue and GPU
-//               gating (Rasterizer.cpp:612-655, :123-281), then one thread per
-//               quad does the vertex transform and quad setup
-//               (Rasterizer.cpp:660-1081) and counts the quad's rows, row-walk
-//               checkpoints and 16x16-block super-tiles.
-//   k_scan      order-preserving prefix sums of those counts.
-//   k_fill      one CTA per chunk: writes each super-tile's quad list in
-//               submission order and the (quad, row) list of the row walk.
-//   k_walk      one thread per (quad, block row): the reference's incremental
-//               float adds along the row, storing the edge offsets and depth
-//               lanes every 8 block columns.
-//   k_raster    one CTA per 8x4-block tile, four threads per 8x8 block: the CTA
-//               filters its super-tile's list into the quads overlapping the
-//               tile, computes (quad, block) fragments 128 at a time and merges
-//               them per block in list order (Rasterizer.cpp:1098-1292).
-//   k_query     queryVisibility + query2D (Rasterizer.cpp:123-349): frustum test
-//               per box, survivors listed per warp and projected by full
-//               warps (k_query_thread: one box per thread in place, for few
-//               boxes); boxes over more than a warp-tile of blocks (two
-//               warp-tiles in k_query_thread) are tested by the whole warp.
+//   k_chunk_gate  one CTA per view: gates the view's commands (the plain
+//                 loop's queryVisibility of the occluder bounds,
+//                 Rasterizer.cpp:123-281; k_gate does it for views of more
+//                 than 1,024 commands, the selection kernels with a
+//                 selector), then lists the chunks holding a drawn command
+//                 with their rank in the view.
+//   k_setup       one CTA per active 256-quad chunk: per-occluder prologue
+//                 (Rasterizer.cpp:612-655), then one thread per quad does the
+//                 vertex transform and quad setup (Rasterizer.cpp:660-1081)
+//                 and counts the quad's rows, row-walk checkpoints and
+//                 16x16-block super-tiles.
+//   k_scan        order-preserving prefix sums of those counts.
+//   k_fill        one CTA per active chunk: writes each super-tile's quad
+//                 list in submission order and the (quad, row) list of the
+//                 row walk.
+//   k_walk_prep   the row walk, one thread per (quad, block row): the
+//                 reference's incremental float adds along the row, storing
+//                 the edge offsets and depth lanes every 8 block columns; then
+//                 the tile preparation, one warp per 8x4-block tile: the
+//                 clear, and the queue of raster units a listed quad reaches.
+//   k_raster      a warp per queued unit of 8 x R blocks (k_raster_cta: a CTA
+//                 of 128 per 8x2-block unit, for launches with few units):
+//                 filters the super-tile list to the quads reaching the unit,
+//                 computes (quad, block) fragments and merges them per block
+//                 in list order (Rasterizer.cpp:1098-1292); each unit writes
+//                 its block rows' minimum hiZ.
+//   k_query       queryVisibility + query2D (Rasterizer.cpp:123-349): frustum
+//                 test per box, survivors listed per warp and projected by
+//                 full warps, boxes over more than a warp-tile of blocks
+//                 tested by the whole warp (k_query_thread: one box per
+//                 thread in place, for few boxes; boxes over more than two
+//                 warp-tiles shared by the CTA's warps).
 //
 // Exactness: every float operation follows the reference's order and
 // rounding (x86_emu.cuh); the block loop sees each quad's primitives in
@@ -243,21 +256,21 @@ __device__ __forceinline__ bool query2d_open_block(const ViewDesc& V, uint32_t b
     return ((__vcmpltu2(row.x, mz2) & cm[0]) | (__vcmpltu2(row.y, mz2) & cm[1]) | (__vcmpltu2(row.z, mz2) & cm[2]) |
             (__vcmpltu2(row.w, mz2) & cm[3])) != 0u;
   };
-  if (!kBatch) {
+  if constexpr (!kBatch) {
     for (int32_t y = sy; y <= ey; ++y)
       if (hit(d[y])) return true;
-    return false;
-  }
+  } else {
 #pragma unroll
-  for (int y0 = 0; y0 < 8; y0 += 4) {  // the block is one 128-byte line
-    if (y0 > ey || y0 + 3 < sy) continue;
-    uint4 row[4];
+    for (int y0 = 0; y0 < 8; y0 += 4) {  // the block is one 128-byte line
+      if (y0 > ey || y0 + 3 < sy) continue;
+      uint4 row[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) row[k] = (y0 + k >= sy && y0 + k <= ey) ? d[y0 + k] : make_uint4(0, 0, 0, 0);
-    bool any = false;
+      for (int k = 0; k < 4; ++k) row[k] = (y0 + k >= sy && y0 + k <= ey) ? d[y0 + k] : make_uint4(0, 0, 0, 0);
+      bool any = false;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) any |= y0 + k >= sy && y0 + k <= ey && hit(row[k]);
-    if (any) return true;
+      for (int k = 0; k < 4; ++k) any |= y0 + k >= sy && y0 + k <= ey && hit(row[k]);
+      if (any) return true;
+    }
   }
   return false;
 }
