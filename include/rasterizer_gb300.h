@@ -251,7 +251,7 @@ int occ_batch_set_zero_depth(occ_batch b, int enable);
  * per thread in place, 1..8 = frustum survivors listed per warp over that many
  * rounds of 32 boxes, raster unit rows: 1, 2 or 4 block rows of 8 blocks,
  * raster threads per unit: 32 (one warp per unit) or 128 (a CTA per unit of
- * 2 rows; 0 in set_tuning: chosen per launch by its unit count), binning
+ * 1 or 2 rows; 0 in set_tuning: chosen per launch by its unit count), binning
  * super-tile edge: 8 or 16 blocks (quads are listed per super-tile; smaller
  * ones give shorter lists and more entries)};
  * msBefore/msAfter[7] as occ_batch_profile (either may be NULL).  No
@@ -263,7 +263,7 @@ int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[OCC_TUNI
  * entry: the default), e.g. to reuse a tuned choice for a batch of the same
  * shape without timing it again.  CTAs per SM and units per fetch up to 64;
  * query form 0, 1..8 or 255; unit rows 0, 1, 2 or 4; threads per unit 0, 32
- * or 128 (with rows 0 or 2); super-tile edge 0, 8 or 16 (a new edge lays the
+ * or 128 (with rows 0, 1 or 2; 0: 1); super-tile edge 0, 8 or 16 (a new edge lays the
  * batch out again).  No reference counterpart. */
 int occ_batch_set_tuning(occ_batch b, const uint32_t tune[OCC_TUNING_FIELDS]);
 /* Work counts of the last launch (syncs): block rows walked, row-walk

@@ -1658,14 +1658,15 @@ int occ_batch_autotune(occ_batch b, uint32_t iterations, uint32_t tuned[9], floa
   OCC_CHECK(search(&LaunchTuning::setupPerSm, 0, upTo(lim[0])));
   OCC_CHECK(search(&LaunchTuning::fillPerSm, 2, upTo(lim[1])));
   OCC_CHECK(search(&LaunchTuning::walkPerSm, 3, {2, 4, 8, 16}));
-  // raster form: one warp per unit of 1, 2 or 4 block rows, or a CTA per 8x2 unit
+  // raster form: one warp per unit of 1, 2 or 4 block rows, or a CTA per unit
+  // of 8x1 or 8x2 blocks (128 + rows)
   {
     float bestMs = 3.0e38f;
     LaunchTuning pick = best;
-    for (uint32_t form : {1u, 2u, 4u, 128u}) {
+    for (uint32_t form : {1u, 2u, 4u, 129u, 130u}) {
       LaunchTuning t = best;
-      t.rasterThreads = form == 128u ? 128u : 32u;
-      t.rasterRows = form == 128u ? 2u : form;
+      t.rasterThreads = form > 128u ? 128u : 32u;
+      t.rasterRows = form > 128u ? form - 128u : form;
       OCC_CHECK(profile_with(b, t, iterations, ms));
       if (ms[4] < bestMs) {
         bestMs = ms[4];
@@ -1744,8 +1745,8 @@ int occ_batch_set_tuning(occ_batch b, const uint32_t tune[9])
     return fail(OCC_ERR_INVALID_ARG, "raster unit rows must be 1, 2 or 4 (0: the default)");
   if (tune[7] != 0 && tune[7] != 32 && tune[7] != 128)
     return fail(OCC_ERR_INVALID_ARG, "raster threads per unit must be 32 or 128 (0: chosen per launch)");
-  if (tune[7] == 128 && tune[6] != 0 && tune[6] != 2)
-    return fail(OCC_ERR_INVALID_ARG, "the 128-thread raster form takes units of 2 block rows");
+  if (tune[7] == 128 && tune[6] == 4)
+    return fail(OCC_ERR_INVALID_ARG, "the 128-thread raster form takes units of 1 or 2 block rows");
   if (tune[8] != 0 && tune[8] != 8 && tune[8] != 16)
     return fail(OCC_ERR_INVALID_ARG, "super-tile edge must be 8 or 16 blocks (0: 16)");
   LaunchTuning t{};

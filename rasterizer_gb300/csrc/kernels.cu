@@ -1681,15 +1681,17 @@ __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks<R>) k_raster(
 
 // ---- k_raster_cta: four warps per raster unit ------------------------------------------
 //
-// The other raster form: one CTA of 128 threads per 8x2-block unit, thread t
-// owning pixel row t%8 of block t/8.  The CTA filters the unit's super-tile
-// list 256 entries a round and computes 128 fragments a round, so a unit with
-// a long list or many fragments finishes four times sooner than on one warp;
+// The other raster form: one CTA of 128 threads per unit of 8 x R blocks (R
+// = 1 or 2), thread t owning pixel row t%8 of block t/8 (the threads past the
+// unit's 8 R blocks hold none).  The CTA filters the unit's super-tile list
+// 256 entries a round and computes 128 fragments a round, so a unit with a
+// long list or many fragments finishes four times sooner than on one warp;
 // the price is CTA barriers between the phases.  Views with few units and
 // long lists (one large view) favour it; batches of many views favour the
-// warp form.
+// warp form.  Units of one block row halve a unit's fragments (the filter
+// still reads the whole list): shorter chains for the heaviest units.
 
-constexpr int kCtaUnitBlocks = kTileW * 2;               // 16 blocks (8 x 2)
+constexpr int kCtaUnitBlocks = kTileW * 2;               // blocks of the largest unit (8 x 2)
 constexpr int kCtaThreads = 8 * kCtaUnitBlocks;          // one thread per block row: 128
 constexpr int kCtaMinBlocks = 8;
 constexpr int kCtaListCap = 512;                         // listed quads buffered per unit
@@ -1819,8 +1821,9 @@ __device__ __forceinline__ void raster_list_cta(const FrameParams& P, const View
   }
 }
 
-// One 8x2-block unit (queue record as raster_unit's, first block row even).
-template <bool kWins>
+// One unit of 8 x R blocks (queue record as raster_unit's; first block row a
+// multiple of R).
+template <int R, bool kWins>
 __device__ __forceinline__ void raster_unit_cta(const FrameParams& P, CtaRasterSmem& S, const uint4 rec)
 {
   const uint32_t tid = threadIdx.x, lane = tid & 31;
@@ -1829,7 +1832,7 @@ __device__ __forceinline__ void raster_unit_cta(const FrameParams& P, CtaRasterS
   const uint32_t tx0 = (lt % V.tilesX) * kTileW, ty0 = (lt / V.tilesX) * kTileH + (rec.x & 3u);
   const uint32_t myBlock = tid >> 3, py = tid & 7;
   const uint32_t bx = tx0 + (myBlock & 7), by = ty0 + (myBlock >> 3);
-  const bool inView = bx < V.blocksX && by < V.blocksY;
+  const bool inView = myBlock < 8u * R && bx < V.blocksX && by < V.blocksY;
   const uint32_t blk = inView ? by * V.blocksX + bx : 0;
   const bool clearing = (V.flags & kViewClear) != 0 && P.phase == 0;
   uint32_t hiz = clearing ? 1u : (inView ? (uint32_t)V.hiz[blk] : 0xFFFFu);
@@ -1838,7 +1841,7 @@ __device__ __forceinline__ void raster_unit_cta(const FrameParams& P, CtaRasterS
   uint32_t own[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const uint32_t listLen = rec.w;
   const uint4* list = P.stList + rec.z;
-  if (py == 0) S.hiz[myBlock] = hiz;
+  if (py == 0 && myBlock < 8u * R) S.hiz[myBlock] = hiz;
   __syncthreads();
   uint32_t n = 0, F = 0;
   // kCtaScanPerRound list entries per round (two consecutive ones per thread),
@@ -1857,7 +1860,7 @@ __device__ __forceinline__ void raster_unit_cta(const FrameParams& P, CtaRasterS
     for (int k = 0; k < 2; ++k) {
       const uint32_t qx0 = e[k].y & 0xFFFFu, qy0 = e[k].y >> 16, qx1 = e[k].z & 0xFFFFu, qy1 = e[k].z >> 16;
       const uint32_t x0 = ::max(qx0, tx0), x1 = ::min(qx1, tx0 + kTileW);
-      const uint32_t y0 = ::max(qy0, ty0), y1 = ::min(qy1, ty0 + 2);
+      const uint32_t y0 = ::max(qy0, ty0), y1 = ::min(qy1, ty0 + R);
       bool o = x0 < x1 && y0 < y1;  // padding entries have an empty box
       if (o) {
         const uint32_t mz = e[k].w;
@@ -1944,9 +1947,9 @@ __device__ __forceinline__ void raster_unit_cta(const FrameParams& P, CtaRasterS
   }
 }
 
-// Persistent CTAs taking queued 8x2 units one at a time; the next record is
-// copied with cp.async while the current unit is rasterised.
-template <bool kWins>
+// Persistent CTAs taking queued units of 8 x R blocks one at a time; the next
+// record is copied with cp.async while the current unit is rasterised.
+template <int R, bool kWins>
 __global__ void __launch_bounds__(kCtaThreads, kCtaMinBlocks) k_raster_cta(FrameParams P)
 {
   __shared__ CtaRasterSmem S;
@@ -1979,10 +1982,10 @@ __global__ void __launch_bounds__(kCtaThreads, kCtaMinBlocks) k_raster_cta(Frame
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
       }
-      raster_unit_cta<kWins>(P, S, rec);
+      raster_unit_cta<R, kWins>(P, S, rec);
       if (threadIdx.x == 0) asm volatile("cp.async.wait_all;" ::: "memory");
       __syncthreads();  // shared state is reused by the next unit; the next record has landed
-      if (threadIdx.x < 2) {  // the unit's two block rows' minimum hiZ (warps 2r, 2r + 1)
+      if (threadIdx.x < (uint32_t)R) {  // the unit's block rows' minimum hiZ (warps 2r, 2r + 1)
         const ViewDesc& V = P.views[rec.y];
         const uint32_t r = threadIdx.x;
         V.tileHiz[4 * (size_t)((rec.x >> 2) - V.tileStart) + (rec.x & 3u) + r] =
@@ -2467,14 +2470,15 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
     go(launch_k(chained, k_fill, grid_of(P.tune.fillPerSm, g_fillPerSm, P.numChunks), kChunk,
                 (size_t)maxStPerView * 64, stream, P));
   mark(3);
-  // raster form: a warp per unit of R block rows, or a CTA per 8x2 unit when
-  // the launch has few units (a warp would leave most of the GPU idle and
-  // long lists in sequence)
+  // raster form: a warp per unit of R block rows, or a CTA per unit of 8 x R
+  // blocks (R = 1 unless tuned to 2) when the launch has few units (a warp
+  // would leave most of the GPU idle and long lists in sequence)
   FrameParams Q = P;
   uint32_t threads = P.tune.rasterThreads;
   if (!threads) threads = P.numTiles * 2u < 4u * g_sms * g_rasterPerSm[1] * kRasterWarps ? 128u : 32u;
   Q.tune.rasterThreads = threads;
-  Q.tune.rasterRows = threads == 128u ? 2u : (P.tune.rasterRows ? P.tune.rasterRows : kDefaultRasterRows);
+  Q.tune.rasterRows = threads == 128u ? (P.tune.rasterRows == 2u ? 2u : kDefaultCtaRows)
+                                      : (P.tune.rasterRows ? P.tune.rasterRows : kDefaultRasterRows);
   if (doRaster && (P.numChunks || P.numTiles)) {
     // tile preparation and the row walk, one launch
     const uint32_t prep = (Q.numTiles + 7) / 8;
@@ -2488,7 +2492,9 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
     const bool w = Q.wins != nullptr;
     if (threads == 128u) {
       const uint32_t grid = grid_of(Q.tune.rasterPerSm, g_rasterCtaPerSm, units);
-      go(launch_k(chained, w ? k_raster_cta<true> : k_raster_cta<false>, grid, kCtaThreads, 0, stream, Q));
+      void (*k)(FrameParams) = R == 1 ? (w ? k_raster_cta<1, true> : k_raster_cta<1, false>)
+                                      : (w ? k_raster_cta<2, true> : k_raster_cta<2, false>);
+      go(launch_k(chained, k, grid, kCtaThreads, 0, stream, Q));
     } else {
       const uint32_t shape = R == 1 ? 0u : (R == 2 ? 1u : 2u);
       const uint32_t grid = grid_of(Q.tune.rasterPerSm, g_rasterPerSm[shape], (units + kRasterWarps - 1) / kRasterWarps);
@@ -2578,7 +2584,7 @@ cudaError_t set_kernel_attributes()
     g_rasterPerSm[1] = (uint32_t)nb;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster<4, true>, kRasterThreads, 0) == cudaSuccess && nb > 0)
     g_rasterPerSm[2] = (uint32_t)nb;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster_cta<true>, kCtaThreads, 0) == cudaSuccess && nb > 0)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_raster_cta<2, true>, kCtaThreads, 0) == cudaSuccess && nb > 0)
     g_rasterCtaPerSm = (uint32_t)nb;
   return cudaSuccess;
 }

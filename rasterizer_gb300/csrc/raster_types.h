@@ -20,6 +20,7 @@ constexpr int kTileW = 8;                 // warp-tile: 8 x 4 blocks, one lane p
 constexpr int kTileH = 4;
 constexpr int kCkSpan = 8;                // row-walk checkpoint every 8 block columns (== kTileW)
 constexpr uint32_t kDefaultRasterRows = 2;  // raster unit: 8 x R blocks of a warp-tile, R = 1, 2 or 4
+constexpr uint32_t kDefaultCtaRows = 1;     // the 128-thread form's unit: 8 x 1 blocks (or 8 x 2)
 constexpr int kMaxUnitsPerTile = kTileH;    // raster units per warp-tile at R = 1
 constexpr int kMaxCmdPerChunk = 40;       // commands are >= 8 quads, so <= 33 per chunk
 constexpr int kCkFloats = 12;             // 4 edge offsets + 8 depth lanes
@@ -161,7 +162,8 @@ constexpr uint32_t kQueryPerThread = 255;
 struct LaunchTuning {
   uint32_t setupPerSm, fillPerSm, walkPerSm, rasterPerSm, rasterChunk;
   uint32_t queryRounds;  // 0: chosen by slot count; else a k_query form (above)
-  uint32_t rasterRows;   // block rows per raster unit: 1, 2 or 4 (0: kDefaultRasterRows)
+  uint32_t rasterRows;   // block rows per raster unit: 1, 2 or 4 (0: kDefaultRasterRows, or
+                         // kDefaultCtaRows for the 128-thread form, which takes 1 or 2)
   uint32_t rasterThreads;  // threads per raster unit: 32 (one warp) or 128 (a CTA, units of 2 rows);
                            // 0: chosen by the launch's unit count
   uint32_t superTile;      // binning super-tile edge in blocks: 8 or 16 (0: kSuperTile); set by the host layout

@@ -272,11 +272,11 @@ def test_autotuned_launch_shapes_keep_results(ctx):
     b.close()
 
 
-@pytest.mark.parametrize("rows,threads,st", [(1, 32, 16), (2, 32, 16), (4, 32, 16), (2, 128, 16), (2, 32, 8),
-                                             (2, 128, 8)])
+@pytest.mark.parametrize("rows,threads,st", [(1, 32, 16), (2, 32, 16), (4, 32, 16), (2, 128, 16), (1, 128, 16),
+                                             (2, 32, 8), (2, 128, 8)])
 def test_raster_unit_shapes(ctx, rows, threads, st):
-    """Raster units of 1, 2 and 4 block rows per warp, and 2-row units per
-    128-thread CTA, with super-tiles of 16 and 8 blocks (choices of the
+    """Raster units of 1, 2 and 4 block rows per warp, and 1- and 2-row units
+    per 128-thread CTA, with super-tiles of 16 and 8 blocks (choices of the
     autotuner), give the oracle's frames: two views on persistent rasterizers,
     frames in the reference's clear (stale depth merged and queried), then in
     the zero-depth clear, with win counting on (the other kernel variant)."""
