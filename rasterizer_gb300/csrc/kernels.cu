@@ -2041,20 +2041,25 @@ __device__ __forceinline__ void query_resolve(const ViewDesc& V, int st, const u
 }
 
 // Boxes with large rectangles are collected per CTA and tested after the
-// CTA's other boxes by all of its warps, one box per warp at a time (a warp
-// testing its own large boxes one after the other would leave the few warps
-// holding several of them to set the stage's time).  All 32 lanes; a box that
-// does not fit the CTA's list is tested by its own warp at once (returns its
-// visibility in `vis`).
+// CTA's other boxes by all of its warps, in pieces of 32 warp-tiles a warp at
+// a time (a warp testing its own large boxes one after the other, or one box
+// whole, would leave the few warps holding the heaviest to set the stage's
+// time).  All 32 lanes; a box that does not fit the CTA's list is tested by
+// its own warp at once (returns its visibility in `vis`).
 constexpr uint32_t kBigPerCta = 256;
 
 struct BigBoxes {
-  uint4 box[kBigPerCta];  // {slot, minX | maxX << 16, minY | maxY << 16, maxZ}
+  uint4 box[kBigPerCta];           // {slot, minX | maxX << 16, minY | maxY << 16, maxZ}
+  uint32_t pieceStart[kBigPerCta];  // first piece of each box (pieces of 32 warp-tiles)
+  uint32_t found[kBigPerCta / 32];  // bit per box: visible (its other pieces are skipped)
+  uint32_t scan[8];
   uint32_t count, next;
 };
 
 __device__ __forceinline__ bool query_big_box(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_t minY,
                                               uint32_t maxY, uint32_t mz, uint32_t lane);
+__device__ __forceinline__ bool query_big_round(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_t minY,
+                                                uint32_t maxY, uint32_t mz, uint32_t t0, uint32_t lane);
 __device__ __forceinline__ uint32_t query_view(const FrameParams& P, uint32_t slot, uint32_t lo, uint32_t hi);
 
 __device__ __forceinline__ void collect_big(const FrameParams& P, BigBoxes& B, bool big, uint32_t slot,
@@ -2081,41 +2086,67 @@ __device__ __forceinline__ void collect_big(const FrameParams& P, BigBoxes& B, b
   }
 }
 
-// After the CTA barrier that follows every collect_big: the warps take the
-// CTA's large boxes one at a time; a visible one sets bit (slot - slot0) of
-// the CTA's bit array `bits`.  All 32 lanes.
-__device__ __forceinline__ void test_big(const FrameParams& P, BigBoxes& B, uint32_t slot0, uint32_t* bits,
-                                         uint32_t lane)
+// Warp-tiles of a box's rectangle.
+__device__ __forceinline__ uint32_t big_tiles(const uint4& e)
 {
-  const uint32_t n = ::min(B.count, kBigPerCta);
+  const uint32_t bx0 = (e.y & 0xFFFFu) >> 3, bx1 = (e.y >> 16) >> 3, by0 = (e.z & 0xFFFFu) >> 3, by1 = (e.z >> 16) >> 3;
+  return (bx1 / kTileW - bx0 / kTileW + 1) * (by1 / kTileH - by0 / kTileH + 1);
+}
+
+// After the CTA barrier that follows every collect_big, all 256 threads of
+// the CTA: each large box is cut into pieces of 32 warp-tiles (offsets by a
+// CTA scan), and the warps take the pieces one at a time; a visible piece
+// marks its box found (its pieces not yet taken are skipped) and sets bit
+// (slot - slot0) of the CTA's bit array `bits`.
+__device__ __forceinline__ void test_big(const FrameParams& P, BigBoxes& B, uint32_t slot0, uint32_t* bits,
+                                         uint32_t tid)
+{
+  const uint32_t n = ::min(B.count, kBigPerCta), lane = tid & 31;
+  if (n == 0) return;  // the same for every thread
+  const uint32_t pieces = tid < n ? (big_tiles(B.box[tid]) + 31) / 32 : 0u;
+  uint32_t total;
+  const uint32_t first = block_exclusive_scan<256>(pieces, total, B.scan);
+  if (tid < n) B.pieceStart[tid] = first;
+  if (tid < kBigPerCta / 32) B.found[tid] = 0;
+  __syncthreads();
   for (;;) {
     uint32_t i = 0;
     if (lane == 0) i = atomicAdd(&B.next, 1u);
     i = __shfl_sync(0xFFFFFFFFu, i, 0);
-    if (i >= n) break;
-    const uint4 e = B.box[i];
+    if (i >= total) break;
+    uint32_t lo = 0, hi = n - 1;  // the box of piece i
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (B.pieceStart[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    if ((B.found[lo >> 5] >> (lo & 31u)) & 1u) continue;
+    const uint4 e = B.box[lo];
     const ViewDesc& V = P.views[query_view(P, e.x, 0, P.numViews - 1)];
-    if (query_big_box(V, e.y & 0xFFFFu, e.y >> 16, e.z & 0xFFFFu, e.z >> 16, e.w, lane) && lane == 0)
+    const uint32_t t0 = 32u * (i - B.pieceStart[lo]);
+    if (query_big_round(V, e.y & 0xFFFFu, e.y >> 16, e.z & 0xFFFFu, e.z >> 16, e.w, t0, lane) && lane == 0) {
+      atomicOr(&B.found[lo >> 5], 1u << (lo & 31u));
       atomicOr(bits + ((e.x - slot0) >> 5), 1u << (e.x & 31u));
+    }
   }
 }
 
-// query2D of one box with a large rectangle by the whole warp: its
-// warp-tiles 32 at a time, one per lane, after their minimum hiZ (a tile whose
-// minimum is >= maxZ holds no block the reference would read).  When few of
-// the 32 tiles pass, each is then tested one block per lane (a tile has 8 x 4
-// = 32 blocks); when many pass, each lane tests its own tile's blocks in
-// sequence.  Returns the same on every lane.
+// query2D of one box with a large rectangle by the whole warp, 32 of its
+// warp-tiles from tile t0 (query_big_round) or all of them: one tile per
+// lane, after their minimum hiZ (a tile whose minimum is >= maxZ holds no
+// block the reference would read).  When few of the 32 tiles pass, each is
+// then tested one block per lane (a tile has 8 x 4 = 32 blocks); when many
+// pass, each lane tests its own tile's blocks in sequence.  Returns the same
+// on every lane.
 constexpr uint32_t kBigSplitMax = 4;  // tiles passing a round, at most, tested a block per lane
 
-__device__ __forceinline__ bool query_big_box(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_t minY,
-                                              uint32_t maxY, uint32_t mz, uint32_t lane)
+__device__ __forceinline__ bool query_big_round(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_t minY,
+                                                uint32_t maxY, uint32_t mz, uint32_t t0, uint32_t lane)
 {
   const uint32_t tilesX = (V.blocksX + kTileW - 1) / kTileW;
   const uint32_t bx0 = minX >> 3, bx1 = maxX >> 3, by0 = minY >> 3, by1 = maxY >> 3;
   const uint32_t tx0 = bx0 / kTileW, ty0 = by0 / kTileH;
   const uint32_t ntx = bx1 / kTileW - tx0 + 1, nt = ntx * (by1 / kTileH - ty0 + 1);
-  for (uint32_t t0 = 0; t0 < nt; t0 += 32) {
+  {
     const uint32_t t = t0 + lane;
     uint32_t tx = 0, ty = 0;
     uint2 rm = make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu);
@@ -2129,8 +2160,7 @@ __device__ __forceinline__ bool query_big_box(const ViewDesc& V, uint32_t minX, 
     uint32_t openMask = __ballot_sync(0xFFFFFFFFu, open);
     if ((uint32_t)__popc(openMask) > kBigSplitMax) {
       const bool hit = open && query2d_tile<true>(V, tx, ty, rm, minX, maxX, minY, maxY, mz);
-      if (__ballot_sync(0xFFFFFFFFu, hit)) return true;
-      continue;
+      return __ballot_sync(0xFFFFFFFFu, hit) != 0;
     }
     while (openMask) {
       const uint32_t tt = t0 + (uint32_t)(__ffs(openMask) - 1);
@@ -2142,6 +2172,15 @@ __device__ __forceinline__ bool query_big_box(const ViewDesc& V, uint32_t minX, 
       if (__ballot_sync(0xFFFFFFFFu, hit)) return true;
     }
   }
+  return false;
+}
+
+__device__ __forceinline__ bool query_big_box(const ViewDesc& V, uint32_t minX, uint32_t maxX, uint32_t minY,
+                                              uint32_t maxY, uint32_t mz, uint32_t lane)
+{
+  const uint32_t nt = big_tiles(make_uint4(0, minX | (maxX << 16), minY | (maxY << 16), 0));
+  for (uint32_t t0 = 0; t0 < nt; t0 += 32)
+    if (query_big_round(V, minX, maxX, minY, maxY, mz, t0, lane)) return true;
   return false;
 }
 
@@ -2241,7 +2280,7 @@ __global__ void __launch_bounds__(256, 4) k_query_thread(FrameParams P)
   collect_big(P, s_big, big, slot, view, rect, maxZ, lane, vis);
   const uint32_t vb = __ballot_sync(0xFFFFFFFFu, vis), nb = __ballot_sync(0xFFFFFFFFu, nc);
   __syncthreads();
-  test_big(P, s_big, blockIdx.x * blockDim.x, s_vis, lane);
+  test_big(P, s_big, blockIdx.x * blockDim.x, s_vis, threadIdx.x);
   __syncthreads();
   if (lane == 0 && slot < P.numQuerySlots) {
     P.visBits[slot >> 5] = vb | s_vis[warp];
