@@ -993,7 +993,7 @@ __global__ void __launch_bounds__(kChunk) k_fill(FrameParams P)
   }
 }
 
-// ---- k_walk ---------------------------------------------------------------------------
+// ---- row walk (k_walk_prep) -------------------------------------------------------------
 // One thread per (quad, block row) of the whole batch: the reference's
 // incremental adds along the row (Rasterizer.cpp:1125-1146), storing the edge
 // offsets and depth lanes at the quad's first column and every 8 block columns.

@@ -135,7 +135,7 @@ struct FrameHeader {
   uint32_t maxCks, maxSt, pad[2];              // largest totals seen since the last check
   // reset at the start of every launch
   uint32_t activeChunks;  // chunks with a drawn command (k_chunk_gate)
-  uint32_t activeTiles;   // warp-tiles whose super-tile has a quad list (k_tile_prep)
+  uint32_t activeTiles;   // queued raster units (tile preparation in k_walk_prep)
   uint32_t tileCursor;    // next entry of the active tile list (k_raster)
   uint32_t pad2;
 };
