@@ -564,7 +564,10 @@ def run_learned(ctx, occ, pmin, pmax, world, rank, dev, args):
             "d2h_bytes_per_step": int(vis_words.nbytes + nc_words.nbytes),
             "path": "as e2e, plus PreparedBatch.setQueries: every view's 100k boxes (min and max float4) from "
                     "page-locked host memory each step, two box sets alternating"},
-        "launches_per_step": 4 + 9}
+        # kernels per graph launch (the ncu launch list agrees): k_features and
+        # k_select_view, then the flush's k_chunk_gate, k_setup, k_scan, k_fill,
+        # k_walk_prep, k_raster, k_query
+        "launches_per_step": 2 + 7}
     # ---- the 256-view workload (mixed resolutions) ----
     k_mv = pick(L.multiview_tracks(centers, quads, NQ, frames=4, seed=9))
     test = L.multiview_tracks(centers, quads, NQ, frames=4, seed=3)
@@ -911,7 +914,7 @@ def run_gpu(args):
     else:
         line.update({"value": plain["value"], "unit": "views/s", "steps": plain["steps"],
                      "ms_per_step": plain["ms_per_step"], "roofline": plain["roofline"], "e2e": plain["e2e"],
-                     "gpu_launches": 9 * plain["steps"], "kernels_ms": plain["kernels_ms"],
+                     "gpu_launches": 7 * plain["steps"], "kernels_ms": plain["kernels_ms"],
                      "config": {"workload": workload_desc(mesh, occ), "parallelism": f"replicas x{world}"}})
     line["plain_single_view"] = dict(plain, workload=workload_desc(mesh, occ))
     if batched is not None:
