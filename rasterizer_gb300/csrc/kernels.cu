@@ -655,16 +655,22 @@ __global__ void __launch_bounds__(256) k_gate_second(FrameParams P)
 // contribute no rows, checkpoints or list entries.
 // With `gate` (views of at most kChunkGateThreads commands, no selection
 // pass), the CTA first gates the view's commands itself, one per thread, in
-// place of k_gate.
+// place of k_gate.  With `reset` (a launch of one view, so one CTA), thread 0
+// resets the launch's counters in place of a memset before the launch.
 constexpr uint32_t kChunkGateThreads = 1024;
 
-__global__ void __launch_bounds__(kChunkGateThreads) k_chunk_gate(FrameParams P, uint32_t gate)
+__global__ void __launch_bounds__(kChunkGateThreads) k_chunk_gate(FrameParams P, uint32_t gate, uint32_t reset)
 {
   __shared__ uint32_t s_scan[kChunkGateThreads / 32];
   __shared__ uint32_t s_base;
   pdl_wait();
   const uint32_t v = blockIdx.x, tid = threadIdx.x;
   const ViewDesc& V = P.views[v];
+  if (reset && tid == 0) {  // before this thread's first atomic on activeChunks; the others are later kernels'
+    P.header->activeChunks = 0;
+    P.header->activeTiles = 0;
+    P.header->tileCursor = 0;
+  }
   if (gate) {
     if (tid < V.cmdCount) gate_cmd(P, V.cmdStart + tid);
     __syncthreads();  // the CTA's cmdDraw stores, visible to its threads
@@ -2481,8 +2487,10 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
     chained = g_pdl && ev == nullptr;
   };
   mark(0);
-  if (doRaster || doQuery) {
-    // activeChunks, activeTiles, tileCursor
+  // activeChunks, activeTiles, tileCursor: reset by the chunk gate when it is
+  // one CTA (one view), else by a memset before the launch
+  const bool resetInGate = doRaster && P.numChunks && P.numViews == 1;
+  if (doRaster && !resetInGate) {
     e = cudaMemsetAsync(&P.header->activeChunks, 0, kHeaderResetWords * sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
   }
@@ -2495,7 +2503,8 @@ static cudaError_t flush_stages(const FrameParams& P, uint32_t numSt, uint32_t m
       if (P.phase) go(launch_k(chained, k_gate_second, (P.numCmds + 7) / 8, 256, 0, stream, P));
       else if (!P.fusedSelect && !inChunkGate)
         go(launch_k(chained, k_gate, (P.numCmds + 255) / 256, 256, 0, stream, P));
-      go(launch_k(chained, k_chunk_gate, P.numViews, kChunkGateThreads, 0, stream, P, inChunkGate ? 1u : 0u));
+      go(launch_k(chained, k_chunk_gate, P.numViews, kChunkGateThreads, 0, stream, P, inChunkGate ? 1u : 0u,
+                  resetInGate ? 1u : 0u));
       go(launch_k(chained, k_setup, grid_of(P.tune.setupPerSm, g_setupPerSm, P.numChunks), kChunk,
                   (size_t)maxStPerView * sizeof(uint32_t), stream, P));
     }
